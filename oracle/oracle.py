@@ -1,0 +1,120 @@
+"""ctypes bindings for the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Loads oracle/libmsvoracle.so, the scalar C restatement of HMMER 3.1b1's
+p7_MSVFilter (src/impl_sse/msvfilter.c:77-213, with the SSV fast path of
+src/impl_sse/ssvfilter.c:1364-1413) and of the MSV stage of p7_Pipeline
+(src/p7_pipeline.c:662-677). Only tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py may import this module.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmsvoracle.so")
+
+
+def build(force: bool = False) -> str:
+    src = os.path.join(HERE, "msv_oracle.c")
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+        subprocess.check_call(["cc", "-O2", "-std=gnu99", "-ffp-contract=off", "-fPIC", "-shared",
+                               "-pthread", src, "-o", LIB_PATH, "-lm"])
+    return LIB_PATH
+
+
+class _Prof(ctypes.Structure):
+    _fields_ = [("M", ctypes.c_int), ("Q", ctypes.c_int), ("Kp", ctypes.c_int),
+                ("rbv", ctypes.c_void_p),
+                ("tbm_b", ctypes.c_uint8), ("tec_b", ctypes.c_uint8),
+                ("base_b", ctypes.c_uint8), ("bias_b", ctypes.c_uint8),
+                ("scale_b", ctypes.c_float), ("mmu", ctypes.c_double), ("mlambda", ctypes.c_double)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = ctypes.CDLL(build())
+        _lib.orc_tjb_b.restype = ctypes.c_uint8
+        _lib.orc_tjb_b.argtypes = [ctypes.c_float, ctypes.c_int]
+        _lib.orc_msv_filter.restype = ctypes.c_int
+        _lib.orc_msv_full.restype = ctypes.c_int
+        _lib.orc_score_from_xj.restype = ctypes.c_float
+        _lib.orc_score_from_xj.argtypes = [ctypes.c_uint8, ctypes.c_uint8, ctypes.c_uint8, ctypes.c_float]
+        _lib.orc_f1_pass.restype = ctypes.c_int
+        _lib.orc_f1_pass.argtypes = [ctypes.c_float, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                     ctypes.c_double, ctypes.POINTER(ctypes.c_float),
+                                     ctypes.POINTER(ctypes.c_double)]
+        _lib.orc_msv_batch.restype = ctypes.c_int
+        _lib.orc_msv_batch.argtypes = [ctypes.POINTER(_Prof), ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_int64, ctypes.c_double, ctypes.c_int,
+                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_void_p, ctypes.c_void_p]
+    return _lib
+
+
+def _prof(p):
+    rbv = np.ascontiguousarray(p.rbv, dtype=np.uint8)
+    s = _Prof(p.M, p.Q, p.Kp, rbv.ctypes.data, p.tbm_b, p.tec_b, p.base_b, p.bias_b,
+              p.scale_b, p.mmu, p.mlambda)
+    return s, rbv
+
+
+def tjb_b(scale_b: float, L: int) -> int:
+    return int(lib().orc_tjb_b(scale_b, L))
+
+
+def score_from_xj(xj: int, tjb: int, base_b: int, scale_b: float) -> float:
+    return float(lib().orc_score_from_xj(xj, tjb, base_b, scale_b))
+
+
+def f1_pass(usc: float, L: int, mmu: float, mlambda: float, F1: float = 0.02):
+    ns = ctypes.c_float()
+    P = ctypes.c_double()
+    r = lib().orc_f1_pass(usc, L, mmu, mlambda, F1, ctypes.byref(ns), ctypes.byref(P))
+    return bool(r), ns.value, P.value
+
+
+def msv_filter(p, dsq_codes, *, full_only: bool = False):
+    """One p7_MSVFilter call on a single sequence (codes without sentinels).
+    Returns (status, xj, sc, path)."""
+    L = len(dsq_codes)
+    dsq = np.empty(L + 2, np.uint8)
+    dsq[0] = dsq[-1] = 255
+    dsq[1:L + 1] = dsq_codes
+    s, keep = _prof(p)
+    xj = ctypes.c_uint8()
+    sc = ctypes.c_float()
+    path = ctypes.c_int(1)
+    tjb = tjb_b(p.scale_b, L)
+    if full_only:
+        st = lib().orc_msv_full(dsq.ctypes.data_as(ctypes.c_void_p), ctypes.c_int(L), ctypes.byref(s),
+                                ctypes.c_uint8(tjb), ctypes.byref(xj), ctypes.byref(sc))
+    else:
+        st = lib().orc_msv_filter(dsq.ctypes.data_as(ctypes.c_void_p), ctypes.c_int(L), ctypes.byref(s),
+                                  ctypes.c_uint8(tjb), ctypes.byref(xj), ctypes.byref(sc),
+                                  ctypes.byref(path))
+    return int(st), int(xj.value), float(sc.value), int(path.value)
+
+
+def msv_batch(p, seqs, *, F1: float = 0.02, nthreads: int = 0):
+    """Oracle over a SeqSet. Returns dict of numpy arrays:
+    status (int32, -1 = empty sequence), xj (uint8), sc (float32), pass (uint8), path (uint8)."""
+    n = seqs.n
+    out = {"status": np.zeros(n, np.int32), "xj": np.zeros(n, np.uint8), "sc": np.zeros(n, np.float32),
+           "pass": np.zeros(n, np.uint8), "path": np.zeros(n, np.uint8)}
+    s, keep = _prof(p)
+    codes = np.ascontiguousarray(seqs.codes, dtype=np.uint8)
+    off = np.ascontiguousarray(seqs.off, dtype=np.int64)
+    if codes.size == 0:
+        codes = np.zeros(1, np.uint8)
+    lib().orc_msv_batch(ctypes.byref(s), codes.ctypes.data, off.ctypes.data, n, F1, nthreads,
+                        out["status"].ctypes.data, out["xj"].ctypes.data, out["sc"].ctypes.data,
+                        out["pass"].ctypes.data, out["path"].ctypes.data)
+    return out

@@ -1,0 +1,193 @@
+/* refgen: golden-vector generator built on the reference HMMER 3.1b1 sources.
+ *
+ * Test infrastructure only. Links the reference's own libraries (compiled by
+ * oracle/ref/Makefile into oracle/_ref/) and runs its real code:
+ *   profile  : p7_hmm_Sample -> p7_Calibrate -> p7_ProfileConfig -> p7_oprofile_Convert
+ *              (hmmer src/p7_hmm.c:877, src/evalues.c:60, src/modelconfig.c:49,
+ *               src/impl_sse/p7_oprofile.c:839) and dumps the MSV part of the
+ *              P7_OPROFILE (impl_sse.h:77-87) plus evparam[MMU, MLAMBDA].
+ *   emit     : p7_ProfileEmit (src/emit.c:186) homologs of that profile, and
+ *              "saturation" sequences (an emitted core repeated R times).
+ *   randseq  : esl_rsq_xfIID (easel/esl_randomseq.c:764) i.i.d. background residues.
+ *   score    : per sequence, exactly the MSV stage of p7_Pipeline
+ *              (src/p7_pipeline.c:662-677, with the per-sequence length
+ *              reconfiguration of src/hmmsearch.c:1402-1404):
+ *              p7_bg_SetLength, p7_oprofile_ReconfigLength, p7_bg_NullOne,
+ *              p7_MSVFilter (impl_sse/msvfilter.c:78), esl_gumbel_surv, F1 gate.
+ *
+ * File formats (little-endian, written and read by this project only):
+ *   profile "MSVPROF1": int32 M, Q, Kp, Lcfg; uint8 tbm,tec,tjb,base,bias,pad[3];
+ *                       float scale; double mmu, mlambda; uint8 rbv[Kp*Q*16]
+ *   seqs    "MSVSEQS1": int64 n, total; int64 off[n+1]; uint8 dsq[total]   (codes, no sentinels)
+ *   result  "MSVRES01": int64 n; int32 status[n]; float sc[n]; double nullsc[n];
+ *                       double P[n]; uint8 pass[n]
+ */
+#include "p7_config.h"
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "easel.h"
+#include "esl_alphabet.h"
+#include "esl_random.h"
+#include "esl_randomseq.h"
+#include "esl_sq.h"
+#include "esl_gumbel.h"
+#include "hmmer.h"
+
+static void die(const char *m) { fprintf(stderr, "refgen: %s\n", m); exit(1); }
+
+typedef struct {
+  ESL_ALPHABET *abc; P7_BG *bg; P7_HMM *hmm; P7_PROFILE *gm; P7_OPROFILE *om;
+} model_t;
+
+/* Sample, calibrate, configure and convert a model exactly as hmmbuild-style
+ * code paths do; calibration uses its default internal RNG (seed 42). */
+static void make_model(model_t *m, int M, uint32_t seed, int Lcfg, int mode)
+{
+  ESL_RANDOMNESS *r = esl_randomness_Create(seed);
+  m->abc = esl_alphabet_Create(eslAMINO);
+  m->bg  = p7_bg_Create(m->abc);
+  if (p7_hmm_Sample(r, M, m->abc, &m->hmm) != eslOK) die("p7_hmm_Sample");
+  if (p7_Calibrate(m->hmm, NULL, NULL, &m->bg, NULL, NULL) != eslOK) die("p7_Calibrate");
+  m->gm = p7_profile_Create(M, m->abc);
+  if (p7_ProfileConfig(m->hmm, m->bg, m->gm, Lcfg, mode) != eslOK) die("p7_ProfileConfig");
+  m->om = p7_oprofile_Create(M, m->abc);
+  if (p7_oprofile_Convert(m->gm, m->om) != eslOK) die("p7_oprofile_Convert");
+  esl_randomness_Destroy(r);
+}
+
+static void write_profile(const model_t *m, int Lcfg, const char *path)
+{
+  FILE *fp = fopen(path, "wb"); if (!fp) die("open profile out");
+  int32_t hdr[4]; int Q = p7O_NQB(m->om->M);
+  hdr[0] = m->om->M; hdr[1] = Q; hdr[2] = m->abc->Kp; hdr[3] = Lcfg;
+  uint8_t b[8] = { m->om->tbm_b, m->om->tec_b, m->om->tjb_b, m->om->base_b, m->om->bias_b, 0, 0, 0 };
+  float scale = m->om->scale_b;
+  double ev[2] = { m->om->evparam[p7_MMU], m->om->evparam[p7_MLAMBDA] };
+  fwrite("MSVPROF1", 1, 8, fp);
+  fwrite(hdr, 4, 4, fp); fwrite(b, 1, 8, fp); fwrite(&scale, 4, 1, fp); fwrite(ev, 8, 2, fp);
+  for (int x = 0; x < m->abc->Kp; x++) fwrite(m->om->rbv[x], 16, Q, fp);
+  fclose(fp);
+}
+
+typedef struct { int64_t n, total; int64_t *off; uint8_t *dsq; } seqs_t;
+
+static void write_seqs(const seqs_t *s, const char *path)
+{
+  FILE *fp = fopen(path, "wb"); if (!fp) die("open seqs out");
+  fwrite("MSVSEQS1", 1, 8, fp);
+  fwrite(&s->n, 8, 1, fp); fwrite(&s->total, 8, 1, fp);
+  fwrite(s->off, 8, s->n + 1, fp); fwrite(s->dsq, 1, s->total, fp);
+  fclose(fp);
+}
+
+static void read_seqs(seqs_t *s, const char *path)
+{
+  char mag[8]; FILE *fp = fopen(path, "rb"); if (!fp) die("open seqs in");
+  if (fread(mag, 1, 8, fp) != 8 || memcmp(mag, "MSVSEQS1", 8)) die("bad seqs magic");
+  if (fread(&s->n, 8, 1, fp) != 1 || fread(&s->total, 8, 1, fp) != 1) die("short seqs");
+  s->off = malloc(8 * (s->n + 1)); s->dsq = malloc(s->total > 0 ? s->total : 1);
+  if (fread(s->off, 8, s->n + 1, fp) != (size_t)(s->n + 1)) die("short offsets");
+  if (fread(s->dsq, 1, s->total, fp) != (size_t) s->total) die("short residues");
+  fclose(fp);
+}
+
+static void push_seq(seqs_t *s, int64_t *cap, const ESL_DSQ *dsq, int L)
+{
+  while (s->total + L > *cap) { *cap = *cap * 2 + L; s->dsq = realloc(s->dsq, *cap); }
+  memcpy(s->dsq + s->total, dsq + 1, L);
+  s->total += L; s->n++;
+  s->off = realloc(s->off, 8 * (s->n + 1)); s->off[s->n] = s->total;
+}
+
+int main(int argc, char **argv)
+{
+  if (argc < 2) die("usage: refgen profile|emit|randseq|score ...");
+  const char *cmd = argv[1];
+
+  if (!strcmp(cmd, "profile")) {            /* profile M seed Lcfg mode out */
+    if (argc != 7) die("profile M seed Lcfg mode(1=local,3=unilocal) out");
+    model_t m; int M = atoi(argv[2]), Lcfg = atoi(argv[4]);
+    make_model(&m, M, (uint32_t) atol(argv[3]), Lcfg, atoi(argv[5]));
+    write_profile(&m, Lcfg, argv[6]);
+    return 0;
+  }
+  if (!strcmp(cmd, "emit")) {               /* emit M seed Lcfg mode n emitseed repeat out */
+    if (argc != 10) die("emit M seed Lcfg mode n emitseed repeat out");
+    model_t m; int M = atoi(argv[2]), Lcfg = atoi(argv[4]);
+    make_model(&m, M, (uint32_t) atol(argv[3]), Lcfg, atoi(argv[5]));
+    int n = atoi(argv[6]), rep = atoi(argv[8]);
+    ESL_RANDOMNESS *r = esl_randomness_Create((uint32_t) atol(argv[7]));
+    ESL_SQ *sq = esl_sq_CreateDigital(m.abc);
+    seqs_t s = {0, 0, NULL, NULL}; int64_t cap = 0;
+    s.off = malloc(8); s.off[0] = 0;
+    ESL_DSQ *buf = NULL;
+    for (int i = 0; i < n; i++) {
+      esl_sq_Reuse(sq);
+      if (p7_ProfileEmit(r, m.hmm, m.gm, m.bg, sq, NULL) != eslOK) die("p7_ProfileEmit");
+      int L = (int) sq->n;
+      if (rep <= 1) { push_seq(&s, &cap, sq->dsq, L); continue; }
+      buf = realloc(buf, (size_t) L * rep + 2);
+      buf[0] = eslDSQ_SENTINEL;
+      for (int k = 0; k < rep; k++) memcpy(buf + 1 + (size_t) k * L, sq->dsq + 1, L);
+      buf[(size_t) L * rep + 1] = eslDSQ_SENTINEL;
+      push_seq(&s, &cap, buf, L * rep);
+    }
+    write_seqs(&s, argv[9]);
+    return 0;
+  }
+  if (!strcmp(cmd, "randseq")) {            /* randseq n L seed out */
+    if (argc != 6) die("randseq n L seed out");
+    ESL_ALPHABET *abc = esl_alphabet_Create(eslAMINO);
+    P7_BG *bg = p7_bg_Create(abc);
+    int n = atoi(argv[2]), L = atoi(argv[3]);
+    ESL_RANDOMNESS *r = esl_randomness_Create((uint32_t) atol(argv[4]));
+    ESL_DSQ *dsq = malloc(L + 2);
+    seqs_t s = {0, 0, NULL, NULL}; int64_t cap = 0;
+    s.off = malloc(8); s.off[0] = 0;
+    for (int i = 0; i < n; i++) {
+      if (esl_rsq_xfIID(r, bg->f, abc->K, L, dsq) != eslOK) die("esl_rsq_xfIID");
+      push_seq(&s, &cap, dsq, L);
+    }
+    write_seqs(&s, argv[5]);
+    return 0;
+  }
+  if (!strcmp(cmd, "score")) {              /* score M seed Lcfg mode seqs out */
+    if (argc != 8) die("score M seed Lcfg mode seqs out");
+    model_t m; int M = atoi(argv[2]), Lcfg = atoi(argv[4]);
+    make_model(&m, M, (uint32_t) atol(argv[3]), Lcfg, atoi(argv[5]));
+    seqs_t s; read_seqs(&s, argv[6]);
+    int64_t maxL = 1;
+    for (int64_t i = 0; i < s.n; i++) if (s.off[i+1] - s.off[i] > maxL) maxL = s.off[i+1] - s.off[i];
+    P7_OMX *ox = p7_omx_Create(M, 0, 0);
+    ESL_DSQ *dsq = malloc(maxL + 2);
+    int32_t *st = calloc(s.n, 4); float *sc = calloc(s.n, 4);
+    double *ns = calloc(s.n, 8), *P = calloc(s.n, 8); uint8_t *pass = calloc(s.n, 1);
+    const double F1 = 0.02;                 /* p7_pipeline.c:210 default */
+    for (int64_t i = 0; i < s.n; i++) {
+      int L = (int) (s.off[i+1] - s.off[i]);
+      float usc, nullsc;
+      if (L == 0) { st[i] = -1; continue; } /* the pipeline skips empty sequences (p7_pipeline.c:662) */
+      dsq[0] = eslDSQ_SENTINEL; memcpy(dsq + 1, s.dsq + s.off[i], L); dsq[L+1] = eslDSQ_SENTINEL;
+      p7_bg_SetLength(m.bg, L);
+      p7_oprofile_ReconfigLength(m.om, L);
+      p7_bg_NullOne(m.bg, dsq, L, &nullsc);
+      st[i] = p7_MSVFilter(dsq, L, m.om, ox, &usc);
+      sc[i] = usc; ns[i] = nullsc;
+      float seq_score = (usc - nullsc) / eslCONST_LOG2;
+      P[i] = esl_gumbel_surv(seq_score, m.om->evparam[p7_MMU], m.om->evparam[p7_MLAMBDA]);
+      pass[i] = (P[i] > F1) ? 0 : 1;
+    }
+    FILE *fp = fopen(argv[7], "wb"); if (!fp) die("open result out");
+    fwrite("MSVRES01", 1, 8, fp); fwrite(&s.n, 8, 1, fp);
+    fwrite(st, 4, s.n, fp); fwrite(sc, 4, s.n, fp); fwrite(ns, 8, s.n, fp);
+    fwrite(P, 8, s.n, fp); fwrite(pass, 1, s.n, fp);
+    fclose(fp);
+    return 0;
+  }
+  die("unknown command");
+  return 1;
+}

@@ -1,0 +1,91 @@
+"""Regenerates the golden MSV vectors in tests/golden/ from the reference itself.
+
+Needs oracle/_ref/refgen, built from the reference's own sources by
+``make -C oracle/ref REF=<reference>/code`` (x86-64 only: the reference MSV is
+SSE2 code). For every case it
+
+  1. samples the profile with HMMER's p7_hmm_Sample / p7_Calibrate /
+     p7_ProfileConfig / p7_oprofile_Convert (``refgen profile``),
+  2. builds a sequence set: fixed tiny lengths, lognormal-length background
+     sequences with 0.5% X, sequences over all 29 codes (gap, degenerate,
+     '*' and '~' included), p7_ProfileEmit homologs, and "saturation"
+     sequences (an emitted sequence repeated R times) that drive the uint8
+     score to overflow,
+  3. scores every sequence with the reference's p7_MSVFilter and the
+     p7_Pipeline MSV stage (``refgen score``).
+
+Files per case NAME: NAME.prof (MSVPROF1), NAME.seqs (MSVSEQS1), NAME.res (MSVRES01).
+Run:  python tests/golden/make_golden.py
+"""
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+from cudahmmsearch_gb300 import formats as F  # noqa: E402
+
+REFGEN = os.path.join(ROOT, "oracle", "_ref", "refgen")
+LCFG = 400
+MODE_UNILOCAL = 3
+
+# (name, M, seed, n_lognormal, lognormal lmax, n_homologs, n_saturation, repeat)
+CASES = [
+    ("m1_s1", 1, 1, 40, 400, 6, 2, 20),
+    ("m2_s1", 2, 1, 40, 400, 6, 2, 20),
+    ("m3_s5", 3, 5, 40, 400, 6, 2, 20),
+    ("m16_s1", 16, 1, 40, 600, 6, 2, 20),
+    ("m17_s2", 17, 2, 40, 600, 6, 2, 20),
+    ("m33_s3", 33, 3, 40, 800, 6, 2, 20),
+    ("m50_s1", 50, 1, 60, 1000, 8, 3, 20),
+    ("m200_s1", 200, 1, 120, 5000, 10, 3, 20),      # the M=200, seed 1 profile of the 20,000-sequence workload
+    ("m400_s1", 400, 1, 80, 3000, 8, 3, 20),        # the M=400, seed 1 profile of the 2,000,000-sequence workload
+    ("m777_s3", 777, 3, 40, 2000, 6, 2, 8),
+    ("m1500_s2", 1500, 2, 30, 2000, 6, 2, 5),
+    ("m2400_s1", 2400, 1, 30, 2000, 6, 3, 5),       # the M=2400, seed 1 profile of the length-extremes workload
+]
+
+
+def run(*args):
+    subprocess.check_call([REFGEN] + [str(a) for a in args])
+
+
+def make_case(name, M, seed, n_ln, lmax, n_hom, n_sat, rep):
+    prof = os.path.join(HERE, name + ".prof")
+    seqs = os.path.join(HERE, name + ".seqs")
+    res = os.path.join(HERE, name + ".res")
+    tmp = os.path.join(HERE, "_tmp.seqs")
+    run("profile", M, seed, LCFG, MODE_UNILOCAL, prof)
+    parts = []
+    for j, L in enumerate([1, 2, 3, 4, 10]):
+        parts.append(F.synth_sequences(6, seed=1000 * seed + M + j, median=L, sigma=0.0, lmin=L, lmax=L))
+    parts.append(F.synth_sequences(n_ln, seed=2000 * seed + M, lmax=lmax))
+    rng = np.random.default_rng(3000 * seed + M)
+    allcodes = [rng.integers(0, F.KP_AMINO, size=int(L), dtype=np.uint8) for L in (1, 5, 37, 250)]
+    allx = [np.full(L, F.CODE_X, np.uint8) for L in (1, 40)]
+    parts.append(F.SeqSet.from_list(allcodes + allx))
+    run("emit", M, seed, 100, MODE_UNILOCAL, n_hom, 17 * seed + 1, 1, tmp)
+    parts.append(F.read_seqs(tmp))
+    run("emit", M, seed, 20, MODE_UNILOCAL, n_sat, 19 * seed + 2, rep, tmp)
+    parts.append(F.read_seqs(tmp))
+    os.remove(tmp)
+    s = F.SeqSet.concat(parts)
+    F.write_seqs(s, seqs)
+    run("score", M, seed, LCFG, MODE_UNILOCAL, seqs, res)
+    r = F.read_results(res)
+    print(f"{name}: M={M} n={s.n} residues={s.total} erange={(r.status == 16).sum()} "
+          f"pass={int(r.passed.sum())}")
+
+
+def main():
+    if not os.path.exists(REFGEN):
+        sys.exit("oracle/_ref/refgen missing: make -C oracle/ref REF=<reference>/code")
+    for c in CASES:
+        make_case(*c)
+
+
+if __name__ == "__main__":
+    main()
