@@ -1,0 +1,273 @@
+"""Benchmark: MSV GCUPS on one GB300 (HMMER3 hmmsearch stage 1).
+
+Default workload (N=1): one sampled profile of M=400 (HMMER p7_hmm_Sample,
+seed 1, reference-generated: tests/golden/m400_s1.prof) against 2,000,000
+synthetic protein sequences (lognormal lengths, median 300, sigma 0.7,
+clipped to [10, 35000], 0.5% X, 2% homologs of the profile) -- the
+"one query at throughput scale" configuration. A step is one full search of
+the database by the profile. GCUPS = M * residues / seconds.
+
+  value : device-timed (CUDA events on the launching stream), database and
+          profile resident in HBM, outputs left on the device.
+  e2e   : the same search through the public API from host buffers, every
+          step: pinned host sequences -> device (packing included), search,
+          per-sequence results back to the host (host wall clock).
+  --impl reference : the reference's MSV algorithm on the host cores (the
+          oracle port; the reference's SSE2 code cannot run on aarch64).
+
+The database (~770 MB) is larger than L2 (129 MB), so no flush is needed.
+For N>1 (torchrun), every rank searches its own database (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from cudahmmsearch_gb300 import formats as F  # noqa: E402
+
+INT_LANE_OPS_PER_CLK_PER_SM = 128   # 4 SMSPs x 32 lanes: measured, see profiles/int_pipe_peak_opbench.md
+
+
+def workload(name, rank=0):
+    if name == "m400_2M":
+        p = F.read_profile(os.path.join(ROOT, "tests", "golden", "m400_s1.prof"))
+        n_total, n_hom = 2_000_000, 40_000
+        bg = F.synth_sequences(n_total - n_hom, seed=1000 + rank, lmax=35000)
+        hom = F.emit_homologs(p, n_hom, seed=2000 + rank, lmax=35000)
+        s = F.SeqSet.concat([bg, hom])
+        cfg = {"workload": "plain MSV, 1 profile M=400 (p7_hmm_Sample seed 1) vs 2,000,000 seqs "
+                           "(lognormal median 300 sigma 0.7 clipped [10,35000], 0.5% X, 2% homologs)",
+               "M": p.M, "n_seqs": s.n, "residues": s.total, "l2_flush": "inputs larger than L2 (129 MB)"}
+        return p, s, cfg
+    if name == "m400_400k":   # smaller case of the same distribution (profiling: > L2, few GB)
+        p = F.read_profile(os.path.join(ROOT, "tests", "golden", "m400_s1.prof"))
+        s = F.SeqSet.concat([F.synth_sequences(392_000, seed=1000 + rank, lmax=35000),
+                             F.emit_homologs(p, 8_000, seed=2000 + rank, lmax=35000)])
+        cfg = {"workload": "plain MSV, M=400 vs 400,000 seqs (same distribution as m400_2M)",
+               "M": p.M, "n_seqs": s.n, "residues": s.total, "l2_flush": "inputs larger than L2 (129 MB)"}
+        return p, s, cfg
+    if name == "m200_20k":
+        p = F.read_profile(os.path.join(ROOT, "tests", "golden", "m200_s1.prof"))
+        s = F.SeqSet.concat([F.synth_sequences(19800, seed=11 + rank, lmax=5000), F.emit_homologs(p, 200, seed=12)])
+        cfg = {"workload": "plain MSV, 1 profile M=200 vs 20,000 seqs (lognormal clipped [10,5000], 1% homologs)",
+               "M": p.M, "n_seqs": s.n, "residues": s.total, "l2_flush": "none (inputs fit in L2)"}
+        return p, s, cfg
+    raise SystemExit(f"unknown workload {name}")
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.rows = []
+        if self.proc is None:
+            return
+        time.sleep(0.25)
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                self.rows.append(f)
+
+    def summary(self):
+        rows = getattr(self, "rows", [])
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_baseline(p, s, budget_s=12.0, nthreads=0):
+    """The oracle port of the reference's p7_MSVFilter (SSV + MSV) on all host
+    cores, on a bounded random sample of the workload's sequences."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(7)
+    cores = os.cpu_count() if nthreads <= 0 else nthreads
+    # calibrate on a small sample, then size the timed sample to ~budget_s
+    idx = rng.choice(s.n, size=min(s.n, 2000), replace=False)
+    sub = s.subset(np.sort(idx))
+    t0 = time.perf_counter()
+    O.msv_batch(p, sub, nthreads=cores)
+    rate = sub.total * p.M / max(1e-6, time.perf_counter() - t0)
+    want = int(min(s.n, max(2000, budget_s * rate / (p.M * max(1.0, s.total / s.n)))))
+    idx = rng.choice(s.n, size=want, replace=False)
+    sub = s.subset(np.sort(idx))
+    t0 = time.perf_counter()
+    O.msv_batch(p, sub, nthreads=cores)
+    dt = time.perf_counter() - t0
+    return {"value": sub.total * p.M / dt / 1e9, "unit": "GCUPS", "cores": cores, "kind": "port",
+            "sample": f"{sub.n} random sequences of the workload ({sub.total} residues, M={p.M}), {dt:.1f} s",
+            "seconds": dt}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    p, s, cfg = workload(args.workload)
+    vals = []
+    for i in range(args.warmup + args.steps):
+        cb = cpu_baseline(p, s, budget_s=max(2.0, 60.0 / (args.steps + args.warmup)))
+        if i >= args.warmup:
+            vals.append(cb["value"])
+    v = float(np.mean(vals))
+    cb["value"] = v
+    line = {"metric": "MSV GCUPS", "value": v, "unit": "GCUPS", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u8", "data": "synthetic", "config": cfg, "impl": "reference",
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="m400_2M")
+    ap.add_argument("--variant", type=int, default=None, help="SSV arithmetic: 0 int8 table, 1 f16 table")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import torch.distributed as dist
+    from cudahmmsearch_gb300 import api
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+
+    p, s, cfg = workload(args.workload, rank)
+    cells = float(p.M) * float(s.total)
+    ctx = api.Context(local)
+    # A dedicated (non-default) stream: its handle is non-NULL, so the library
+    # launches on it and the CUDA events below time exactly those launches.
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    prof = api.DeviceProfile(ctx, p, args.variant)
+    db = api.DeviceDB(ctx, s)
+    out = torch.empty(2 * s.n, dtype=torch.uint8, device="cuda")
+    d_xj, d_fl = out.data_ptr(), out.data_ptr() + s.n
+
+    def step():
+        api.search_device(ctx, prof, db, d_xj, d_fl)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    launches0 = api.kernel_launches()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for i in range(args.steps):
+            ev[i][0].record(stream)
+            step()
+            ev[i][1].record(stream)
+        t1.record(stream)
+        torch.cuda.synchronize()
+    launches = api.kernel_launches() - launches0
+    if world > 1:
+        dist.barrier()
+    total_ms = t0.elapsed_time(t1)
+    per = [a.elapsed_time(b) for a, b in ev]
+    t_max = torch.tensor([total_ms], device="cuda")
+    if world > 1:
+        dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
+    total_ms = float(t_max.item())
+    value = cells * world * args.steps / (total_ms * 1e-3) / 1e9
+
+    # correctness spot-check of the timed outputs against the oracle (outside the timed region)
+    xj_all = out[:s.n].cpu().numpy()
+    fl_all = out[s.n:].cpu().numpy()
+
+    # e2e through the public API from pinned host buffers
+    codes_pin = torch.from_numpy(s.codes).pin_memory()
+    off_np = s.off
+    e2e_times = []
+    for i in range(args.e2e_steps + 1 if args.e2e_steps > 0 else 0):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        seqset = F.SeqSet(codes_pin.numpy(), off_np)
+        db2 = api.DeviceDB(ctx, seqset)
+        xj, fl = api.search(ctx, prof, db2)
+        db2.close()
+        dt = time.perf_counter() - t
+        if i > 0:
+            e2e_times.append(dt)
+    if e2e_times:
+        assert np.array_equal(xj, xj_all) and np.array_equal(fl, fl_all)
+    e2e_val = cells / float(np.mean(e2e_times)) / 1e9 if e2e_times else None
+
+    clocks = clk.summary()
+    sm_mhz = clocks["sm_mhz"] or 2070.0
+    nsm = torch.cuda.get_device_properties(local).multi_processor_count
+    peak_tops = nsm * INT_LANE_OPS_PER_CLK_PER_SM * sm_mhz * 1e6 / 1e12
+    kern_ms = float(np.mean(per))
+    achieved_tops = cells / (kern_ms * 1e-3) / 1e12          # 1 cell = 1 packed int32 op (4 uint8 lane-ops)
+    roofline = {"bound": "int32-pipe", "achieved": achieved_tops, "peak": peak_tops, "unit": "Tops/s",
+                "frac": achieved_tops / peak_tops, "traffic": None,
+                "peak_note": f"{nsm} SMs x {INT_LANE_OPS_PER_CLK_PER_SM} int32 lane-ops/clk x median SM clock {sm_mhz:.0f} MHz (measured)",
+                "hbm": {"achieved": (s.total + 2 * s.n) / (kern_ms * 1e-3) / 1e9, "peak": 6783.5,
+                        "unit": "GB/s", "frac": (s.total + 2 * s.n) / (kern_ms * 1e-3) / 1e9 / 6783.5,
+                        "peak_note": "of measured (MEASURED_PEAKS.json hbm_gbs)"}}
+    fullfrac = float(((fl_all & api.FLAG_FULL) != 0).mean())
+    line = {"metric": "MSV GCUPS", "value": value, "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            "config": dict(cfg, variant=prof.variant, full_msv_fraction=fullfrac,
+                           pass_fraction=float(((fl_all & api.FLAG_PASS) != 0).mean())),
+            "e2e": {"value": e2e_val, "unit": "GCUPS", "h2d_bytes_per_step": int(s.total + 8 * (s.n + 1)),
+                    "d2h_bytes_per_step": int(2 * s.n), "path": "msvgb_db_create + msvgb_search from pinned host memory"},
+            "gpu_launches": int(launches), "clocks": clocks, "roofline": roofline}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(p, s)
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,228 @@
+"""Python mirror of the reference's MSV interface over the C ABI (include/msvgb.h).
+
+The names follow HMMER's: ``MSVFilter(dsq, L, om, ox)`` is p7_MSVFilter
+(src/impl_sse/msvfilter.c:78) and ``pipeline_msv_stage`` is the MSV stage of
+p7_Pipeline (src/p7_pipeline.c:662-677). Everything runs through
+libmsvgb.so; importing this module on a machine without it, or creating a
+Context without a CUDA device, raises instead of falling back to the CPU.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import formats as F
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmsvgb.so")
+
+eslOK, eslEMEM, eslEINVAL, eslESYS, eslERANGE = 0, 5, 11, 12, 16
+FLAG_ERANGE, FLAG_PASS, FLAG_FULL, FLAG_EMPTY = 0x01, 0x02, 0x04, 0x08
+
+# Every function declared in include/msvgb.h.
+EXPORTS = [
+    "msvgb_ctx_create", "msvgb_ctx_destroy", "msvgb_ctx_set_stream", "msvgb_last_error",
+    "msvgb_kernel_launches", "msvgb_MSVFilter", "msvgb_profile_create", "msvgb_profile_destroy",
+    "msvgb_profile_M", "msvgb_profile_create_ex", "msvgb_profile_variant", "msvgb_db_create", "msvgb_db_destroy", "msvgb_db_nseq", "msvgb_db_residues",
+    "msvgb_search", "msvgb_search_device", "msvgb_tjb_b", "msvgb_score", "msvgb_f1_pass",
+]
+
+
+class MSVError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"status {code}: {msg}")
+        self.code = code
+
+
+class _Om(ctypes.Structure):
+    _fields_ = [("M", ctypes.c_int), ("Kp", ctypes.c_int), ("rbv", ctypes.c_void_p),
+                ("tbm_b", ctypes.c_uint8), ("tec_b", ctypes.c_uint8), ("tjb_b", ctypes.c_uint8),
+                ("base_b", ctypes.c_uint8), ("bias_b", ctypes.c_uint8),
+                ("scale_b", ctypes.c_float), ("mmu", ctypes.c_float), ("mlambda", ctypes.c_float)]
+
+
+class _Omx(ctypes.Structure):
+    _fields_ = [("allocQ16", ctypes.c_int), ("M", ctypes.c_int)]
+
+
+_lib = None
+
+
+def lib():
+    """Loads libmsvgb.so (built by cudahmmsearch_gb300/build.py or __graft_entry__.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, i32, i64, u8, f32, f64 = (ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_uint8,
+                                  ctypes.c_float, ctypes.c_double)
+    sig = {
+        "msvgb_ctx_create": (i32, [i32, ctypes.POINTER(vp)]),
+        "msvgb_ctx_destroy": (i32, [vp]),
+        "msvgb_ctx_set_stream": (i32, [vp, vp]),
+        "msvgb_last_error": (ctypes.c_char_p, []),
+        "msvgb_kernel_launches": (ctypes.c_uint64, []),
+        "msvgb_MSVFilter": (i32, [vp, vp, i32, ctypes.POINTER(_Om), ctypes.POINTER(_Omx), ctypes.POINTER(f32)]),
+        "msvgb_profile_create": (i32, [vp, ctypes.POINTER(_Om), ctypes.POINTER(vp)]),
+        "msvgb_profile_create_ex": (i32, [vp, ctypes.POINTER(_Om), i32, ctypes.POINTER(vp)]),
+        "msvgb_profile_variant": (i32, [vp]),
+        "msvgb_profile_destroy": (i32, [vp]),
+        "msvgb_profile_M": (i32, [vp]),
+        "msvgb_db_create": (i32, [vp, vp, vp, i64, ctypes.POINTER(vp)]),
+        "msvgb_db_destroy": (i32, [vp]),
+        "msvgb_db_nseq": (i64, [vp]),
+        "msvgb_db_residues": (i64, [vp]),
+        "msvgb_search": (i32, [vp, vp, vp, f64, vp, vp]),
+        "msvgb_search_device": (i32, [vp, vp, vp, f64, vp, vp]),
+        "msvgb_tjb_b": (u8, [f32, i32]),
+        "msvgb_score": (f32, [u8, u8, i32, u8, f32]),
+        "msvgb_f1_pass": (i32, [f32, i32, f32, f32, f64, ctypes.POINTER(f64)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype, fn.argtypes = res, args
+    _lib = L
+    return L
+
+
+def _check(code):
+    if code != eslOK:
+        raise MSVError(code, lib().msvgb_last_error().decode())
+    return code
+
+
+def kernel_launches() -> int:
+    return int(lib().msvgb_kernel_launches())
+
+
+def _om_struct(p: F.Profile, tjb_b: int = 0):
+    rbv = np.ascontiguousarray(p.rbv, dtype=np.uint8)
+    om = _Om(p.M, p.Kp, rbv.ctypes.data, p.tbm_b, p.tec_b, tjb_b, p.base_b, p.bias_b,
+             p.scale_b, p.mmu, p.mlambda)
+    return om, rbv
+
+
+class Context:
+    """One GPU and one CUDA stream (msvgb_ctx)."""
+
+    def __init__(self, device: int = 0):
+        h = ctypes.c_void_p()
+        _check(lib().msvgb_ctx_create(device, ctypes.byref(h)))
+        self.h = h
+
+    def set_stream(self, stream_handle: int | None):
+        _check(lib().msvgb_ctx_set_stream(self.h, ctypes.c_void_p(stream_handle or 0)))
+
+    def close(self):
+        if self.h:
+            lib().msvgb_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- p7_MSVFilter drop-in --------------------------------------------------
+    def MSVFilter(self, dsq: np.ndarray, L: int, om: F.Profile, tjb_b: int, allocQ16: int | None = None):
+        """p7_MSVFilter(dsq, L, om, ox, &sc): dsq holds sentinels at 0 and L+1.
+        Returns (status, sc). status is eslOK or eslERANGE; raises on eslEINVAL."""
+        dsq = np.ascontiguousarray(dsq, dtype=np.uint8)
+        o, keep = _om_struct(om, tjb_b)
+        ox = _Omx(om.Q if allocQ16 is None else allocQ16, 0)
+        sc = ctypes.c_float()
+        st = lib().msvgb_MSVFilter(self.h, dsq.ctypes.data, L, ctypes.byref(o), ctypes.byref(ox), ctypes.byref(sc))
+        if st not in (eslOK, eslERANGE):
+            raise MSVError(st, lib().msvgb_last_error().decode())
+        return st, float(sc.value)
+
+
+class DeviceProfile:
+    """A profile resident in HBM (msvgb_profile)."""
+
+    def __init__(self, ctx: Context, p: F.Profile, variant: int | None = None):
+        o, keep = _om_struct(p)
+        h = ctypes.c_void_p()
+        if variant is None:
+            _check(lib().msvgb_profile_create(ctx.h, ctypes.byref(o), ctypes.byref(h)))
+        else:
+            _check(lib().msvgb_profile_create_ex(ctx.h, ctypes.byref(o), variant, ctypes.byref(h)))
+        self.h, self.ctx, self.profile = h, ctx, p
+        self.variant = int(lib().msvgb_profile_variant(h))
+
+    def close(self):
+        if self.h:
+            lib().msvgb_profile_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class DeviceDB:
+    """A packed, length-sorted sequence database resident in HBM (msvgb_db)."""
+
+    def __init__(self, ctx: Context, seqs: F.SeqSet):
+        codes = np.ascontiguousarray(seqs.codes, dtype=np.uint8)
+        if codes.size == 0:
+            codes = np.zeros(1, np.uint8)
+        off = np.ascontiguousarray(seqs.off, dtype=np.int64)
+        h = ctypes.c_void_p()
+        _check(lib().msvgb_db_create(ctx.h, codes.ctypes.data, off.ctypes.data, seqs.n, ctypes.byref(h)))
+        self.h, self.ctx, self.n, self.lengths = h, ctx, seqs.n, seqs.lengths.copy()
+        self.residues = int(seqs.total)
+
+    def close(self):
+        if self.h:
+            lib().msvgb_db_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def search(ctx: Context, prof: DeviceProfile, db: DeviceDB, F1: float = 0.02):
+    """Plain path: one profile, one launch. Returns (xj uint8[n], flags uint8[n])."""
+    xj = np.zeros(db.n, np.uint8)
+    fl = np.zeros(db.n, np.uint8)
+    _check(lib().msvgb_search(ctx.h, prof.h, db.h, F1, xj.ctypes.data, fl.ctypes.data))
+    return xj, fl
+
+
+def search_device(ctx: Context, prof: DeviceProfile, db: DeviceDB, d_xj: int, d_flags: int, F1: float = 0.02):
+    """Asynchronous search writing to device pointers (on the context's stream)."""
+    _check(lib().msvgb_search_device(ctx.h, prof.h, db.h, F1, ctypes.c_void_p(d_xj), ctypes.c_void_p(d_flags)))
+
+
+def tjb_b(scale_b: float, L: int) -> int:
+    return int(lib().msvgb_tjb_b(scale_b, L))
+
+
+def scores(p: F.Profile, lengths: np.ndarray, xj: np.ndarray, flags: np.ndarray) -> np.ndarray:
+    """Float MSV scores (nats) from xJ, as p7_MSVFilter writes them (msvfilter.c:205-210)."""
+    out = np.empty(len(xj), np.float32)
+    f = lib().msvgb_score
+    for i in range(len(xj)):
+        out[i] = f(int(xj[i]), int(flags[i]), int(lengths[i]), p.base_b, p.scale_b)
+    return out
+
+
+def pipeline_msv_stage(ctx: Context, prof: DeviceProfile, db: DeviceDB, F1: float = 0.02):
+    """MSV stage of p7_Pipeline over a whole database (p7_pipeline.c:662-677):
+    returns (passed indices, their float scores usc, xj, flags). Sequences of
+    length 0 are skipped as the reference does."""
+    xj, fl = search(ctx, prof, db, F1)
+    idx = np.nonzero(fl & FLAG_PASS)[0]
+    usc = scores(prof.profile, db.lengths[idx], xj[idx], fl[idx])
+    return idx, usc, xj, fl

@@ -1,0 +1,558 @@
+// msv_api.cu -- host side of the C ABI in include/msvgb.h.
+//
+// Owns the device-resident profile layout (the GB300 replacement of the fork's
+// loadOM, code/src/GPUFunction.cu:260-294), the packed length-sorted database
+// (replacing loadDBQuad/loadCUDA, GPUFunction.cu:219-255, 332-415, and the
+// offline dbsort.c/hmmsort.cpp length sort), the per-length tables that keep
+// every floating-point expression on the host, and the launches.
+//
+// Host floating point must round exactly like the reference's x86 build, so
+// this file is compiled with -ffp-contract=off (no fused multiply-add).
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "../../include/msvgb.h"
+#include "msv_device.cuh"
+#include "msv_kernel_impl.cuh"
+
+using namespace msvgb;
+
+namespace msvgb {
+template <int C, bool F16> cudaError_t launch_search(const LaunchArgs &a, int num_sms);
+}
+
+// ------------------------------------------------------------------------------
+// errors
+static thread_local std::string g_err;
+static std::atomic<uint64_t> g_launches{0};
+
+static int fail(int code, const std::string &msg) { g_err = msg; return code; }
+#define CUDA_TRY(expr)                                                                       \
+  do {                                                                                       \
+    cudaError_t _e = (expr);                                                                 \
+    if (_e != cudaSuccess)                                                                   \
+      return fail(MSVGB_eslESYS, std::string(#expr) + ": " + cudaGetErrorString(_e));         \
+  } while (0)
+
+extern "C" const char *msvgb_last_error(void) { return g_err.c_str(); }
+extern "C" uint64_t msvgb_kernel_launches(void) { return g_launches.load(); }
+
+// ------------------------------------------------------------------------------
+// exact host arithmetic of the reference
+
+// unbiased_byteify(logf(3/(L+3))): src/impl_sse/p7_oprofile.c:511-519, 920-925
+extern "C" uint8_t msvgb_tjb_b(float scale_b, int L) {
+  float sc = logf(3.0f / (float) (L + 3));
+  sc = -1.0f * roundf(scale_b * sc);
+  return (sc > 255.) ? 255 : (uint8_t) sc;
+}
+
+// msvfilter.c:205-210
+static float score_from_xj(int xj, int tjb, int base, float scale) {
+  float sc = ((float) (xj - tjb) - (float) base);
+  sc /= scale;
+  sc -= 3.0;
+  return sc;
+}
+
+extern "C" float msvgb_score(uint8_t xj, uint8_t flags, int L, uint8_t base_b, float scale_b) {
+  if (flags & MSVGB_FLAG_ERANGE) return INFINITY;
+  return score_from_xj(xj, msvgb_tjb_b(scale_b, L), base_b, scale_b);
+}
+
+// p7_bg_SetLength/p7_bg_NullOne (src/p7_bg.c:191-199, 359-363), seq_score and
+// the F1 test of p7_Pipeline (src/p7_pipeline.c:673-676), esl_gumbel_surv
+// (easel/esl_gumbel.c:129-137).
+extern "C" int msvgb_f1_pass(float usc, int L, float mmu, float mlambda, double F1, double *ret_P) {
+  // C semantics: log() of a float argument is computed in double (C++'s
+  // float overload of log would round differently).
+  float p1 = (float) L / (float) (L + 1);
+  float nullsc = (float) ((double) (float) L * ::log((double) p1) + ::log(1. - (double) p1));
+  float seq_score = (usc - nullsc) / 0.69314718055994529;
+  double y = (double) mlambda * ((double) seq_score - (double) mmu);
+  double ey = -exp(-y);
+  double P = (fabs(ey) < 5e-9) ? -ey : 1 - exp(ey);
+  if (ret_P) *ret_P = P;
+  return (P > F1) ? 0 : 1;
+}
+
+// ------------------------------------------------------------------------------
+// objects
+
+struct msvgb_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t own = nullptr;
+  cudaStream_t stream = nullptr;
+  unsigned long long *d_ticket = nullptr;
+  std::mutex mu;                                        // serialises the single-call path
+  std::unordered_map<uint64_t, msvgb_profile *> cache;  // single-call profile cache
+  // single-call scratch
+  uint8_t *d_seq = nullptr; size_t d_seq_cap = 0;
+  uint8_t *d_tab = nullptr; size_t d_tab_cap = 0;
+  int64_t *d_meta = nullptr;                            // start, orig (int64), len (int32) for n=1
+  uint8_t *d_out = nullptr;
+};
+
+struct LenTables {      // per (profile, database, F1)
+  const msvgb_db *db = nullptr;
+  double F1 = -1.0;
+  uint8_t *d_tjb = nullptr;
+  uint8_t *d_xjmin = nullptr;
+};
+
+struct msvgb_profile {
+  msvgb_ctx *ctx = nullptr;
+  int M = 0, C = 0, f16 = 0;
+  uint8_t tbm = 0, tec = 0, base = 0, bias = 0;
+  float scale = 0.f, mmu = 0.f, mlambda = 0.f;
+  uint32_t *d_stab = nullptr, *d_mtab = nullptr;
+  std::vector<LenTables> tables;
+};
+
+struct msvgb_db {
+  msvgb_ctx *ctx = nullptr;
+  int64_t n = 0, residues = 0;
+  int Lmax = 0;
+  uint8_t *d_codes = nullptr;
+  int64_t *d_start = nullptr, *d_orig = nullptr;
+  int32_t *d_len = nullptr;
+  std::vector<int32_t> distinct_len;  // sorted ascending
+  uint64_t serial = 0;
+};
+
+static std::atomic<uint64_t> g_db_serial{1};
+
+// Supported DP widths (words per lane); the warp spans 64*C model nodes.
+static const int kC[] = {2, 4, 6, 8, 10, 12, 14, 16, 20, 24, 28, 32, 40, 48};
+static const int kMaxC = 48;
+static const int kMaxF16C = 32;
+
+static int choose_C(int M) {
+  int need = (M + 63) / 64;
+  for (int c : kC) if (c >= need) return c;
+  return -1;
+}
+
+static cudaError_t dispatch(int C, bool f16, const LaunchArgs &a, int sms) {
+#define CASE_I8(c)  case c: return launch_search<c, false>(a, sms);
+#define CASE_F16(c) case c: return launch_search<c, true>(a, sms);
+  if (f16) {
+    switch (C) { CASE_F16(2) CASE_F16(4) CASE_F16(6) CASE_F16(8) CASE_F16(10) CASE_F16(12)
+                 CASE_F16(14) CASE_F16(16) CASE_F16(20) CASE_F16(24) CASE_F16(28) CASE_F16(32) }
+  } else {
+    switch (C) { CASE_I8(2) CASE_I8(4) CASE_I8(6) CASE_I8(8) CASE_I8(10) CASE_I8(12) CASE_I8(14)
+                 CASE_I8(16) CASE_I8(20) CASE_I8(24) CASE_I8(28) CASE_I8(32) CASE_I8(40) CASE_I8(48) }
+  }
+  return cudaErrorInvalidValue;
+#undef CASE_I8
+#undef CASE_F16
+}
+
+// ------------------------------------------------------------------------------
+// context
+
+extern "C" int msvgb_ctx_create(int device, msvgb_ctx **ret_ctx) {
+  if (!ret_ctx) return fail(MSVGB_eslEINVAL, "ret_ctx is NULL");
+  *ret_ctx = nullptr;
+  int ndev = 0;
+  CUDA_TRY(cudaGetDeviceCount(&ndev));
+  if (device < 0 || device >= ndev) return fail(MSVGB_eslEINVAL, "no such CUDA device");
+  CUDA_TRY(cudaSetDevice(device));
+  msvgb_ctx *c = new msvgb_ctx();
+  c->device = device;
+  cudaError_t e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_ticket, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_meta, 4 * sizeof(int64_t));
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_out, 64);
+  if (e != cudaSuccess) {
+    msvgb_ctx_destroy(c);
+    return fail(MSVGB_eslESYS, std::string("context setup: ") + cudaGetErrorString(e));
+  }
+  c->stream = c->own;
+  *ret_ctx = c;
+  return MSVGB_eslOK;
+}
+
+extern "C" int msvgb_ctx_destroy(msvgb_ctx *c) {
+  if (!c) return MSVGB_eslOK;
+  cudaSetDevice(c->device);
+  for (auto &kv : c->cache) msvgb_profile_destroy(kv.second);
+  c->cache.clear();
+  if (c->own) cudaStreamSynchronize(c->own);
+  cudaFree(c->d_ticket); cudaFree(c->d_meta); cudaFree(c->d_out);
+  cudaFree(c->d_seq); cudaFree(c->d_tab);
+  if (c->own) cudaStreamDestroy(c->own);
+  delete c;
+  return MSVGB_eslOK;
+}
+
+extern "C" int msvgb_ctx_set_stream(msvgb_ctx *c, void *stream) {
+  if (!c) return fail(MSVGB_eslEINVAL, "ctx is NULL");
+  c->stream = stream ? (cudaStream_t) stream : c->own;
+  return MSVGB_eslOK;
+}
+
+// ------------------------------------------------------------------------------
+// profile: host re-layout of the striped rbv into the kernels' lane layout
+
+static inline int rbv_at(const msvgb_om *om, int Q, int x, int k) {   // k = 1..M
+  const int q = (k - 1) % Q, z = (k - 1) / Q;
+  return om->rbv[((size_t) x * Q + q) * 16 + z];
+}
+
+// node held by DP word w, half h of lane l (1-based)
+static inline int node_of(int C, int lane, int w, int h) { return lane * 2 * C + h * C + w + 1; }
+
+static int profile_build(msvgb_ctx *ctx, const msvgb_om *om, int want_f16, msvgb_profile **ret) {
+  if (!om || !ret) return fail(MSVGB_eslEINVAL, "NULL argument");
+  if (om->M < 1) return fail(MSVGB_eslEINVAL, "profile M must be >= 1");
+  if (om->Kp != 29) return fail(MSVGB_eslEINVAL, "only the amino alphabet (Kp = 29) is supported");
+  if (!om->rbv) return fail(MSVGB_eslEINVAL, "rbv is NULL");
+  const int C = choose_C(om->M);
+  if (C < 0) return fail(MSVGB_eslEINVAL, "profile M exceeds the supported maximum (3072 nodes)");
+  const int M = om->M, Q = std::max(2, (M - 1) / 16 + 1), bias = om->bias_b;
+  const bool f16 = want_f16 && C <= kMaxF16C;
+
+  // SSV costs s = bias - rbv clamped to [-128, 127]; nodes past M and the pad
+  // residue get -128, which floors every cell (u < 128) like the reference's
+  // padding cost 255 / sbv 127 does.
+  auto s_of = [&](int x, int k) -> int {
+    if (x >= 29 || k > M) return -128;
+    int s = bias - rbv_at(om, Q, x, k);
+    return std::min(127, std::max(-128, s));
+  };
+  auto n_of = [&](int x, int k) -> int {   // MSV: 255 - rbv; padding rbv = 255 -> 0
+    if (x >= 29 || k > M) return 0;
+    return 255 - rbv_at(om, Q, x, k);
+  };
+  const size_t mwords = (size_t) NRES * (C / 2) * 32;
+  const size_t swords = f16 ? (size_t) NRES * C * 32 : mwords;
+  std::vector<uint32_t> st(swords), mt(mwords);
+  for (int x = 0; x < NRES; ++x)
+    for (int l = 0; l < 32; ++l) {
+      for (int p = 0; p < C / 2; ++p) {
+        const int k0 = node_of(C, l, 2 * p, 0), k1 = node_of(C, l, 2 * p + 1, 0);
+        const int k2 = node_of(C, l, 2 * p, 1), k3 = node_of(C, l, 2 * p + 1, 1);
+        const size_t i = ((size_t) x * (C / 2) + p) * 32 + l;
+        mt[i] = (uint32_t) n_of(x, k0) | ((uint32_t) n_of(x, k1) << 8) |
+                ((uint32_t) n_of(x, k2) << 16) | ((uint32_t) n_of(x, k3) << 24);
+        if (!f16)
+          st[i] = (uint32_t) (uint8_t) s_of(x, k0) | ((uint32_t) (uint8_t) s_of(x, k1) << 8) |
+                  ((uint32_t) (uint8_t) s_of(x, k2) << 16) | ((uint32_t) (uint8_t) s_of(x, k3) << 24);
+      }
+      if (f16)
+        for (int w = 0; w < C; ++w) {
+          const __half lo = __float2half((float) s_of(x, node_of(C, l, w, 0)));
+          const __half hi = __float2half((float) s_of(x, node_of(C, l, w, 1)));
+          uint16_t blo, bhi;
+          memcpy(&blo, &lo, 2); memcpy(&bhi, &hi, 2);
+          st[((size_t) x * C + w) * 32 + l] = (uint32_t) blo | ((uint32_t) bhi << 16);
+        }
+    }
+
+  msvgb_profile *p = new msvgb_profile();
+  p->ctx = ctx; p->M = M; p->C = C; p->f16 = f16 ? 1 : 0;
+  p->tbm = om->tbm_b; p->tec = om->tec_b; p->base = om->base_b; p->bias = om->bias_b;
+  p->scale = om->scale_b; p->mmu = om->mmu; p->mlambda = om->mlambda;
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e == cudaSuccess) e = cudaMalloc(&p->d_stab, swords * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&p->d_mtab, mwords * 4);
+  if (e == cudaSuccess) e = cudaMemcpy(p->d_stab, st.data(), swords * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(p->d_mtab, mt.data(), mwords * 4, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    msvgb_profile_destroy(p);
+    return fail(e == cudaErrorMemoryAllocation ? MSVGB_eslEMEM : MSVGB_eslESYS,
+                std::string("profile upload: ") + cudaGetErrorString(e));
+  }
+  *ret = p;
+  return MSVGB_eslOK;
+}
+
+static int default_f16() { return 0; }
+
+extern "C" int msvgb_profile_create(msvgb_ctx *ctx, const msvgb_om *om, msvgb_profile **ret) {
+  if (!ctx) return fail(MSVGB_eslEINVAL, "ctx is NULL");
+  if (ret) *ret = nullptr;
+  return profile_build(ctx, om, default_f16(), ret);
+}
+
+extern "C" int msvgb_profile_create_ex(msvgb_ctx *ctx, const msvgb_om *om, int variant, msvgb_profile **ret) {
+  if (!ctx) return fail(MSVGB_eslEINVAL, "ctx is NULL");
+  if (variant != 0 && variant != 1) return fail(MSVGB_eslEINVAL, "ssv_variant must be 0 or 1");
+  if (ret) *ret = nullptr;
+  return profile_build(ctx, om, variant, ret);
+}
+
+extern "C" int msvgb_profile_variant(const msvgb_profile *p) { return p ? p->f16 : -1; }
+
+extern "C" int msvgb_profile_destroy(msvgb_profile *p) {
+  if (!p) return MSVGB_eslOK;
+  cudaSetDevice(p->ctx->device);
+  for (auto &t : p->tables) { cudaFree(t.d_tjb); cudaFree(t.d_xjmin); }
+  cudaFree(p->d_stab); cudaFree(p->d_mtab);
+  delete p;
+  return MSVGB_eslOK;
+}
+
+extern "C" int msvgb_profile_M(const msvgb_profile *p) { return p ? p->M : -1; }
+
+// ------------------------------------------------------------------------------
+// per-length tables: tjb_b(L) and the smallest xJ that passes F1 at length L
+
+static int xjmin_for(const msvgb_profile *p, int L, double F1) {
+  const int tjb = msvgb_tjb_b(p->scale, L);
+  auto pass = [&](int xj) {
+    return msvgb_f1_pass(score_from_xj(xj, tjb, p->base, p->scale), L, p->mmu, p->mlambda, F1, nullptr) != 0;
+  };
+  // P is non-increasing in xJ; binary search, then confirm the boundary.
+  int lo = 0, hi = 255;                  // answer in [lo, hi]; 255 = no xJ < 255 passes
+  while (lo < hi) {
+    const int mid = (lo + hi) / 2;
+    if (pass(mid)) hi = mid; else lo = mid + 1;
+  }
+  if (lo < 255 && !pass(lo)) return -1;
+  if (lo > 0 && pass(lo - 1)) return -1;
+  return lo;
+}
+
+static int ensure_tables(msvgb_profile *p, const msvgb_db *db, double F1, LenTables **out) {
+  for (auto &t : p->tables)
+    if (t.db == db && t.F1 == F1) { *out = &t; return MSVGB_eslOK; }
+  const int Lmax = db->Lmax;
+  std::vector<uint8_t> tjb(Lmax + 1), xjm(Lmax + 1, 255);
+  for (int L = 0; L <= Lmax; ++L) tjb[L] = msvgb_tjb_b(p->scale, L);
+  for (int L : db->distinct_len) {
+    if (L == 0) continue;
+    const int v = xjmin_for(p, L, F1);
+    if (v < 0) return fail(MSVGB_eslESYS, "F1 pass set is not monotone in xJ");
+    xjm[L] = (uint8_t) v;
+  }
+  LenTables t; t.db = db; t.F1 = F1;
+  cudaError_t e = cudaMalloc(&t.d_tjb, Lmax + 1);
+  if (e == cudaSuccess) e = cudaMalloc(&t.d_xjmin, Lmax + 1);
+  if (e == cudaSuccess) e = cudaMemcpy(t.d_tjb, tjb.data(), Lmax + 1, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(t.d_xjmin, xjm.data(), Lmax + 1, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(t.d_tjb); cudaFree(t.d_xjmin);
+    return fail(MSVGB_eslESYS, std::string("length tables: ") + cudaGetErrorString(e));
+  }
+  if (p->tables.size() >= 8) {           // bounded cache
+    cudaFree(p->tables.front().d_tjb); cudaFree(p->tables.front().d_xjmin);
+    p->tables.erase(p->tables.begin());
+  }
+  p->tables.push_back(t);
+  *out = &p->tables.back();
+  return MSVGB_eslOK;
+}
+
+// ------------------------------------------------------------------------------
+// database: sort by length (longest first), pad each sequence to 16 bytes
+
+extern "C" int msvgb_db_create(msvgb_ctx *ctx, const uint8_t *codes, const int64_t *off, int64_t n,
+                               msvgb_db **ret) {
+  if (!ctx || !ret || (n > 0 && (!off || !codes))) return fail(MSVGB_eslEINVAL, "NULL argument");
+  *ret = nullptr;
+  if (n < 0) return fail(MSVGB_eslEINVAL, "n < 0");
+  std::vector<int64_t> idx(n);
+  int Lmax = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t L = off[i + 1] - off[i];
+    if (L < 0 || L > (int64_t) 100000000) return fail(MSVGB_eslEINVAL, "bad sequence offsets");
+    Lmax = std::max<int>(Lmax, (int) L);
+    idx[i] = i;
+  }
+  for (int64_t i = 0; i < off[n] - off[0]; ++i)
+    if (codes[off[0] + i] >= 29) return fail(MSVGB_eslEINVAL, "residue code >= 29 (Kp)");
+  std::stable_sort(idx.begin(), idx.end(), [&](int64_t a, int64_t b) {
+    return off[a + 1] - off[a] > off[b + 1] - off[b];
+  });
+  std::vector<int64_t> start(n), orig(n);
+  std::vector<int32_t> len(n);
+  int64_t pos = 0;
+  for (int64_t s = 0; s < n; ++s) {
+    const int64_t i = idx[s], L = off[i + 1] - off[i];
+    start[s] = pos; orig[s] = i; len[s] = (int32_t) L;
+    pos += ((L + 15) / 16) * 16;
+  }
+  const int64_t bytes = pos + 64;                 // tail so a 16-byte over-read stays inside
+  std::vector<uint8_t> packed(bytes, (uint8_t) PAD_CODE);
+  for (int64_t s = 0; s < n; ++s) {
+    const int64_t i = orig[s];
+    memcpy(packed.data() + start[s], codes + off[i], (size_t) len[s]);
+  }
+  msvgb_db *db = new msvgb_db();
+  db->ctx = ctx; db->n = n; db->residues = off[n] - off[0]; db->Lmax = Lmax;
+  db->serial = g_db_serial.fetch_add(1);
+  {
+    std::vector<int32_t> dl(len.begin(), len.end());
+    std::sort(dl.begin(), dl.end());
+    dl.erase(std::unique(dl.begin(), dl.end()), dl.end());
+    db->distinct_len = std::move(dl);
+  }
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e == cudaSuccess) e = cudaMalloc(&db->d_codes, bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&db->d_start, std::max<int64_t>(n, 1) * 8);
+  if (e == cudaSuccess) e = cudaMalloc(&db->d_orig, std::max<int64_t>(n, 1) * 8);
+  if (e == cudaSuccess) e = cudaMalloc(&db->d_len, std::max<int64_t>(n, 1) * 4);
+  if (e == cudaSuccess) e = cudaMemcpy(db->d_codes, packed.data(), bytes, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && n) e = cudaMemcpy(db->d_start, start.data(), n * 8, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && n) e = cudaMemcpy(db->d_orig, orig.data(), n * 8, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && n) e = cudaMemcpy(db->d_len, len.data(), n * 4, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    msvgb_db_destroy(db);
+    return fail(e == cudaErrorMemoryAllocation ? MSVGB_eslEMEM : MSVGB_eslESYS,
+                std::string("database upload: ") + cudaGetErrorString(e));
+  }
+  *ret = db;
+  return MSVGB_eslOK;
+}
+
+extern "C" int msvgb_db_destroy(msvgb_db *db) {
+  if (!db) return MSVGB_eslOK;
+  cudaSetDevice(db->ctx->device);
+  cudaFree(db->d_codes); cudaFree(db->d_start); cudaFree(db->d_orig); cudaFree(db->d_len);
+  delete db;
+  return MSVGB_eslOK;
+}
+extern "C" int64_t msvgb_db_nseq(const msvgb_db *db) { return db ? db->n : -1; }
+extern "C" int64_t msvgb_db_residues(const msvgb_db *db) { return db ? db->residues : -1; }
+
+// ------------------------------------------------------------------------------
+// search
+
+static int launch_one(msvgb_ctx *c, const msvgb_profile *p, const DbDev &dbv, const uint8_t *d_tjb,
+                      const uint8_t *d_xjmin, uint8_t *d_xj, uint8_t *d_flags, int skip_empty = 1) {
+  ProfDev P;
+  P.M = p->M; P.C = p->C; P.tbm = p->tbm; P.tec = p->tec; P.base = p->base; P.bias = p->bias;
+  P.stab = p->d_stab; P.mtab = p->d_mtab; P.tjb = d_tjb; P.xjmin = d_xjmin; P.ssv_f16 = p->f16;
+  LaunchArgs a;
+  a.P = P; a.db = dbv; a.out_xj = d_xj; a.out_flags = d_flags; a.ticket = c->d_ticket;
+  a.stream = c->stream; a.grid = 0; a.skip_empty = skip_empty;
+  CUDA_TRY(cudaMemsetAsync(c->d_ticket, 0, sizeof(unsigned long long), c->stream));
+  CUDA_TRY(dispatch(p->C, p->f16 != 0, a, c->num_sms));
+  g_launches.fetch_add(1);
+  return MSVGB_eslOK;
+}
+
+extern "C" int msvgb_search_device(msvgb_ctx *c, const msvgb_profile *pc, const msvgb_db *db, double F1,
+                                   void *d_xj, void *d_flags) {
+  if (!c || !pc || !db || (!d_xj && db->n) || (!d_flags && db->n)) return fail(MSVGB_eslEINVAL, "NULL argument");
+  if (pc->ctx != c || db->ctx != c) return fail(MSVGB_eslEINVAL, "objects belong to another context");
+  if (db->n == 0) return MSVGB_eslOK;
+  msvgb_profile *p = const_cast<msvgb_profile *>(pc);
+  CUDA_TRY(cudaSetDevice(c->device));
+  LenTables *t = nullptr;
+  int st = ensure_tables(p, db, F1, &t);
+  if (st != MSVGB_eslOK) return st;
+  DbDev dbv{db->d_codes, db->d_start, db->d_len, db->d_orig, db->n};
+  return launch_one(c, p, dbv, t->d_tjb, t->d_xjmin, (uint8_t *) d_xj, (uint8_t *) d_flags);
+}
+
+extern "C" int msvgb_search(msvgb_ctx *c, const msvgb_profile *p, const msvgb_db *db, double F1,
+                            uint8_t *out_xj, uint8_t *out_flags) {
+  if (!c || !p || !db || (db->n && (!out_xj || !out_flags))) return fail(MSVGB_eslEINVAL, "NULL argument");
+  if (db->n == 0) return MSVGB_eslOK;
+  CUDA_TRY(cudaSetDevice(c->device));
+  uint8_t *d = nullptr;
+  CUDA_TRY(cudaMallocAsync((void **) &d, 2 * (size_t) db->n, c->stream));
+  int st = msvgb_search_device(c, p, db, F1, d, d + db->n);
+  if (st == MSVGB_eslOK) {
+    cudaError_t e = cudaMemcpyAsync(out_xj, d, db->n, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out_flags, d + db->n, db->n, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) st = fail(MSVGB_eslESYS, std::string("search: ") + cudaGetErrorString(e));
+  }
+  cudaFreeAsync(d, c->stream);
+  if (st == MSVGB_eslOK) CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return st;
+}
+
+// ------------------------------------------------------------------------------
+// drop-in single call
+
+static uint64_t fnv1a(const void *data, size_t n, uint64_t h) {
+  const uint8_t *b = (const uint8_t *) data;
+  for (size_t i = 0; i < n; ++i) { h ^= b[i]; h *= 1099511628211ull; }
+  return h;
+}
+
+static uint64_t om_key(const msvgb_om *om) {
+  const int Q = std::max(2, (om->M - 1) / 16 + 1);
+  uint64_t h = 1469598103934665603ull;
+  h = fnv1a(&om->M, sizeof(int), h);
+  h = fnv1a(&om->tbm_b, 1, h); h = fnv1a(&om->tec_b, 1, h);
+  h = fnv1a(&om->base_b, 1, h); h = fnv1a(&om->bias_b, 1, h);
+  h = fnv1a(&om->scale_b, sizeof(float), h);
+  return fnv1a(om->rbv, (size_t) om->Kp * Q * 16, h);
+}
+
+static int ensure_cap(uint8_t **ptr, size_t *cap, size_t need) {
+  if (*cap >= need) return MSVGB_eslOK;
+  cudaFree(*ptr); *ptr = nullptr; *cap = 0;
+  size_t n = std::max<size_t>(need, 4096);
+  CUDA_TRY(cudaMalloc(ptr, n));
+  *cap = n;
+  return MSVGB_eslOK;
+}
+
+extern "C" int msvgb_MSVFilter(msvgb_ctx *c, const uint8_t *dsq, int L, const msvgb_om *om, msvgb_omx *ox,
+                               float *ret_sc) {
+  if (!c || !dsq || !om || !ox || !ret_sc) return fail(MSVGB_eslEINVAL, "NULL argument");
+  const int Q = std::max(2, (om->M - 1) / 16 + 1);
+  if (Q > ox->allocQ16) return fail(MSVGB_eslEINVAL, "DP matrix allocated too small");   // msvfilter.c:103
+  ox->M = om->M;
+  if (L < 0) return fail(MSVGB_eslEINVAL, "L < 0");
+  for (int i = 1; i <= L; ++i)
+    if (dsq[i] >= 29) return fail(MSVGB_eslEINVAL, "residue code >= 29 (Kp)");
+  std::lock_guard<std::mutex> lock(c->mu);
+  CUDA_TRY(cudaSetDevice(c->device));
+  const uint64_t key = om_key(om);
+  msvgb_profile *p = nullptr;
+  auto it = c->cache.find(key);
+  if (it != c->cache.end()) p = it->second;
+  else {
+    int st = profile_build(c, om, default_f16(), &p);
+    if (st != MSVGB_eslOK) return st;
+    if (c->cache.size() >= 64) { msvgb_profile_destroy(c->cache.begin()->second); c->cache.erase(c->cache.begin()); }
+    c->cache[key] = p;
+  }
+  // residues padded to 16 bytes with the pad code; the tjb table holds the
+  // caller's om->tjb_b at index L (the reference reads om->tjb_b as set).
+  const size_t padded = ((size_t) L + 15) / 16 * 16 + 64;
+  int st = ensure_cap(&c->d_seq, &c->d_seq_cap, padded);
+  if (st != MSVGB_eslOK) return st;
+  st = ensure_cap(&c->d_tab, &c->d_tab_cap, 2 * ((size_t) L + 1));
+  if (st != MSVGB_eslOK) return st;
+  std::vector<uint8_t> h(padded, (uint8_t) PAD_CODE);
+  if (L) memcpy(h.data(), dsq + 1, (size_t) L);
+  std::vector<uint8_t> tab(2 * ((size_t) L + 1), 0);
+  tab[L] = om->tjb_b;                                  // tjb table
+  tab[(size_t) L + 1 + L] = 255;                       // xjmin: pass flag unused here
+  int64_t meta[4] = {0, 0, 0, 0};                      // start = 0, orig = 0, len (int32) in meta[2]
+  int32_t len32 = L;
+  memcpy(&meta[2], &len32, 4);
+  CUDA_TRY(cudaMemcpyAsync(c->d_seq, h.data(), padded, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(c->d_tab, tab.data(), tab.size(), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(c->d_meta, meta, sizeof(meta), cudaMemcpyHostToDevice, c->stream));
+  DbDev dbv{c->d_seq, c->d_meta, (const int32_t *) (c->d_meta + 2), c->d_meta + 1, 1};
+  st = launch_one(c, p, dbv, c->d_tab, c->d_tab + L + 1, c->d_out, c->d_out + 1, 0);
+  if (st != MSVGB_eslOK) return st;
+  uint8_t res[2];
+  CUDA_TRY(cudaMemcpyAsync(res, c->d_out, 2, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  if (res[1] & MSVGB_FLAG_ERANGE) { *ret_sc = INFINITY; return MSVGB_eslERANGE; }
+  *ret_sc = score_from_xj(res[0], om->tjb_b, om->base_b, om->scale_b);
+  return MSVGB_eslOK;
+}

@@ -1,0 +1,103 @@
+// msv_kernel_impl.cuh -- the search kernel and its launcher (instantiated per C
+// in inst_*.cu so the translation units compile in parallel).
+#pragma once
+#include <cuda_fp16.h>
+#include "msv_device.cuh"
+
+namespace msvgb {
+
+struct LaunchArgs {
+  ProfDev             P;
+  DbDev               db;
+  uint8_t            *out_xj;     // [n] in original sequence order
+  uint8_t            *out_flags;  // [n]
+  unsigned long long *ticket;     // zeroed before the launch
+  cudaStream_t        stream;
+  int                 grid;       // 0: fill the GPU
+  int                 skip_empty; // 1: L == 0 is skipped as p7_Pipeline does; 0: scored like p7_MSVFilter
+};
+
+constexpr int WARPS_PER_CTA = 8;
+
+template <int C, bool F16>
+constexpr size_t smem_bytes() {
+  return ((size_t) (F16 ? NRES * C * 32 : NRES * (C / 2) * 32) + (size_t) NRES * (C / 2) * 32) * 4;
+}
+
+// Persistent kernel: every CTA stages the profile's cost tables into shared
+// memory once, then its warps pull sequences (longest first) from a global
+// ticket until the database is exhausted.
+template <int C, bool F16>
+__global__ void __launch_bounds__(WARPS_PER_CTA * 32)
+msv_search_kernel(ProfDev P, DbDev db, uint8_t *__restrict__ out_xj, uint8_t *__restrict__ out_flags,
+                  unsigned long long *__restrict__ ticket, int skip_empty) {
+  extern __shared__ __align__(16) uint32_t smem[];
+  constexpr int SW = F16 ? NRES * C * 32 : NRES * (C / 2) * 32;   // words of the SSV table
+  constexpr int MW = NRES * (C / 2) * 32;                          // words of the MSV table
+  uint32_t *stab = smem;
+  uint32_t *mtab = smem + SW;
+  {
+    const uint4 *gs = reinterpret_cast<const uint4 *>(P.stab);
+    const uint4 *gm = reinterpret_cast<const uint4 *>(P.mtab);
+    uint4 *ss = reinterpret_cast<uint4 *>(stab);
+    uint4 *sm = reinterpret_cast<uint4 *>(mtab);
+    for (int i = threadIdx.x; i < SW / 4; i += blockDim.x) ss[i] = __ldg(gs + i);
+    for (int i = threadIdx.x; i < MW / 4; i += blockDim.x) sm[i] = __ldg(gm + i);
+  }
+  __syncthreads();
+
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    unsigned long long s = 0;
+    if (lane == 0) s = atomicAdd(ticket, 1ull);
+    s = __shfl_sync(FULL, s, 0);
+    if (s >= (unsigned long long) db.n) break;
+    const int L = db.len[s];
+    const int64_t oi = db.orig[s];
+    if (L == 0 && skip_empty) {
+      if (lane == 0) { out_xj[oi] = 0; out_flags[oi] = 0x08; }   // MSVGB_FLAG_EMPTY
+      continue;
+    }
+    const uint32_t *sq = reinterpret_cast<const uint32_t *>(db.codes + db.start[s]);
+    int xj, full;
+    const int st = msv_one<C, F16>(P, stab, mtab, sq, L, lane, xj, full);
+    if (lane == 0) {
+      int flags = full ? 0x04 : 0;
+      if (st == ST_ERANGE) flags |= 0x01 | 0x02;                 // +inf always passes F1
+      else if (xj >= P.xjmin[L]) flags |= 0x02;
+      out_xj[oi] = (uint8_t) xj;
+      out_flags[oi] = (uint8_t) flags;
+    }
+  }
+}
+
+template <int C, bool F16>
+cudaError_t launch_search(const LaunchArgs &a, int num_sms) {
+  auto kern = msv_search_kernel<C, F16>;
+  constexpr size_t smem = smem_bytes<C, F16>();
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  int grid = a.grid;
+  if (grid <= 0) {
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, WARPS_PER_CTA * 32, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    grid = per_sm * num_sms;
+    const long long need = (a.db.n + WARPS_PER_CTA - 1) / WARPS_PER_CTA;
+    if (need < grid) grid = (int) (need > 0 ? need : 1);
+  }
+  kern<<<grid, WARPS_PER_CTA * 32, smem, a.stream>>>(a.P, a.db, a.out_xj, a.out_flags, a.ticket, a.skip_empty);
+  return cudaGetLastError();
+}
+
+}  // namespace msvgb
+
+#define MSVGB_INSTANTIATE_I8(C) \
+  template cudaError_t msvgb::launch_search<C, false>(const msvgb::LaunchArgs &, int);
+#define MSVGB_INSTANTIATE_F16(C) \
+  template cudaError_t msvgb::launch_search<C, true>(const msvgb::LaunchArgs &, int);

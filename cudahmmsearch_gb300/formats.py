@@ -210,7 +210,9 @@ def synth_sequences(n: int, *, seed: int, median: float = 300.0, sigma: float = 
     """Synthetic protein database: residues i.i.d. from the HMMER amino
     background with a fraction ``x_frac`` replaced by X (code 26), lengths
     lognormal(ln median, sigma) clipped to [lmin, lmax]; optionally a fraction
-    of lengths uniform in ``uniform_range``."""
+    of lengths uniform in ``uniform_range``. Residues are drawn through a
+    65536-entry inverse-CDF table in chunks, so hundreds of millions of
+    residues take seconds."""
     rng = np.random.default_rng(seed)
     lens = np.exp(rng.normal(np.log(median), sigma, size=n))
     lens = np.clip(np.rint(lens), lmin, lmax).astype(np.int64)
@@ -220,10 +222,60 @@ def synth_sequences(n: int, *, seed: int, median: float = 300.0, sigma: float = 
     off = np.zeros(n + 1, np.int64)
     np.cumsum(lens, out=off[1:])
     total = int(off[-1])
-    cdf = np.cumsum(AMINO_BG.astype(np.float64))
-    cdf /= cdf[-1]
-    codes = np.searchsorted(cdf, rng.random(total), side="right").astype(np.uint8)
-    codes = np.minimum(codes, K_AMINO - 1)
-    if x_frac > 0:
-        codes[rng.random(total) < x_frac] = CODE_X
+    p = AMINO_BG.astype(np.float64) / AMINO_BG.astype(np.float64).sum() * (1.0 - x_frac)
+    cdf = np.cumsum(np.concatenate([p, [x_frac]]))
+    lut = np.searchsorted(cdf, (np.arange(65536) + 0.5) / 65536.0, side="right")
+    lut = np.minimum(lut, K_AMINO).astype(np.uint8)
+    lut[lut == K_AMINO] = CODE_X
+    codes = np.empty(total, np.uint8)
+    step = 1 << 26
+    for a in range(0, total, step):
+        b = min(total, a + step)
+        codes[a:b] = lut[rng.integers(0, 65536, size=b - a, dtype=np.uint16)]
     return SeqSet(codes, off)
+
+
+def emission_probs(p: Profile) -> np.ndarray:
+    """Approximate match emission probabilities per node, float64 [M, 20]:
+    e_k(x) proportional to f(x) * exp(msc(k,x)) with msc recovered from the
+    quantised cost, msc ~ (bias - rbv) / scale (inverse of biased_byteify,
+    src/impl_sse/p7_oprofile.c:495-503)."""
+    costs = p.node_costs()[:K_AMINO].astype(np.float64).T          # [M, 20]
+    msc = (p.bias_b - costs) / p.scale_b
+    e = AMINO_BG[None, :].astype(np.float64) * np.exp(msc)
+    return e / e.sum(axis=1, keepdims=True)
+
+
+def emit_homologs(p: Profile, n: int, *, seed: int, flank_median: float = 150.0,
+                  repeat: int = 1, lmax: int = 35000) -> SeqSet:
+    """Synthetic homologs of a profile: a local, mostly ungapped walk through
+    the model's match states (random start node and length, ~1% insert and
+    ~1% delete events) emitting from emission_probs(), between background
+    flanks. With repeat > 1 the emitted core is repeated (drives scores to
+    overflow)."""
+    rng = np.random.default_rng(seed)
+    e = emission_probs(p)
+    cdf = np.cumsum(e, axis=1)
+    cdf /= cdf[:, -1:]
+    bg = np.cumsum(AMINO_BG.astype(np.float64))
+    bg /= bg[-1]
+    out = []
+    for _ in range(n):
+        k0 = int(rng.integers(0, max(1, p.M // 3)))
+        k1 = int(rng.integers(min(p.M, k0 + max(1, p.M // 2)), p.M + 1))
+        ks = np.arange(k0, max(k1, k0 + 1))
+        ks = ks[rng.random(len(ks)) >= 0.01]                   # deletions
+        core = (cdf[ks] < rng.random(len(ks))[:, None]).sum(axis=1)
+        ins = rng.random(len(core)) < 0.01                      # insertions after a node
+        if ins.any():
+            extra = np.searchsorted(bg, rng.random(int(ins.sum())), side="right")
+            core = np.insert(core, np.nonzero(ins)[0] + 1, extra)
+        core = np.minimum(core, K_AMINO - 1).astype(np.uint8)
+        if repeat > 1:
+            core = np.tile(core, repeat)
+        fl = rng.exponential(flank_median, size=2).astype(np.int64)
+        left = np.minimum(np.searchsorted(bg, rng.random(fl[0]), side="right"), K_AMINO - 1)
+        right = np.minimum(np.searchsorted(bg, rng.random(fl[1]), side="right"), K_AMINO - 1)
+        seq = np.concatenate([left.astype(np.uint8), core, right.astype(np.uint8)])[:lmax]
+        out.append(seq if len(seq) else core[:1])
+    return SeqSet.from_list(out)

@@ -1,0 +1,132 @@
+/* msvgb.h -- C ABI of the GB300 MSV filter (HMMER3 hmmsearch stage 1).
+ *
+ * Plain C: pointers, sizes and status codes only. Status codes are Easel's
+ * (easel/easel.h:95-114): eslOK 0, eslEMEM 5, eslEINVAL 11, eslESYS 12,
+ * eslERANGE 16. No function calls exit(); a CUDA failure returns eslESYS and
+ * msvgb_last_error() describes it.
+ *
+ * Residues are Easel digital codes 0..28 for the amino alphabet
+ * (easel/esl_alphabet.c:275); 255 (eslDSQ_SENTINEL) only at dsq[0], dsq[L+1]
+ * in the single-call entry point.
+ *
+ * Results are bit-exact with the reference CPU p7_MSVFilter
+ * (src/impl_sse/msvfilter.c:77-213, SSV first, src/impl_sse/ssvfilter.c:1364-1413):
+ * the same uint8 xJ, the same float score (+inf on overflow) and the same
+ * F1 pass flag of the p7_Pipeline MSV stage (src/p7_pipeline.c:662-677).
+ */
+#ifndef MSVGB_H
+#define MSVGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MSVGB_eslOK      0
+#define MSVGB_eslEMEM    5
+#define MSVGB_eslEINVAL 11
+#define MSVGB_eslESYS   12
+#define MSVGB_eslERANGE 16
+
+/* Per-(profile, sequence) result flags written by the search entry points. */
+#define MSVGB_FLAG_ERANGE 0x01  /* score overflowed: +inf (eslERANGE)                      */
+#define MSVGB_FLAG_PASS   0x02  /* passes the MSV-stage F1 P-value gate                    */
+#define MSVGB_FLAG_FULL   0x04  /* SSV was undecided; the full MSV recurrence ran          */
+#define MSVGB_FLAG_EMPTY  0x08  /* L == 0: skipped, as p7_Pipeline does (p7_pipeline.c:662) */
+
+/* Read-only view of the MSV fields of a P7_OPROFILE (src/impl_sse/impl_sse.h:77-87).
+ * rbv is the striped [Kp][Q][16] uint8 table with Q = max(2, ceil(M/16)):
+ * byte z of vector q for residue x holds the biased cost of node k = q+1+z*Q
+ * (src/impl_sse/p7_oprofile.c:619-635); pass om->rbv[0] (the vectors are contiguous). */
+typedef struct {
+  int            M;
+  int            Kp;        /* 29 (amino) */
+  const uint8_t *rbv;
+  uint8_t        tbm_b, tec_b, tjb_b, base_b, bias_b;
+  float          scale_b;
+  float          mmu, mlambda;   /* om->evparam[p7_MMU], om->evparam[p7_MLAMBDA] */
+} msvgb_om;
+
+/* The part of P7_OMX that p7_MSVFilter reads and writes (impl_sse.h:185-199). */
+typedef struct {
+  int allocQ16;
+  int M;
+} msvgb_omx;
+
+typedef struct msvgb_ctx     msvgb_ctx;      /* one GPU, one stream, device buffers   */
+typedef struct msvgb_profile msvgb_profile;  /* a profile resident in HBM             */
+typedef struct msvgb_db      msvgb_db;       /* a packed sequence database in HBM     */
+
+/* ---- context ---------------------------------------------------------------- */
+int         msvgb_ctx_create(int device, msvgb_ctx **ret_ctx);
+int         msvgb_ctx_destroy(msvgb_ctx *ctx);
+/* Launch on an external cudaStream_t (passed as void*); NULL restores the context's own. */
+int         msvgb_ctx_set_stream(msvgb_ctx *ctx, void *cuda_stream);
+const char *msvgb_last_error(void);
+/* Count of kernels this library has launched in the calling process. */
+uint64_t    msvgb_kernel_launches(void);
+
+/* ---- drop-in single call -----------------------------------------------------
+ * Replaces p7_MSVFilter(dsq, L, om, ox, ret_sc) (src/impl_sse/impl_sse.h:327,
+ * src/impl_sse/msvfilter.c:78). dsq[1..L] are codes, dsq[0], dsq[L+1] sentinels.
+ * om->tjb_b must already hold the value for this L (p7_oprofile_ReconfigLength),
+ * as the reference requires. Returns eslOK or eslERANGE (*ret_sc = +inf);
+ * eslEINVAL if p7O_NQB(om->M) > ox->allocQ16 (msvfilter.c:103). Sets ox->M = om->M.
+ * The profile is uploaded once and cached by content. Thread-safe (serialised
+ * per context). */
+int msvgb_MSVFilter(msvgb_ctx *ctx, const uint8_t *dsq, int L, const msvgb_om *om,
+                    msvgb_omx *ox, float *ret_sc);
+
+/* ---- resident profile and database --------------------------------------------
+ * Upload replaces the device side of p7_oprofile_Convert's MSV part
+ * (src/impl_sse/p7_oprofile.c:601-640, mf_conversion; sf_conversion :549-590):
+ * the striped rbv bytes are re-laid for the kernels. om->tjb_b is ignored here:
+ * the search recomputes it per target length (p7_oprofile_ReconfigMSVLength,
+ * p7_oprofile.c:920-925). */
+int msvgb_profile_create(msvgb_ctx *ctx, const msvgb_om *om, msvgb_profile **ret_prof);
+/* Same with an explicit SSV arithmetic variant: 0 = int8 cost table, packed
+ * 16-bit integer cells (default); 1 = f16 cost table, f16x2 cells (exact on
+ * these integers; used where its 2x larger table fits in shared memory,
+ * otherwise variant 0 is used). msvgb_profile_variant() tells which. */
+int msvgb_profile_create_ex(msvgb_ctx *ctx, const msvgb_om *om, int ssv_variant, msvgb_profile **ret_prof);
+int msvgb_profile_variant(const msvgb_profile *prof);
+int msvgb_profile_destroy(msvgb_profile *prof);
+int msvgb_profile_M(const msvgb_profile *prof);
+
+/* Packs n sequences (codes[off[i] .. off[i+1]), no sentinels) into HBM:
+ * sorted by length (longest first), each padded to 16 bytes. Replaces the
+ * fork's loadDBQuad/loadCUDA host packing (code/src/GPUFunction.cu:219-255,
+ * 332-415) and its offline dbsort/hmmsort length sort. Codes must be < 29. */
+int     msvgb_db_create(msvgb_ctx *ctx, const uint8_t *codes, const int64_t *off, int64_t n,
+                        msvgb_db **ret_db);
+int     msvgb_db_destroy(msvgb_db *db);
+int64_t msvgb_db_nseq(const msvgb_db *db);
+int64_t msvgb_db_residues(const msvgb_db *db);
+
+/* ---- search ---------------------------------------------------------------------
+ * Plain path: one profile per launch. For every sequence i of db (original
+ * order) writes out_xj[i] (final uint8 xJ; 255 on overflow) and out_flags[i]
+ * (MSVGB_FLAG_*), with the pass flag at P-value threshold F1 (default 0.02,
+ * src/p7_pipeline.c:210). Host output buffers; returns after the copy. */
+int msvgb_search(msvgb_ctx *ctx, const msvgb_profile *prof, const msvgb_db *db, double F1,
+                 uint8_t *out_xj, uint8_t *out_flags);
+
+/* Same, outputs left in device memory (d_xj, d_flags: n bytes each, device
+ * pointers), asynchronous on the context's stream. */
+int msvgb_search_device(msvgb_ctx *ctx, const msvgb_profile *prof, const msvgb_db *db, double F1,
+                        void *d_xj, void *d_flags);
+
+/* ---- host-side score helpers (exact reference expressions) --------------------- */
+/* tjb_b for target length L (p7_oprofile.c:511-519, 920-925). */
+uint8_t msvgb_tjb_b(float scale_b, int L);
+/* MSV score in nats from xJ (msvfilter.c:205-210); +inf when flags has ERANGE. */
+float   msvgb_score(uint8_t xj, uint8_t flags, int L, uint8_t base_b, float scale_b);
+/* MSV-stage gate of p7_Pipeline (p7_pipeline.c:666-676): 1 if P <= F1. */
+int     msvgb_f1_pass(float usc, int L, float mmu, float mlambda, double F1, double *ret_P);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

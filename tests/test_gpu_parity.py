@@ -1,0 +1,173 @@
+"""GPU parity through the C ABI (libmsvgb.so) against the reference's golden
+vectors and the oracle. Bit-exact: xJ, float score bit pattern (+inf on
+overflow) and the F1 pass flag, for both SSV arithmetic variants."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from cudahmmsearch_gb300 import api
+from cudahmmsearch_gb300 import formats as F
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+CASES = sorted(os.path.basename(p)[:-5] for p in glob.glob(os.path.join(GOLDEN, "*.prof")))
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = api.Context(0)
+    yield c
+    c.close()
+
+
+def load_case(name):
+    return (F.read_profile(os.path.join(GOLDEN, name + ".prof")),
+            F.read_seqs(os.path.join(GOLDEN, name + ".seqs")),
+            F.read_results(os.path.join(GOLDEN, name + ".res")))
+
+
+def check_against_oracle(p, s, xj, fl, o):
+    nonempty = s.lengths > 0
+    assert np.array_equal((fl & api.FLAG_ERANGE) != 0, o["status"] == F.eslERANGE)
+    ok = o["status"] == F.eslOK
+    assert np.array_equal(xj[ok], o["xj"][ok])
+    assert np.array_equal(((fl & api.FLAG_PASS) != 0)[nonempty], o["pass"][nonempty] == 1)
+    assert np.array_equal(((fl & api.FLAG_FULL) != 0)[nonempty], o["path"][nonempty] == 1)
+    assert np.all((fl[~nonempty] & api.FLAG_EMPTY) != 0)
+
+
+@pytest.mark.parametrize("variant", [0, 1])
+@pytest.mark.parametrize("name", CASES)
+def test_search_matches_reference_golden(ctx, name, variant):
+    p, s, r = load_case(name)
+    dp = api.DeviceProfile(ctx, p, variant)
+    db = api.DeviceDB(ctx, s)
+    xj, fl = api.search(ctx, dp, db)
+    assert np.array_equal((fl & api.FLAG_ERANGE) != 0, r.status == F.eslERANGE)
+    assert np.array_equal((fl & api.FLAG_PASS) != 0, r.passed == 1)
+    sc = api.scores(p, s.lengths, xj, fl)
+    assert np.array_equal(sc.view(np.uint32), r.sc.view(np.uint32))
+
+
+@pytest.mark.parametrize("name", ["m1_s1", "m17_s2", "m200_s1", "m2400_s1"])
+def test_dropin_msvfilter_matches_reference_golden(ctx, name):
+    p, s, r = load_case(name)
+    for i in range(0, s.n, max(1, s.n // 25)):
+        L = int(s.lengths[i])
+        dsq = np.concatenate([[255], s.seq(i), [255]]).astype(np.uint8)
+        st, sc = ctx.MSVFilter(dsq, L, p, api.tjb_b(p.scale_b, L))
+        assert st == r.status[i]
+        assert np.float32(sc).view(np.uint32) == r.sc[i].view(np.uint32)
+
+
+def test_dropin_rejects_small_omx(ctx):
+    p, s, r = load_case("m200_s1")
+    dsq = np.concatenate([[255], s.seq(0), [255]]).astype(np.uint8)
+    with pytest.raises(api.MSVError) as e:
+        ctx.MSVFilter(dsq, int(s.lengths[0]), p, 10, allocQ16=p.Q - 1)
+    assert e.value.code == api.eslEINVAL
+
+
+def test_dropin_empty_sequence_matches_oracle(ctx):
+    p, _, _ = load_case("m50_s1")
+    st, sc = ctx.MSVFilter(np.array([255, 255], np.uint8), 0, p, api.tjb_b(p.scale_b, 0))
+    ost, oxj, osc, _ = O.msv_filter(p, np.zeros(0, np.uint8))
+    assert st == ost and np.float32(sc).view(np.uint32) == np.float32(osc).view(np.uint32)
+
+
+@pytest.mark.parametrize("variant", [0, 1])
+def test_m200_20000_sequences_match_oracle(ctx, variant):
+    """The M=200 (seed 1) profile against 20,000 synthetic sequences: lognormal
+    lengths (median 300, sigma 0.7) clipped to [10, 5000], 0.5% X, 1% homologs."""
+    p, _, _ = load_case("m200_s1")
+    bgs = F.synth_sequences(19800, seed=11, lmax=5000)
+    hom = F.emit_homologs(p, 200, seed=12)
+    s = F.SeqSet.concat([bgs, hom])
+    o = O.msv_batch(p, s)
+    dp = api.DeviceProfile(ctx, p, variant)
+    db = api.DeviceDB(ctx, s)
+    xj, fl = api.search(ctx, dp, db)
+    check_against_oracle(p, s, xj, fl, o)
+    assert o["pass"].sum() >= 200
+
+
+def test_m400_50000_subset_matches_oracle(ctx):
+    """50,000-sequence subset of the M=400 workload (lengths clipped to [10, 35000], 2% homologs)."""
+    p, _, _ = load_case("m400_s1")
+    s = F.SeqSet.concat([F.synth_sequences(49000, seed=21, lmax=35000), F.emit_homologs(p, 1000, seed=22)])
+    o = O.msv_batch(p, s)
+    xj, fl = api.search(ctx, api.DeviceProfile(ctx, p), api.DeviceDB(ctx, s))
+    check_against_oracle(p, s, xj, fl, o)
+
+
+def test_m2400_length_extremes_and_saturation(ctx):
+    """M=2400: lognormal plus long uniform [5000, 35000] lengths, and saturation
+    sequences (an emitted core repeated 20 times) that must overflow to +inf."""
+    p, _, _ = load_case("m2400_s1")
+    s = F.SeqSet.concat([F.synth_sequences(1800, seed=31, lmax=35000, uniform_frac=0.1),
+                         F.emit_homologs(p, 100, seed=32, repeat=20)])
+    o = O.msv_batch(p, s)
+    xj, fl = api.search(ctx, api.DeviceProfile(ctx, p), api.DeviceDB(ctx, s))
+    check_against_oracle(p, s, xj, fl, o)
+    assert (o["status"] == F.eslERANGE).sum() >= 50
+
+
+@pytest.mark.parametrize("M", [1, 2, 3, 15, 16, 17, 63, 64, 65, 127, 128, 129, 1000, 3072])
+def test_model_size_corners(ctx, M):
+    """Node counts around the striping and lane boundaries, random profiles
+    built directly from cost tables, tiny and all-X sequences."""
+    rng = np.random.default_rng(M)
+    costs = rng.integers(0, 40, size=(F.KP_AMINO, M)).astype(np.uint8)
+    costs[20] = 255; costs[27:] = 255                       # gap, '*', '~': -inf scores
+    p = F.profile_from_node_costs(costs, tbm_b=int(rng.integers(5, 60)), tec_b=3, base_b=190,
+                                  bias_b=int(rng.integers(5, 40)), scale_b=3.0 / 0.6931471805599453,
+                                  mmu=-9.0, mlambda=0.69)
+    seqs = [rng.integers(0, 20, size=L).astype(np.uint8) for L in (1, 2, 3, 4, 5, 7, 16, 17, 100, 333)]
+    seqs += [np.full(50, F.CODE_X, np.uint8), np.zeros(0, np.uint8), rng.integers(0, 29, size=77).astype(np.uint8)]
+    s = F.SeqSet.from_list(seqs)
+    o = O.msv_batch(p, s)
+    for variant in (0, 1):
+        xj, fl = api.search(ctx, api.DeviceProfile(ctx, p, variant), api.DeviceDB(ctx, s))
+        check_against_oracle(p, s, xj, fl, o)
+
+
+@pytest.mark.parametrize("bias,tbm,base", [(0, 0, 190), (126, 5, 190), (200, 10, 190), (40, 100, 190),
+                                           (14, 120, 100), (60, 40, 255), (90, 130, 190)])
+def test_extreme_scalar_costs(ctx, bias, tbm, base):
+    """Bias/transition corners: SSV guard off, tjb+tbm wrapping mod 256,
+    base below tjb+tbm, bias >= 65 where the xB clamp matters."""
+    rng = np.random.default_rng(bias * 1000 + tbm)
+    M = 150
+    costs = rng.integers(0, 255, size=(F.KP_AMINO, M)).astype(np.uint8)
+    p = F.profile_from_node_costs(costs, tbm_b=tbm, tec_b=3, base_b=base, bias_b=bias,
+                                  scale_b=3.0 / 0.6931471805599453, mmu=-9.0, mlambda=0.69)
+    s = F.SeqSet.concat([F.synth_sequences(300, seed=bias + 7, lmax=3000),
+                         F.SeqSet.from_list([rng.integers(0, 20, size=L).astype(np.uint8) for L in (1, 2, 9, 40000)])])
+    o = O.msv_batch(p, s)
+    for variant in (0, 1):
+        xj, fl = api.search(ctx, api.DeviceProfile(ctx, p, variant), api.DeviceDB(ctx, s))
+        check_against_oracle(p, s, xj, fl, o)
+
+
+def test_invalid_inputs_rejected(ctx):
+    p, s, _ = load_case("m50_s1")
+    bad = F.SeqSet.from_list([np.array([1, 2, 29], np.uint8)])
+    with pytest.raises(api.MSVError) as e:
+        api.DeviceDB(ctx, bad)
+    assert e.value.code == api.eslEINVAL
+    big = F.profile_from_node_costs(np.zeros((29, 3073), np.uint8), tbm_b=10, tec_b=3, base_b=190,
+                                    bias_b=10, scale_b=4.328085, mmu=-9.0, mlambda=0.69)
+    with pytest.raises(api.MSVError) as e:
+        api.DeviceProfile(ctx, big)
+    assert e.value.code == api.eslEINVAL
+
+
+def test_kernel_launch_counter_advances(ctx):
+    p, s, _ = load_case("m50_s1")
+    before = api.kernel_launches()
+    api.search(ctx, api.DeviceProfile(ctx, p), api.DeviceDB(ctx, s))
+    assert api.kernel_launches() == before + 1
