@@ -24,8 +24,10 @@
 #include "../../include/msvgb.h"
 #include "msv_device.cuh"
 #include "msv_kernel_impl.cuh"
+#include "msv_internal.h"
 
 using namespace msvgb;
+using namespace msvgb_detail;
 
 namespace msvgb {
 template <int C, bool F16> cudaError_t launch_search(const LaunchArgs &a, int num_sms);
@@ -36,7 +38,9 @@ template <int C, bool F16> cudaError_t launch_search(const LaunchArgs &a, int nu
 static thread_local std::string g_err;
 static std::atomic<uint64_t> g_launches{0};
 
-static int fail(int code, const std::string &msg) { g_err = msg; return code; }
+namespace msvgb_detail {
+int fail(int code, const std::string &msg) { g_err = msg; return code; }
+}  // namespace msvgb_detail
 #define CUDA_TRY(expr)                                                                       \
   do {                                                                                       \
     cudaError_t _e = (expr);                                                                 \
@@ -46,6 +50,7 @@ static int fail(int code, const std::string &msg) { g_err = msg; return code; }
 
 extern "C" const char *msvgb_last_error(void) { return g_err.c_str(); }
 extern "C" uint64_t msvgb_kernel_launches(void) { return g_launches.load(); }
+void msvgb_detail::count_launch() { g_launches.fetch_add(1); }
 
 // ------------------------------------------------------------------------------
 // exact host arithmetic of the reference
@@ -89,48 +94,6 @@ extern "C" int msvgb_f1_pass(float usc, int L, float mmu, float mlambda, double 
 // ------------------------------------------------------------------------------
 // objects
 
-struct msvgb_ctx {
-  int device = 0;
-  int num_sms = 0;
-  cudaStream_t own = nullptr;
-  cudaStream_t stream = nullptr;
-  unsigned long long *d_ticket = nullptr;
-  std::mutex mu;                                        // serialises the single-call path
-  std::unordered_map<uint64_t, msvgb_profile *> cache;  // single-call profile cache
-  // single-call scratch
-  uint8_t *d_seq = nullptr; size_t d_seq_cap = 0;
-  uint8_t *d_tab = nullptr; size_t d_tab_cap = 0;
-  int64_t *d_meta = nullptr;                            // start, orig (int64), len (int32) for n=1
-  uint8_t *d_out = nullptr;
-};
-
-struct LenTables {      // per (profile, database, F1)
-  const msvgb_db *db = nullptr;
-  double F1 = -1.0;
-  uint8_t *d_tjb = nullptr;
-  uint8_t *d_xjmin = nullptr;
-};
-
-struct msvgb_profile {
-  msvgb_ctx *ctx = nullptr;
-  int M = 0, C = 0, f16 = 0;
-  uint8_t tbm = 0, tec = 0, base = 0, bias = 0;
-  float scale = 0.f, mmu = 0.f, mlambda = 0.f;
-  uint32_t *d_stab = nullptr, *d_mtab = nullptr;
-  std::vector<LenTables> tables;
-};
-
-struct msvgb_db {
-  msvgb_ctx *ctx = nullptr;
-  int64_t n = 0, residues = 0;
-  int Lmax = 0;
-  uint8_t *d_codes = nullptr;
-  int64_t *d_start = nullptr, *d_orig = nullptr;
-  int32_t *d_len = nullptr;
-  std::vector<int32_t> distinct_len;  // sorted ascending
-  uint64_t serial = 0;
-};
-
 static std::atomic<uint64_t> g_db_serial{1};
 
 // Supported DP widths (words per lane); the warp spans 64*C model nodes.
@@ -144,7 +107,7 @@ static int choose_C(int M) {
   return -1;
 }
 
-static cudaError_t dispatch(int C, bool f16, const LaunchArgs &a, int sms) {
+cudaError_t msvgb_detail::dispatch(int C, bool f16, const LaunchArgs &a, int sms) {
 #define CASE_I8(c)  case c: return launch_search<c, false>(a, sms);
 #define CASE_F16(c) case c: return launch_search<c, true>(a, sms);
   if (f16) {
@@ -311,7 +274,7 @@ extern "C" int msvgb_profile_M(const msvgb_profile *p) { return p ? p->M : -1; }
 // ------------------------------------------------------------------------------
 // per-length tables: tjb_b(L) and the smallest xJ that passes F1 at length L
 
-static int xjmin_for(const msvgb_profile *p, int L, double F1) {
+int msvgb_detail::xjmin_for(const msvgb_profile *p, int L, double F1) {
   const int tjb = msvgb_tjb_b(p->scale, L);
   auto pass = [&](int xj) {
     return msvgb_f1_pass(score_from_xj(xj, tjb, p->base, p->scale), L, p->mmu, p->mlambda, F1, nullptr) != 0;

@@ -1,0 +1,67 @@
+// msv_internal.h -- definitions shared by the translation units of the C ABI
+// (not part of the public interface).
+#pragma once
+#include <cstdint>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/msvgb.h"
+#include "msv_kernel_impl.cuh"
+
+struct msvgb_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t own = nullptr;
+  cudaStream_t stream = nullptr;
+  unsigned long long *d_ticket = nullptr;
+  std::mutex mu;                                        // serialises the single-call path
+  std::unordered_map<uint64_t, msvgb_profile *> cache;  // single-call profile cache
+  // single-call scratch
+  uint8_t *d_seq = nullptr; size_t d_seq_cap = 0;
+  uint8_t *d_tab = nullptr; size_t d_tab_cap = 0;
+  int64_t *d_meta = nullptr;                            // start, orig (int64), len (int32) for n=1
+  uint8_t *d_out = nullptr;
+};
+
+struct LenTables {      // per (profile, database, F1)
+  const msvgb_db *db = nullptr;
+  double F1 = -1.0;
+  uint8_t *d_tjb = nullptr;
+  uint8_t *d_xjmin = nullptr;
+};
+
+struct msvgb_profile {
+  msvgb_ctx *ctx = nullptr;
+  int M = 0, C = 0, f16 = 0;
+  uint8_t tbm = 0, tec = 0, base = 0, bias = 0;
+  float scale = 0.f, mmu = 0.f, mlambda = 0.f;
+  uint32_t *d_stab = nullptr, *d_mtab = nullptr;
+  std::vector<LenTables> tables;
+};
+
+struct msvgb_db {
+  msvgb_ctx *ctx = nullptr;
+  int64_t n = 0, residues = 0;
+  int Lmax = 0;
+  uint8_t *d_codes = nullptr;
+  int64_t *d_start = nullptr, *d_orig = nullptr;
+  int32_t *d_len = nullptr;
+  std::vector<int32_t> distinct_len;  // sorted ascending
+  uint64_t serial = 0;
+};
+
+namespace msvgb_detail {
+// Records msg as the calling thread's last error and returns code.
+int fail(int code, const std::string &msg);
+// Launches the search kernel instantiated for C words per lane.
+cudaError_t dispatch(int C, bool f16, const msvgb::LaunchArgs &a, int sms);
+// Smallest xJ passing the F1 gate at length L (255: none); -1 if the pass set
+// is not monotone in xJ.
+int xjmin_for(const msvgb_profile *p, int L, double F1);
+// Adds one to the count msvgb_kernel_launches() reports.
+void count_launch();
+}  // namespace msvgb_detail
