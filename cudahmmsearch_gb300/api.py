@@ -27,6 +27,7 @@ EXPORTS = [
     "msvgb_kernel_launches", "msvgb_MSVFilter", "msvgb_profile_create", "msvgb_profile_destroy",
     "msvgb_profile_M", "msvgb_profile_create_ex", "msvgb_profile_variant", "msvgb_db_create", "msvgb_db_destroy", "msvgb_db_nseq", "msvgb_db_residues",
     "msvgb_search", "msvgb_search_device", "msvgb_tjb_b", "msvgb_score", "msvgb_f1_pass",
+    "msvgb_search_static",
 ]
 
 
@@ -81,6 +82,7 @@ def lib():
         "msvgb_tjb_b": (u8, [f32, i32]),
         "msvgb_score": (f32, [u8, u8, i32, u8, f32]),
         "msvgb_f1_pass": (i32, [f32, i32, f32, f32, f64, ctypes.POINTER(f64)]),
+        "msvgb_search_static": (i32, [vp, vp, f64, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

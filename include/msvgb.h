@@ -118,6 +118,28 @@ int msvgb_search(msvgb_ctx *ctx, const msvgb_profile *prof, const msvgb_db *db, 
 int msvgb_search_device(msvgb_ctx *ctx, const msvgb_profile *prof, const msvgb_db *db, double F1,
                         void *d_xj, void *d_flags);
 
+/* ---- allocation-free search ------------------------------------------------------
+ * No counterpart in the reference. For callers that cannot allocate device
+ * memory once they are running: a process whose GPU memory is all owned by
+ * another allocator, or a latency-bound loop that bans cudaMalloc after
+ * start-up (it can synchronise the device and can fail under memory
+ * pressure). Create the profile and database at set-up time, then call this
+ * with output buffers (n bytes each, device pointers) you already own; the
+ * call itself calls no cudaMalloc, cudaFree or other allocating routine.
+ * Its scratch (the work ticket and the per-length tables msvgb_search would
+ * allocate) is one static device array of about 129 KiB that every GPU
+ * loading this library keeps until the process exits, so sequences longer
+ * than MSVGB_STATIC_MAX_LEN are rejected with eslEINVAL. All calls share that
+ * array: calls whose work overlaps on the GPU (different streams, or
+ * different host threads) race and must be serialised by the caller. The
+ * first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * Asynchronous on cuda_stream (NULL: the context's stream); results equal
+ * msvgb_search_device's. */
+#define MSVGB_STATIC_MAX_LEN 65535
+int msvgb_search_static(const msvgb_profile *prof, const msvgb_db *db, double F1,
+                        void *d_xj, void *d_flags, void *cuda_stream);
+
 /* ---- host-side score helpers (exact reference expressions) --------------------- */
 /* tjb_b for target length L (p7_oprofile.c:511-519, 920-925). */
 uint8_t msvgb_tjb_b(float scale_b, int L);
