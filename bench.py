@@ -34,7 +34,7 @@ sys.path.insert(0, ROOT)
 
 from cudahmmsearch_gb300 import formats as F  # noqa: E402
 
-INT_LANE_OPS_PER_CLK_PER_SM = 128   # 4 SMSPs x 32 lanes: measured, see profiles/int_pipe_peak_opbench.md
+INT_LANE_OPS_PER_CLK_PER_SM = 128   # 4 SM sub-partitions x 32 lanes: nominal issue width
 
 
 def workload(name, rank=0):
@@ -243,12 +243,14 @@ def main():
     clocks = clk.summary()
     sm_mhz = clocks["sm_mhz"] or 2070.0
     nsm = torch.cuda.get_device_properties(local).multi_processor_count
-    peak_tops = nsm * INT_LANE_OPS_PER_CLK_PER_SM * sm_mhz * 1e6 / 1e12
+    peak_tops = api.measure_int_peak(local) / 1e12        # measured now, same GPU and clock regime
     kern_ms = float(np.mean(per))
     achieved_tops = cells / (kern_ms * 1e-3) / 1e12          # 1 cell = 1 packed int32 op (4 uint8 lane-ops)
     roofline = {"bound": "int32-pipe", "achieved": achieved_tops, "peak": peak_tops, "unit": "Tops/s",
                 "frac": achieved_tops / peak_tops, "traffic": None,
-                "peak_note": f"{nsm} SMs x {INT_LANE_OPS_PER_CLK_PER_SM} int32 lane-ops/clk x median SM clock {sm_mhz:.0f} MHz (measured)",
+                "peak_note": f"measured: msvgb_measure_int_peak (independent max.s32/xor over {nsm} SMs); "
+                             f"nominal {nsm} SMs x {INT_LANE_OPS_PER_CLK_PER_SM} lane-ops/clk x {sm_mhz:.0f} MHz = "
+                             f"{nsm * INT_LANE_OPS_PER_CLK_PER_SM * sm_mhz * 1e6 / 1e12:.1f} Tops/s",
                 "hbm": {"achieved": (s.total + 2 * s.n) / (kern_ms * 1e-3) / 1e9, "peak": 6783.5,
                         "unit": "GB/s", "frac": (s.total + 2 * s.n) / (kern_ms * 1e-3) / 1e9 / 6783.5,
                         "peak_note": "of measured (MEASURED_PEAKS.json hbm_gbs)"}}

@@ -27,7 +27,7 @@ EXPORTS = [
     "msvgb_kernel_launches", "msvgb_MSVFilter", "msvgb_profile_create", "msvgb_profile_destroy",
     "msvgb_profile_M", "msvgb_profile_create_ex", "msvgb_profile_variant", "msvgb_db_create", "msvgb_db_destroy", "msvgb_db_nseq", "msvgb_db_residues",
     "msvgb_search", "msvgb_search_device", "msvgb_tjb_b", "msvgb_score", "msvgb_f1_pass",
-    "msvgb_search_static",
+    "msvgb_search_static", "msvgb_measure_int_peak",
 ]
 
 
@@ -83,6 +83,7 @@ def lib():
         "msvgb_score": (f32, [u8, u8, i32, u8, f32]),
         "msvgb_f1_pass": (i32, [f32, i32, f32, f32, f64, ctypes.POINTER(f64)]),
         "msvgb_search_static": (i32, [vp, vp, f64, vp, vp, vp]),
+        "msvgb_measure_int_peak": (i32, [i32, ctypes.POINTER(f64)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -205,6 +206,13 @@ def search(ctx: Context, prof: DeviceProfile, db: DeviceDB, F1: float = 0.02):
 def search_device(ctx: Context, prof: DeviceProfile, db: DeviceDB, d_xj: int, d_flags: int, F1: float = 0.02):
     """Asynchronous search writing to device pointers (on the context's stream)."""
     _check(lib().msvgb_search_device(ctx.h, prof.h, db.h, F1, ctypes.c_void_p(d_xj), ctypes.c_void_p(d_flags)))
+
+
+def measure_int_peak(device: int = 0) -> float:
+    """Sustained 32-bit integer ops/s over all SMs (integer-pipe roofline denominator)."""
+    v = ctypes.c_double()
+    _check(lib().msvgb_measure_int_peak(device, ctypes.byref(v)))
+    return v.value
 
 
 def tjb_b(scale_b: float, L: int) -> int:

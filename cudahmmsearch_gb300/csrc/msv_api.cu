@@ -96,14 +96,19 @@ extern "C" int msvgb_f1_pass(float usc, int L, float mmu, float mlambda, double 
 
 static std::atomic<uint64_t> g_db_serial{1};
 
-// Supported DP widths (words per lane); the warp spans 64*C model nodes.
-static const int kC[] = {2, 4, 6, 8, 10, 12, 14, 16, 20, 24, 28, 32, 40, 48};
-static const int kMaxC = 48;
+// DP widths (32-bit words per lane; the warp spans 64*C nodes). f16 tables:
+// every C up to 32. int8 tables: even C (two DP words per table word).
+static const int kI8C[] = {2, 4, 6, 8, 10, 12, 14, 16, 18, 20, 22, 24, 26, 28, 30, 32, 34, 36, 40, 44, 48, 50};
 static const int kMaxF16C = 32;
 
-static int choose_C(int M) {
-  int need = (M + 63) / 64;
-  for (int c : kC) if (c >= need) return c;
+// Smallest C whose warp spans more than M nodes: node 64*C must be padding
+// (the kernels rely on it for the begin value of node 1).
+static int need_C(int M) { return M / 64 + 1; }
+
+static int choose_C(int M, bool f16) {
+  const int need = need_C(M);
+  if (f16) return need <= kMaxF16C ? need : -1;
+  for (int c : kI8C) if (c >= need) return c;
   return -1;
 }
 
@@ -111,11 +116,18 @@ cudaError_t msvgb_detail::dispatch(int C, bool f16, const LaunchArgs &a, int sms
 #define CASE_I8(c)  case c: return launch_search<c, false>(a, sms);
 #define CASE_F16(c) case c: return launch_search<c, true>(a, sms);
   if (f16) {
-    switch (C) { CASE_F16(2) CASE_F16(4) CASE_F16(6) CASE_F16(8) CASE_F16(10) CASE_F16(12)
-                 CASE_F16(14) CASE_F16(16) CASE_F16(20) CASE_F16(24) CASE_F16(28) CASE_F16(32) }
+    switch (C) {
+      CASE_F16(1) CASE_F16(2) CASE_F16(3) CASE_F16(4) CASE_F16(5) CASE_F16(6) CASE_F16(7) CASE_F16(8)
+      CASE_F16(9) CASE_F16(10) CASE_F16(11) CASE_F16(12) CASE_F16(13) CASE_F16(14) CASE_F16(15) CASE_F16(16)
+      CASE_F16(17) CASE_F16(18) CASE_F16(19) CASE_F16(20) CASE_F16(21) CASE_F16(22) CASE_F16(23) CASE_F16(24)
+      CASE_F16(25) CASE_F16(26) CASE_F16(27) CASE_F16(28) CASE_F16(29) CASE_F16(30) CASE_F16(31) CASE_F16(32)
+    }
   } else {
-    switch (C) { CASE_I8(2) CASE_I8(4) CASE_I8(6) CASE_I8(8) CASE_I8(10) CASE_I8(12) CASE_I8(14)
-                 CASE_I8(16) CASE_I8(20) CASE_I8(24) CASE_I8(28) CASE_I8(32) CASE_I8(40) CASE_I8(48) }
+    switch (C) {
+      CASE_I8(2) CASE_I8(4) CASE_I8(6) CASE_I8(8) CASE_I8(10) CASE_I8(12) CASE_I8(14) CASE_I8(16)
+      CASE_I8(18) CASE_I8(20) CASE_I8(22) CASE_I8(24) CASE_I8(26) CASE_I8(28) CASE_I8(30) CASE_I8(32)
+      CASE_I8(34) CASE_I8(36) CASE_I8(40) CASE_I8(44) CASE_I8(48) CASE_I8(50)
+    }
   }
   return cudaErrorInvalidValue;
 #undef CASE_I8
@@ -139,6 +151,7 @@ extern "C" int msvgb_ctx_create(int device, msvgb_ctx **ret_ctx) {
   if (e == cudaSuccess) e = cudaMalloc(&c->d_ticket, sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMalloc(&c->d_meta, 4 * sizeof(int64_t));
   if (e == cudaSuccess) e = cudaMalloc(&c->d_out, 64);
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_bad, sizeof(int));
   if (e != cudaSuccess) {
     msvgb_ctx_destroy(c);
     return fail(MSVGB_eslESYS, std::string("context setup: ") + cudaGetErrorString(e));
@@ -155,7 +168,8 @@ extern "C" int msvgb_ctx_destroy(msvgb_ctx *c) {
   c->cache.clear();
   if (c->own) cudaStreamSynchronize(c->own);
   cudaFree(c->d_ticket); cudaFree(c->d_meta); cudaFree(c->d_out);
-  cudaFree(c->d_seq); cudaFree(c->d_tab);
+  cudaFree(c->d_seq); cudaFree(c->d_tab); cudaFree(c->d_bad);
+  if (c->h_stage) cudaFreeHost(c->h_stage);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
   return MSVGB_eslOK;
@@ -183,10 +197,10 @@ static int profile_build(msvgb_ctx *ctx, const msvgb_om *om, int want_f16, msvgb
   if (om->M < 1) return fail(MSVGB_eslEINVAL, "profile M must be >= 1");
   if (om->Kp != 29) return fail(MSVGB_eslEINVAL, "only the amino alphabet (Kp = 29) is supported");
   if (!om->rbv) return fail(MSVGB_eslEINVAL, "rbv is NULL");
-  const int C = choose_C(om->M);
-  if (C < 0) return fail(MSVGB_eslEINVAL, "profile M exceeds the supported maximum (3072 nodes)");
+  const bool f16 = want_f16 && need_C(om->M) <= kMaxF16C;
+  const int C = choose_C(om->M, f16);
+  if (C < 0) return fail(MSVGB_eslEINVAL, "profile M exceeds the supported maximum (3199 nodes)");
   const int M = om->M, Q = std::max(2, (M - 1) / 16 + 1), bias = om->bias_b;
-  const bool f16 = want_f16 && C <= kMaxF16C;
 
   // SSV costs s = bias - rbv clamped to [-128, 127]; nodes past M and the pad
   // residue get -128, which floors every cell (u < 128) like the reference's
@@ -200,33 +214,42 @@ static int profile_build(msvgb_ctx *ctx, const msvgb_om *om, int want_f16, msvgb
     if (x >= 29 || k > M) return 0;
     return 255 - rbv_at(om, Q, x, k);
   };
-  const size_t mwords = (size_t) NRES * (C / 2) * 32;
-  const size_t swords = f16 ? (size_t) NRES * C * 32 : mwords;
+  const int NP = (C + 1) / 2;                       // MSV table words per lane
+  const size_t mwords = (size_t) NRES * NP * 32;
+  const size_t swords = f16 ? (size_t) NRES * C * 32 : (size_t) NRES * (C / 2) * 32;
   std::vector<uint32_t> st(swords), mt(mwords);
+  auto f16bits = [](int v) -> uint32_t {
+    const __half h = __float2half((float) v);
+    uint16_t b; memcpy(&b, &h, 2); return b;
+  };
+  const int Q4 = C / 4, R = C % 4;
+  const size_t a_words = (size_t) NRES * Q4 * 32 * 4, b_words = (R >= 2) ? (size_t) NRES * 32 * 2 : 0;
   for (int x = 0; x < NRES; ++x)
     for (int l = 0; l < 32; ++l) {
-      for (int p = 0; p < C / 2; ++p) {
-        const int k0 = node_of(C, l, 2 * p, 0), k1 = node_of(C, l, 2 * p + 1, 0);
-        const int k2 = node_of(C, l, 2 * p, 1), k3 = node_of(C, l, 2 * p + 1, 1);
-        const size_t i = ((size_t) x * (C / 2) + p) * 32 + l;
-        mt[i] = (uint32_t) n_of(x, k0) | ((uint32_t) n_of(x, k1) << 8) |
-                ((uint32_t) n_of(x, k2) << 16) | ((uint32_t) n_of(x, k3) << 24);
+      for (int p = 0; p < NP; ++p) {
+        const int w0 = 2 * p, w1 = 2 * p + 1;
+        const int k0 = node_of(C, l, w0, 0), k2 = node_of(C, l, w0, 1);
+        const int k1 = w1 < C ? node_of(C, l, w1, 0) : M + 1, k3 = w1 < C ? node_of(C, l, w1, 1) : M + 1;
+        mt[((size_t) x * NP + p) * 32 + l] = (uint32_t) n_of(x, k0) | ((uint32_t) n_of(x, k1) << 8) |
+                                            ((uint32_t) n_of(x, k2) << 16) | ((uint32_t) n_of(x, k3) << 24);
         if (!f16)
-          st[i] = (uint32_t) (uint8_t) s_of(x, k0) | ((uint32_t) (uint8_t) s_of(x, k1) << 8) |
-                  ((uint32_t) (uint8_t) s_of(x, k2) << 16) | ((uint32_t) (uint8_t) s_of(x, k3) << 24);
+          st[((size_t) x * (C / 2) + p) * 32 + l] =
+              (uint32_t) (uint8_t) s_of(x, k0) | ((uint32_t) (uint8_t) s_of(x, k1) << 8) |
+              ((uint32_t) (uint8_t) s_of(x, k2) << 16) | ((uint32_t) (uint8_t) s_of(x, k3) << 24);
       }
       if (f16)
         for (int w = 0; w < C; ++w) {
-          const __half lo = __float2half((float) s_of(x, node_of(C, l, w, 0)));
-          const __half hi = __float2half((float) s_of(x, node_of(C, l, w, 1)));
-          uint16_t blo, bhi;
-          memcpy(&blo, &lo, 2); memcpy(&bhi, &hi, 2);
-          st[((size_t) x * C + w) * 32 + l] = (uint32_t) blo | ((uint32_t) bhi << 16);
+          const uint32_t v = f16bits(s_of(x, node_of(C, l, w, 0))) | (f16bits(s_of(x, node_of(C, l, w, 1))) << 16);
+          size_t i;                                  // F16Layout<C> in msv_device.cuh
+          if (w < 4 * Q4)      i = (((size_t) x * Q4 + w / 4) * 32 + l) * 4 + (w % 4);
+          else if (R >= 2 && w < 4 * Q4 + 2) i = a_words + ((size_t) x * 32 + l) * 2 + (w - 4 * Q4);
+          else                 i = a_words + b_words + (size_t) x * 32 + l;
+          st[i] = v;
         }
     }
 
   msvgb_profile *p = new msvgb_profile();
-  p->ctx = ctx; p->M = M; p->C = C; p->f16 = f16 ? 1 : 0;
+  p->ctx = ctx; p->device = ctx->device; p->M = M; p->C = C; p->f16 = f16 ? 1 : 0;
   p->tbm = om->tbm_b; p->tec = om->tec_b; p->base = om->base_b; p->bias = om->bias_b;
   p->scale = om->scale_b; p->mmu = om->mmu; p->mlambda = om->mlambda;
   cudaError_t e = cudaSetDevice(ctx->device);
@@ -243,7 +266,7 @@ static int profile_build(msvgb_ctx *ctx, const msvgb_om *om, int want_f16, msvgb
   return MSVGB_eslOK;
 }
 
-static int default_f16() { return 0; }
+static int default_f16() { return 1; }
 
 extern "C" int msvgb_profile_create(msvgb_ctx *ctx, const msvgb_om *om, msvgb_profile **ret) {
   if (!ctx) return fail(MSVGB_eslEINVAL, "ctx is NULL");
@@ -262,7 +285,7 @@ extern "C" int msvgb_profile_variant(const msvgb_profile *p) { return p ? p->f16
 
 extern "C" int msvgb_profile_destroy(msvgb_profile *p) {
   if (!p) return MSVGB_eslOK;
-  cudaSetDevice(p->ctx->device);
+  cudaSetDevice(p->device);
   for (auto &t : p->tables) { cudaFree(t.d_tjb); cudaFree(t.d_xjmin); }
   cudaFree(p->d_stab); cudaFree(p->d_mtab);
   delete p;
@@ -323,60 +346,89 @@ static int ensure_tables(msvgb_profile *p, const msvgb_db *db, double F1, LenTab
 // ------------------------------------------------------------------------------
 // database: sort by length (longest first), pad each sequence to 16 bytes
 
+// Host work is O(n + Lmax): a stable counting sort of the lengths (longest
+// first) and the padded offsets. The residues go to the device in one copy
+// (a DMA when the caller's buffer is pinned) and a kernel scatters, pads and
+// validates them.
 extern "C" int msvgb_db_create(msvgb_ctx *ctx, const uint8_t *codes, const int64_t *off, int64_t n,
                                msvgb_db **ret) {
   if (!ctx || !ret || (n > 0 && (!off || !codes))) return fail(MSVGB_eslEINVAL, "NULL argument");
   *ret = nullptr;
   if (n < 0) return fail(MSVGB_eslEINVAL, "n < 0");
-  std::vector<int64_t> idx(n);
   int Lmax = 0;
   for (int64_t i = 0; i < n; ++i) {
     const int64_t L = off[i + 1] - off[i];
     if (L < 0 || L > (int64_t) 100000000) return fail(MSVGB_eslEINVAL, "bad sequence offsets");
-    Lmax = std::max<int>(Lmax, (int) L);
-    idx[i] = i;
+    if (L > Lmax) Lmax = (int) L;
   }
-  for (int64_t i = 0; i < off[n] - off[0]; ++i)
-    if (codes[off[0] + i] >= 29) return fail(MSVGB_eslEINVAL, "residue code >= 29 (Kp)");
-  std::stable_sort(idx.begin(), idx.end(), [&](int64_t a, int64_t b) {
-    return off[a + 1] - off[a] > off[b + 1] - off[b];
-  });
-  std::vector<int64_t> start(n), orig(n);
-  std::vector<int32_t> len(n);
+  // stable counting sort, descending length
+  std::vector<int64_t> first(Lmax + 2, 0);
+  for (int64_t i = 0; i < n; ++i) first[off[i + 1] - off[i]]++;
+  std::vector<int32_t> distinct;
+  int64_t acc = 0;
+  for (int L = Lmax; L >= 0; --L) {
+    const int64_t cnt = first[L];
+    first[L] = acc;
+    acc += cnt;
+    if (cnt) distinct.push_back(L);
+  }
+  std::reverse(distinct.begin(), distinct.end());
+  // metadata in pinned staging: start, orig, src (int64) and len (int32) per sorted slot
+  const size_t need = (size_t) std::max<int64_t>(n, 1) * (3 * 8 + 4);
+  if (ctx->h_stage_cap < need) {
+    if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+    ctx->h_stage = nullptr; ctx->h_stage_cap = 0;
+    CUDA_TRY(cudaMallocHost(&ctx->h_stage, need));
+    ctx->h_stage_cap = need;
+  }
+  CUDA_TRY(cudaStreamSynchronize(ctx->stream));          // the staging buffer may still feed a copy
+  int64_t *h_start = (int64_t *) ctx->h_stage, *h_orig = h_start + n, *h_src = h_orig + n;
+  int32_t *h_len = (int32_t *) (h_src + n);
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t L = off[i + 1] - off[i], s = first[L]++;
+    h_orig[s] = i; h_len[s] = (int32_t) L; h_src[s] = off[i] - off[0];
+  }
   int64_t pos = 0;
-  for (int64_t s = 0; s < n; ++s) {
-    const int64_t i = idx[s], L = off[i + 1] - off[i];
-    start[s] = pos; orig[s] = i; len[s] = (int32_t) L;
-    pos += ((L + 15) / 16) * 16;
-  }
+  for (int64_t s = 0; s < n; ++s) { h_start[s] = pos; pos += ((int64_t) h_len[s] + 15) / 16 * 16; }
   const int64_t bytes = pos + 64;                 // tail so a 16-byte over-read stays inside
-  std::vector<uint8_t> packed(bytes, (uint8_t) PAD_CODE);
-  for (int64_t s = 0; s < n; ++s) {
-    const int64_t i = orig[s];
-    memcpy(packed.data() + start[s], codes + off[i], (size_t) len[s]);
-  }
+  const int64_t total = n ? off[n] - off[0] : 0;
+
   msvgb_db *db = new msvgb_db();
-  db->ctx = ctx; db->n = n; db->residues = off[n] - off[0]; db->Lmax = Lmax;
+  db->ctx = ctx; db->device = ctx->device; db->n = n; db->residues = total; db->Lmax = Lmax;
   db->serial = g_db_serial.fetch_add(1);
-  {
-    std::vector<int32_t> dl(len.begin(), len.end());
-    std::sort(dl.begin(), dl.end());
-    dl.erase(std::unique(dl.begin(), dl.end()), dl.end());
-    db->distinct_len = std::move(dl);
-  }
+  db->distinct_len = std::move(distinct);
+  cudaStream_t st = ctx->stream;
+  uint8_t *d_raw = nullptr; int64_t *d_src = nullptr;
+  int bad = 0;
   cudaError_t e = cudaSetDevice(ctx->device);
   if (e == cudaSuccess) e = cudaMalloc(&db->d_codes, bytes);
   if (e == cudaSuccess) e = cudaMalloc(&db->d_start, std::max<int64_t>(n, 1) * 8);
   if (e == cudaSuccess) e = cudaMalloc(&db->d_orig, std::max<int64_t>(n, 1) * 8);
   if (e == cudaSuccess) e = cudaMalloc(&db->d_len, std::max<int64_t>(n, 1) * 4);
-  if (e == cudaSuccess) e = cudaMemcpy(db->d_codes, packed.data(), bytes, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess && n) e = cudaMemcpy(db->d_start, start.data(), n * 8, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess && n) e = cudaMemcpy(db->d_orig, orig.data(), n * 8, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess && n) e = cudaMemcpy(db->d_len, len.data(), n * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMallocAsync((void **) &d_raw, std::max<int64_t>(total, 1), st);
+  if (e == cudaSuccess) e = cudaMallocAsync((void **) &d_src, std::max<int64_t>(n, 1) * 8, st);
+  if (e == cudaSuccess && total) e = cudaMemcpyAsync(d_raw, codes + off[0], total, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && n) e = cudaMemcpyAsync(db->d_start, h_start, n * 8, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && n) e = cudaMemcpyAsync(db->d_orig, h_orig, n * 8, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && n) e = cudaMemcpyAsync(d_src, h_src, n * 8, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && n) e = cudaMemcpyAsync(db->d_len, h_len, n * 4, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_bad, 0, sizeof(int), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(db->d_codes + pos, PAD_CODE, 64, st);
+  if (e == cudaSuccess) e = launch_pack(d_raw, d_src, db->d_start, db->d_len, n, db->d_codes, ctx->d_bad,
+                                        ctx->num_sms, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, ctx->d_bad, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (d_raw) cudaFreeAsync(d_raw, st);
+  if (d_src) cudaFreeAsync(d_src, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess && n) count_launch();
   if (e != cudaSuccess) {
     msvgb_db_destroy(db);
     return fail(e == cudaErrorMemoryAllocation ? MSVGB_eslEMEM : MSVGB_eslESYS,
                 std::string("database upload: ") + cudaGetErrorString(e));
+  }
+  if (bad) {
+    msvgb_db_destroy(db);
+    return fail(MSVGB_eslEINVAL, "residue code >= 29 (Kp)");
   }
   *ret = db;
   return MSVGB_eslOK;
@@ -384,7 +436,7 @@ extern "C" int msvgb_db_create(msvgb_ctx *ctx, const uint8_t *codes, const int64
 
 extern "C" int msvgb_db_destroy(msvgb_db *db) {
   if (!db) return MSVGB_eslOK;
-  cudaSetDevice(db->ctx->device);
+  cudaSetDevice(db->device);
   cudaFree(db->d_codes); cudaFree(db->d_start); cudaFree(db->d_orig); cudaFree(db->d_len);
   delete db;
   return MSVGB_eslOK;

@@ -79,11 +79,14 @@ __device__ __forceinline__ uint32_t max_f16x2(uint32_t a, uint32_t b) {
   uint32_t d; asm("max.f16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b)); return d;
 }
 
-// Diagonal predecessor of DP word 0: low half <- high half of lane-1's word C-1
-// (node 0 / begin for lane 0), high half <- low half of this lane's word C-1.
-__device__ __forceinline__ uint32_t pred_word0(uint32_t last, int lane) {
-  uint32_t up = __shfl_up_sync(FULL, last, 1);
-  up = lane ? up : 0u;             // 0 is the begin/floor value in both phases
+// Diagonal predecessor of DP word 0: low half <- high half of lane-1's word C-1,
+// high half <- low half of this lane's word C-1. Lane 0 reads lane 31, whose
+// last node 64*C is always a padding node (the host picks C with 64*C > M):
+// its cell is 0 -- the begin/floor value node 0 must supply -- in phase B
+// always, and in phase A whenever no cell has reached the overflow bound
+// (after that the outcome no longer depends on any cell value).
+__device__ __forceinline__ uint32_t pred_word0(uint32_t last, int src_lane) {
+  const uint32_t up = __shfl_sync(FULL, last, src_lane);
   return prmt(last, up, 0x1076u);  // bytes [up.b2, up.b3, last.b0, last.b1]
 }
 
@@ -91,8 +94,9 @@ __device__ __forceinline__ uint32_t pred_word0(uint32_t last, int lane) {
 // Table word (x, p, lane) bytes: [s(2p,h0), s(2p+1,h0), s(2p,h1), s(2p+1,h1)].
 template <int C>
 __device__ __forceinline__ void ssv_row_i8(uint32_t (&dp)[C], uint32_t &acc0, uint32_t &acc1,
-                                           const uint32_t *__restrict__ t, int lane) {
-  const uint32_t pred0 = pred_word0(dp[C - 1], lane);
+                                           const uint32_t *__restrict__ t, int src_lane) {
+  static_assert(C % 2 == 0, "the int8 table packs two DP words per table word");
+  const uint32_t pred0 = pred_word0(dp[C - 1], src_lane);
 #pragma unroll
   for (int p = C / 2 - 1; p >= 0; --p) {
     const uint32_t tw = t[p * 32];
@@ -105,16 +109,40 @@ __device__ __forceinline__ void ssv_row_i8(uint32_t (&dp)[C], uint32_t &acc0, ui
   }
 }
 
-// ---- Phase A: SSV row, f16 table (one f16x2 word per DP word) --------------------
+// ---- Phase A: SSV row, f16 table ----------------------------------------------
+// One f16x2 cost word per DP word. For residue x the lane's C words sit in
+// up to three lane-contiguous regions so that every load is a conflict-free
+// vector load: quads [x][q][lane][4] (LDS.128), then a pair [x][lane][2]
+// (LDS.64) if C%4 >= 2, then a single [x][lane] (LDS.32) if C is odd.
+template <int C>
+struct F16Layout {
+  static constexpr int Q4 = C / 4, R = C % 4;
+  static constexpr int A_WORDS = NRES * Q4 * 32 * 4;                 // quads
+  static constexpr int B_WORDS = (R >= 2) ? NRES * 32 * 2 : 0;       // pair
+  static constexpr int C_WORDS = (R & 1) ? NRES * 32 : 0;            // single
+  static constexpr int WORDS = A_WORDS + B_WORDS + C_WORDS;          // == NRES * 32 * C
+};
+
 template <int C>
 __device__ __forceinline__ void ssv_row_f16(uint32_t (&dp)[C], uint32_t &acc0, uint32_t &acc1,
-                                            const uint32_t *__restrict__ t, int lane) {
-  const uint32_t one2 = 0x3C003C00u;             // f16x2 (1.0, 1.0)
-  const uint32_t pred0 = pred_word0(dp[C - 1], lane);
+                                            const uint32_t *__restrict__ tab, int x, int lane, int src_lane) {
+  using Lay = F16Layout<C>;
+  constexpr uint32_t one2 = 0x3C003C00u;        // f16x2 (1.0, 1.0)
+  uint32_t s[C];
+#pragma unroll
+  for (int q = 0; q < Lay::Q4; ++q) {
+    const uint4 v = *reinterpret_cast<const uint4 *>(tab + ((x * Lay::Q4 + q) * 32 + lane) * 4);
+    s[4 * q] = v.x; s[4 * q + 1] = v.y; s[4 * q + 2] = v.z; s[4 * q + 3] = v.w;
+  }
+  if constexpr (Lay::R >= 2) {
+    const uint2 v = *reinterpret_cast<const uint2 *>(tab + Lay::A_WORDS + (x * 32 + lane) * 2);
+    s[4 * Lay::Q4] = v.x; s[4 * Lay::Q4 + 1] = v.y;
+  }
+  if constexpr (Lay::R & 1) s[C - 1] = tab[Lay::A_WORDS + Lay::B_WORDS + x * 32 + lane];
+  const uint32_t pred0 = pred_word0(dp[C - 1], src_lane);
 #pragma unroll
   for (int w = C - 1; w >= 0; --w) {
-    const uint32_t s = t[w * 32];
-    dp[w] = fma_relu_f16x2(w ? dp[w - 1] : pred0, one2, s);
+    dp[w] = fma_relu_f16x2(w ? dp[w - 1] : pred0, one2, s[w]);
     if (w & 1) acc1 = max_f16x2(acc1, dp[w]); else acc0 = max_f16x2(acc0, dp[w]);
   }
 }
@@ -126,18 +154,21 @@ __device__ __forceinline__ void ssv_row_f16(uint32_t (&dp)[C], uint32_t &acc0, u
 // previous row's overflow test (xE + bias >= 255 -> ERANGE) did not fire.
 template <int C>
 __device__ __forceinline__ uint32_t msv_row(uint32_t (&dp)[C], uint32_t xBp, uint32_t kneg,
-                                            const uint32_t *__restrict__ t, int lane) {
-  const uint32_t pred0 = pred_word0(dp[C - 1], lane);
+                                            const uint32_t *__restrict__ t, int src_lane) {
+  constexpr int NP = (C + 1) / 2;                 // table words per lane: 4 nodes each
+  const uint32_t pred0 = pred_word0(dp[C - 1], src_lane);
   uint32_t acc0 = 0u, acc1 = 0u;
 #pragma unroll
-  for (int p = C / 2 - 1; p >= 0; --p) {
+  for (int p = NP - 1; p >= 0; --p) {
     const uint32_t tw = t[p * 32];
     const uint32_t nA = tw & 0x00FF00FFu;          // bytes 0,2 zero-extended
     const uint32_t nB = (tw >> 8) & 0x00FF00FFu;   // bytes 1,3 zero-extended
     // halves of max(..) and n are <= 255: a 32-bit add cannot carry across halves
-    dp[2 * p + 1] = max_relu_s16x2(add_s16x2(max_s16x2(dp[2 * p], xBp) + nB, kneg), 0u);
-    dp[2 * p]     = max_relu_s16x2(add_s16x2(max_s16x2(p ? dp[2 * p - 1] : pred0, xBp) + nA, kneg), 0u);
-    acc1 = max_s16x2(acc1, dp[2 * p + 1]);
+    if (2 * p + 1 < C) {
+      dp[2 * p + 1] = max_relu_s16x2(add_s16x2(max_s16x2(dp[2 * p], xBp) + nB, kneg), 0u);
+      acc1 = max_s16x2(acc1, dp[2 * p + 1]);
+    }
+    dp[2 * p] = max_relu_s16x2(add_s16x2(max_s16x2(p ? dp[2 * p - 1] : pred0, xBp) + nA, kneg), 0u);
     acc0 = max_s16x2(acc0, dp[2 * p]);
   }
   const uint32_t a = max_s16x2(acc0, acc1);
@@ -161,8 +192,7 @@ __device__ __forceinline__ int msv_one(const ProfDev &P, const uint32_t *__restr
 #pragma unroll
     for (int w = 0; w < C; ++w) dp[w] = 0u;
     uint32_t acc0 = 0u, acc1 = 0u;
-    constexpr int TSTRIDE = F16 ? C * 32 : (C / 2) * 32;
-    const uint32_t *tl = stab + lane;
+    const int src_lane = (lane + 31) & 31;
     uint32_t nextw = (L > 0) ? __ldg(sq) : 0u;
     for (int i0 = 0; i0 < L; i0 += 4) {
       const uint32_t w4 = nextw;
@@ -172,12 +202,12 @@ __device__ __forceinline__ int msv_one(const ProfDev &P, const uint32_t *__restr
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const int x = (w4 >> (8 * j)) & 0xFF;
-        if (F16) ssv_row_f16<C>(dp, acc0, acc1, tl + x * TSTRIDE, lane);
-        else     ssv_row_i8<C>(dp, acc0, acc1, tl + x * TSTRIDE, lane);
+        if constexpr (F16) ssv_row_f16<C>(dp, acc0, acc1, stab, x, lane, src_lane);
+        else               ssv_row_i8<C>(dp, acc0, acc1, stab + lane + x * ((C / 2) * 32), src_lane);
       }
     }
     int umax;
-    if (F16) {
+    if constexpr (F16) {
       const __half2 a = __hmax2(*reinterpret_cast<const __half2 *>(&acc0),
                                 *reinterpret_cast<const __half2 *>(&acc1));
       float f = fmaxf(__low2float(a), __high2float(a));
@@ -218,6 +248,7 @@ __device__ __forceinline__ int msv_one(const ProfDev &P, const uint32_t *__restr
   int xJ = 0, xB = max(base - tjbm, 0);
   const uint32_t kneg = ((uint32_t) (bias - 255) & 0xFFFFu) * 0x00010001u;
   const uint32_t *tl = mtab + lane;
+  const int src_lane = (lane + 31) & 31;
   uint32_t nextw = (L > 0) ? __ldg(sq) : 0u;
   for (int i0 = 0; i0 < L; i0 += 4) {
     const uint32_t w4 = nextw;
@@ -227,7 +258,7 @@ __device__ __forceinline__ int msv_one(const ProfDev &P, const uint32_t *__restr
       if (i0 + j < L) {
         const int x = (w4 >> (8 * j)) & 0xFF;
         const uint32_t xBp = (uint32_t) min(xB, 255 - bias) * 0x00010001u;
-        uint32_t r = msv_row<C>(dp, xBp, kneg, tl + x * ((C / 2) * 32), lane);
+        uint32_t r = msv_row<C>(dp, xBp, kneg, tl + x * (((C + 1) / 2) * 32), src_lane);
         const int xE = (int) __reduce_max_sync(FULL, r);
         if (xE + bias >= 255) { xj_out = 255; return ST_ERANGE; }   // adds(xE,bias)==255
         xJ = max(xJ, max(xE - tec, 0));

@@ -25,6 +25,8 @@ struct msvgb_ctx {
   uint8_t *d_tab = nullptr; size_t d_tab_cap = 0;
   int64_t *d_meta = nullptr;                            // start, orig (int64), len (int32) for n=1
   uint8_t *d_out = nullptr;
+  int *d_bad = nullptr;                                 // database packing: invalid-code flag
+  void *h_stage = nullptr; size_t h_stage_cap = 0;      // pinned staging for database metadata
 };
 
 struct LenTables {      // per (profile, database, F1)
@@ -36,6 +38,7 @@ struct LenTables {      // per (profile, database, F1)
 
 struct msvgb_profile {
   msvgb_ctx *ctx = nullptr;
+  int device = 0;            // own copy: destroy must not touch ctx (it may be gone)
   int M = 0, C = 0, f16 = 0;
   uint8_t tbm = 0, tec = 0, base = 0, bias = 0;
   float scale = 0.f, mmu = 0.f, mlambda = 0.f;
@@ -45,6 +48,7 @@ struct msvgb_profile {
 
 struct msvgb_db {
   msvgb_ctx *ctx = nullptr;
+  int device = 0;            // own copy: destroy must not touch ctx (it may be gone)
   int64_t n = 0, residues = 0;
   int Lmax = 0;
   uint8_t *d_codes = nullptr;
@@ -64,4 +68,8 @@ cudaError_t dispatch(int C, bool f16, const msvgb::LaunchArgs &a, int sms);
 int xjmin_for(const msvgb_profile *p, int L, double F1);
 // Adds one to the count msvgb_kernel_launches() reports.
 void count_launch();
+// Scatters raw residues into the packed database layout (msv_pack.cu); sets
+// *bad to nonzero if any code is >= 29.
+cudaError_t launch_pack(const uint8_t *raw, const int64_t *src, const int64_t *start, const int32_t *len,
+                        int64_t n, uint8_t *packed, int *bad, int num_sms, cudaStream_t stream);
 }  // namespace msvgb_detail

@@ -20,8 +20,8 @@ struct LaunchArgs {
 constexpr int WARPS_PER_CTA = 8;
 
 template <int C, bool F16>
-constexpr size_t smem_bytes() {
-  return ((size_t) (F16 ? NRES * C * 32 : NRES * (C / 2) * 32) + (size_t) NRES * (C / 2) * 32) * 4;
+constexpr size_t smem_bytes() {   // SSV table + MSV table
+  return ((size_t) (F16 ? NRES * C * 32 : NRES * (C / 2) * 32) + (size_t) NRES * ((C + 1) / 2) * 32) * 4;
 }
 
 // Persistent kernel: every CTA stages the profile's cost tables into shared
@@ -33,7 +33,7 @@ msv_search_kernel(ProfDev P, DbDev db, uint8_t *__restrict__ out_xj, uint8_t *__
                   unsigned long long *__restrict__ ticket, int skip_empty) {
   extern __shared__ __align__(16) uint32_t smem[];
   constexpr int SW = F16 ? NRES * C * 32 : NRES * (C / 2) * 32;   // words of the SSV table
-  constexpr int MW = NRES * (C / 2) * 32;                          // words of the MSV table
+  constexpr int MW = NRES * ((C + 1) / 2) * 32;                    // words of the MSV table
   uint32_t *stab = smem;
   uint32_t *mtab = smem + SW;
   {
@@ -91,6 +91,7 @@ cudaError_t launch_search(const LaunchArgs &a, int num_sms) {
     const long long need = (a.db.n + WARPS_PER_CTA - 1) / WARPS_PER_CTA;
     if (need < grid) grid = (int) (need > 0 ? need : 1);
   }
+  (void) cudaGetLastError();   // clear a stale error left by an unrelated call
   kern<<<grid, WARPS_PER_CTA * 32, smem, a.stream>>>(a.P, a.db, a.out_xj, a.out_flags, a.ticket, a.skip_empty);
   return cudaGetLastError();
 }

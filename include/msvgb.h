@@ -55,6 +55,8 @@ typedef struct {
   int M;
 } msvgb_omx;
 
+/* Objects created on a context (profiles, databases) may be destroyed before
+ * or after it; searches need their context alive. */
 typedef struct msvgb_ctx     msvgb_ctx;      /* one GPU, one stream, device buffers   */
 typedef struct msvgb_profile msvgb_profile;  /* a profile resident in HBM             */
 typedef struct msvgb_db      msvgb_db;       /* a packed sequence database in HBM     */
@@ -117,6 +119,13 @@ int msvgb_search(msvgb_ctx *ctx, const msvgb_profile *prof, const msvgb_db *db, 
  * pointers), asynchronous on the context's stream. */
 int msvgb_search_device(msvgb_ctx *ctx, const msvgb_profile *prof, const msvgb_db *db, double F1,
                         void *d_xj, void *d_flags);
+
+/* ---- measurement ------------------------------------------------------------------
+ * Sustained rate of independent 32-bit integer operations over all SMs of the
+ * device (ops/s), measured by a short kernel: the denominator of the
+ * integer-pipe roofline (one DP cell = one packed 32-bit op). No reference
+ * counterpart. */
+int msvgb_measure_int_peak(int device, double *ops_per_second);
 
 /* ---- allocation-free search ------------------------------------------------------
  * No counterpart in the reference. For callers that cannot allocate device

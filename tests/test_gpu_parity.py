@@ -159,7 +159,7 @@ def test_invalid_inputs_rejected(ctx):
     with pytest.raises(api.MSVError) as e:
         api.DeviceDB(ctx, bad)
     assert e.value.code == api.eslEINVAL
-    big = F.profile_from_node_costs(np.zeros((29, 3073), np.uint8), tbm_b=10, tec_b=3, base_b=190,
+    big = F.profile_from_node_costs(np.zeros((29, 3200), np.uint8), tbm_b=10, tec_b=3, base_b=190,
                                     bias_b=10, scale_b=4.328085, mmu=-9.0, mlambda=0.69)
     with pytest.raises(api.MSVError) as e:
         api.DeviceProfile(ctx, big)
@@ -168,6 +168,7 @@ def test_invalid_inputs_rejected(ctx):
 
 def test_kernel_launch_counter_advances(ctx):
     p, s, _ = load_case("m50_s1")
+    prof, db = api.DeviceProfile(ctx, p), api.DeviceDB(ctx, s)
     before = api.kernel_launches()
-    api.search(ctx, api.DeviceProfile(ctx, p), api.DeviceDB(ctx, s))
+    api.search(ctx, prof, db)
     assert api.kernel_launches() == before + 1
