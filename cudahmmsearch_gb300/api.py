@@ -27,7 +27,8 @@ EXPORTS = [
     "msvgb_kernel_launches", "msvgb_MSVFilter", "msvgb_profile_create", "msvgb_profile_destroy",
     "msvgb_profile_M", "msvgb_profile_create_ex", "msvgb_profile_variant", "msvgb_db_create", "msvgb_db_destroy", "msvgb_db_nseq", "msvgb_db_residues",
     "msvgb_search", "msvgb_search_device", "msvgb_tjb_b", "msvgb_score", "msvgb_f1_pass",
-    "msvgb_search_static", "msvgb_measure_int_peak",
+    "msvgb_search_static", "msvgb_measure_int_peak", "msvgb_sample_om", "msvgb_calibrate",
+    "msvgb_batch_create", "msvgb_batch_run", "msvgb_batch_items", "msvgb_batch_destroy", "msvgb_search_batch",
 ]
 
 
@@ -84,6 +85,13 @@ def lib():
         "msvgb_f1_pass": (i32, [f32, i32, f32, f32, f64, ctypes.POINTER(f64)]),
         "msvgb_search_static": (i32, [vp, vp, f64, vp, vp, vp]),
         "msvgb_measure_int_peak": (i32, [i32, ctypes.POINTER(f64)]),
+        "msvgb_sample_om": (i32, [ctypes.c_uint32, i32, vp, ctypes.POINTER(_Om), ctypes.POINTER(f64)]),
+        "msvgb_calibrate": (i32, [vp, ctypes.POINTER(_Om), f64]),
+        "msvgb_batch_create": (i32, [vp, vp, i32, vp, f64, vp, vp, ctypes.POINTER(vp)]),
+        "msvgb_batch_run": (i32, [vp]),
+        "msvgb_batch_items": (i64, [vp]),
+        "msvgb_batch_destroy": (i32, [vp]),
+        "msvgb_search_batch": (i32, [vp, vp, i32, vp, f64, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -208,11 +216,73 @@ def search_device(ctx: Context, prof: DeviceProfile, db: DeviceDB, d_xj: int, d_
     _check(lib().msvgb_search_device(ctx.h, prof.h, db.h, F1, ctypes.c_void_p(d_xj), ctypes.c_void_p(d_flags)))
 
 
+def sample_profile(M: int, seed: int, ctx: "Context | None" = None) -> F.Profile:
+    """A profile sampled as HMMER's p7_hmm_Sample(seed) + p7_ProfileConfig +
+    p7_oprofile_Convert would make it; with a context, also calibrated
+    (p7_MSVMu on the GPU), else mmu = 0."""
+    Q = F.nqb(M)
+    rbv = np.zeros((F.KP_AMINO, Q, 16), np.uint8)
+    om = _Om()
+    lam = ctypes.c_double()
+    _check(lib().msvgb_sample_om(seed, M, rbv.ctypes.data, ctypes.byref(om), ctypes.byref(lam)))
+    if ctx is not None:
+        _check(lib().msvgb_calibrate(ctx.h, ctypes.byref(om), lam.value))
+    return F.Profile(M=M, rbv=rbv, tbm_b=om.tbm_b, tec_b=om.tec_b, base_b=om.base_b, bias_b=om.bias_b,
+                     scale_b=float(np.float32(om.scale_b)), mmu=float(np.float32(om.mmu)),
+                     mlambda=float(np.float32(om.mlambda)))
+
+
 def measure_int_peak(device: int = 0) -> float:
     """Sustained 32-bit integer ops/s over all SMs (integer-pipe roofline denominator)."""
     v = ctypes.c_double()
     _check(lib().msvgb_measure_int_peak(device, ctypes.byref(v)))
     return v.value
+
+
+def _om_array(profiles):
+    structs, keep = [], []
+    for p in profiles:
+        o, k = _om_struct(p)
+        structs.append(o)
+        keep.append(k)
+    arr = (ctypes.POINTER(_Om) * len(structs))(*[ctypes.pointer(o) for o in structs])
+    return arr, (structs, keep)
+
+
+def search_batch(ctx: Context, profiles, db: DeviceDB, F1: float = 0.02):
+    """Many profiles in one persistent launch. Returns (xj, flags) as uint8 [nprof, n]."""
+    arr, keep = _om_array(profiles)
+    xj = np.zeros((len(profiles), db.n), np.uint8)
+    fl = np.zeros((len(profiles), db.n), np.uint8)
+    _check(lib().msvgb_search_batch(ctx.h, ctypes.cast(arr, ctypes.c_void_p), len(profiles), db.h, F1,
+                                    xj.ctypes.data, fl.ctypes.data))
+    return xj, fl
+
+
+class Batch:
+    """A captured batched search (msvgb_batch): run() replays the CUDA graph."""
+
+    def __init__(self, ctx: Context, profiles, db: DeviceDB, d_xj: int, d_flags: int, F1: float = 0.02):
+        arr, keep = _om_array(profiles)
+        h = ctypes.c_void_p()
+        _check(lib().msvgb_batch_create(ctx.h, ctypes.cast(arr, ctypes.c_void_p), len(profiles), db.h, F1,
+                                        ctypes.c_void_p(d_xj), ctypes.c_void_p(d_flags), ctypes.byref(h)))
+        self.h = h
+        self.items = int(lib().msvgb_batch_items(h))
+
+    def run(self):
+        _check(lib().msvgb_batch_run(self.h))
+
+    def close(self):
+        if self.h:
+            lib().msvgb_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def tjb_b(scale_b: float, L: int) -> int:

@@ -192,14 +192,18 @@ static inline int rbv_at(const msvgb_om *om, int Q, int x, int k) {   // k = 1..
 // node held by DP word w, half h of lane l (1-based)
 static inline int node_of(int C, int lane, int w, int h) { return lane * 2 * C + h * C + w + 1; }
 
-static int profile_build(msvgb_ctx *ctx, const msvgb_om *om, int want_f16, msvgb_profile **ret) {
+// Builds the device tables of a profile. force_C > 0 imposes the DP width
+// (the batched kernel uses a coarser set of widths); it must exceed M/64.
+int msvgb_detail::profile_build_width(msvgb_ctx *ctx, const msvgb_om *om, int want_f16, int force_C,
+                                      msvgb_profile **ret) {
   if (!om || !ret) return fail(MSVGB_eslEINVAL, "NULL argument");
   if (om->M < 1) return fail(MSVGB_eslEINVAL, "profile M must be >= 1");
   if (om->Kp != 29) return fail(MSVGB_eslEINVAL, "only the amino alphabet (Kp = 29) is supported");
   if (!om->rbv) return fail(MSVGB_eslEINVAL, "rbv is NULL");
-  const bool f16 = want_f16 && need_C(om->M) <= kMaxF16C;
-  const int C = choose_C(om->M, f16);
+  const bool f16 = want_f16 && (force_C > 0 ? force_C : need_C(om->M)) <= kMaxF16C;
+  const int C = force_C > 0 ? force_C : choose_C(om->M, f16);
   if (C < 0) return fail(MSVGB_eslEINVAL, "profile M exceeds the supported maximum (3199 nodes)");
+  if (C < need_C(om->M) || (!f16 && (C & 1))) return fail(MSVGB_eslEINVAL, "DP width too small for M");
   const int M = om->M, Q = std::max(2, (M - 1) / 16 + 1), bias = om->bias_b;
 
   // SSV costs s = bias - rbv clamped to [-128, 127]; nodes past M and the pad
@@ -266,6 +270,10 @@ static int profile_build(msvgb_ctx *ctx, const msvgb_om *om, int want_f16, msvgb
   return MSVGB_eslOK;
 }
 
+static int profile_build(msvgb_ctx *ctx, const msvgb_om *om, int want_f16, msvgb_profile **ret) {
+  return msvgb_detail::profile_build_width(ctx, om, want_f16, 0, ret);
+}
+
 static int default_f16() { return 1; }
 
 extern "C" int msvgb_profile_create(msvgb_ctx *ctx, const msvgb_om *om, msvgb_profile **ret) {
@@ -313,7 +321,7 @@ int msvgb_detail::xjmin_for(const msvgb_profile *p, int L, double F1) {
   return lo;
 }
 
-static int ensure_tables(msvgb_profile *p, const msvgb_db *db, double F1, LenTables **out) {
+int msvgb_detail::ensure_tables(msvgb_profile *p, const msvgb_db *db, double F1, LenTables **out) {
   for (auto &t : p->tables)
     if (t.db == db && t.F1 == F1) { *out = &t; return MSVGB_eslOK; }
   const int Lmax = db->Lmax;

@@ -66,6 +66,10 @@ cudaError_t dispatch(int C, bool f16, const msvgb::LaunchArgs &a, int sms);
 // Smallest xJ passing the F1 gate at length L (255: none); -1 if the pass set
 // is not monotone in xJ.
 int xjmin_for(const msvgb_profile *p, int L, double F1);
+// Device tables of a profile; force_C > 0 imposes the DP width.
+int profile_build_width(msvgb_ctx *ctx, const msvgb_om *om, int want_f16, int force_C, msvgb_profile **ret);
+// Per-length tjb_b and pass-threshold tables of (profile, database, F1), cached in the profile.
+int ensure_tables(msvgb_profile *p, const msvgb_db *db, double F1, LenTables **out);
 // Adds one to the count msvgb_kernel_launches() reports.
 void count_launch();
 // Scatters raw residues into the packed database layout (msv_pack.cu); sets

@@ -120,6 +120,20 @@ int msvgb_search(msvgb_ctx *ctx, const msvgb_profile *prof, const msvgb_db *db, 
 int msvgb_search_device(msvgb_ctx *ctx, const msvgb_profile *prof, const msvgb_db *db, double F1,
                         void *d_xj, void *d_flags);
 
+/* ---- profile preparation ----------------------------------------------------------
+ * Sample a random profile HMM of M nodes exactly as HMMER's p7_hmm_Sample does
+ * with esl_randomness_Create(seed) (src/p7_hmm.c:877-918), configure its match
+ * scores against the amino background (p7_ProfileConfig, src/modelconfig.c:165-176)
+ * and convert them to the MSV bytes (mf_conversion, src/impl_sse/p7_oprofile.c:601-640).
+ * rbv must hold Kp * max(2, ceil(M/16)) * 16 = 29 * Q * 16 bytes; om->rbv points
+ * to it. om->mlambda and *ret_lambda get p7_Lambda (src/evalues.c:186-192);
+ * om->mmu is left 0 until msvgb_calibrate. Host only. */
+int msvgb_sample_om(uint32_t seed, int M, uint8_t *rbv, msvgb_om *om, double *ret_lambda);
+/* p7_MSVMu (src/evalues.c:240-283) with p7_Calibrate's default RNG and sizes
+ * (esl_randomness_CreateFast(42), 200 sequences of length 200): scores them
+ * with this library's GPU search and sets om->mmu (and om->mlambda = lambda). */
+int msvgb_calibrate(msvgb_ctx *ctx, msvgb_om *om, double lambda);
+
 /* ---- measurement ------------------------------------------------------------------
  * Sustained rate of independent 32-bit integer operations over all SMs of the
  * device (ops/s), measured by a short kernel: the denominator of the
@@ -148,6 +162,24 @@ int msvgb_measure_int_peak(int device, double *ops_per_second);
 #define MSVGB_STATIC_MAX_LEN 65535
 int msvgb_search_static(const msvgb_profile *prof, const msvgb_db *db, double F1,
                         void *d_xj, void *d_flags, void *cuda_stream);
+
+/* ---- batched search: many profiles, one persistent launch ------------------------
+ * All nprof profiles (M <= 2047 each) against db in a single persistent kernel
+ * over a (profile, sequence-chunk) work queue, captured once as a CUDA graph;
+ * each msvgb_batch_run replays it asynchronously on the context's stream.
+ * Outputs are device buffers of nprof * n bytes, profile-major:
+ * d_xj[p * n + i], d_flags[p * n + i] as msvgb_search writes them.
+ * The stock hmmsearch scores one query at a time (src/hmmsearch.c:356-560);
+ * this is the multi-query form of its MSV stage. */
+typedef struct msvgb_batch msvgb_batch;
+int     msvgb_batch_create(msvgb_ctx *ctx, const msvgb_om *const *oms, int nprof, const msvgb_db *db,
+                           double F1, void *d_xj, void *d_flags, msvgb_batch **ret_batch);
+int     msvgb_batch_run(msvgb_batch *batch);
+int64_t msvgb_batch_items(const msvgb_batch *batch);
+int     msvgb_batch_destroy(msvgb_batch *batch);
+/* Convenience: create, run once, copy the nprof * n results to host buffers, destroy. */
+int     msvgb_search_batch(msvgb_ctx *ctx, const msvgb_om *const *oms, int nprof, const msvgb_db *db,
+                           double F1, uint8_t *out_xj, uint8_t *out_flags);
 
 /* ---- host-side score helpers (exact reference expressions) --------------------- */
 /* tjb_b for target length L (p7_oprofile.c:511-519, 920-925). */
