@@ -35,6 +35,10 @@ sys.path.insert(0, ROOT)
 from cudahmmsearch_gb300 import formats as F  # noqa: E402
 
 INT_LANE_OPS_PER_CLK_PER_SM = 128   # 4 SM sub-partitions x 32 lanes: nominal issue width
+# DRAM bytes per residue per search launch, from the ncu capture summarised in
+# profiles/msv_search_kernel_f16_m400_400k.md (169.4 MB for 154.56 M residues);
+# the launch reads each residue once, so traffic scales with the residue count.
+DRAM_BYTES_PER_RESIDUE = 169.4e6 / 154.56e6
 
 
 def workload(name, rank=0):
@@ -53,6 +57,14 @@ def workload(name, rank=0):
         s = F.SeqSet.concat([F.synth_sequences(392_000, seed=1000 + rank, lmax=35000),
                              F.emit_homologs(p, 8_000, seed=2000 + rank, lmax=35000)])
         cfg = {"workload": "plain MSV, M=400 vs 400,000 seqs (same distribution as m400_2M)",
+               "M": p.M, "n_seqs": s.n, "residues": s.total, "l2_flush": "inputs larger than L2 (129 MB)"}
+        return p, s, cfg
+    if name == "m2400_200k":  # length extremes: long targets and overflow-to-infinity
+        p = F.read_profile(os.path.join(ROOT, "tests", "golden", "m2400_s1.prof"))
+        s = F.SeqSet.concat([F.synth_sequences(199_000, seed=7000 + rank, lmax=35000, uniform_frac=0.1),
+                             F.emit_homologs(p, 1_000, seed=7100 + rank, repeat=20, lmax=60000)])
+        cfg = {"workload": "length extremes: M=2400 (p7_hmm_Sample seed 1) vs 200,000 seqs (90% lognormal "
+                           "median 300, 10% uniform [5000,35000]) + 1,000 saturation seqs (emitted core x20)",
                "M": p.M, "n_seqs": s.n, "residues": s.total, "l2_flush": "inputs larger than L2 (129 MB)"}
         return p, s, cfg
     if name == "m200_20k":
@@ -334,7 +346,10 @@ def main():
     kern_ms = float(np.mean(per))
     achieved_tops = cells / (kern_ms * 1e-3) / 1e12          # 1 cell = 1 packed int32 op (4 uint8 lane-ops)
     roofline = {"bound": "int32-pipe", "achieved": achieved_tops, "peak": peak_tops, "unit": "Tops/s",
-                "frac": achieved_tops / peak_tops, "traffic": None,
+                "frac": achieved_tops / peak_tops,
+                "traffic": DRAM_BYTES_PER_RESIDUE * s.total,
+                "traffic_note": "DRAM bytes per launch scaled by residues from an ncu capture of the same kernel "
+                                "on 400,000 sequences (profiles/msv_search_kernel_f16_m400_400k.md)",
                 "peak_note": f"measured: msvgb_measure_int_peak (independent max.s32/xor over {nsm} SMs); "
                              f"nominal {nsm} SMs x {INT_LANE_OPS_PER_CLK_PER_SM} lane-ops/clk x {sm_mhz:.0f} MHz = "
                              f"{nsm * INT_LANE_OPS_PER_CLK_PER_SM * sm_mhz * 1e6 / 1e12:.1f} Tops/s",

@@ -99,7 +99,9 @@ static std::atomic<uint64_t> g_db_serial{1};
 // DP widths (32-bit words per lane; the warp spans 64*C nodes). f16 tables:
 // every C up to 32. int8 tables: even C (two DP words per table word).
 static const int kI8C[] = {2, 4, 6, 8, 10, 12, 14, 16, 18, 20, 22, 24, 26, 28, 30, 32, 34, 36, 40, 44, 48, 50};
-static const int kMaxF16C = 32;
+static const int kF16C[] = {1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 17, 18, 19, 20, 21, 22,
+                            23, 24, 25, 26, 27, 28, 29, 30, 31, 32, 34, 36, 38, 40};
+static const int kMaxF16C = 40;
 
 // Smallest C whose warp spans more than M nodes: node 64*C must be padding
 // (the kernels rely on it for the begin value of node 1).
@@ -107,7 +109,7 @@ static int need_C(int M) { return M / 64 + 1; }
 
 static int choose_C(int M, bool f16) {
   const int need = need_C(M);
-  if (f16) return need <= kMaxF16C ? need : -1;
+  if (f16) { for (int c : kF16C) if (c >= need) return c; return -1; }
   for (int c : kI8C) if (c >= need) return c;
   return -1;
 }
@@ -121,6 +123,7 @@ cudaError_t msvgb_detail::dispatch(int C, bool f16, const LaunchArgs &a, int sms
       CASE_F16(9) CASE_F16(10) CASE_F16(11) CASE_F16(12) CASE_F16(13) CASE_F16(14) CASE_F16(15) CASE_F16(16)
       CASE_F16(17) CASE_F16(18) CASE_F16(19) CASE_F16(20) CASE_F16(21) CASE_F16(22) CASE_F16(23) CASE_F16(24)
       CASE_F16(25) CASE_F16(26) CASE_F16(27) CASE_F16(28) CASE_F16(29) CASE_F16(30) CASE_F16(31) CASE_F16(32)
+      CASE_F16(34) CASE_F16(36) CASE_F16(38) CASE_F16(40)
     }
   } else {
     switch (C) {
@@ -200,7 +203,8 @@ int msvgb_detail::profile_build_width(msvgb_ctx *ctx, const msvgb_om *om, int wa
   if (om->M < 1) return fail(MSVGB_eslEINVAL, "profile M must be >= 1");
   if (om->Kp != 29) return fail(MSVGB_eslEINVAL, "only the amino alphabet (Kp = 29) is supported");
   if (!om->rbv) return fail(MSVGB_eslEINVAL, "rbv is NULL");
-  const bool f16 = want_f16 && (force_C > 0 ? force_C : need_C(om->M)) <= kMaxF16C;
+  const bool f16 = want_f16 && (force_C > 0 ? force_C : choose_C(om->M, true)) > 0 &&
+                   (force_C > 0 ? force_C : choose_C(om->M, true)) <= kMaxF16C;
   const int C = force_C > 0 ? force_C : choose_C(om->M, f16);
   if (C < 0) return fail(MSVGB_eslEINVAL, "profile M exceeds the supported maximum (3199 nodes)");
   if (C < need_C(om->M) || (!f16 && (C & 1))) return fail(MSVGB_eslEINVAL, "DP width too small for M");

@@ -28,7 +28,7 @@
 
 namespace msvgb {
 
-constexpr int NRES = 32;       // residue slots in device tables: codes 0..28, pad 29, 30..31 unused
+constexpr int NRES = 30;       // residue slots in device tables: codes 0..28, pad 29
 constexpr int PAD_CODE = 29;   // padding residue after a sequence's end: floor costs everywhere
 constexpr unsigned FULL = 0xffffffffu;
 

@@ -18,6 +18,7 @@ struct LaunchArgs {
 };
 
 constexpr int WARPS_PER_CTA = 8;
+constexpr int MAX_WARPS_PER_CTA = 16;   // used when the tables leave room for one CTA per SM
 
 template <int C, bool F16>
 constexpr size_t smem_bytes() {   // SSV table + MSV table
@@ -28,7 +29,7 @@ constexpr size_t smem_bytes() {   // SSV table + MSV table
 // memory once, then its warps pull sequences (longest first) from a global
 // ticket until the database is exhausted.
 template <int C, bool F16>
-__global__ void __launch_bounds__(WARPS_PER_CTA * 32)
+__global__ void __launch_bounds__(MAX_WARPS_PER_CTA * 32)
 msv_search_kernel(ProfDev P, DbDev db, uint8_t *__restrict__ out_xj, uint8_t *__restrict__ out_flags,
                   unsigned long long *__restrict__ ticket, int skip_empty) {
   extern __shared__ __align__(16) uint32_t smem[];
@@ -81,18 +82,22 @@ cudaError_t launch_search(const LaunchArgs &a, int num_sms) {
     if (e != cudaSuccess) return e;
     configured = true;
   }
+  // 8-warp CTAs; 16 when the shared-memory tables allow only one CTA per SM
+  int threads = WARPS_PER_CTA * 32;
+  if (2 * smem > 227 * 1024) threads = MAX_WARPS_PER_CTA * 32;
   int grid = a.grid;
   if (grid <= 0) {
     int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, WARPS_PER_CTA * 32, smem);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;
     grid = per_sm * num_sms;
-    const long long need = (a.db.n + WARPS_PER_CTA - 1) / WARPS_PER_CTA;
+    const int warps = threads / 32;
+    const long long need = (a.db.n + warps - 1) / warps;
     if (need < grid) grid = (int) (need > 0 ? need : 1);
   }
   (void) cudaGetLastError();   // clear a stale error left by an unrelated call
-  kern<<<grid, WARPS_PER_CTA * 32, smem, a.stream>>>(a.P, a.db, a.out_xj, a.out_flags, a.ticket, a.skip_empty);
+  kern<<<grid, threads, smem, a.stream>>>(a.P, a.db, a.out_xj, a.out_flags, a.ticket, a.skip_empty);
   return cudaGetLastError();
 }
 
