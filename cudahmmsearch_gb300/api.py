@@ -29,6 +29,8 @@ EXPORTS = [
     "msvgb_search", "msvgb_search_device", "msvgb_tjb_b", "msvgb_score", "msvgb_f1_pass",
     "msvgb_search_static", "msvgb_measure_int_peak", "msvgb_sample_om", "msvgb_calibrate",
     "msvgb_batch_create", "msvgb_batch_run", "msvgb_batch_items", "msvgb_batch_destroy", "msvgb_search_batch",
+    "msvgb_server_create", "msvgb_server_slots", "msvgb_server_submit", "msvgb_server_wait",
+    "msvgb_server_launches", "msvgb_server_destroy",
 ]
 
 
@@ -92,6 +94,12 @@ def lib():
         "msvgb_batch_items": (i64, [vp]),
         "msvgb_batch_destroy": (i32, [vp]),
         "msvgb_search_batch": (i32, [vp, vp, i32, vp, f64, vp, vp]),
+        "msvgb_server_create": (i32, [vp, vp, f64, i32, ctypes.c_size_t, ctypes.POINTER(vp)]),
+        "msvgb_server_slots": (i32, [vp]),
+        "msvgb_server_submit": (i32, [vp, ctypes.POINTER(_Om), ctypes.POINTER(ctypes.c_uint64)]),
+        "msvgb_server_wait": (i32, [vp, ctypes.c_uint64, vp, vp, f64]),
+        "msvgb_server_launches": (ctypes.c_uint64, [vp]),
+        "msvgb_server_destroy": (i32, [vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -276,6 +284,47 @@ class Batch:
     def close(self):
         if self.h:
             lib().msvgb_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Continuous-batching serving loop over a resident database (msvgb_server).
+    submit() admits a query (blocking while all device slots are busy) and
+    returns a ticket; wait() returns its (xj, flags). Thread-safe."""
+
+    def __init__(self, ctx: Context, db: DeviceDB, F1: float = 0.02, max_slots: int = 64,
+                 mem_budget: int = 2 << 30):
+        h = ctypes.c_void_p()
+        _check(lib().msvgb_server_create(ctx.h, db.h, F1, max_slots, mem_budget, ctypes.byref(h)))
+        self.h, self.db = h, db
+        self.slots = int(lib().msvgb_server_slots(h))
+
+    def submit(self, p: F.Profile) -> int:
+        o, keep = _om_struct(p)
+        t = ctypes.c_uint64()
+        _check(lib().msvgb_server_submit(self.h, ctypes.byref(o), ctypes.byref(t)))
+        return t.value
+
+    def wait(self, ticket: int, timeout_s: float = 120.0, want=True):
+        xj = np.zeros(self.db.n, np.uint8) if want else None
+        fl = np.zeros(self.db.n, np.uint8) if want else None
+        _check(lib().msvgb_server_wait(self.h, ticket, xj.ctypes.data if want else None,
+                                       fl.ctypes.data if want else None, timeout_s))
+        return xj, fl
+
+    @property
+    def launches(self) -> int:
+        return int(lib().msvgb_server_launches(self.h))
+
+    def close(self):
+        if self.h:
+            lib().msvgb_server_destroy(self.h)
             self.h = None
 
     def __del__(self):

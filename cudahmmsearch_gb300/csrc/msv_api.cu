@@ -197,17 +197,10 @@ static inline int node_of(int C, int lane, int w, int h) { return lane * 2 * C +
 
 // Builds the device tables of a profile. force_C > 0 imposes the DP width
 // (the batched kernel uses a coarser set of widths); it must exceed M/64.
-int msvgb_detail::profile_build_width(msvgb_ctx *ctx, const msvgb_om *om, int want_f16, int force_C,
-                                      msvgb_profile **ret) {
-  if (!om || !ret) return fail(MSVGB_eslEINVAL, "NULL argument");
-  if (om->M < 1) return fail(MSVGB_eslEINVAL, "profile M must be >= 1");
-  if (om->Kp != 29) return fail(MSVGB_eslEINVAL, "only the amino alphabet (Kp = 29) is supported");
-  if (!om->rbv) return fail(MSVGB_eslEINVAL, "rbv is NULL");
-  const bool f16 = want_f16 && (force_C > 0 ? force_C : choose_C(om->M, true)) > 0 &&
-                   (force_C > 0 ? force_C : choose_C(om->M, true)) <= kMaxF16C;
-  const int C = force_C > 0 ? force_C : choose_C(om->M, f16);
-  if (C < 0) return fail(MSVGB_eslEINVAL, "profile M exceeds the supported maximum (3199 nodes)");
-  if (C < need_C(om->M) || (!f16 && (C & 1))) return fail(MSVGB_eslEINVAL, "DP width too small for M");
+// Host images of a profile's device tables at DP width C: the SSV costs
+// (f16x2 regions of F16Layout<C>, or int8x4) and the MSV costs (uint8x4).
+int msvgb_detail::build_cost_tables(const msvgb_om *om, int f16, int C, std::vector<uint32_t> &st,
+                                    std::vector<uint32_t> &mt) {
   const int M = om->M, Q = std::max(2, (M - 1) / 16 + 1), bias = om->bias_b;
 
   // SSV costs s = bias - rbv clamped to [-128, 127]; nodes past M and the pad
@@ -225,7 +218,8 @@ int msvgb_detail::profile_build_width(msvgb_ctx *ctx, const msvgb_om *om, int wa
   const int NP = (C + 1) / 2;                       // MSV table words per lane
   const size_t mwords = (size_t) NRES * NP * 32;
   const size_t swords = f16 ? (size_t) NRES * C * 32 : (size_t) NRES * (C / 2) * 32;
-  std::vector<uint32_t> st(swords), mt(mwords);
+  st.assign(swords, 0u);
+  mt.assign(mwords, 0u);
   auto f16bits = [](int v) -> uint32_t {
     const __half h = __float2half((float) v);
     uint16_t b; memcpy(&b, &h, 2); return b;
@@ -256,6 +250,24 @@ int msvgb_detail::profile_build_width(msvgb_ctx *ctx, const msvgb_om *om, int wa
         }
     }
 
+  return MSVGB_eslOK;
+}
+
+int msvgb_detail::profile_build_width(msvgb_ctx *ctx, const msvgb_om *om, int want_f16, int force_C,
+                                      msvgb_profile **ret) {
+  if (!om || !ret) return fail(MSVGB_eslEINVAL, "NULL argument");
+  if (om->M < 1) return fail(MSVGB_eslEINVAL, "profile M must be >= 1");
+  if (om->Kp != 29) return fail(MSVGB_eslEINVAL, "only the amino alphabet (Kp = 29) is supported");
+  if (!om->rbv) return fail(MSVGB_eslEINVAL, "rbv is NULL");
+  const bool f16 = want_f16 && (force_C > 0 ? force_C : choose_C(om->M, true)) > 0 &&
+                   (force_C > 0 ? force_C : choose_C(om->M, true)) <= kMaxF16C;
+  const int C = force_C > 0 ? force_C : choose_C(om->M, f16);
+  if (C < 0) return fail(MSVGB_eslEINVAL, "profile M exceeds the supported maximum (3199 nodes)");
+  if (C < need_C(om->M) || (!f16 && (C & 1))) return fail(MSVGB_eslEINVAL, "DP width too small for M");
+  std::vector<uint32_t> st, mt;
+  build_cost_tables(om, f16 ? 1 : 0, C, st, mt);
+  const size_t swords = st.size(), mwords = mt.size();
+  const int M = om->M;
   msvgb_profile *p = new msvgb_profile();
   p->ctx = ctx; p->device = ctx->device; p->M = M; p->C = C; p->f16 = f16 ? 1 : 0;
   p->tbm = om->tbm_b; p->tec = om->tec_b; p->base = om->base_b; p->bias = om->bias_b;

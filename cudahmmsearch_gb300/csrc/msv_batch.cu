@@ -18,16 +18,13 @@
 
 #include "../../include/msvgb.h"
 #include "msv_internal.h"
+#include "msv_multi.cuh"
 
 using namespace msvgb;
 using msvgb_detail::fail;
 
 namespace {
 
-// DP widths available in the batched kernel; a profile whose tight width is
-// not listed runs at the next larger one (extra nodes are padding).
-constexpr int kBatchC[] = {1, 2, 3, 4, 5, 6, 7, 8, 10, 12, 14, 16, 20, 24, 28, 32};
-constexpr int kBatchMaxC = 32;
 
 struct BatchItem {
   int32_t prof;
@@ -45,35 +42,12 @@ struct BatchArgs {
   unsigned long long *ticket;
 };
 
-template <int C>
-__device__ __forceinline__ void run_seq(const ProfDev &P, const uint32_t *stab, const uint32_t *mtab,
-                                        const DbDev &db, int64_t s, int lane, uint8_t *out_xj,
-                                        uint8_t *out_flags) {
-  const int L = db.len[s];
-  const int64_t oi = db.orig[s];
-  if (L == 0) {
-    if (lane == 0) { out_xj[oi] = 0; out_flags[oi] = 0x08; }
-    return;
-  }
-  const uint32_t *sq = reinterpret_cast<const uint32_t *>(db.codes + db.start[s]);
-  int xj, full;
-  const int st = msv_one<C, true>(P, stab, mtab, sq, L, lane, xj, full);
-  if (lane == 0) {
-    int flags = full ? 0x04 : 0;
-    if (st == ST_ERANGE) flags |= 0x01 | 0x02;
-    else if (xj >= P.xjmin[L]) flags |= 0x02;
-    out_xj[oi] = (uint8_t) xj;
-    out_flags[oi] = (uint8_t) flags;
-  }
-}
-
 __global__ void __launch_bounds__(512) msv_batch_kernel(BatchArgs a) {
   extern __shared__ __align__(16) uint32_t smem[];
   __shared__ long long item_sh;
   __shared__ int loaded_sh;
   __shared__ unsigned long long next_seq;
   const int lane = threadIdx.x & 31;
-  const int nthreads = blockDim.x;
   if (threadIdx.x == 0) loaded_sh = -1;
   for (;;) {
     __syncthreads();                                   // previous item fully done
@@ -90,11 +64,7 @@ __global__ void __launch_bounds__(512) msv_batch_kernel(BatchArgs a) {
     uint32_t *stab = smem;
     uint32_t *mtab = smem + NRES * C * 32;
     if (loaded_sh != item.prof) {                       // stage this profile's tables
-      const int sw = NRES * C * 32, mw = NRES * ((C + 1) / 2) * 32;
-      const uint4 *gs = reinterpret_cast<const uint4 *>(P.stab);
-      const uint4 *gm = reinterpret_cast<const uint4 *>(P.mtab);
-      for (int i = threadIdx.x; i < sw / 4; i += nthreads) reinterpret_cast<uint4 *>(stab)[i] = __ldg(gs + i);
-      for (int i = threadIdx.x; i < mw / 4; i += nthreads) reinterpret_cast<uint4 *>(mtab)[i] = __ldg(gm + i);
+      stage_tables(P, smem);
       __syncthreads();
       if (threadIdx.x == 0) loaded_sh = item.prof;
     }
@@ -107,24 +77,11 @@ __global__ void __launch_bounds__(512) msv_batch_kernel(BatchArgs a) {
       k = __shfl_sync(FULL, k, 0);
       if ((long long) k >= nseq) break;
       const int64_t s = item.s_begin + (int64_t) k;
-      switch (C) {
-#define MSVGB_BATCH_CASE(c) case c: run_seq<c>(P, stab, mtab, a.db, s, lane, oxj, ofl); break;
-        MSVGB_BATCH_CASE(1) MSVGB_BATCH_CASE(2) MSVGB_BATCH_CASE(3) MSVGB_BATCH_CASE(4)
-        MSVGB_BATCH_CASE(5) MSVGB_BATCH_CASE(6) MSVGB_BATCH_CASE(7) MSVGB_BATCH_CASE(8)
-        MSVGB_BATCH_CASE(10) MSVGB_BATCH_CASE(12) MSVGB_BATCH_CASE(14) MSVGB_BATCH_CASE(16)
-        MSVGB_BATCH_CASE(20) MSVGB_BATCH_CASE(24) MSVGB_BATCH_CASE(28) MSVGB_BATCH_CASE(32)
-#undef MSVGB_BATCH_CASE
-        default: break;
-      }
+      run_seq_any(C, P, stab, mtab, a.db, s, lane, oxj, ofl);
     }
   }
 }
 
-int batch_C(int M) {
-  const int need = M / 64 + 1;
-  for (int c : kBatchC) if (c >= need) return c;
-  return -1;
-}
 
 }  // namespace
 
@@ -170,7 +127,7 @@ extern "C" int msvgb_batch_create(msvgb_ctx *ctx, const msvgb_om *const *oms, in
   int cmax = 1;
   for (int i = 0; i < nprof; ++i) {
     if (!oms[i]) { msvgb_batch_destroy(b); return fail(MSVGB_eslEINVAL, "NULL profile"); }
-    const int C = batch_C(oms[i]->M);
+    const int C = multi_C(oms[i]->M);
     if (C < 0) { msvgb_batch_destroy(b); return fail(MSVGB_eslEINVAL, "batched profiles are limited to M <= 2047"); }
     msvgb_profile *p = nullptr;
     int st = msvgb_detail::profile_build_width(ctx, oms[i], 1, C, &p);
@@ -188,7 +145,7 @@ extern "C" int msvgb_batch_create(msvgb_ctx *ctx, const msvgb_om *const *oms, in
   // work items: profile-major, largest models first; chunks of the sorted
   // database sized so there are several items per CTA
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return oms[x]->M > oms[y]->M; });
-  b->smem = ((size_t) NRES * cmax * 32 + (size_t) NRES * ((cmax + 1) / 2) * 32) * 4;
+  b->smem = multi_smem_bytes(cmax);
   b->threads = b->smem > 100 * 1024 ? 512 : 256;
   e = cudaFuncSetAttribute(msv_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) b->smem);
   int per_sm = 0;

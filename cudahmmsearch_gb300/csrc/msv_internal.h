@@ -68,6 +68,8 @@ cudaError_t dispatch(int C, bool f16, const msvgb::LaunchArgs &a, int sms);
 int xjmin_for(const msvgb_profile *p, int L, double F1);
 // Device tables of a profile; force_C > 0 imposes the DP width.
 int profile_build_width(msvgb_ctx *ctx, const msvgb_om *om, int want_f16, int force_C, msvgb_profile **ret);
+// Host images of the device cost tables of a profile at DP width C.
+int build_cost_tables(const msvgb_om *om, int f16, int C, std::vector<uint32_t> &st, std::vector<uint32_t> &mt);
 // Per-length tjb_b and pass-threshold tables of (profile, database, F1), cached in the profile.
 int ensure_tables(msvgb_profile *p, const msvgb_db *db, double F1, LenTables **out);
 // Adds one to the count msvgb_kernel_launches() reports.

@@ -1,0 +1,396 @@
+// msv_serve.cu -- serving loop: continuous batching of query profiles
+// against a database resident in HBM.
+//
+// A persistent kernel consumes (request slot, sequence chunk) work items from
+// a ring in host-mapped memory that the host keeps appending to while the
+// kernel runs. A request is admitted when a device-memory slot is free (its
+// cost tables, per-length tables and result buffers live in the slot), its
+// items are published by advancing the ring's tail, and CTAs already running
+// pick them up between items: requests that arrive while others are on the
+// GPU overlap with them on the device. Each finished item bumps the slot's
+// completion counter (host-mapped, system-scope atomics), which the host polls.
+//
+// Every device-side wait is bounded: a CTA that finds no work for about half a
+// second leaves (re-checking the ring once more after leaving, so a request
+// published at that moment is not lost); the host relaunches the kernel when
+// it publishes work and no CTA is alive.
+//
+// The reference's counterpart is the per-block host loop of the fork's
+// pipeline_thread (code/src/cudaHmmsearch.cu:725-810) and, conceptually, the
+// hmmpgmd daemon's resident sequence cache (src/hmmdwrkr.c:600-646).
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/msvgb.h"
+#include "msv_internal.h"
+#include "msv_multi.cuh"
+
+using namespace msvgb;
+using msvgb_detail::fail;
+
+namespace {
+
+constexpr int kMaxSlots = 256;
+constexpr int kIdleIters = 400000;          // x ~1 us sleeps: a CTA leaves after ~0.5 s without work
+
+struct ServeCtl {                            // host-mapped
+  unsigned long long tail;                   // items published (host writes)
+  int stop;                                  // host asks the kernel to leave
+  int live;                                  // CTAs currently running
+  unsigned long long done[kMaxSlots];        // finished items per slot (device increments)
+};
+
+struct ServeItem {
+  int32_t slot, gen;
+  int64_t s_begin, s_end;
+};
+
+struct SlotOut { uint8_t *xj, *flags; };
+
+struct ServeArgs {
+  ServeCtl *ctl;
+  unsigned long long *head;                  // device memory: items claimed
+  const ServeItem *ring;                     // host-mapped
+  long long cap;
+  const ProfDev *slots;                      // device memory, one per slot
+  const SlotOut *outs;
+  DbDev db;
+};
+
+__device__ __forceinline__ unsigned long long ld_acquire_sys(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ int ld_volatile_i32(const int *p) { return *(const volatile int *) p; }
+
+__global__ void __launch_bounds__(512) msv_serve_kernel(ServeArgs a) {
+  extern __shared__ __align__(16) uint32_t smem[];
+  __shared__ long long item_sh;
+  __shared__ ServeItem it_sh;
+  __shared__ int loaded_slot, loaded_gen;
+  __shared__ unsigned long long next_seq;
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) { loaded_slot = -1; loaded_gen = -1; atomicAdd_system(&a.ctl->live, 1); }
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      long long got = -1;
+      for (int iter = 0; iter < kIdleIters; ++iter) {
+        const unsigned long long t = ld_acquire_sys(&a.ctl->tail);
+        const unsigned long long h = *(volatile unsigned long long *) a.head;
+        if (h < t) {
+          if (atomicCAS(a.head, h, h + 1) == h) { got = (long long) h; break; }
+          continue;
+        }
+        if (ld_volatile_i32(&a.ctl->stop)) break;
+        __nanosleep(1000);
+      }
+      if (got < 0) {
+        // leave, then look once more: a request published while we were
+        // deciding to leave is picked up here or by the host's relaunch
+        atomicSub_system(&a.ctl->live, 1);
+        __threadfence_system();
+        const unsigned long long t = ld_acquire_sys(&a.ctl->tail);
+        const unsigned long long h = *(volatile unsigned long long *) a.head;
+        if (h < t && !ld_volatile_i32(&a.ctl->stop)) { atomicAdd_system(&a.ctl->live, 1); got = -2; }
+      }
+      if (got >= 0) {
+        const volatile ServeItem *src = a.ring + (got % a.cap);
+        it_sh.slot = src->slot; it_sh.gen = src->gen; it_sh.s_begin = src->s_begin; it_sh.s_end = src->s_end;
+      }
+      item_sh = got;
+      next_seq = 0ull;
+    }
+    __syncthreads();
+    const long long got = item_sh;
+    if (got == -2) continue;
+    if (got < 0) break;
+    const ServeItem item = it_sh;
+    const ProfDev &P = a.slots[item.slot];
+    const int C = P.C;
+    if (loaded_slot != item.slot || loaded_gen != item.gen) {
+      stage_tables(P, smem);
+      __syncthreads();
+      if (threadIdx.x == 0) { loaded_slot = item.slot; loaded_gen = item.gen; }
+    }
+    const uint32_t *stab = smem;
+    const uint32_t *mtab = smem + NRES * C * 32;
+    const SlotOut o = a.outs[item.slot];
+    const int64_t nseq = item.s_end - item.s_begin;
+    for (;;) {
+      unsigned long long k = 0;
+      if (lane == 0) k = atomicAdd(&next_seq, 1ull);
+      k = __shfl_sync(FULL, k, 0);
+      if ((long long) k >= nseq) break;
+      run_seq_any(C, P, stab, mtab, a.db, item.s_begin + (int64_t) k, lane, o.xj, o.flags);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence_system();                           // results visible before the count
+      atomicAdd_system(&a.ctl->done[item.slot], 1ull);
+    }
+  }
+}
+
+}  // namespace
+
+struct msvgb_server {
+  msvgb_ctx *ctx = nullptr;
+  const msvgb_db *db = nullptr;
+  int device = 0;
+  double F1 = 0.02;
+  int nslots = 0;
+  size_t smem = 0;
+  int threads = 512, grid = 0;
+  int64_t items_per_req = 0;
+  std::vector<int64_t> chunk_begin;          // item boundaries over the sorted database
+  // device
+  uint8_t *d_slot_mem = nullptr;
+  size_t slot_bytes = 0, tab_off_m = 0, tab_off_tjb = 0, tab_off_xjm = 0, off_xj = 0, off_fl = 0;
+  ProfDev *d_slots = nullptr;
+  SlotOut *d_outs = nullptr;
+  unsigned long long *d_head = nullptr;
+  // host-mapped
+  ServeCtl *h_ctl = nullptr, *d_ctl = nullptr;
+  ServeItem *h_ring = nullptr, *d_ring = nullptr;
+  long long cap = 0;
+  // host state
+  std::mutex mu;
+  std::condition_variable slot_freed;
+  std::vector<int> free_slots;
+  std::vector<int> gen;
+  std::vector<uint64_t> ticket_of;
+  uint64_t next_ticket = 1;
+  unsigned long long tail = 0;
+  cudaStream_t upload = nullptr;
+  std::vector<cudaStream_t> kstreams;
+  size_t next_kstream = 0;
+  std::vector<uint8_t> tjb;                  // shared per-length tjb_b table (scale of the first profile)
+  float tjb_scale = -1.f;
+  uint64_t launches = 0;
+  cudaEvent_t last_done = nullptr;           // completes when the latest launch has fully exited
+  bool launched = false;
+};
+
+// True while the most recent launch has CTAs running or still to start.
+static bool kernel_running(msvgb_server *s) {
+  return s->launched && cudaEventQuery(s->last_done) == cudaErrorNotReady;
+}
+
+static int launch_serve(msvgb_server *s) {
+  ServeArgs a;
+  a.ctl = s->d_ctl; a.head = s->d_head; a.ring = s->d_ring; a.cap = s->cap;
+  a.slots = s->d_slots; a.outs = s->d_outs;
+  a.db = DbDev{s->db->d_codes, s->db->d_start, s->db->d_len, s->db->d_orig, s->db->n};
+  cudaStream_t st = s->kstreams[s->next_kstream++ % s->kstreams.size()];
+  (void) cudaGetLastError();
+  msv_serve_kernel<<<s->grid, s->threads, s->smem, st>>>(a);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaEventRecord(s->last_done, st);
+  if (e != cudaSuccess) return fail(MSVGB_eslESYS, std::string("serve launch: ") + cudaGetErrorString(e));
+  s->launched = true;
+  s->launches++;
+  msvgb_detail::count_launch();
+  return MSVGB_eslOK;
+}
+
+extern "C" int msvgb_server_destroy(msvgb_server *s) {
+  if (!s) return MSVGB_eslOK;
+  cudaSetDevice(s->device);
+  if (s->h_ctl) {
+    __atomic_store_n(&s->h_ctl->stop, 1, __ATOMIC_SEQ_CST);
+    for (auto st : s->kstreams) cudaStreamSynchronize(st);
+  }
+  for (auto st : s->kstreams) cudaStreamDestroy(st);
+  if (s->last_done) cudaEventDestroy(s->last_done);
+  if (s->upload) { cudaStreamSynchronize(s->upload); cudaStreamDestroy(s->upload); }
+  cudaFree(s->d_slot_mem); cudaFree(s->d_slots); cudaFree(s->d_outs); cudaFree(s->d_head);
+  if (s->h_ctl) cudaFreeHost(s->h_ctl);
+  if (s->h_ring) cudaFreeHost(s->h_ring);
+  delete s;
+  return MSVGB_eslOK;
+}
+
+extern "C" int msvgb_server_create(msvgb_ctx *ctx, const msvgb_db *db, double F1, int max_slots,
+                                   size_t mem_budget, msvgb_server **ret) {
+  if (!ctx || !db || !ret || max_slots < 1) return fail(MSVGB_eslEINVAL, "msvgb_server_create: bad arguments");
+  *ret = nullptr;
+  msvgb_server *s = new msvgb_server();
+  s->ctx = ctx; s->db = db; s->device = ctx->device; s->F1 = F1;
+  cudaError_t e = cudaSetDevice(ctx->device);
+  // slot layout: f16 SSV table and MSV table at the widest batched width, per-length tables, results
+  const size_t tab = multi_smem_bytes(kMultiMaxC);
+  auto align = [](size_t x) { return (x + 255) / 256 * 256; };
+  s->tab_off_m = (size_t) NRES * kMultiMaxC * 32 * 4;
+  s->tab_off_tjb = align(tab);
+  s->tab_off_xjm = s->tab_off_tjb + align((size_t) db->Lmax + 1);
+  s->off_xj = s->tab_off_xjm + align((size_t) db->Lmax + 1);
+  s->off_fl = s->off_xj + align((size_t) db->n);
+  s->slot_bytes = s->off_fl + align((size_t) db->n);
+  // admission bound: as many slots as the budget holds (at least one)
+  s->nslots = std::max(1, std::min({max_slots, kMaxSlots, (int) std::max<size_t>(1, mem_budget / s->slot_bytes)}));
+  s->smem = tab;
+  e = cudaFuncSetAttribute(msv_serve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) s->smem);
+  int per_sm = 0;
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, msv_serve_kernel, s->threads, s->smem);
+  s->grid = std::max(1, per_sm) * ctx->num_sms;
+  // items per request: several per CTA, by residue count
+  std::vector<int32_t> len(db->n);
+  if (e == cudaSuccess && db->n) e = cudaMemcpy(len.data(), db->d_len, db->n * 4, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) { msvgb_server_destroy(s); return fail(MSVGB_eslESYS, std::string("server setup: ") + cudaGetErrorString(e)); }
+  const double per_item = std::max(4096.0, (double) db->residues / (2.0 * s->grid));
+  for (int64_t i = 0; i < db->n;) {
+    s->chunk_begin.push_back(i);
+    double acc = 0;
+    const int64_t i0 = i;
+    while (i < db->n && (acc < per_item || i - i0 < s->threads / 32)) acc += std::max(1, len[i++]);
+  }
+  s->chunk_begin.push_back(db->n);
+  s->items_per_req = (int64_t) s->chunk_begin.size() - 1;
+  s->cap = (long long) s->nslots * std::max<int64_t>(1, s->items_per_req) + 1;
+  if (e == cudaSuccess) e = cudaMalloc(&s->d_slot_mem, s->slot_bytes * s->nslots);
+  if (e == cudaSuccess) e = cudaMalloc(&s->d_slots, sizeof(ProfDev) * s->nslots);
+  if (e == cudaSuccess) e = cudaMalloc(&s->d_outs, sizeof(SlotOut) * s->nslots);
+  if (e == cudaSuccess) e = cudaMalloc(&s->d_head, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMemset(s->d_head, 0, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaHostAlloc(&s->h_ctl, sizeof(ServeCtl), cudaHostAllocMapped);
+  if (e == cudaSuccess) e = cudaHostAlloc(&s->h_ring, sizeof(ServeItem) * s->cap, cudaHostAllocMapped);
+  if (e == cudaSuccess) e = cudaHostGetDevicePointer((void **) &s->d_ctl, s->h_ctl, 0);
+  if (e == cudaSuccess) e = cudaHostGetDevicePointer((void **) &s->d_ring, s->h_ring, 0);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->upload, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->last_done, cudaEventDisableTiming);
+  for (int i = 0; e == cudaSuccess && i < 4; ++i) {
+    cudaStream_t st;
+    e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) s->kstreams.push_back(st);
+  }
+  if (e != cudaSuccess) { msvgb_server_destroy(s); return fail(MSVGB_eslEMEM, std::string("server memory: ") + cudaGetErrorString(e)); }
+  memset(s->h_ctl, 0, sizeof(ServeCtl));
+  std::vector<SlotOut> outs(s->nslots);
+  for (int i = 0; i < s->nslots; ++i) {
+    uint8_t *base = s->d_slot_mem + s->slot_bytes * i;
+    outs[i] = SlotOut{base + s->off_xj, base + s->off_fl};
+    s->free_slots.push_back(s->nslots - 1 - i);
+  }
+  s->gen.assign(s->nslots, 0);
+  s->ticket_of.assign(s->nslots, 0);
+  e = cudaMemcpy(s->d_outs, outs.data(), sizeof(SlotOut) * s->nslots, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) { msvgb_server_destroy(s); return fail(MSVGB_eslESYS, cudaGetErrorString(e)); }
+  *ret = s;
+  return MSVGB_eslOK;
+}
+
+extern "C" int msvgb_server_slots(const msvgb_server *s) { return s ? s->nslots : -1; }
+
+extern "C" int msvgb_server_submit(msvgb_server *s, const msvgb_om *om, uint64_t *ret_ticket) {
+  if (!s || !om || !ret_ticket) return fail(MSVGB_eslEINVAL, "msvgb_server_submit: bad arguments");
+  const int C = multi_C(om->M);
+  if (C < 0) return fail(MSVGB_eslEINVAL, "served profiles are limited to M <= 2047");
+  cudaError_t e = cudaSetDevice(s->device);
+  if (e != cudaSuccess) return fail(MSVGB_eslESYS, cudaGetErrorString(e));
+  // host-side tables first (no lock held): costs and the per-length pass thresholds
+  std::vector<uint32_t> st, mt;
+  int rc = msvgb_detail::build_cost_tables(om, 1, C, st, mt);
+  if (rc != MSVGB_eslOK) return rc;
+  msvgb_profile tmp;                                   // scalar view for the threshold search
+  tmp.M = om->M; tmp.C = C; tmp.tbm = om->tbm_b; tmp.tec = om->tec_b; tmp.base = om->base_b;
+  tmp.bias = om->bias_b; tmp.scale = om->scale_b; tmp.mmu = om->mmu; tmp.mlambda = om->mlambda;
+  const int Lmax = s->db->Lmax;
+  std::vector<uint8_t> xjm(Lmax + 1, 255), tjb(Lmax + 1);
+  for (int L = 0; L <= Lmax; ++L) tjb[L] = msvgb_tjb_b(om->scale_b, L);
+  for (int L : s->db->distinct_len) {
+    if (L == 0) continue;
+    const int v = msvgb_detail::xjmin_for(&tmp, L, s->F1);
+    if (v < 0) return fail(MSVGB_eslESYS, "F1 pass set is not monotone in xJ");
+    xjm[L] = (uint8_t) v;
+  }
+  // admission: wait for a free slot
+  int slot;
+  uint64_t ticket;
+  {
+    std::unique_lock<std::mutex> lk(s->mu);
+    s->slot_freed.wait(lk, [&] { return !s->free_slots.empty(); });
+    slot = s->free_slots.back();
+    s->free_slots.pop_back();
+    ticket = s->next_ticket++;
+    s->ticket_of[slot] = ticket;
+    s->gen[slot]++;
+  }
+  uint8_t *base = s->d_slot_mem + s->slot_bytes * slot;
+  ProfDev P;
+  P.M = om->M; P.C = C; P.tbm = om->tbm_b; P.tec = om->tec_b; P.base = om->base_b; P.bias = om->bias_b;
+  P.stab = (const uint32_t *) base; P.mtab = (const uint32_t *) (base + (size_t) NRES * C * 32 * 4);
+  P.tjb = base + s->tab_off_tjb; P.xjmin = base + s->tab_off_xjm; P.ssv_f16 = 1;
+  __atomic_store_n(&s->h_ctl->done[slot], 0ull, __ATOMIC_SEQ_CST);
+  e = cudaMemcpyAsync(base, st.data(), st.size() * 4, cudaMemcpyHostToDevice, s->upload);
+  if (e == cudaSuccess) e = cudaMemcpyAsync((uint8_t *) P.mtab, mt.data(), mt.size() * 4, cudaMemcpyHostToDevice, s->upload);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(base + s->tab_off_tjb, tjb.data(), Lmax + 1, cudaMemcpyHostToDevice, s->upload);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(base + s->tab_off_xjm, xjm.data(), Lmax + 1, cudaMemcpyHostToDevice, s->upload);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_slots + slot, &P, sizeof(ProfDev), cudaMemcpyHostToDevice, s->upload);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->upload);       // visible before the items are
+  if (e != cudaSuccess) return fail(MSVGB_eslESYS, std::string("serve upload: ") + cudaGetErrorString(e));
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    for (int64_t k = 0; k < s->items_per_req; ++k) {
+      ServeItem &it = s->h_ring[(s->tail + k) % s->cap];
+      it.slot = slot; it.gen = s->gen[slot];
+      it.s_begin = s->chunk_begin[k]; it.s_end = s->chunk_begin[k + 1];
+    }
+    s->tail += s->items_per_req;
+    __atomic_store_n(&s->h_ctl->tail, s->tail, __ATOMIC_SEQ_CST);     // publish
+    if (!kernel_running(s)) {                                         // the loop left: start it
+      int r = launch_serve(s);
+      if (r != MSVGB_eslOK) return r;
+    }
+  }
+  *ret_ticket = ((uint64_t) slot << 48) | ticket;
+  return MSVGB_eslOK;
+}
+
+extern "C" int msvgb_server_wait(msvgb_server *s, uint64_t ticket, uint8_t *out_xj, uint8_t *out_flags,
+                                 double timeout_s) {
+  if (!s) return fail(MSVGB_eslEINVAL, "NULL server");
+  const int slot = (int) (ticket >> 48);
+  if (slot < 0 || slot >= s->nslots || s->ticket_of[slot] != (ticket & 0xFFFFFFFFFFFFull))
+    return fail(MSVGB_eslEINVAL, "unknown ticket");
+  const auto t0 = std::chrono::steady_clock::now();
+  for (;;) {
+    const unsigned long long d = __atomic_load_n(&s->h_ctl->done[slot], __ATOMIC_ACQUIRE);
+    if ((int64_t) d >= s->items_per_req) break;
+    const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (el > timeout_s) return fail(MSVGB_eslESYS, "msvgb_server_wait: timed out");
+    if (__atomic_load_n(&s->h_ctl->live, __ATOMIC_ACQUIRE) == 0) {
+      std::lock_guard<std::mutex> lk(s->mu);                          // the loop left with work
+      if (!kernel_running(s)) {                                       // still queued: restart it
+        int r = launch_serve(s);
+        if (r != MSVGB_eslOK) return r;
+      }
+    }
+    std::this_thread::sleep_for(std::chrono::microseconds(50));
+  }
+  cudaSetDevice(s->device);
+  uint8_t *base = s->d_slot_mem + s->slot_bytes * slot;
+  cudaError_t e = cudaSuccess;
+  if (out_xj) e = cudaMemcpy(out_xj, base + s->off_xj, s->db->n, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && out_flags) e = cudaMemcpy(out_flags, base + s->off_fl, s->db->n, cudaMemcpyDeviceToHost);
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->ticket_of[slot] = 0;
+    s->free_slots.push_back(slot);
+  }
+  s->slot_freed.notify_one();
+  if (e != cudaSuccess) return fail(MSVGB_eslESYS, std::string("serve results: ") + cudaGetErrorString(e));
+  return MSVGB_eslOK;
+}
+
+extern "C" uint64_t msvgb_server_launches(const msvgb_server *s) { return s ? s->launches : 0; }

@@ -181,6 +181,30 @@ int     msvgb_batch_destroy(msvgb_batch *batch);
 int     msvgb_search_batch(msvgb_ctx *ctx, const msvgb_om *const *oms, int nprof, const msvgb_db *db,
                            double F1, uint8_t *out_xj, uint8_t *out_flags);
 
+/* ---- serving loop: continuous batching over a resident database -----------------
+ * A persistent kernel consumes (request, sequence-chunk) work items that
+ * submissions keep appending while it runs, so queries arriving while others
+ * are on the GPU overlap with them on the device. Each request occupies one
+ * device-memory slot (its cost tables, per-length tables and n-byte results);
+ * the number of slots is min(max_slots, mem_budget / slot size), and
+ * msvgb_server_submit blocks until a slot is free (admission by memory).
+ * Profiles up to M = 2047. The database must outlive the server.
+ * The counterpart in the reference is the fork's per-block pipeline thread
+ * (code/src/cudaHmmsearch.cu:725-810) and hmmpgmd's resident sequence cache
+ * (src/hmmdwrkr.c:600-646); the calls are thread-safe. */
+typedef struct msvgb_server msvgb_server;
+int      msvgb_server_create(msvgb_ctx *ctx, const msvgb_db *db, double F1, int max_slots, size_t mem_budget,
+                             msvgb_server **ret_server);
+int      msvgb_server_slots(const msvgb_server *server);
+/* Admits one query (blocking while no slot is free) and returns its ticket. */
+int      msvgb_server_submit(msvgb_server *server, const msvgb_om *om, uint64_t *ret_ticket);
+/* Waits (at most timeout_s seconds) for a ticket, copies its n results to
+ * host buffers (either may be NULL) and frees its slot. */
+int      msvgb_server_wait(msvgb_server *server, uint64_t ticket, uint8_t *out_xj, uint8_t *out_flags,
+                           double timeout_s);
+uint64_t msvgb_server_launches(const msvgb_server *server);
+int      msvgb_server_destroy(msvgb_server *server);
+
 /* ---- host-side score helpers (exact reference expressions) --------------------- */
 /* tjb_b for target length L (p7_oprofile.c:511-519, 920-925). */
 uint8_t msvgb_tjb_b(float scale_b, int L);

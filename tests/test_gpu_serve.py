@@ -1,0 +1,72 @@
+"""The serving loop (msvgb_server) through the C ABI: every query's result in
+the mix equals the same query run alone on the single-query path (MSV results
+are integers: bit-exact); admission blocks while all slots are busy; the
+persistent kernel leaves when idle and is restarted by the next submission."""
+import concurrent.futures as cf
+import time
+
+import numpy as np
+import pytest
+
+from cudahmmsearch_gb300 import api
+from cudahmmsearch_gb300 import formats as F
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def env():
+    ctx = api.Context(0)
+    profs = [api.sample_profile(M, 300 + i, ctx) for i, M in enumerate([60, 150, 400, 777, 1300, 2047, 90, 500])]
+    s = F.SeqSet.concat([F.synth_sequences(6000, seed=61, lmax=5000),
+                         F.emit_homologs(profs[2], 20, seed=62), F.emit_homologs(profs[4], 20, seed=63),
+                         F.emit_homologs(profs[3], 5, seed=64, repeat=20)])
+    db = api.DeviceDB(ctx, s)
+    alone = [api.search(ctx, api.DeviceProfile(ctx, p), db) for p in profs]
+    yield ctx, profs, db, alone
+    ctx.close()
+
+
+def test_results_in_the_mix_equal_results_alone(env):
+    ctx, profs, db, alone = env
+    srv = api.Server(ctx, db, max_slots=16)
+    tickets = [srv.submit(p) for p in profs]          # all in flight together
+    for t, (xj, fl) in zip(tickets, alone):
+        gx, gf = srv.wait(t)
+        assert np.array_equal(gx, xj) and np.array_equal(gf, fl)
+    srv.close()
+
+
+def test_admission_blocks_until_a_slot_frees(env):
+    ctx, profs, db, alone = env
+    srv = api.Server(ctx, db, max_slots=2)
+    assert srv.slots == 2
+    order = [i % len(profs) for i in range(12)]
+    with cf.ThreadPoolExecutor(max_workers=12) as ex:
+        def one(i):
+            t = srv.submit(profs[i])
+            return i, srv.wait(t)
+        for i, (gx, gf) in ex.map(one, order):
+            assert np.array_equal(gx, alone[i][0]) and np.array_equal(gf, alone[i][1])
+    srv.close()
+
+
+def test_idle_kernel_leaves_and_restarts(env):
+    ctx, profs, db, alone = env
+    srv = api.Server(ctx, db, max_slots=4)
+    gx, gf = srv.wait(srv.submit(profs[0]))
+    assert np.array_equal(gx, alone[0][0])
+    time.sleep(1.5)                                   # longer than the kernel's idle bound
+    gx, gf = srv.wait(srv.submit(profs[5]))
+    assert np.array_equal(gx, alone[5][0]) and np.array_equal(gf, alone[5][1])
+    assert srv.launches >= 2
+    srv.close()
+
+
+def test_memory_budget_bounds_slots(env):
+    ctx, profs, db, alone = env
+    srv = api.Server(ctx, db, max_slots=64, mem_budget=1)
+    assert srv.slots == 1
+    gx, gf = srv.wait(srv.submit(profs[1]))
+    assert np.array_equal(gf, alone[1][1])
+    srv.close()
