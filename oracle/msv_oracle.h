@@ -68,6 +68,11 @@ int orc_msv_batch(const orc_profile *om, const uint8_t *residues, const int64_t 
                   int64_t n, double F1, int nthreads,
                   int32_t *status, uint8_t *xj, float *sc, uint8_t *pass, uint8_t *path);
 
+/* Vectorized port of the reference's SSE2 algorithm (msv_port.c): the timed
+ * CPU baseline. Same outputs as orc_msv_batch (path not reported). */
+int port_msv_batch(const orc_profile *om, const uint8_t *residues, const int64_t *off, int64_t n,
+                   double F1, int nthreads, int32_t *status, uint8_t *xj, float *sc, uint8_t *pass);
+
 #ifdef __cplusplus
 }
 #endif
