@@ -30,7 +30,7 @@ EXPORTS = [
     "msvgb_search_static", "msvgb_measure_int_peak", "msvgb_sample_om", "msvgb_calibrate",
     "msvgb_batch_create", "msvgb_batch_run", "msvgb_batch_items", "msvgb_batch_destroy", "msvgb_search_batch",
     "msvgb_server_create", "msvgb_server_slots", "msvgb_server_submit", "msvgb_server_wait",
-    "msvgb_server_launches", "msvgb_server_destroy",
+    "msvgb_server_launches", "msvgb_server_destroy", "msvgb_pipeline_run",
 ]
 
 
@@ -100,6 +100,8 @@ def lib():
         "msvgb_server_wait": (i32, [vp, ctypes.c_uint64, vp, vp, f64]),
         "msvgb_server_launches": (ctypes.c_uint64, [vp]),
         "msvgb_server_destroy": (i32, [vp]),
+        "msvgb_pipeline_run": (i32, [vp, ctypes.POINTER(_Om), vp, vp, i64, i64, f64, i32, vp, vp,
+                                     ctypes.POINTER(i64)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -332,6 +334,32 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+SURVIVOR_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_float,
+                               ctypes.c_uint8, ctypes.c_uint8)
+
+
+def pipeline_run(ctx: Context, p: F.Profile, seqs: F.SeqSet, on_survivor=None, *, block_size: int = 100_000,
+                 F1: float = 0.02, n_workers: int = 4):
+    """hmmsearch-style driver: blocks scored on the GPU, survivors of the F1
+    gate handed to on_survivor(index, usc, xj, flags) on CPU worker threads.
+    Returns n_past_msv."""
+    o, keep = _om_struct(p)
+    codes = np.ascontiguousarray(seqs.codes, dtype=np.uint8)
+    if codes.size == 0:
+        codes = np.zeros(1, np.uint8)
+    off = np.ascontiguousarray(seqs.off, dtype=np.int64)
+    cb = None
+    if on_survivor is not None:
+        def _cb(user, i, usc, xj, fl):
+            return 1 if on_survivor(int(i), float(usc), int(xj), int(fl)) else 0
+        cb = SURVIVOR_FN(_cb)
+    n_past = ctypes.c_int64()
+    _check(lib().msvgb_pipeline_run(ctx.h, ctypes.byref(o), codes.ctypes.data, off.ctypes.data, seqs.n,
+                                    block_size, F1, n_workers, ctypes.cast(cb, ctypes.c_void_p) if cb else None,
+                                    None, ctypes.byref(n_past)))
+    return n_past.value
 
 
 def tjb_b(scale_b: float, L: int) -> int:

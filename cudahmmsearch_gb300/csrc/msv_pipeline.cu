@@ -1,0 +1,110 @@
+// msv_pipeline.cu -- the hmmsearch driver's threading around the GPU MSV stage.
+//
+// The reference driver (src/hmmsearch.c:1317-1406; the fork's
+// code/src/cudaHmmsearch.cu:670-810) has a reader thread filling blocks of
+// sequences and worker threads running p7_Pipeline on each; the fork gave the
+// MSV filter of a block to the GPU and ran p7_PipelineShort (p7_pipeline.c:887)
+// on the rest. Here: the calling thread is the GPU submitter -- it uploads
+// and scores one block after another -- while N CPU workers take each scored
+// block, compute the MSV score of every sequence that passes the F1 gate
+// (with the reference's exact expression) and hand it to the caller's
+// continuation (the place p7_PipelineShort plugs in: bias filter, Viterbi,
+// Forward, domain definition). Upload and search of block k+1 overlap the CPU
+// work on block k.
+#include <atomic>
+#include <condition_variable>
+#include <deque>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/msvgb.h"
+#include "msv_internal.h"
+
+using msvgb_detail::fail;
+
+namespace {
+
+struct Block {
+  int64_t b0 = 0, b1 = 0;
+  std::vector<uint8_t> xj, fl;
+};
+
+}  // namespace
+
+extern "C" int msvgb_pipeline_run(msvgb_ctx *ctx, const msvgb_om *om, const uint8_t *codes, const int64_t *off,
+                                  int64_t n, int64_t block_size, double F1, int n_workers,
+                                  msvgb_survivor_fn fn, void *user, int64_t *ret_n_past_msv) {
+  if (!ctx || !om || (n > 0 && (!codes || !off)) || block_size < 1 || n < 0)
+    return fail(MSVGB_eslEINVAL, "msvgb_pipeline_run: bad arguments");
+  if (n_workers < 1) n_workers = 1;
+  msvgb_profile *prof = nullptr;
+  int st = msvgb_profile_create(ctx, om, &prof);
+  if (st != MSVGB_eslOK) return st;
+
+  std::mutex mu;
+  std::condition_variable cv_push, cv_pop;
+  std::deque<Block *> q;
+  const size_t qcap = 2;                       // blocks scored ahead of the workers
+  bool producing = true;
+  std::atomic<int64_t> n_past{0};
+  std::atomic<int> abort_flag{0};
+
+  auto worker = [&]() {
+    for (;;) {
+      Block *b = nullptr;
+      {
+        std::unique_lock<std::mutex> lk(mu);
+        cv_pop.wait(lk, [&] { return !q.empty() || !producing; });
+        if (q.empty()) return;
+        b = q.front();
+        q.pop_front();
+      }
+      cv_push.notify_one();
+      for (int64_t i = b->b0; i < b->b1 && !abort_flag.load(); ++i) {
+        const uint8_t xj = b->xj[i - b->b0], fl = b->fl[i - b->b0];
+        if (!(fl & MSVGB_FLAG_PASS)) continue;              // P > F1: rejected by the MSV stage
+        const int L = (int) (off[i + 1] - off[i]);
+        const float usc = msvgb_score(xj, fl, L, om->base_b, om->scale_b);
+        n_past.fetch_add(1);
+        if (fn && fn(user, i, usc, xj, fl) != 0) abort_flag.store(1);
+      }
+      delete b;
+    }
+  };
+  std::vector<std::thread> workers;
+  for (int t = 0; t < n_workers; ++t) workers.emplace_back(worker);
+
+  // GPU submitter: upload + score one block after another
+  for (int64_t b0 = 0; b0 < n && st == MSVGB_eslOK && !abort_flag.load(); b0 += block_size) {
+    const int64_t b1 = std::min(n, b0 + block_size);
+    Block *blk = new Block();
+    blk->b0 = b0; blk->b1 = b1;
+    blk->xj.resize(b1 - b0); blk->fl.resize(b1 - b0);
+    msvgb_db *db = nullptr;
+    st = msvgb_db_create(ctx, codes, off + b0, b1 - b0, &db);
+    if (st == MSVGB_eslOK) st = msvgb_search(ctx, prof, db, F1, blk->xj.data(), blk->fl.data());
+    msvgb_db_destroy(db);
+    if (st != MSVGB_eslOK) { delete blk; break; }
+    {
+      std::unique_lock<std::mutex> lk(mu);
+      cv_push.wait(lk, [&] { return q.size() < qcap; });
+      q.push_back(blk);
+    }
+    cv_pop.notify_one();
+  }
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    producing = false;
+  }
+  cv_pop.notify_all();
+  for (auto &t : workers) t.join();
+  for (Block *b : q) delete b;
+  msvgb_profile_destroy(prof);
+  if (ret_n_past_msv) *ret_n_past_msv = n_past.load();
+  if (st == MSVGB_eslOK && abort_flag.load()) return fail(MSVGB_eslFAIL, "the continuation asked to stop");
+  return st;
+}

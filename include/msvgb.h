@@ -25,6 +25,7 @@ extern "C" {
 #endif
 
 #define MSVGB_eslOK      0
+#define MSVGB_eslFAIL    1
 #define MSVGB_eslEMEM    5
 #define MSVGB_eslEINVAL 11
 #define MSVGB_eslESYS   12
@@ -204,6 +205,22 @@ int      msvgb_server_wait(msvgb_server *server, uint64_t ticket, uint8_t *out_x
                            double timeout_s);
 uint64_t msvgb_server_launches(const msvgb_server *server);
 int      msvgb_server_destroy(msvgb_server *server);
+
+/* ---- pipeline driver: streamed blocks, GPU MSV stage, CPU continuation -----------
+ * The threading of hmmsearch's search loop (src/hmmsearch.c:1317-1406; the
+ * fork's code/src/cudaHmmsearch.cu:670-810) around the MSV stage: the calling
+ * thread uploads and scores blocks of block_size sequences on the GPU, one
+ * after another, while n_workers CPU threads take each scored block and call
+ * fn for every sequence that passes the F1 gate, with its MSV score usc (nats,
+ * +inf on overflow) -- where p7_PipelineShort (src/p7_pipeline.c:887) would
+ * continue with the bias filter and the later stages. fn runs concurrently on
+ * the worker threads; returning nonzero stops the run (eslFAIL). Sequences
+ * are codes[off[i] .. off[i+1]) (any off[0]); *ret_n_past_msv counts passes
+ * (the pipeline's n_past_msv). */
+typedef int (*msvgb_survivor_fn)(void *user, int64_t seq_index, float usc, uint8_t xj, uint8_t flags);
+int msvgb_pipeline_run(msvgb_ctx *ctx, const msvgb_om *om, const uint8_t *codes, const int64_t *off,
+                       int64_t n, int64_t block_size, double F1, int n_workers,
+                       msvgb_survivor_fn fn, void *user, int64_t *ret_n_past_msv);
 
 /* ---- host-side score helpers (exact reference expressions) --------------------- */
 /* tjb_b for target length L (p7_oprofile.c:511-519, 920-925). */
