@@ -339,7 +339,7 @@ int msvgb_detail::xjmin_for(const msvgb_profile *p, int L, double F1) {
 
 int msvgb_detail::ensure_tables(msvgb_profile *p, const msvgb_db *db, double F1, LenTables **out) {
   for (auto &t : p->tables)
-    if (t.db == db && t.F1 == F1) { *out = &t; return MSVGB_eslOK; }
+    if (t.db_serial == db->serial && t.F1 == F1) { *out = &t; return MSVGB_eslOK; }
   const int Lmax = db->Lmax;
   std::vector<uint8_t> tjb(Lmax + 1), xjm(Lmax + 1, 255);
   for (int L = 0; L <= Lmax; ++L) tjb[L] = msvgb_tjb_b(p->scale, L);
@@ -349,7 +349,7 @@ int msvgb_detail::ensure_tables(msvgb_profile *p, const msvgb_db *db, double F1,
     if (v < 0) return fail(MSVGB_eslESYS, "F1 pass set is not monotone in xJ");
     xjm[L] = (uint8_t) v;
   }
-  LenTables t; t.db = db; t.F1 = F1;
+  LenTables t; t.db_serial = db->serial; t.F1 = F1;
   cudaError_t e = cudaMalloc(&t.d_tjb, Lmax + 1);
   if (e == cudaSuccess) e = cudaMalloc(&t.d_xjmin, Lmax + 1);
   if (e == cudaSuccess) e = cudaMemcpy(t.d_tjb, tjb.data(), Lmax + 1, cudaMemcpyHostToDevice);

@@ -30,7 +30,7 @@ struct msvgb_ctx {
 };
 
 struct LenTables {      // per (profile, database, F1)
-  const msvgb_db *db = nullptr;
+  uint64_t db_serial = 0;  // the database's unique serial (addresses are reused after destroy)
   double F1 = -1.0;
   uint8_t *d_tjb = nullptr;
   uint8_t *d_xjmin = nullptr;

@@ -172,3 +172,18 @@ def test_kernel_launch_counter_advances(ctx):
     before = api.kernel_launches()
     api.search(ctx, prof, db)
     assert api.kernel_launches() == before + 1
+
+
+def test_profile_reused_across_databases_at_the_same_address(ctx):
+    """A profile caches per-database length tables; a database created after
+    another was destroyed (often at the same device address) must not reuse
+    the old tables."""
+    p, _, _ = load_case("m200_s1")
+    prof = api.DeviceProfile(ctx, p)
+    for k in range(4):
+        s = F.SeqSet.concat([F.synth_sequences(300, seed=90 + k, lmax=300 + 1500 * k), F.emit_homologs(p, 5, seed=k)])
+        db = api.DeviceDB(ctx, s)
+        xj, fl = api.search(ctx, prof, db)
+        o = O.msv_batch(p, s)
+        check_against_oracle(p, s, xj, fl, o)
+        db.close()
