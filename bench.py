@@ -137,11 +137,16 @@ def cpu_baseline(p, s, budget_s=12.0, nthreads=0):
     want = int(min(s.n, max(4000, budget_s * rate / (p.M * max(1.0, s.total / s.n)))))
     idx = rng.choice(s.n, size=want, replace=False)
     sub = s.subset(np.sort(idx))
+    reps = 0
     t0 = time.perf_counter()
-    _, used = O.port_batch(p, sub, nthreads=cores)
+    while True:                      # repeat a sample smaller than the budget until it is spent
+        _, used = O.port_batch(p, sub, nthreads=cores)
+        reps += 1
+        if time.perf_counter() - t0 >= budget_s or reps >= 200:
+            break
     dt = time.perf_counter() - t0
-    return {"value": sub.total * p.M / dt / 1e9, "unit": "GCUPS", "cores": used, "kind": "port",
-            "sample": f"{sub.n} random sequences of the workload ({sub.total} residues, M={p.M}), {dt:.1f} s; "
+    return {"value": reps * sub.total * p.M / dt / 1e9, "unit": "GCUPS", "cores": used, "kind": "port",
+            "sample": f"{sub.n} random sequences of the workload ({sub.total} residues, M={p.M}) x{reps}, {dt:.1f} s; "
                       "vectorized port of the reference SSE2 p7_MSVFilter (NEON), bit-exact with its golden vectors",
             "seconds": dt}
 
@@ -405,15 +410,19 @@ def main():
     # e2e through the public API from pinned host buffers
     codes_pin = torch.from_numpy(s.codes).pin_memory()
     off_np = s.off
-    e2e_times = []
+    e2e_times, e2e_parts = [], []
     for i in range(args.e2e_steps + 1 if args.e2e_steps > 0 else 0):
         torch.cuda.synchronize()
         t = time.perf_counter()
         seqset = F.SeqSet(codes_pin.numpy(), off_np)
         db2 = api.DeviceDB(ctx, seqset)
+        t_db = time.perf_counter()
         xj, fl = api.search(ctx, prof, db2)
+        t_search = time.perf_counter()
         db2.close()
         dt = time.perf_counter() - t
+        e2e_parts.append({"db_create_ms": (t_db - t) * 1e3, "search_ms": (t_search - t_db) * 1e3,
+                          "destroy_ms": (t + dt - t_search) * 1e3})
         if i > 0:
             e2e_times.append(dt)
     if e2e_times:
@@ -444,6 +453,7 @@ def main():
             "config": dict(cfg, variant=prof.variant, full_msv_fraction=fullfrac,
                            pass_fraction=float(((fl_all & api.FLAG_PASS) != 0).mean())),
             "e2e": {"value": e2e_val, "unit": "GCUPS", "h2d_bytes_per_step": int(s.total + 8 * (s.n + 1)),
+                    "breakdown_last_step": e2e_parts[-1] if e2e_parts else None,
                     "d2h_bytes_per_step": int(2 * s.n), "path": "msvgb_db_create + msvgb_search from pinned host memory"},
             "gpu_launches": int(launches), "clocks": clocks, "roofline": roofline}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

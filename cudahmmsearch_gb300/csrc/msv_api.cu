@@ -10,11 +10,13 @@
 // this file is compiled with -ffp-contract=off (no fused multiply-add).
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -310,7 +312,11 @@ extern "C" int msvgb_profile_variant(const msvgb_profile *p) { return p ? p->f16
 extern "C" int msvgb_profile_destroy(msvgb_profile *p) {
   if (!p) return MSVGB_eslOK;
   cudaSetDevice(p->device);
-  for (auto &t : p->tables) { cudaFree(t.d_tjb); cudaFree(t.d_xjmin); }
+  for (auto *t : p->tables) {
+    cudaFree(t->d_tjb); cudaFree(t->d_xjmin);
+    for (void *r : t->retired) cudaFree(r);
+    delete t;
+  }
   cudaFree(p->d_stab); cudaFree(p->d_mtab);
   delete p;
   return MSVGB_eslOK;
@@ -338,32 +344,51 @@ int msvgb_detail::xjmin_for(const msvgb_profile *p, int L, double F1) {
 }
 
 int msvgb_detail::ensure_tables(msvgb_profile *p, const msvgb_db *db, double F1, LenTables **out) {
-  for (auto &t : p->tables)
-    if (t.db_serial == db->serial && t.F1 == F1) { *out = &t; return MSVGB_eslOK; }
-  const int Lmax = db->Lmax;
-  std::vector<uint8_t> tjb(Lmax + 1), xjm(Lmax + 1, 255);
-  for (int L = 0; L <= Lmax; ++L) tjb[L] = msvgb_tjb_b(p->scale, L);
+  std::lock_guard<std::mutex> lk(p->tables_mu);
+  LenTables *t = nullptr;
+  for (auto *x : p->tables) if (x->F1 == F1) t = x;
+  if (!t) {
+    if (p->tables.size() >= 8) return fail(MSVGB_eslEINVAL, "too many distinct F1 thresholds for one profile");
+    t = new LenTables();
+    t->F1 = F1;
+    p->tables.push_back(t);
+  }
+  const int need = db->Lmax + 1;
+  bool dirty = false;
+  if (need > t->cap) {                                  // grow: host images and device buffers
+    const int cap = std::max({need, 2 * t->cap, 1024});
+    t->tjb.resize(cap);
+    for (int L = t->cap; L < cap; ++L) t->tjb[L] = msvgb_tjb_b(p->scale, L);
+    t->xjm.resize(cap, -1);
+    uint8_t *nt = nullptr, *nx = nullptr;
+    cudaError_t e = cudaMalloc(&nt, cap);
+    if (e == cudaSuccess) e = cudaMalloc(&nx, cap);
+    if (e != cudaSuccess) {
+      cudaFree(nt); cudaFree(nx);
+      return fail(MSVGB_eslEMEM, std::string("length tables: ") + cudaGetErrorString(e));
+    }
+    if (t->d_tjb) { t->retired.push_back(t->d_tjb); t->retired.push_back(t->d_xjmin); }
+    t->d_tjb = nt; t->d_xjmin = nx;
+    t->cap = cap;
+    dirty = true;
+  }
   for (int L : db->distinct_len) {
-    if (L == 0) continue;
+    if (L == 0 || t->xjm[L] >= 0) continue;
     const int v = xjmin_for(p, L, F1);
     if (v < 0) return fail(MSVGB_eslESYS, "F1 pass set is not monotone in xJ");
-    xjm[L] = (uint8_t) v;
+    t->xjm[L] = (int16_t) v;
+    dirty = true;
   }
-  LenTables t; t.db_serial = db->serial; t.F1 = F1;
-  cudaError_t e = cudaMalloc(&t.d_tjb, Lmax + 1);
-  if (e == cudaSuccess) e = cudaMalloc(&t.d_xjmin, Lmax + 1);
-  if (e == cudaSuccess) e = cudaMemcpy(t.d_tjb, tjb.data(), Lmax + 1, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(t.d_xjmin, xjm.data(), Lmax + 1, cudaMemcpyHostToDevice);
-  if (e != cudaSuccess) {
-    cudaFree(t.d_tjb); cudaFree(t.d_xjmin);
-    return fail(MSVGB_eslESYS, std::string("length tables: ") + cudaGetErrorString(e));
+  if (dirty) {
+    std::vector<uint8_t> x(t->cap);
+    for (int L = 0; L < t->cap; ++L) x[L] = t->xjm[L] < 0 ? 255 : (uint8_t) t->xjm[L];
+    // ordered on the context's stream before the searches that read them
+    cudaError_t e = cudaMemcpyAsync(t->d_tjb, t->tjb.data(), t->cap, cudaMemcpyHostToDevice, p->ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(t->d_xjmin, x.data(), t->cap, cudaMemcpyHostToDevice, p->ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(p->ctx->stream);
+    if (e != cudaSuccess) return fail(MSVGB_eslESYS, std::string("length tables: ") + cudaGetErrorString(e));
   }
-  if (p->tables.size() >= 8) {           // bounded cache
-    cudaFree(p->tables.front().d_tjb); cudaFree(p->tables.front().d_xjmin);
-    p->tables.erase(p->tables.begin());
-  }
-  p->tables.push_back(t);
-  *out = &p->tables.back();
+  *out = t;
   return MSVGB_eslOK;
 }
 
@@ -374,78 +399,164 @@ int msvgb_detail::ensure_tables(msvgb_profile *p, const msvgb_db *db, double F1,
 // first) and the padded offsets. The residues go to the device in one copy
 // (a DMA when the caller's buffer is pinned) and a kernel scatters, pads and
 // validates them.
+// Phase timings of msvgb_db_create on stderr when MSVGB_TRACE is set.
+static bool trace_on() { static const bool on = getenv("MSVGB_TRACE") != nullptr; return on; }
+struct PhaseTimer {
+  std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+  void mark(const char *what) {
+    if (!trace_on()) return;
+    const auto now = std::chrono::steady_clock::now();
+    fprintf(stderr, "msvgb: %-28s %8.3f ms\n", what, std::chrono::duration<double, std::milli>(now - t).count());
+    t = now;
+  }
+};
+
 extern "C" int msvgb_db_create(msvgb_ctx *ctx, const uint8_t *codes, const int64_t *off, int64_t n,
                                msvgb_db **ret) {
   if (!ctx || !ret || (n > 0 && (!off || !codes))) return fail(MSVGB_eslEINVAL, "NULL argument");
+  PhaseTimer pt;
   *ret = nullptr;
   if (n < 0) return fail(MSVGB_eslEINVAL, "n < 0");
+  const int64_t total = n ? off[n] - off[0] : 0;
+  if (total < 0) return fail(MSVGB_eslEINVAL, "bad sequence offsets");
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->stream;
+
+  // The residues go first: their DMA runs while the host sorts the lengths.
+  uint8_t *d_raw = nullptr;
+  CUDA_TRY(cudaMallocAsync((void **) &d_raw, std::max<int64_t>(total, 1), st));
+  if (total) {
+    cudaError_t e = cudaMemcpyAsync(d_raw, codes + off[0], total, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) { cudaFreeAsync(d_raw, st); return fail(MSVGB_eslESYS, cudaGetErrorString(e)); }
+  }
+
+  // Lengths: validation, Lmax and per-thread histograms, in parallel.
+  const int T = (int) std::max<int64_t>(1, std::min<int64_t>(std::max(1u, std::thread::hardware_concurrency()),
+                                                             std::min<int64_t>(32, n / 65536 + 1)));
+  std::vector<int> lmax_t(T, 0), bad_t(T, 0);
+  auto range = [&](int t) { return std::make_pair(n * t / T, n * (t + 1) / T); };
+  auto par = [&](auto &&fn) {
+    std::vector<std::thread> th;
+    for (int t = 1; t < T; ++t) th.emplace_back(fn, t);
+    fn(0);
+    for (auto &x : th) x.join();
+  };
+  par([&](int t) {
+    auto [lo, hi] = range(t);
+    int m = 0, bad = 0;
+    for (int64_t i = lo; i < hi; ++i) {
+      const int64_t L = off[i + 1] - off[i];
+      if (L < 0 || L > (int64_t) 100000000) bad = 1; else if (L > m) m = (int) L;
+    }
+    lmax_t[t] = m; bad_t[t] = bad;
+  });
   int Lmax = 0;
-  for (int64_t i = 0; i < n; ++i) {
-    const int64_t L = off[i + 1] - off[i];
-    if (L < 0 || L > (int64_t) 100000000) return fail(MSVGB_eslEINVAL, "bad sequence offsets");
-    if (L > Lmax) Lmax = (int) L;
+  for (int t = 0; t < T; ++t) {
+    if (bad_t[t]) { cudaFreeAsync(d_raw, st); cudaStreamSynchronize(st); return fail(MSVGB_eslEINVAL, "bad sequence offsets"); }
+    Lmax = std::max(Lmax, lmax_t[t]);
   }
-  // stable counting sort, descending length
-  std::vector<int64_t> first(Lmax + 2, 0);
-  for (int64_t i = 0; i < n; ++i) first[off[i + 1] - off[i]]++;
+  // stable counting sort by descending length: per-thread counts, then each
+  // thread's first slot for each length (lengths are ranked first when they
+  // are too large for a direct table)
+  std::vector<int32_t> rank_of;                  // length -> dense rank, only for huge Lmax
+  int R = Lmax;
+  if (Lmax > (1 << 20)) {
+    std::vector<int32_t> ls(n);
+    for (int64_t i = 0; i < n; ++i) ls[i] = (int32_t) (off[i + 1] - off[i]);
+    std::sort(ls.begin(), ls.end());
+    ls.erase(std::unique(ls.begin(), ls.end()), ls.end());
+    rank_of = std::move(ls);                     // sorted distinct lengths
+    R = (int) rank_of.size() - 1;
+  }
+  auto key = [&](int64_t L) -> int64_t {
+    if (rank_of.empty()) return L;
+    return std::lower_bound(rank_of.begin(), rank_of.end(), (int32_t) L) - rank_of.begin();
+  };
+  std::vector<std::vector<int64_t>> cnt(T, std::vector<int64_t>(R + 1, 0));
+  par([&](int t) {
+    auto [lo, hi] = range(t);
+    int64_t *c = cnt[t].data();
+    for (int64_t i = lo; i < hi; ++i) c[key(off[i + 1] - off[i])]++;
+  });
   std::vector<int32_t> distinct;
-  int64_t acc = 0;
-  for (int L = Lmax; L >= 0; --L) {
-    const int64_t cnt = first[L];
-    first[L] = acc;
-    acc += cnt;
-    if (cnt) distinct.push_back(L);
+  {
+    int64_t acc = 0;
+    for (int k = R; k >= 0; --k) {
+      int64_t tot = 0;
+      for (int t = 0; t < T; ++t) { const int64_t c = cnt[t][k]; cnt[t][k] = acc + tot; tot += c; }
+      acc += tot;
+      if (tot) distinct.push_back(rank_of.empty() ? k : rank_of[k]);
+    }
+    std::reverse(distinct.begin(), distinct.end());
   }
-  std::reverse(distinct.begin(), distinct.end());
+  pt.mark("length scan + histograms");
   // metadata in pinned staging: start, orig, src (int64) and len (int32) per sorted slot
   const size_t need = (size_t) std::max<int64_t>(n, 1) * (3 * 8 + 4);
   if (ctx->h_stage_cap < need) {
+    cudaStreamSynchronize(st);                          // the old staging may still feed a copy
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     ctx->h_stage = nullptr; ctx->h_stage_cap = 0;
-    CUDA_TRY(cudaMallocHost(&ctx->h_stage, need));
+    cudaError_t e = cudaMallocHost(&ctx->h_stage, need);
+    if (e != cudaSuccess) { cudaFreeAsync(d_raw, st); return fail(MSVGB_eslEMEM, cudaGetErrorString(e)); }
     ctx->h_stage_cap = need;
   }
-  CUDA_TRY(cudaStreamSynchronize(ctx->stream));          // the staging buffer may still feed a copy
   int64_t *h_start = (int64_t *) ctx->h_stage, *h_orig = h_start + n, *h_src = h_orig + n;
   int32_t *h_len = (int32_t *) (h_src + n);
-  for (int64_t i = 0; i < n; ++i) {
-    const int64_t L = off[i + 1] - off[i], s = first[L]++;
-    h_orig[s] = i; h_len[s] = (int32_t) L; h_src[s] = off[i] - off[0];
-  }
-  int64_t pos = 0;
-  for (int64_t s = 0; s < n; ++s) { h_start[s] = pos; pos += ((int64_t) h_len[s] + 15) / 16 * 16; }
+  par([&](int t) {
+    auto [lo, hi] = range(t);
+    int64_t *slot = cnt[t].data();
+    for (int64_t i = lo; i < hi; ++i) {
+      const int64_t L = off[i + 1] - off[i], s = slot[key(L)]++;
+      h_orig[s] = i; h_len[s] = (int32_t) L; h_src[s] = off[i] - off[0];
+    }
+  });
+  // padded start offsets: per-thread partial sums, then an exclusive scan
+  std::vector<int64_t> part(T + 1, 0);
+  par([&](int t) {
+    auto [lo, hi] = range(t);
+    int64_t sum = 0;
+    for (int64_t s = lo; s < hi; ++s) sum += ((int64_t) h_len[s] + 15) / 16 * 16;
+    part[t + 1] = sum;
+  });
+  for (int t = 0; t < T; ++t) part[t + 1] += part[t];
+  par([&](int t) {
+    auto [lo, hi] = range(t);
+    int64_t pos = part[t];
+    for (int64_t s = lo; s < hi; ++s) { h_start[s] = pos; pos += ((int64_t) h_len[s] + 15) / 16 * 16; }
+  });
+  const int64_t pos = part[T];
+  pt.mark("placement + offsets");
   const int64_t bytes = pos + 64;                 // tail so a 16-byte over-read stays inside
-  const int64_t total = n ? off[n] - off[0] : 0;
 
   msvgb_db *db = new msvgb_db();
   db->ctx = ctx; db->device = ctx->device; db->n = n; db->residues = total; db->Lmax = Lmax;
   db->serial = g_db_serial.fetch_add(1);
   db->distinct_len = std::move(distinct);
-  cudaStream_t st = ctx->stream;
-  uint8_t *d_raw = nullptr; int64_t *d_src = nullptr;
+  int64_t *d_src = nullptr;
   int bad = 0;
-  cudaError_t e = cudaSetDevice(ctx->device);
-  if (e == cudaSuccess) e = cudaMalloc(&db->d_codes, bytes);
+  cudaError_t e = cudaMalloc(&db->d_codes, bytes);
   if (e == cudaSuccess) e = cudaMalloc(&db->d_start, std::max<int64_t>(n, 1) * 8);
   if (e == cudaSuccess) e = cudaMalloc(&db->d_orig, std::max<int64_t>(n, 1) * 8);
   if (e == cudaSuccess) e = cudaMalloc(&db->d_len, std::max<int64_t>(n, 1) * 4);
-  if (e == cudaSuccess) e = cudaMallocAsync((void **) &d_raw, std::max<int64_t>(total, 1), st);
   if (e == cudaSuccess) e = cudaMallocAsync((void **) &d_src, std::max<int64_t>(n, 1) * 8, st);
-  if (e == cudaSuccess && total) e = cudaMemcpyAsync(d_raw, codes + off[0], total, cudaMemcpyHostToDevice, st);
+  pt.mark("device allocations");
   if (e == cudaSuccess && n) e = cudaMemcpyAsync(db->d_start, h_start, n * 8, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess && n) e = cudaMemcpyAsync(db->d_orig, h_orig, n * 8, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess && n) e = cudaMemcpyAsync(d_src, h_src, n * 8, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess && n) e = cudaMemcpyAsync(db->d_len, h_len, n * 4, cudaMemcpyHostToDevice, st);
+  if (trace_on() && e == cudaSuccess) { e = cudaStreamSynchronize(st); pt.mark("uploads (rest of raw + metadata)"); }
   if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_bad, 0, sizeof(int), st);
   if (e == cudaSuccess) e = cudaMemsetAsync(db->d_codes + pos, PAD_CODE, 64, st);
   if (e == cudaSuccess) e = launch_pack(d_raw, d_src, db->d_start, db->d_len, n, db->d_codes, ctx->d_bad,
                                         ctx->num_sms, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, ctx->d_bad, sizeof(int), cudaMemcpyDeviceToHost, st);
-  if (d_raw) cudaFreeAsync(d_raw, st);
+  cudaFreeAsync(d_raw, st);
   if (d_src) cudaFreeAsync(d_src, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  pt.mark("pack kernel + frees");
   if (e == cudaSuccess && n) count_launch();
   if (e != cudaSuccess) {
+    cudaStreamSynchronize(st);
     msvgb_db_destroy(db);
     return fail(e == cudaErrorMemoryAllocation ? MSVGB_eslEMEM : MSVGB_eslESYS,
                 std::string("database upload: ") + cudaGetErrorString(e));

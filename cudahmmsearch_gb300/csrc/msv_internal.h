@@ -29,11 +29,18 @@ struct msvgb_ctx {
   void *h_stage = nullptr; size_t h_stage_cap = 0;      // pinned staging for database metadata
 };
 
-struct LenTables {      // per (profile, database, F1)
-  uint64_t db_serial = 0;  // the database's unique serial (addresses are reused after destroy)
+// Per-length tables of a profile at one F1 threshold: tjb_b(L) and the
+// smallest passing xJ at length L. They depend on L only, not on the
+// database, so they grow with the longest sequence seen and entries are
+// computed for the lengths that occur.
+struct LenTables {
   double F1 = -1.0;
+  int cap = 0;                        // entries 0..cap-1
+  std::vector<uint8_t> tjb;
+  std::vector<int16_t> xjm;           // -1: not computed yet
   uint8_t *d_tjb = nullptr;
-  uint8_t *d_xjmin = nullptr;
+  uint8_t *d_xjmin = nullptr;         // 255 where not computed (never read)
+  std::vector<void *> retired;        // smaller device tables of earlier sizes (kernels may still read them)
 };
 
 struct msvgb_profile {
@@ -43,7 +50,8 @@ struct msvgb_profile {
   uint8_t tbm = 0, tec = 0, base = 0, bias = 0;
   float scale = 0.f, mmu = 0.f, mlambda = 0.f;
   uint32_t *d_stab = nullptr, *d_mtab = nullptr;
-  std::vector<LenTables> tables;
+  std::vector<LenTables *> tables;    // one per F1 value used
+  std::mutex tables_mu;
 };
 
 struct msvgb_db {
