@@ -25,11 +25,15 @@ constexpr size_t smem_bytes() {   // SSV table + MSV table
   return ((size_t) (F16 ? NRES * C * 32 : NRES * (C / 2) * 32) + (size_t) NRES * ((C + 1) / 2) * 32) * 4;
 }
 
+// Threads per CTA: 8 warps, or 16 when the tables leave room for only one CTA per SM.
+template <int C, bool F16>
+constexpr int cta_threads() { return 2 * smem_bytes<C, F16>() > 227 * 1024 ? MAX_WARPS_PER_CTA * 32 : WARPS_PER_CTA * 32; }
+
 // Persistent kernel: every CTA stages the profile's cost tables into shared
 // memory once, then its warps pull sequences (longest first) from a global
 // ticket until the database is exhausted.
 template <int C, bool F16>
-__global__ void __launch_bounds__(MAX_WARPS_PER_CTA * 32)
+__global__ void __launch_bounds__(cta_threads<C, F16>())
 msv_search_kernel(ProfDev P, DbDev db, uint8_t *__restrict__ out_xj, uint8_t *__restrict__ out_flags,
                   unsigned long long *__restrict__ ticket, int skip_empty) {
   extern __shared__ __align__(16) uint32_t smem[];
@@ -82,9 +86,7 @@ cudaError_t launch_search(const LaunchArgs &a, int num_sms) {
     if (e != cudaSuccess) return e;
     configured = true;
   }
-  // 8-warp CTAs; 16 when the shared-memory tables allow only one CTA per SM
-  int threads = WARPS_PER_CTA * 32;
-  if (2 * smem > 227 * 1024) threads = MAX_WARPS_PER_CTA * 32;
+  constexpr int threads = cta_threads<C, F16>();
   int grid = a.grid;
   if (grid <= 0) {
     int per_sm = 0;
