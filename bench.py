@@ -42,7 +42,7 @@ INT_LANE_OPS_PER_CLK_PER_SM = 128   # 4 SM sub-partitions x 32 lanes: nominal is
 DRAM_BYTES_PER_RESIDUE = 169.4e6 / 154.56e6
 
 
-def workload(name, rank=0):
+def workload(name, rank=0, args=None):
     if name == "m400_2M":
         p = F.read_profile(os.path.join(ROOT, "tests", "golden", "m400_s1.prof"))
         n_total, n_hom = 2_000_000, 40_000
@@ -73,6 +73,17 @@ def workload(name, rank=0):
         s = F.SeqSet.concat([F.synth_sequences(19800, seed=11 + rank, lmax=5000), F.emit_homologs(p, 200, seed=12)])
         cfg = {"workload": "plain MSV, 1 profile M=200 vs 20,000 seqs (lognormal clipped [10,5000], 1% homologs)",
                "M": p.M, "n_seqs": s.n, "residues": s.total, "l2_flush": "none (inputs fit in L2)"}
+        return p, s, cfg
+    if name == "sampled":     # any model length: p7_hmm_Sample-style profile of length M, m400_2M's sequence law
+        from cudahmmsearch_gb300 import api
+        p = api.sample_profile(args.M, 1, api.Context(0))
+        n_hom = args.nseq // 50
+        s = F.SeqSet.concat([F.synth_sequences(args.nseq - n_hom, seed=1000 + rank, lmax=35000),
+                             F.emit_homologs(p, n_hom, seed=2000 + rank, lmax=35000)])
+        cfg = {"workload": f"plain MSV, 1 sampled profile M={args.M} (seed 1) vs {s.n:,} seqs "
+                           "(lognormal median 300 sigma 0.7 clipped [10,35000], 0.5% X, 2% homologs)",
+               "M": p.M, "n_seqs": s.n, "residues": s.total,
+               "l2_flush": "inputs larger than L2 (129 MB)" if s.total > 129e6 else "none (inputs fit in L2)"}
         return p, s, cfg
     raise SystemExit(f"unknown workload {name}")
 
@@ -155,7 +166,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    p, s, cfg = workload(args.workload)
+    p, s, cfg = workload(args.workload, 0, args)
     vals = []
     for i in range(args.warmup + args.steps):
         cb = cpu_baseline(p, s, budget_s=max(2.0, 60.0 / (args.steps + args.warmup)))
@@ -329,6 +340,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="m400_2M")
     ap.add_argument("--variant", type=int, default=None, help="SSV arithmetic: 0 int8 table, 1 f16 table")
+    ap.add_argument("--lanes", type=int, default=None, help="lanes per sequence of the SSV pass (32, 16, 8)")
+    ap.add_argument("--M", type=int, default=100, help="sampled workload: model length")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--nprof", type=int, default=256, help="batch workload: number of profiles")
@@ -358,7 +371,7 @@ def main():
     if args.workload == "serve":
         return run_serve(args, api, torch, api.Context(local), local)
 
-    p, s, cfg = workload(args.workload, rank)
+    p, s, cfg = workload(args.workload, rank, args)
     cells = float(p.M) * float(s.total)
     ctx = api.Context(local)
     # A dedicated (non-default) stream: its handle is non-NULL, so the library
@@ -367,6 +380,8 @@ def main():
     torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     prof = api.DeviceProfile(ctx, p, args.variant)
+    if args.lanes:
+        prof.set_lanes(args.lanes)
     db = api.DeviceDB(ctx, s)
     out = torch.empty(2 * s.n, dtype=torch.uint8, device="cuda")
     d_xj, d_fl = out.data_ptr(), out.data_ptr() + s.n
@@ -450,7 +465,7 @@ def main():
     line = {"metric": "MSV GCUPS", "value": value, "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-            "config": dict(cfg, variant=prof.variant, full_msv_fraction=fullfrac,
+            "config": dict(cfg, variant=prof.variant, lanes=prof.lanes, full_msv_fraction=fullfrac,
                            pass_fraction=float(((fl_all & api.FLAG_PASS) != 0).mean())),
             "e2e": {"value": e2e_val, "unit": "GCUPS", "h2d_bytes_per_step": int(s.total + 8 * (s.n + 1)),
                     "breakdown_last_step": e2e_parts[-1] if e2e_parts else None,

@@ -25,7 +25,8 @@ FLAG_ERANGE, FLAG_PASS, FLAG_FULL, FLAG_EMPTY = 0x01, 0x02, 0x04, 0x08
 EXPORTS = [
     "msvgb_ctx_create", "msvgb_ctx_destroy", "msvgb_ctx_set_stream", "msvgb_last_error",
     "msvgb_kernel_launches", "msvgb_MSVFilter", "msvgb_profile_create", "msvgb_profile_destroy",
-    "msvgb_profile_M", "msvgb_profile_create_ex", "msvgb_profile_variant", "msvgb_db_create", "msvgb_db_destroy", "msvgb_db_nseq", "msvgb_db_residues",
+    "msvgb_profile_M", "msvgb_profile_create_ex", "msvgb_profile_variant", "msvgb_profile_set_lanes",
+    "msvgb_profile_lanes", "msvgb_db_create", "msvgb_db_destroy", "msvgb_db_nseq", "msvgb_db_residues",
     "msvgb_search", "msvgb_search_device", "msvgb_tjb_b", "msvgb_score", "msvgb_f1_pass",
     "msvgb_search_static", "msvgb_measure_int_peak", "msvgb_sample_om", "msvgb_calibrate",
     "msvgb_batch_create", "msvgb_batch_run", "msvgb_batch_items", "msvgb_batch_destroy", "msvgb_search_batch",
@@ -74,6 +75,8 @@ def lib():
         "msvgb_profile_create": (i32, [vp, ctypes.POINTER(_Om), ctypes.POINTER(vp)]),
         "msvgb_profile_create_ex": (i32, [vp, ctypes.POINTER(_Om), i32, ctypes.POINTER(vp)]),
         "msvgb_profile_variant": (i32, [vp]),
+        "msvgb_profile_set_lanes": (i32, [vp, ctypes.POINTER(_Om), i32]),
+        "msvgb_profile_lanes": (i32, [vp]),
         "msvgb_profile_destroy": (i32, [vp]),
         "msvgb_profile_M": (i32, [vp]),
         "msvgb_db_create": (i32, [vp, vp, vp, i64, ctypes.POINTER(vp)]),
@@ -175,6 +178,15 @@ class DeviceProfile:
             _check(lib().msvgb_profile_create_ex(ctx.h, ctypes.byref(o), variant, ctypes.byref(h)))
         self.h, self.ctx, self.profile = h, ctx, p
         self.variant = int(lib().msvgb_profile_variant(h))
+
+    def set_lanes(self, lanes: int):
+        """Lanes per sequence of the SSV pass (32, 16 or 8)."""
+        o, keep = _om_struct(self.profile)
+        _check(lib().msvgb_profile_set_lanes(self.h, ctypes.byref(o), lanes))
+
+    @property
+    def lanes(self) -> int:
+        return int(lib().msvgb_profile_lanes(self.h))
 
     def close(self):
         if self.h:

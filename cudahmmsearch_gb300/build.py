@@ -17,9 +17,9 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmsvgb.so")
 
-SOURCES = ["msv_api.cu", "msv_noalloc.cu", "msv_probe.cu", "msv_pack.cu", "msv_sample.cu", "msv_batch.cu", "msv_serve.cu", "msv_pipeline.cu", "inst_a.cu", "inst_b.cu", "inst_c.cu", "inst_d.cu",
+SOURCES = ["inst_g16.cu", "inst_g8.cu", "msv_api.cu", "msv_noalloc.cu", "msv_probe.cu", "msv_pack.cu", "msv_sample.cu", "msv_batch.cu", "msv_serve.cu", "msv_pipeline.cu", "inst_a.cu", "inst_b.cu", "inst_c.cu", "inst_d.cu",
            "inst_e.cu", "inst_f.cu"]
-HEADERS = ["msv_device.cuh", "msv_kernel_impl.cuh", "msv_internal.h", "msv_multi.cuh", os.path.join("..", "..", "include", "msvgb.h")]
+HEADERS = ["msv_device.cuh", "msv_kernel_impl.cuh", "msv_internal.h", "msv_multi.cuh", "msv_group.cuh", os.path.join("..", "..", "include", "msvgb.h")]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",

@@ -139,6 +139,27 @@ cudaError_t msvgb_detail::dispatch(int C, bool f16, const LaunchArgs &a, int sms
 #undef CASE_F16
 }
 
+namespace msvgb {
+template <int C, int G> cudaError_t launch_ssv_group(const GroupArgs &a, int num_sms);
+}
+
+cudaError_t msvgb_detail::dispatch_group(int C, int G, const GroupArgs &a, int sms) {
+#define G16(c) case c: return launch_ssv_group<c, 16>(a, sms);
+#define G8(c)  case c: return launch_ssv_group<c, 8>(a, sms);
+  if (G == 16) {
+    switch (C) { G16(2) G16(3) G16(4) G16(5) G16(6) G16(7) G16(8) G16(9) G16(10) G16(11) G16(12) G16(13)
+                 G16(14) G16(15) G16(16) G16(17) G16(18) G16(19) G16(20) G16(21) G16(22) G16(23) G16(24)
+                 G16(25) G16(26) G16(27) G16(28) G16(29) G16(30) G16(31) G16(32) }
+  } else if (G == 8) {
+    switch (C) { G8(2) G8(3) G8(4) G8(5) G8(6) G8(7) G8(8) G8(9) G8(10) G8(11) G8(12) G8(13)
+                 G8(14) G8(15) G8(16) G8(17) G8(18) G8(19) G8(20) G8(21) G8(22) G8(23) G8(24)
+                 G8(25) G8(26) G8(27) G8(28) G8(29) G8(30) G8(31) G8(32) }
+  }
+  return cudaErrorInvalidValue;
+#undef G16
+#undef G8
+}
+
 // ------------------------------------------------------------------------------
 // context
 
@@ -157,6 +178,7 @@ extern "C" int msvgb_ctx_create(int device, msvgb_ctx **ret_ctx) {
   if (e == cudaSuccess) e = cudaMalloc(&c->d_meta, 4 * sizeof(int64_t));
   if (e == cudaSuccess) e = cudaMalloc(&c->d_out, 64);
   if (e == cudaSuccess) e = cudaMalloc(&c->d_bad, sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_aux, 2 * sizeof(unsigned long long));
   if (e != cudaSuccess) {
     msvgb_ctx_destroy(c);
     return fail(MSVGB_eslESYS, std::string("context setup: ") + cudaGetErrorString(e));
@@ -173,7 +195,7 @@ extern "C" int msvgb_ctx_destroy(msvgb_ctx *c) {
   c->cache.clear();
   if (c->own) cudaStreamSynchronize(c->own);
   cudaFree(c->d_ticket); cudaFree(c->d_meta); cudaFree(c->d_out);
-  cudaFree(c->d_seq); cudaFree(c->d_tab); cudaFree(c->d_bad);
+  cudaFree(c->d_seq); cudaFree(c->d_tab); cudaFree(c->d_bad); cudaFree(c->d_aux); cudaFree(c->d_list);
   if (c->h_stage) cudaFreeHost(c->h_stage);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
@@ -317,12 +339,61 @@ extern "C" int msvgb_profile_destroy(msvgb_profile *p) {
     for (void *r : t->retired) cudaFree(r);
     delete t;
   }
-  cudaFree(p->d_stab); cudaFree(p->d_mtab);
+  cudaFree(p->d_stab); cudaFree(p->d_mtab); cudaFree(p->d_stab_g);
   delete p;
   return MSVGB_eslOK;
 }
 
 extern "C" int msvgb_profile_M(const msvgb_profile *p) { return p ? p->M : -1; }
+
+// G-lane SSV table: node g*2C + h*C + w + 1 of lane g in word w, half h.
+static std::vector<uint32_t> build_group_table(const msvgb_om *om, int C, int G) {
+  const int M = om->M, Q = std::max(2, (M - 1) / 16 + 1), bias = om->bias_b;
+  auto s_of = [&](int x, int k) -> int {
+    if (x >= 29 || k > M) return -128;
+    return std::min(127, std::max(-128, bias - rbv_at(om, Q, x, k)));
+  };
+  auto f16bits = [](int v) -> uint32_t {
+    const __half h = __float2half((float) v);
+    uint16_t b; memcpy(&b, &h, 2); return b;
+  };
+  const int Q4 = C / 4, R = C % 4;
+  const size_t a_words = (size_t) NRES * Q4 * G * 4, b_words = (R >= 2) ? (size_t) NRES * G * 2 : 0;
+  std::vector<uint32_t> st((size_t) NRES * C * G);
+  for (int x = 0; x < NRES; ++x)
+    for (int g = 0; g < G; ++g)
+      for (int w = 0; w < C; ++w) {
+        const int k0 = g * 2 * C + w + 1, k1 = g * 2 * C + C + w + 1;
+        const uint32_t v = f16bits(s_of(x, k0)) | (f16bits(s_of(x, k1)) << 16);
+        size_t i;                                           // GroupLayout<C, G>
+        if (w < 4 * Q4)                     i = (((size_t) x * Q4 + w / 4) * G + g) * 4 + (w % 4);
+        else if (R >= 2 && w < 4 * Q4 + 2) i = a_words + ((size_t) x * G + g) * 2 + (w - 4 * Q4);
+        else                                i = a_words + b_words + (size_t) x * G + g;
+        st[i] = v;
+      }
+  return st;
+}
+
+extern "C" int msvgb_profile_set_lanes(msvgb_profile *p, const msvgb_om *om, int G) {
+  if (!p || !om) return fail(MSVGB_eslEINVAL, "NULL argument");
+  if (om->M != p->M) return fail(MSVGB_eslEINVAL, "om does not match the profile");
+  if (G == 32) { p->G = 32; return MSVGB_eslOK; }
+  if (G != 16 && G != 8) return fail(MSVGB_eslEINVAL, "lanes per sequence must be 32, 16 or 8");
+  const int C = p->M / (2 * G) + 1;                       // 2*C*G > M: the last node is padding
+  if (C > 32) return fail(MSVGB_eslEINVAL, "model too long for this many lanes per sequence");
+  if (C < 2) return fail(MSVGB_eslEINVAL, "model too short for this many lanes per sequence");
+  std::vector<uint32_t> st = build_group_table(om, C, G);
+  CUDA_TRY(cudaSetDevice(p->device));
+  uint32_t *d = nullptr;
+  CUDA_TRY(cudaMalloc(&d, st.size() * 4));
+  cudaError_t e = cudaMemcpy(d, st.data(), st.size() * 4, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) { cudaFree(d); return fail(MSVGB_eslESYS, cudaGetErrorString(e)); }
+  cudaFree(p->d_stab_g);
+  p->d_stab_g = d; p->Cg = C; p->G = G;
+  return MSVGB_eslOK;
+}
+
+extern "C" int msvgb_profile_lanes(const msvgb_profile *p) { return p ? p->G : -1; }
 
 // ------------------------------------------------------------------------------
 // per-length tables: tjb_b(L) and the smallest xJ that passes F1 at length L
@@ -607,7 +678,34 @@ extern "C" int msvgb_search_device(msvgb_ctx *c, const msvgb_profile *pc, const 
   int st = ensure_tables(p, db, F1, &t);
   if (st != MSVGB_eslOK) return st;
   DbDev dbv{db->d_codes, db->d_start, db->d_len, db->d_orig, db->n};
-  return launch_one(c, p, dbv, t->d_tjb, t->d_xjmin, (uint8_t *) d_xj, (uint8_t *) d_flags);
+  if (p->G == 32 || !p->d_stab_g)
+    return launch_one(c, p, dbv, t->d_tjb, t->d_xjmin, (uint8_t *) d_xj, (uint8_t *) d_flags);
+  // G-lane SSV pass, then the full MSV on the sequences it left undecided
+  if (c->list_cap < (size_t) db->n) {
+    CUDA_TRY(cudaStreamSynchronize(c->stream));            // the old list may still be read
+    cudaFree(c->d_list); c->d_list = nullptr; c->list_cap = 0;
+    CUDA_TRY(cudaMalloc(&c->d_list, sizeof(int64_t) * db->n));
+    c->list_cap = db->n;
+  }
+  ProfDev P;
+  P.M = p->M; P.C = p->Cg; P.tbm = p->tbm; P.tec = p->tec; P.base = p->base; P.bias = p->bias;
+  P.stab = p->d_stab_g; P.mtab = p->d_mtab; P.tjb = t->d_tjb; P.xjmin = t->d_xjmin; P.ssv_f16 = 1;
+  GroupArgs g;
+  g.P = P; g.db = dbv; g.out_xj = (uint8_t *) d_xj; g.out_flags = (uint8_t *) d_flags;
+  g.ticket = c->d_ticket; g.undecided = c->d_list; g.n_undecided = c->d_aux + 1; g.stream = c->stream;
+  CUDA_TRY(cudaMemsetAsync(c->d_ticket, 0, sizeof(unsigned long long), c->stream));
+  CUDA_TRY(cudaMemsetAsync(c->d_aux, 0, 2 * sizeof(unsigned long long), c->stream));
+  CUDA_TRY(dispatch_group(p->Cg, p->G, g, c->num_sms));
+  count_launch();
+  ProfDev Pb;
+  Pb.M = p->M; Pb.C = p->C; Pb.tbm = p->tbm; Pb.tec = p->tec; Pb.base = p->base; Pb.bias = p->bias;
+  Pb.stab = p->d_stab; Pb.mtab = p->d_mtab; Pb.tjb = t->d_tjb; Pb.xjmin = t->d_xjmin; Pb.ssv_f16 = p->f16;
+  LaunchArgs a;
+  a.P = Pb; a.db = dbv; a.out_xj = (uint8_t *) d_xj; a.out_flags = (uint8_t *) d_flags; a.ticket = c->d_aux;
+  a.stream = c->stream; a.grid = 0; a.skip_empty = 1; a.list = c->d_list; a.list_count = c->d_aux + 1;
+  CUDA_TRY(dispatch(p->C, p->f16 != 0, a, c->num_sms));
+  count_launch();
+  return MSVGB_eslOK;
 }
 
 extern "C" int msvgb_search(msvgb_ctx *c, const msvgb_profile *p, const msvgb_db *db, double F1,

@@ -22,6 +22,7 @@
 //  * MSV: sat_add(max(mpv,xB),bias) never clips before the row whose overflow
 //    test fires, except through xB; clamping xB to 255-bias per row reproduces it.
 #pragma once
+#include <atomic>
 #include <cstdint>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -177,17 +178,38 @@ __device__ __forceinline__ uint32_t msv_row(uint32_t (&dp)[C], uint32_t xBp, uin
 
 // Scores one (profile, sequence). Returns status; *xj_out the final xJ;
 // *full_out whether phase B ran.
+// Decision logic of p7_SSVFilter (ssvfilter.c:1364-1413) from the maximum
+// cell u_max of the J-free recurrence, in the reference's own uint16
+// arithmetic. The reference's xE is the max over cells of the unsigned byte
+// (u+128); any cell with u >= 127-bias makes it >= 255-bias (first-crossing
+// argument: a diagonal rises by at most bias per step), otherwise xE = u_max+128.
+// Returns ST_OK / ST_ERANGE, or -1 when SSV is undecided.
+__device__ __forceinline__ int ssv_decide(int umax, int tjb, int tbm, int tec, int base, int bias, int &xj_out) {
+  const int d = base - tjb - tbm;
+  if (umax >= 127 - bias) {
+    if (d >= 128) { xj_out = 255; return ST_ERANGE; }
+    return -1;                                   // the plain MSV may not overflow
+  }
+  uint16_t xE = (uint16_t) (umax + 128);
+  xE = (uint16_t) (xE + base - tjb - tbm);
+  xE = (uint16_t) (xE - 128);
+  if (xE >= 255 - bias) { xj_out = 255; return ST_ERANGE; }
+  const uint16_t xJ = (uint16_t) (xE - tec);
+  if (xJ <= base) { xj_out = xJ; return ST_OK; }
+  return -1;                                     // the J state could have been used
+}
+
 template <int C, bool F16>
 __device__ __forceinline__ int msv_one(const ProfDev &P, const uint32_t *__restrict__ stab,
                                        const uint32_t *__restrict__ mtab,
                                        const uint32_t *__restrict__ sq, int L, int lane,
-                                       int &xj_out, int &full_out) {
+                                       int &xj_out, int &full_out, bool skip_ssv = false) {
   const int tjb  = P.tjb[L];
   const int tbm  = P.tbm, tec = P.tec, base = P.base, bias = P.bias;
   full_out = 0;
 
   // ---------- Phase A: SSV (ssvfilter.c:1364-1413) ----------
-  if (tjb + tbm + tec + bias < 127) {
+  if (!skip_ssv && tjb + tbm + tec + bias < 127) {
     uint32_t dp[C];
 #pragma unroll
     for (int w = 0; w < C; ++w) dp[w] = 0u;
@@ -220,23 +242,8 @@ __device__ __forceinline__ int msv_one(const ProfDev &P, const uint32_t *__restr
     }
     umax = (int) __reduce_max_sync(FULL, (unsigned) umax);
 
-    // Decision logic of p7_SSVFilter, in its own uint16 arithmetic. The
-    // reference's xE is max over cells of the unsigned byte (u+128); any cell
-    // with u >= 127-bias makes it >= 255-bias (first-crossing argument: a
-    // diagonal rises by at most bias per step), and otherwise xE = umax+128.
-    const int d = base - tjb - tbm;
-    if (umax >= 127 - bias) {
-      if (d >= 128) { xj_out = 255; return ST_ERANGE; }
-      // d < 128: the plain MSV may not overflow -> undecided, fall through
-    } else {
-      uint16_t xE = (uint16_t) (umax + 128);
-      xE = (uint16_t) (xE + base - tjb - tbm);
-      xE = (uint16_t) (xE - 128);
-      if (xE >= 255 - bias) { xj_out = 255; return ST_ERANGE; }
-      const uint16_t xJ = (uint16_t) (xE - tec);
-      if (xJ <= base) { xj_out = xJ; return ST_OK; }
-      // the J state could have been used: undecided
-    }
+    const int st = ssv_decide(umax, tjb, tbm, tec, base, bias, xj_out);
+    if (st >= 0) return st;
   }
 
   // ---------- Phase B: full MSV (msvfilter.c:112-212) ----------
@@ -268,6 +275,19 @@ __device__ __forceinline__ int msv_one(const ProfDev &P, const uint32_t *__restr
   }
   xj_out = xJ;
   return ST_OK;
+}
+
+// The dynamic shared memory opt-in of a kernel, once per device (the
+// attribute belongs to the current device's context).
+inline cudaError_t ensure_smem_attr(const void *kern, size_t smem, std::atomic<unsigned long long> &done) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (done.load(std::memory_order_acquire) & bit) return cudaSuccess;
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+  if (e == cudaSuccess) done.fetch_or(bit, std::memory_order_release);
+  return e;
 }
 
 }  // namespace msvgb

@@ -1,0 +1,176 @@
+// msv_group.cuh -- SSV pass with G < 32 lanes per sequence.
+//
+// For small models a whole warp per sequence leaves each lane only a few DP
+// words per row, so the per-row overhead (the shuffle, the residue decode,
+// the table address) dominates. Here G lanes (8 or 16) score one sequence and
+// a warp carries 32/G sequences in lockstep: each group owns its sequence
+// state (index, row, residue word) and fetches the next sequence when its own
+// ends, while all lanes execute the same row code every step (finished groups
+// run pad rows, whose costs keep every cell at the floor). Lane g of a group
+// owns nodes g*2C+1 .. (g+1)*2C with the same two-way striping as the 32-lane
+// kernel. Only phase A (SSV) runs here; sequences SSV leaves undecided, or
+// whose length disables SSV, are appended to a list that the 32-lane kernel
+// then scores with the full MSV recurrence (list mode).
+#pragma once
+#include "msv_device.cuh"
+
+namespace msvgb {
+
+template <int C, int G>
+struct GroupLayout {
+  static constexpr int Q4 = C / 4, R = C % 4;
+  static constexpr int A_WORDS = NRES * Q4 * G * 4;              // quads [x][q][g][4]
+  static constexpr int B_WORDS = (R >= 2) ? NRES * G * 2 : 0;    // pair  [x][g][2]
+  static constexpr int C_WORDS = (R & 1) ? NRES * G : 0;         // single [x][g]
+  static constexpr int WORDS = A_WORDS + B_WORDS + C_WORDS;      // == NRES * C * G
+};
+
+template <int C, int G>
+__device__ __forceinline__ void ssv_row_group(uint32_t (&dp)[C], uint32_t &acc0, uint32_t &acc1,
+                                              const uint32_t *__restrict__ tab, int x, int glane, int src_lane) {
+  using Lay = GroupLayout<C, G>;
+  constexpr uint32_t one2 = 0x3C003C00u;
+  uint32_t s[C];
+#pragma unroll
+  for (int q = 0; q < Lay::Q4; ++q) {
+    const uint4 v = *reinterpret_cast<const uint4 *>(tab + ((x * Lay::Q4 + q) * G + glane) * 4);
+    s[4 * q] = v.x; s[4 * q + 1] = v.y; s[4 * q + 2] = v.z; s[4 * q + 3] = v.w;
+  }
+  if constexpr (Lay::R >= 2) {
+    const uint2 v = *reinterpret_cast<const uint2 *>(tab + Lay::A_WORDS + (x * G + glane) * 2);
+    s[4 * Lay::Q4] = v.x; s[4 * Lay::Q4 + 1] = v.y;
+  }
+  if constexpr (Lay::R & 1) s[C - 1] = tab[Lay::A_WORDS + Lay::B_WORDS + x * G + glane];
+  const uint32_t pred0 = pred_word0(dp[C - 1], src_lane);   // all 32 lanes, every row
+#pragma unroll
+  for (int w = C - 1; w >= 0; --w) {
+    dp[w] = fma_relu_f16x2(w ? dp[w - 1] : pred0, one2, s[w]);
+    if (w & 1) acc1 = max_f16x2(acc1, dp[w]); else acc0 = max_f16x2(acc0, dp[w]);
+  }
+}
+
+struct GroupArgs {
+  ProfDev P;                       // P.stab: the G-lane f16 SSV table
+  DbDev db;
+  uint8_t *out_xj, *out_flags;
+  unsigned long long *ticket;
+  int64_t *undecided;              // sorted indices left for the full MSV pass
+  unsigned long long *n_undecided;
+  cudaStream_t stream;
+};
+
+constexpr uint32_t kPadWord = 0x1D1D1D1Du;   // four PAD_CODE residues
+
+template <int C, int G>
+__global__ void __launch_bounds__(256)
+msv_ssv_group_kernel(ProfDev P, DbDev db, uint8_t *__restrict__ out_xj, uint8_t *__restrict__ out_flags,
+                     unsigned long long *__restrict__ ticket, int64_t *__restrict__ undecided,
+                     unsigned long long *__restrict__ n_undecided) {
+  extern __shared__ __align__(16) uint32_t smem[];
+  using Lay = GroupLayout<C, G>;
+  {
+    const uint4 *gs = reinterpret_cast<const uint4 *>(P.stab);
+    uint4 *ss = reinterpret_cast<uint4 *>(smem);
+    for (int i = threadIdx.x; i < Lay::WORDS / 4; i += blockDim.x) ss[i] = __ldg(gs + i);
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, glane = lane % G, gbase = lane - glane;
+  const int src_lane = gbase + (glane + G - 1) % G;
+  const unsigned gmask = (G == 32) ? FULL : (((1u << G) - 1u) << gbase);
+  const int tbm = P.tbm, tec = P.tec, base = P.base, bias = P.bias;
+
+  int64_t s = 0;
+  int L = 0, i = 0, tjb = 0;
+  const uint32_t *sq = nullptr;
+  uint32_t nextw = kPadWord;
+  bool need = true, done = false;
+  uint32_t dp[C];
+  uint32_t acc0 = 0u, acc1 = 0u;
+#pragma unroll
+  for (int w = 0; w < C; ++w) dp[w] = 0u;
+
+  for (;;) {
+    if (need && !done) {                              // group-uniform: take the next sequence
+      unsigned long long t = 0;
+      if (glane == 0) t = atomicAdd(ticket, 1ull);
+      t = __shfl_sync(gmask, t, gbase);
+      if (t >= (unsigned long long) db.n) {
+        done = true;
+      } else {
+        s = (int64_t) t;
+        L = db.len[s];
+        tjb = P.tjb[L];
+        if (L == 0) {                                 // skipped, as p7_Pipeline does
+          if (glane == 0) { const int64_t oi = db.orig[s]; out_xj[oi] = 0; out_flags[oi] = 0x08; }
+        } else if (tjb + tbm + tec + bias >= 127) {   // SSV disabled for this length: full MSV
+          if (glane == 0) undecided[atomicAdd(n_undecided, 1ull)] = s;
+        } else {
+          sq = reinterpret_cast<const uint32_t *>(db.codes + db.start[s]);
+          nextw = __ldg(sq);
+          i = 0;
+          need = false;
+#pragma unroll
+          for (int w = 0; w < C; ++w) dp[w] = 0u;
+          acc0 = acc1 = 0u;
+        }
+      }
+    }
+    if (__all_sync(FULL, done)) break;
+    const bool active = !need && !done;
+    const uint32_t w4 = active ? nextw : kPadWord;
+    if (active && i + 4 < L) nextw = __ldg(sq + (i >> 2) + 1);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) ssv_row_group<C, G>(dp, acc0, acc1, smem, (w4 >> (8 * j)) & 0xFF, glane, src_lane);
+    i += 4;
+    const bool fin = active && i >= L;
+    if (__any_sync(FULL, fin)) {                      // group maxima (all lanes take part)
+      const __half2 a = __hmax2(*reinterpret_cast<const __half2 *>(&acc0),
+                                *reinterpret_cast<const __half2 *>(&acc1));
+      float f = fminf(fmaxf(__low2float(a), __high2float(a)), 4096.0f);
+#pragma unroll
+      for (int off = G / 2; off >= 1; off >>= 1) f = fmaxf(f, __shfl_xor_sync(FULL, f, off));
+      if (fin) {
+        int xj = 0;
+        const int st = ssv_decide((int) f, tjb, tbm, tec, base, bias, xj);
+        if (glane == 0) {
+          if (st < 0) {
+            undecided[atomicAdd(n_undecided, 1ull)] = s;
+          } else {
+            const int64_t oi = db.orig[s];
+            int flags = 0;
+            if (st == ST_ERANGE) flags |= 0x01 | 0x02;
+            else if (xj >= P.xjmin[L]) flags |= 0x02;
+            out_xj[oi] = (uint8_t) xj;
+            out_flags[oi] = (uint8_t) flags;
+          }
+        }
+        need = true;
+      }
+    }
+  }
+}
+
+template <int C, int G>
+cudaError_t launch_ssv_group(const GroupArgs &a, int num_sms) {
+  auto kern = msv_ssv_group_kernel<C, G>;
+  constexpr size_t smem = (size_t) GroupLayout<C, G>::WORDS * 4;
+  static std::atomic<unsigned long long> configured{0};
+  {
+    cudaError_t e = ensure_smem_attr((const void *) kern, smem, configured);
+    if (e != cudaSuccess) return e;
+  }
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem);
+  if (e != cudaSuccess) return e;
+  int grid = std::max(1, per_sm) * num_sms;
+  const long long need = (a.db.n * G + 255) / 256;        // 256 threads hold 256/G sequences
+  if (need < grid) grid = (int) std::max(1LL, need);
+  (void) cudaGetLastError();
+  kern<<<grid, 256, smem, a.stream>>>(a.P, a.db, a.out_xj, a.out_flags, a.ticket, a.undecided, a.n_undecided);
+  return cudaGetLastError();
+}
+
+}  // namespace msvgb
+
+#define MSVGB_INSTANTIATE_GROUP(C, G) \
+  template cudaError_t msvgb::launch_ssv_group<C, G>(const msvgb::GroupArgs &, int);

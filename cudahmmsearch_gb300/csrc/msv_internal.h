@@ -11,6 +11,7 @@
 
 #include "../../include/msvgb.h"
 #include "msv_kernel_impl.cuh"
+#include "msv_group.cuh"
 
 struct msvgb_ctx {
   int device = 0;
@@ -26,6 +27,8 @@ struct msvgb_ctx {
   int64_t *d_meta = nullptr;                            // start, orig (int64), len (int32) for n=1
   uint8_t *d_out = nullptr;
   int *d_bad = nullptr;                                 // database packing: invalid-code flag
+  int64_t *d_list = nullptr; size_t list_cap = 0;       // G-lane search: sequences left for the full MSV
+  unsigned long long *d_aux = nullptr;                  // [0] second ticket, [1] list count
   void *h_stage = nullptr; size_t h_stage_cap = 0;      // pinned staging for database metadata
 };
 
@@ -50,6 +53,9 @@ struct msvgb_profile {
   uint8_t tbm = 0, tec = 0, base = 0, bias = 0;
   float scale = 0.f, mmu = 0.f, mlambda = 0.f;
   uint32_t *d_stab = nullptr, *d_mtab = nullptr;
+  int G = 32;                         // lanes per sequence in the SSV pass (32: fused kernel)
+  int Cg = 0;                         // DP words per lane of the G-lane table
+  uint32_t *d_stab_g = nullptr;       // f16 SSV table in the G-lane layout
   std::vector<LenTables *> tables;    // one per F1 value used
   std::mutex tables_mu;
 };
@@ -78,6 +84,8 @@ int xjmin_for(const msvgb_profile *p, int L, double F1);
 int profile_build_width(msvgb_ctx *ctx, const msvgb_om *om, int want_f16, int force_C, msvgb_profile **ret);
 // Host images of the device cost tables of a profile at DP width C.
 int build_cost_tables(const msvgb_om *om, int f16, int C, std::vector<uint32_t> &st, std::vector<uint32_t> &mt);
+// Launches the G-lane SSV pass (msv_group.cuh).
+cudaError_t dispatch_group(int C, int G, const msvgb::GroupArgs &a, int sms);
 // Per-length tjb_b and pass-threshold tables of (profile, database, F1), cached in the profile.
 int ensure_tables(msvgb_profile *p, const msvgb_db *db, double F1, LenTables **out);
 // Adds one to the count msvgb_kernel_launches() reports.

@@ -15,6 +15,10 @@ struct LaunchArgs {
   cudaStream_t        stream;
   int                 grid;       // 0: fill the GPU
   int                 skip_empty; // 1: L == 0 is skipped as p7_Pipeline does; 0: scored like p7_MSVFilter
+  // List mode: score only the sorted sequences list[0 .. *list_count) with the
+  // full MSV recurrence (they are the ones the G-lane SSV pass left undecided).
+  const int64_t            *list = nullptr;
+  const unsigned long long *list_count = nullptr;
 };
 
 constexpr int WARPS_PER_CTA = 8;
@@ -35,7 +39,8 @@ constexpr int cta_threads() { return 2 * smem_bytes<C, F16>() > 227 * 1024 ? MAX
 template <int C, bool F16>
 __global__ void __launch_bounds__(cta_threads<C, F16>())
 msv_search_kernel(ProfDev P, DbDev db, uint8_t *__restrict__ out_xj, uint8_t *__restrict__ out_flags,
-                  unsigned long long *__restrict__ ticket, int skip_empty) {
+                  unsigned long long *__restrict__ ticket, int skip_empty,
+                  const int64_t *__restrict__ list, const unsigned long long *__restrict__ list_count) {
   extern __shared__ __align__(16) uint32_t smem[];
   constexpr int SW = F16 ? NRES * C * 32 : NRES * (C / 2) * 32;   // words of the SSV table
   constexpr int MW = NRES * ((C + 1) / 2) * 32;                    // words of the MSV table
@@ -52,11 +57,13 @@ msv_search_kernel(ProfDev P, DbDev db, uint8_t *__restrict__ out_xj, uint8_t *__
   __syncthreads();
 
   const int lane = threadIdx.x & 31;
+  const unsigned long long nitems = list ? *list_count : (unsigned long long) db.n;
   for (;;) {
     unsigned long long s = 0;
     if (lane == 0) s = atomicAdd(ticket, 1ull);
     s = __shfl_sync(FULL, s, 0);
-    if (s >= (unsigned long long) db.n) break;
+    if (s >= nitems) break;
+    if (list) s = (unsigned long long) list[s];
     const int L = db.len[s];
     const int64_t oi = db.orig[s];
     if (L == 0 && skip_empty) {
@@ -65,7 +72,7 @@ msv_search_kernel(ProfDev P, DbDev db, uint8_t *__restrict__ out_xj, uint8_t *__
     }
     const uint32_t *sq = reinterpret_cast<const uint32_t *>(db.codes + db.start[s]);
     int xj, full;
-    const int st = msv_one<C, F16>(P, stab, mtab, sq, L, lane, xj, full);
+    const int st = msv_one<C, F16>(P, stab, mtab, sq, L, lane, xj, full, list != nullptr);
     if (lane == 0) {
       int flags = full ? 0x04 : 0;
       if (st == ST_ERANGE) flags |= 0x01 | 0x02;                 // +inf always passes F1
@@ -80,11 +87,10 @@ template <int C, bool F16>
 cudaError_t launch_search(const LaunchArgs &a, int num_sms) {
   auto kern = msv_search_kernel<C, F16>;
   constexpr size_t smem = smem_bytes<C, F16>();
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+  static std::atomic<unsigned long long> configured{0};
+  {
+    cudaError_t e = ensure_smem_attr((const void *) kern, smem, configured);
     if (e != cudaSuccess) return e;
-    configured = true;
   }
   constexpr int threads = cta_threads<C, F16>();
   int grid = a.grid;
@@ -96,10 +102,11 @@ cudaError_t launch_search(const LaunchArgs &a, int num_sms) {
     grid = per_sm * num_sms;
     const int warps = threads / 32;
     const long long need = (a.db.n + warps - 1) / warps;
-    if (need < grid) grid = (int) (need > 0 ? need : 1);
+    if (!a.list && need < grid) grid = (int) (need > 0 ? need : 1);
   }
   (void) cudaGetLastError();   // clear a stale error left by an unrelated call
-  kern<<<grid, threads, smem, a.stream>>>(a.P, a.db, a.out_xj, a.out_flags, a.ticket, a.skip_empty);
+  kern<<<grid, threads, smem, a.stream>>>(a.P, a.db, a.out_xj, a.out_flags, a.ticket, a.skip_empty,
+                                               a.list, a.list_count);
   return cudaGetLastError();
 }
 

@@ -95,6 +95,14 @@ int msvgb_profile_create(msvgb_ctx *ctx, const msvgb_om *om, msvgb_profile **ret
  * otherwise variant 0 is used). msvgb_profile_variant() tells which. */
 int msvgb_profile_create_ex(msvgb_ctx *ctx, const msvgb_om *om, int ssv_variant, msvgb_profile **ret_prof);
 int msvgb_profile_variant(const msvgb_profile *prof);
+/* Lanes per sequence of the SSV pass: 32 (default; one warp per sequence, SSV
+ * and full MSV in one kernel), or 16 / 8 (2 / 4 sequences per warp in
+ * lockstep, for small models: each lane then holds more DP words per row);
+ * with 16 or 8 the sequences SSV leaves undecided are finished by the full
+ * MSV in a second launch. om must be the profile's own MSV fields. Needs
+ * M < 64 * G and, for G < 32, M >= 2 * G. Chosen by msvgb_autotune. */
+int msvgb_profile_set_lanes(msvgb_profile *prof, const msvgb_om *om, int lanes);
+int msvgb_profile_lanes(const msvgb_profile *prof);
 int msvgb_profile_destroy(msvgb_profile *prof);
 int msvgb_profile_M(const msvgb_profile *prof);
 
