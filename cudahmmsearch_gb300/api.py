@@ -19,6 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libmsvgb.so")
 
 eslOK, eslEMEM, eslEINVAL, eslESYS, eslERANGE = 0, 5, 11, 12, 16
+eslENOTFOUND, eslEFORMAT, eslEINCOMPAT, eslEWRITE = 6, 7, 10, 27
 FLAG_ERANGE, FLAG_PASS, FLAG_FULL, FLAG_EMPTY = 0x01, 0x02, 0x04, 0x08
 
 # Every function declared in include/msvgb.h.
@@ -32,6 +33,7 @@ EXPORTS = [
     "msvgb_batch_create", "msvgb_batch_run", "msvgb_batch_items", "msvgb_batch_destroy", "msvgb_search_batch",
     "msvgb_server_create", "msvgb_server_slots", "msvgb_server_submit", "msvgb_server_wait",
     "msvgb_server_launches", "msvgb_server_destroy", "msvgb_pipeline_run",
+    "msvgb_autotune", "msvgb_tune_save", "msvgb_tune_load", "msvgb_tune_lanes",
 ]
 
 
@@ -76,6 +78,10 @@ def lib():
         "msvgb_profile_create_ex": (i32, [vp, ctypes.POINTER(_Om), i32, ctypes.POINTER(vp)]),
         "msvgb_profile_variant": (i32, [vp]),
         "msvgb_profile_set_lanes": (i32, [vp, ctypes.POINTER(_Om), i32]),
+        "msvgb_autotune": (i32, [vp, ctypes.c_double]),
+        "msvgb_tune_save": (i32, [vp, ctypes.c_char_p]),
+        "msvgb_tune_load": (i32, [vp, ctypes.c_char_p]),
+        "msvgb_tune_lanes": (i32, [vp, i32, i32, ctypes.POINTER(i32)]),
         "msvgb_profile_lanes": (i32, [vp]),
         "msvgb_profile_destroy": (i32, [vp]),
         "msvgb_profile_M": (i32, [vp]),
@@ -151,6 +157,34 @@ class Context:
             self.close()
         except Exception:
             pass
+
+    # -- lane-count autotuner ---------------------------------------------------
+    def autotune(self, budget_s: float = 0.0, cache: str | None = None) -> str:
+        """Lanes per sequence per (model length, target-length bin) for this GPU.
+        With cache: load it when it was measured on this GPU model, else measure
+        and write it. Returns "loaded" or "measured"."""
+        if cache and os.path.exists(cache):
+            st = lib().msvgb_tune_load(self.h, cache.encode())
+            if st == eslOK:
+                return "loaded"
+            if st not in (eslEFORMAT, eslEINCOMPAT):
+                _check(st)
+        _check(lib().msvgb_autotune(self.h, budget_s))
+        if cache:
+            _check(lib().msvgb_tune_save(self.h, cache.encode()))
+        return "measured"
+
+    def tune_save(self, path: str):
+        _check(lib().msvgb_tune_save(self.h, path.encode()))
+
+    def tune_load(self, path: str):
+        _check(lib().msvgb_tune_load(self.h, path.encode()))
+
+    def tune_lanes(self, M: int, L: int = -1):
+        """(lanes, variant) the context picks for model length M and target length L (-1: mix)."""
+        v = ctypes.c_int()
+        g = lib().msvgb_tune_lanes(self.h, M, L, ctypes.byref(v))
+        return int(g), int(v.value)
 
     # -- p7_MSVFilter drop-in --------------------------------------------------
     def MSVFilter(self, dsq: np.ndarray, L: int, om: F.Profile, tjb_b: int, allocQ16: int | None = None):

@@ -198,6 +198,7 @@ extern "C" int msvgb_ctx_destroy(msvgb_ctx *c) {
   cudaFree(c->d_seq); cudaFree(c->d_tab); cudaFree(c->d_bad); cudaFree(c->d_aux); cudaFree(c->d_list);
   if (c->h_stage) cudaFreeHost(c->h_stage);
   if (c->own) cudaStreamDestroy(c->own);
+  msvgb_detail::tune_free(c);
   delete c;
   return MSVGB_eslOK;
 }
@@ -316,10 +317,20 @@ static int profile_build(msvgb_ctx *ctx, const msvgb_om *om, int want_f16, msvgb
 
 static int default_f16() { return 1; }
 
+// Lanes per sequence and SSV table type from the context's tuning table (or
+// the fixed rule) for the whole length mix.
 extern "C" int msvgb_profile_create(msvgb_ctx *ctx, const msvgb_om *om, msvgb_profile **ret) {
   if (!ctx) return fail(MSVGB_eslEINVAL, "ctx is NULL");
   if (ret) *ret = nullptr;
-  return profile_build(ctx, om, default_f16(), ret);
+  if (!om) return fail(MSVGB_eslEINVAL, "om is NULL");
+  int variant = default_f16();
+  const int G = om->M >= 1 ? msvgb_detail::lanes_for(ctx, om->M, -1, &variant) : 32;
+  int st = profile_build(ctx, om, G < 32 ? 1 : variant, ret);
+  if (st == MSVGB_eslOK && G < 32 && (*ret)->f16) {
+    st = msvgb_profile_set_lanes(*ret, om, G);
+    if (st != MSVGB_eslOK) { msvgb_profile_destroy(*ret); *ret = nullptr; }
+  }
+  return st;
 }
 
 extern "C" int msvgb_profile_create_ex(msvgb_ctx *ctx, const msvgb_om *om, int variant, msvgb_profile **ret) {
@@ -347,7 +358,7 @@ extern "C" int msvgb_profile_destroy(msvgb_profile *p) {
 extern "C" int msvgb_profile_M(const msvgb_profile *p) { return p ? p->M : -1; }
 
 // G-lane SSV table: node g*2C + h*C + w + 1 of lane g in word w, half h.
-static std::vector<uint32_t> build_group_table(const msvgb_om *om, int C, int G) {
+std::vector<uint32_t> msvgb_detail::build_group_table(const msvgb_om *om, int C, int G) {
   const int M = om->M, Q = std::max(2, (M - 1) / 16 + 1), bias = om->bias_b;
   auto s_of = [&](int x, int k) -> int {
     if (x >= 29 || k > M) return -128;

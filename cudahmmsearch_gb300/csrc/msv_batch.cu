@@ -4,12 +4,17 @@
 // The work queue holds (profile, sequence-chunk) items over the length-sorted
 // database: profile-major (largest models first), and within a profile from
 // the longest sequences to the shortest, so the tail of the launch is made of
-// short items. Each CTA pops an item, stages that profile's cost tables into
-// shared memory if it is not the one already there, and its warps take the
-// chunk's sequences one by one (one warp per sequence, as in the single-query
-// kernel). The profile's DP width C is a per-item runtime value dispatched to
-// a compile-time instantiation, so profiles of any length share one launch.
+// short items. Each CTA pops an item, stages that item's cost tables into
+// shared memory if they are not the ones already there, and scores the chunk:
+// one warp per sequence (SSV and MSV fused, as in the single-query kernel), or
+// for items whose (model length, target-length bin) the lane choice puts on 16
+// or 8 lanes, the lane-group SSV pass and then the full MSV on the sequences
+// it left undecided. DP widths and lane counts are per-item runtime values
+// dispatched to compile-time instantiations, so profiles of any length share
+// one launch.
 #include <algorithm>
+#include <array>
+#include <climits>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -27,13 +32,13 @@ namespace {
 
 
 struct BatchItem {
-  int32_t prof;
-  int32_t pad;
+  int32_t var;                 // profile variant (tables at one lane count)
+  int32_t prof;                // output block
   int64_t s_begin, s_end;      // sorted-sequence range
 };
 
 struct BatchArgs {
-  const ProfDev *profs;        // [nprof], f16 tables
+  const ProfDev *vars;         // [nvar]: each profile at the lane counts its items use
   DbDev db;
   const BatchItem *items;
   int64_t nitems;
@@ -46,39 +51,27 @@ __global__ void __launch_bounds__(512) msv_batch_kernel(BatchArgs a) {
   extern __shared__ __align__(16) uint32_t smem[];
   __shared__ long long item_sh;
   __shared__ int loaded_sh;
-  __shared__ unsigned long long next_seq;
-  const int lane = threadIdx.x & 31;
+  __shared__ ChunkShared cs;
   if (threadIdx.x == 0) loaded_sh = -1;
   for (;;) {
     __syncthreads();                                   // previous item fully done
     if (threadIdx.x == 0) {
       item_sh = (long long) atomicAdd(a.ticket, 1ull);
-      next_seq = 0ull;
+      cs.next_seq = 0u; cs.n_und = 0u; cs.next_und = 0u;
     }
     __syncthreads();
     const long long it = item_sh;
     if (it >= a.nitems) break;
     const BatchItem item = a.items[it];
-    const ProfDev &P = a.profs[item.prof];
-    const int C = P.C;
-    uint32_t *stab = smem;
-    uint32_t *mtab = smem + NRES * C * 32;
-    if (loaded_sh != item.prof) {                       // stage this profile's tables
+    const ProfDev &P = a.vars[item.var];
+    if (loaded_sh != item.var) {                        // stage this variant's tables
       stage_tables(P, smem);
       __syncthreads();
-      if (threadIdx.x == 0) loaded_sh = item.prof;
+      if (threadIdx.x == 0) loaded_sh = item.var;
     }
     uint8_t *oxj = a.out_xj + (int64_t) item.prof * a.db.n;
     uint8_t *ofl = a.out_flags + (int64_t) item.prof * a.db.n;
-    const int64_t nseq = item.s_end - item.s_begin;
-    for (;;) {
-      unsigned long long k = 0;
-      if (lane == 0) k = atomicAdd(&next_seq, 1ull);
-      k = __shfl_sync(FULL, k, 0);
-      if ((long long) k >= nseq) break;
-      const int64_t s = item.s_begin + (int64_t) k;
-      run_seq_any(C, P, stab, mtab, a.db, s, lane, oxj, ofl);
-    }
+    run_chunk(P, smem, smem + ssv_words(P), a.db, item.s_begin, item.s_end - item.s_begin, oxj, ofl, cs);
   }
 }
 
@@ -91,9 +84,11 @@ struct msvgb_batch {
   int nprof = 0;
   int64_t n = 0;
   std::vector<msvgb_profile *> own;     // re-laid profiles at the batch DP widths
-  ProfDev *d_profs = nullptr;
+  std::vector<uint32_t *> gtabs;        // lane-group SSV tables
+  ProfDev *d_vars = nullptr;
   BatchItem *d_items = nullptr;
   int64_t nitems = 0;
+  int nvars = 0;
   unsigned long long *d_ticket = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -106,14 +101,20 @@ extern "C" int msvgb_batch_destroy(msvgb_batch *b) {
   cudaSetDevice(b->device);
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->graph) cudaGraphDestroy(b->graph);
-  cudaFree(b->d_profs); cudaFree(b->d_items); cudaFree(b->d_ticket);
+  cudaFree(b->d_vars); cudaFree(b->d_items); cudaFree(b->d_ticket);
+  for (auto *t : b->gtabs) cudaFree(t);
   for (auto *p : b->own) msvgb_profile_destroy(p);
   delete b;
   return MSVGB_eslOK;
 }
 
-extern "C" int msvgb_batch_create(msvgb_ctx *ctx, const msvgb_om *const *oms, int nprof, const msvgb_db *db,
-                                  double F1, void *d_xj, void *d_flags, msvgb_batch **ret) {
+// Work items: for each profile (largest models first), for each target-length
+// bin of the sorted database (longest first), chunks of about per_item
+// residues -- at most kChunkMaxSeqs sequences when the bin's lane count is
+// below 32 -- all scored with the variant the lane choice gives that
+// (profile, bin).
+int msvgb_detail::batch_create(msvgb_ctx *ctx, const msvgb_om *const *oms, int nprof, const msvgb_db *db,
+                               double F1, void *d_xj, void *d_flags, int force_lanes, msvgb_batch **ret) {
   if (!ctx || !oms || nprof < 1 || !db || !ret || (db->n && (!d_xj || !d_flags)))
     return fail(MSVGB_eslEINVAL, "msvgb_batch_create: bad arguments");
   *ret = nullptr;
@@ -121,14 +122,34 @@ extern "C" int msvgb_batch_create(msvgb_ctx *ctx, const msvgb_om *const *oms, in
   b->ctx = ctx; b->device = ctx->device; b->nprof = nprof; b->n = db->n;
   cudaError_t e = cudaSetDevice(ctx->device);
   if (e != cudaSuccess) { delete b; return fail(MSVGB_eslESYS, cudaGetErrorString(e)); }
-  // profiles re-laid at the batch DP widths (f16 SSV tables) with their length tables
-  std::vector<ProfDev> hp(nprof);
-  std::vector<int> order(nprof);
-  int cmax = 1;
+  auto bail = [&](int code, const std::string &msg) { msvgb_batch_destroy(b); return fail(code, msg); };
+
+  // length bins of the sorted (descending) database: bin_end[k] = first sorted index of a shorter bin
+  std::vector<int32_t> len(db->n);
+  if (db->n) {
+    e = cudaMemcpy(len.data(), db->d_len, db->n * 4, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return bail(MSVGB_eslESYS, cudaGetErrorString(e));
+  }
+  struct Range { int bin; int64_t a, b; };
+  std::vector<Range> ranges;                                  // longest bin first
+  for (int64_t s = 0; s < db->n;) {
+    const int bin = msvgb_detail::lbin_of(len[s]);
+    int64_t t = s;
+    while (t < db->n && msvgb_detail::lbin_of(len[t]) == bin) ++t;
+    ranges.push_back(Range{bin, s, t});
+    s = t;
+  }
+
+  // variants: every profile at 32 lanes (its MSV table serves all), plus the
+  // lane-group tables its bins ask for
+  std::vector<ProfDev> vars;
+  std::vector<std::array<int, msvgb_detail::kNLBins>> var_of(nprof);
+  size_t smem = 0;
   for (int i = 0; i < nprof; ++i) {
-    if (!oms[i]) { msvgb_batch_destroy(b); return fail(MSVGB_eslEINVAL, "NULL profile"); }
-    const int C = multi_C(oms[i]->M);
-    if (C < 0) { msvgb_batch_destroy(b); return fail(MSVGB_eslEINVAL, "batched profiles are limited to M <= 2047"); }
+    if (!oms[i]) return bail(MSVGB_eslEINVAL, "NULL profile");
+    const int M = oms[i]->M;
+    const int C = multi_C(M);
+    if (C < 0) return bail(MSVGB_eslEINVAL, "batched profiles are limited to M <= 2047");
     msvgb_profile *p = nullptr;
     int st = msvgb_detail::profile_build_width(ctx, oms[i], 1, C, &p);
     if (st != MSVGB_eslOK) { msvgb_batch_destroy(b); return st; }
@@ -136,54 +157,77 @@ extern "C" int msvgb_batch_create(msvgb_ctx *ctx, const msvgb_om *const *oms, in
     LenTables *t = nullptr;
     st = msvgb_detail::ensure_tables(p, db, F1, &t);
     if (st != MSVGB_eslOK) { msvgb_batch_destroy(b); return st; }
-    ProfDev &P = hp[i];
+    ProfDev P;
     P.M = p->M; P.C = p->C; P.tbm = p->tbm; P.tec = p->tec; P.base = p->base; P.bias = p->bias;
     P.stab = p->d_stab; P.mtab = p->d_mtab; P.tjb = t->d_tjb; P.xjmin = t->d_xjmin; P.ssv_f16 = 1;
-    cmax = std::max(cmax, C);
-    order[i] = i;
+    P.G = 32; P.Cg = 0;
+    int vidx[3] = {-1, -1, -1};                               // 32, 16, 8 lanes
+    for (int bin = 0; bin < msvgb_detail::kNLBins; ++bin) {
+      int G = force_lanes ? force_lanes : msvgb_detail::lanes_for(ctx, M, bin, nullptr);
+      if (G < 32 && group_C(M, G) < 0) G = 32;
+      const int k = G == 32 ? 0 : G == 16 ? 1 : 2;
+      if (vidx[k] < 0) {
+        ProfDev V = P;
+        if (G < 32) {
+          V.G = G; V.Cg = group_C(M, G);
+          const std::vector<uint32_t> gt = msvgb_detail::build_group_table(oms[i], V.Cg, G);
+          uint32_t *d = nullptr;
+          e = cudaMalloc(&d, gt.size() * 4);
+          if (e == cudaSuccess) b->gtabs.push_back(d);
+          if (e == cudaSuccess) e = cudaMemcpy(d, gt.data(), gt.size() * 4, cudaMemcpyHostToDevice);
+          if (e != cudaSuccess) return bail(MSVGB_eslEMEM, std::string("batch tables: ") + cudaGetErrorString(e));
+          V.stab = d;
+        }
+        vidx[k] = (int) vars.size();
+        vars.push_back(V);
+        smem = std::max(smem, ((size_t) ssv_words(V) + (size_t) NRES * ((C + 1) / 2) * 32) * 4);
+      }
+      var_of[i][bin] = vidx[k];
+    }
   }
-  // work items: profile-major, largest models first; chunks of the sorted
-  // database sized so there are several items per CTA
+  b->nvars = (int) vars.size();
+  std::vector<int> order(nprof);
+  for (int i = 0; i < nprof; ++i) order[i] = i;
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return oms[x]->M > oms[y]->M; });
-  b->smem = multi_smem_bytes(cmax);
+
+  b->smem = smem;
   b->threads = b->smem > 100 * 1024 ? 512 : 256;
   e = cudaFuncSetAttribute(msv_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) b->smem);
   int per_sm = 0;
   if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, msv_batch_kernel, b->threads, b->smem);
-  if (e != cudaSuccess) { msvgb_batch_destroy(b); return fail(MSVGB_eslESYS, std::string("batch kernel setup: ") + cudaGetErrorString(e)); }
+  if (e != cudaSuccess) return bail(MSVGB_eslESYS, std::string("batch kernel setup: ") + cudaGetErrorString(e));
   b->grid = std::max(1, per_sm) * ctx->num_sms;
-  std::vector<int32_t> len(db->n);
-  if (db->n) {
-    e = cudaMemcpy(len.data(), db->d_len, db->n * 4, cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) { msvgb_batch_destroy(b); return fail(MSVGB_eslESYS, cudaGetErrorString(e)); }
-  }
+
   const double want_items = 8.0 * b->grid;
   const double per_item = std::max(4096.0, (double) db->residues * nprof / want_items);
+  const int64_t min_seqs = b->threads / 32;
   std::vector<BatchItem> items;
   for (int oi = 0; oi < nprof; ++oi) {
     const int pi = order[oi];
-    int64_t s = 0;
-    while (s < db->n) {
-      int64_t e2 = s;
-      double acc = 0;
-      const int64_t min_seqs = b->threads / 32;
-      while (e2 < db->n && (acc < per_item || e2 - s < min_seqs)) acc += std::max(1, len[e2++]);
-      items.push_back(BatchItem{pi, 0, s, e2});
-      s = e2;
+    for (const Range &r : ranges) {
+      const int v = var_of[pi][r.bin];
+      const int64_t max_seqs = vars[v].G < 32 ? kChunkMaxSeqs : INT64_MAX;
+      for (int64_t s = r.a; s < r.b;) {
+        int64_t e2 = s;
+        double acc = 0;
+        while (e2 < r.b && e2 - s < max_seqs && (acc < per_item || e2 - s < min_seqs)) acc += std::max(1, len[e2++]);
+        items.push_back(BatchItem{v, pi, s, e2});
+        s = e2;
+      }
     }
   }
   b->nitems = (int64_t) items.size();
-  e = cudaMalloc(&b->d_profs, sizeof(ProfDev) * nprof);
+  e = cudaMalloc(&b->d_vars, sizeof(ProfDev) * std::max(1, b->nvars));
   if (e == cudaSuccess) e = cudaMalloc(&b->d_items, sizeof(BatchItem) * std::max<int64_t>(1, b->nitems));
   if (e == cudaSuccess) e = cudaMalloc(&b->d_ticket, sizeof(unsigned long long));
-  if (e == cudaSuccess) e = cudaMemcpy(b->d_profs, hp.data(), sizeof(ProfDev) * nprof, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(b->d_vars, vars.data(), sizeof(ProfDev) * b->nvars, cudaMemcpyHostToDevice);
   if (e == cudaSuccess && b->nitems)
     e = cudaMemcpy(b->d_items, items.data(), sizeof(BatchItem) * b->nitems, cudaMemcpyHostToDevice);
-  if (e != cudaSuccess) { msvgb_batch_destroy(b); return fail(MSVGB_eslESYS, std::string("batch upload: ") + cudaGetErrorString(e)); }
+  if (e != cudaSuccess) return bail(MSVGB_eslESYS, std::string("batch upload: ") + cudaGetErrorString(e));
 
   // capture: reset the ticket, run the persistent kernel
   BatchArgs a;
-  a.profs = b->d_profs; a.db = DbDev{db->d_codes, db->d_start, db->d_len, db->d_orig, db->n};
+  a.vars = b->d_vars; a.db = DbDev{db->d_codes, db->d_start, db->d_len, db->d_orig, db->n};
   a.items = b->d_items; a.nitems = b->nitems;
   a.out_xj = (uint8_t *) d_xj; a.out_flags = (uint8_t *) d_flags; a.ticket = b->d_ticket;
   cudaStream_t cs = nullptr;
@@ -198,9 +242,14 @@ extern "C" int msvgb_batch_create(msvgb_ctx *ctx, const msvgb_om *const *oms, in
   }
   if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
   if (cs) cudaStreamDestroy(cs);
-  if (e != cudaSuccess) { msvgb_batch_destroy(b); return fail(MSVGB_eslESYS, std::string("batch graph: ") + cudaGetErrorString(e)); }
+  if (e != cudaSuccess) return bail(MSVGB_eslESYS, std::string("batch graph: ") + cudaGetErrorString(e));
   *ret = b;
   return MSVGB_eslOK;
+}
+
+extern "C" int msvgb_batch_create(msvgb_ctx *ctx, const msvgb_om *const *oms, int nprof, const msvgb_db *db,
+                                  double F1, void *d_xj, void *d_flags, msvgb_batch **ret) {
+  return msvgb_detail::batch_create(ctx, oms, nprof, db, F1, d_xj, d_flags, 0, ret);
 }
 
 extern "C" int msvgb_batch_run(msvgb_batch *b) {

@@ -38,13 +38,15 @@ enum : int { ST_OK = 0, ST_ERANGE = 1 };
 
 struct ProfDev {
   int      M;
-  int      C;            // DP words per lane (even): the warp covers 64*C nodes >= M
+  int      C;            // DP words per lane of the 32-lane kernels: the warp covers 64*C nodes > M
   int      tbm, tec, base, bias;
   const uint32_t *stab;  // SSV costs, see layout_ssv_*() in the host code
   const uint32_t *mtab;  // MSV costs, 255 - rbv, uint8x4 [NRES][C/2][32]
   const uint8_t  *tjb;   // [Lmax+1] tjb_b per target length
   const uint8_t  *xjmin; // [Lmax+1] smallest passing xJ per length (255: xJ never passes)
   int      ssv_f16;      // 1: stab is f16x2 [NRES][C][32]; 0: int8x4 [NRES][C/2][32]
+  int      G = 32;       // lanes per sequence of the SSV pass; < 32: stab is the lane-group table
+  int      Cg = 0;       // DP words per lane of the lane-group SSV pass (G < 32)
 };
 
 struct DbDev {

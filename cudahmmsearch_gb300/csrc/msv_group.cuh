@@ -61,19 +61,14 @@ struct GroupArgs {
 
 constexpr uint32_t kPadWord = 0x1D1D1D1Du;   // four PAD_CODE residues
 
-template <int C, int G>
-__global__ void __launch_bounds__(256)
-msv_ssv_group_kernel(ProfDev P, DbDev db, uint8_t *__restrict__ out_xj, uint8_t *__restrict__ out_flags,
-                     unsigned long long *__restrict__ ticket, int64_t *__restrict__ undecided,
-                     unsigned long long *__restrict__ n_undecided) {
-  extern __shared__ __align__(16) uint32_t smem[];
-  using Lay = GroupLayout<C, G>;
-  {
-    const uint4 *gs = reinterpret_cast<const uint4 *>(P.stab);
-    uint4 *ss = reinterpret_cast<uint4 *>(smem);
-    for (int i = threadIdx.x; i < Lay::WORDS / 4; i += blockDim.x) ss[i] = __ldg(gs + i);
-  }
-  __syncthreads();
+// The lockstep SSV loop of one warp. fetch() (called by lane 0 of a group)
+// returns the next sorted sequence index, or a negative value when there is
+// none; undecided(s) (lane 0 of a group) records a sequence that needs the full
+// MSV. Decided sequences (and empty ones) are written to out_xj / out_flags.
+template <int C, int G, class Fetch, class Undecided>
+__device__ __forceinline__ void ssv_group_loop(const ProfDev &P, const uint32_t *__restrict__ tab, const DbDev &db,
+                                               uint8_t *__restrict__ out_xj, uint8_t *__restrict__ out_flags,
+                                               Fetch fetch, Undecided undecided) {
   const int lane = threadIdx.x & 31, glane = lane % G, gbase = lane - glane;
   const int src_lane = gbase + (glane + G - 1) % G;
   const unsigned gmask = (G == 32) ? FULL : (((1u << G) - 1u) << gbase);
@@ -91,10 +86,10 @@ msv_ssv_group_kernel(ProfDev P, DbDev db, uint8_t *__restrict__ out_xj, uint8_t 
 
   for (;;) {
     if (need && !done) {                              // group-uniform: take the next sequence
-      unsigned long long t = 0;
-      if (glane == 0) t = atomicAdd(ticket, 1ull);
+      long long t = 0;
+      if (glane == 0) t = fetch();
       t = __shfl_sync(gmask, t, gbase);
-      if (t >= (unsigned long long) db.n) {
+      if (t < 0) {
         done = true;
       } else {
         s = (int64_t) t;
@@ -103,7 +98,7 @@ msv_ssv_group_kernel(ProfDev P, DbDev db, uint8_t *__restrict__ out_xj, uint8_t 
         if (L == 0) {                                 // skipped, as p7_Pipeline does
           if (glane == 0) { const int64_t oi = db.orig[s]; out_xj[oi] = 0; out_flags[oi] = 0x08; }
         } else if (tjb + tbm + tec + bias >= 127) {   // SSV disabled for this length: full MSV
-          if (glane == 0) undecided[atomicAdd(n_undecided, 1ull)] = s;
+          if (glane == 0) undecided(s);
         } else {
           sq = reinterpret_cast<const uint32_t *>(db.codes + db.start[s]);
           nextw = __ldg(sq);
@@ -120,7 +115,7 @@ msv_ssv_group_kernel(ProfDev P, DbDev db, uint8_t *__restrict__ out_xj, uint8_t 
     const uint32_t w4 = active ? nextw : kPadWord;
     if (active && i + 4 < L) nextw = __ldg(sq + (i >> 2) + 1);
 #pragma unroll
-    for (int j = 0; j < 4; ++j) ssv_row_group<C, G>(dp, acc0, acc1, smem, (w4 >> (8 * j)) & 0xFF, glane, src_lane);
+    for (int j = 0; j < 4; ++j) ssv_row_group<C, G>(dp, acc0, acc1, tab, (w4 >> (8 * j)) & 0xFF, glane, src_lane);
     i += 4;
     const bool fin = active && i >= L;
     if (__any_sync(FULL, fin)) {                      // group maxima (all lanes take part)
@@ -134,7 +129,7 @@ msv_ssv_group_kernel(ProfDev P, DbDev db, uint8_t *__restrict__ out_xj, uint8_t 
         const int st = ssv_decide((int) f, tjb, tbm, tec, base, bias, xj);
         if (glane == 0) {
           if (st < 0) {
-            undecided[atomicAdd(n_undecided, 1ull)] = s;
+            undecided(s);
           } else {
             const int64_t oi = db.orig[s];
             int flags = 0;
@@ -148,6 +143,48 @@ msv_ssv_group_kernel(ProfDev P, DbDev db, uint8_t *__restrict__ out_xj, uint8_t 
       }
     }
   }
+}
+
+// Stand-alone SSV pass over the whole database (sorted order, global ticket);
+// undecided sequences go to a global list for the full-MSV launch.
+template <int C, int G>
+__global__ void __launch_bounds__(256)
+msv_ssv_group_kernel(ProfDev P, DbDev db, uint8_t *__restrict__ out_xj, uint8_t *__restrict__ out_flags,
+                     unsigned long long *__restrict__ ticket, int64_t *__restrict__ undecided,
+                     unsigned long long *__restrict__ n_undecided) {
+  extern __shared__ __align__(16) uint32_t smem[];
+  using Lay = GroupLayout<C, G>;
+  {
+    const uint4 *gs = reinterpret_cast<const uint4 *>(P.stab);
+    uint4 *ss = reinterpret_cast<uint4 *>(smem);
+    for (int i = threadIdx.x; i < Lay::WORDS / 4; i += blockDim.x) ss[i] = __ldg(gs + i);
+  }
+  __syncthreads();
+  const unsigned long long n = (unsigned long long) db.n;
+  ssv_group_loop<C, G>(
+      P, smem, db, out_xj, out_flags,
+      [&]() -> long long {
+        const unsigned long long t = atomicAdd(ticket, 1ull);
+        return t < n ? (long long) t : -1ll;
+      },
+      [&](int64_t s) { undecided[atomicAdd(n_undecided, 1ull)] = s; });
+}
+
+// SSV pass of one CTA over the sorted sequences [s0, s0 + nseq) (a work item
+// of the multi-profile kernels): next_seq and n_und are shared counters the
+// caller zeroed; und (room for nseq entries) receives the chunk-relative
+// indices of the undecided sequences.
+template <int C, int G>
+__device__ __forceinline__ void ssv_group_chunk(const ProfDev &P, const uint32_t *tab, const DbDev &db, int64_t s0,
+                                                int nseq, uint8_t *oxj, uint8_t *ofl, unsigned *next_seq,
+                                                uint16_t *und, unsigned *n_und) {
+  ssv_group_loop<C, G>(
+      P, tab, db, oxj, ofl,
+      [&]() -> long long {
+        const unsigned k = atomicAdd(next_seq, 1u);
+        return k < (unsigned) nseq ? (long long) (s0 + k) : -1ll;
+      },
+      [&](int64_t s) { und[atomicAdd(n_und, 1u)] = (uint16_t) (s - s0); });
 }
 
 template <int C, int G>

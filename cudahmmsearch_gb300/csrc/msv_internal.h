@@ -13,6 +13,8 @@
 #include "msv_kernel_impl.cuh"
 #include "msv_group.cuh"
 
+struct TuneTable;                                       // msv_tune.cu
+
 struct msvgb_ctx {
   int device = 0;
   int num_sms = 0;
@@ -30,6 +32,8 @@ struct msvgb_ctx {
   int64_t *d_list = nullptr; size_t list_cap = 0;       // G-lane search: sequences left for the full MSV
   unsigned long long *d_aux = nullptr;                  // [0] second ticket, [1] list count
   void *h_stage = nullptr; size_t h_stage_cap = 0;      // pinned staging for database metadata
+  TuneTable *tune = nullptr;                            // lane counts measured by msvgb_autotune
+  std::mutex tune_mu;
 };
 
 // Per-length tables of a profile at one F1 threshold: tjb_b(L) and the
@@ -73,6 +77,8 @@ struct msvgb_db {
 };
 
 namespace msvgb_detail {
+// HMMER's amino background frequencies, Easel code order A..Y (msv_sample.cu).
+extern const float kAminoBg[20];
 // Records msg as the calling thread's last error and returns code.
 int fail(int code, const std::string &msg);
 // Launches the search kernel instantiated for C words per lane.
@@ -88,6 +94,22 @@ int build_cost_tables(const msvgb_om *om, int f16, int C, std::vector<uint32_t> 
 cudaError_t dispatch_group(int C, int G, const msvgb::GroupArgs &a, int sms);
 // Per-length tjb_b and pass-threshold tables of (profile, database, F1), cached in the profile.
 int ensure_tables(msvgb_profile *p, const msvgb_db *db, double F1, LenTables **out);
+// Lane-group SSV table of a profile (layout GroupLayout<C, G>, msv_group.cuh).
+std::vector<uint32_t> build_group_table(const msvgb_om *om, int C, int G);
+// Target-length bins of the lane choice: [0,150) [150,600) [600,2400) [2400,inf).
+constexpr int kNLBins = 4;
+int lbin_of(int L);
+// Whether the lane-group SSV pass supports G lanes for a model of length M.
+bool lanes_valid(int M, int G);
+// Lanes per sequence for model length M on target-length bin lbin (-1: the
+// whole mix), from the context's tuning table or the fixed rule; *variant
+// (may be NULL) gets the SSV table type for 32 lanes.
+int lanes_for(msvgb_ctx *c, int M, int lbin, int *variant);
+void tune_free(msvgb_ctx *c);
+// msvgb_batch_create with every (profile, length bin) at force_lanes lanes
+// where the model length allows it (0: the context's choice).
+int batch_create(msvgb_ctx *ctx, const msvgb_om *const *oms, int nprof, const msvgb_db *db, double F1,
+                 void *d_xj, void *d_flags, int force_lanes, msvgb_batch **ret);
 // Adds one to the count msvgb_kernel_launches() reports.
 void count_launch();
 // Scatters raw residues into the packed database layout (msv_pack.cu); sets

@@ -29,16 +29,19 @@
 
 using msvgb_detail::fail;
 
+// HMMER's amino background (src/hmmer.c:163-186), Easel code order A..Y.
+const float msvgb_detail::kAminoBg[20] = {
+    0.0787945f, 0.0151600f, 0.0535222f, 0.0668298f, 0.0397062f, 0.0695071f, 0.0229198f,
+    0.0590092f, 0.0594422f, 0.0963728f, 0.0237718f, 0.0414386f, 0.0482904f, 0.0395639f,
+    0.0540978f, 0.0683364f, 0.0540687f, 0.0673417f, 0.0114135f, 0.0304133f};
+
 namespace {
 
 constexpr int K = 20, KP = 29;
 constexpr double kLog2 = 0.69314718055994529;   // eslCONST_LOG2
 constexpr double kE = 2.71828182845904523536028747135;
 
-// HMMER's amino background (src/hmmer.c:163-186), Easel code order A..Y.
-constexpr float kBg[K] = {0.0787945f, 0.0151600f, 0.0535222f, 0.0668298f, 0.0397062f, 0.0695071f, 0.0229198f,
-                          0.0590092f, 0.0594422f, 0.0963728f, 0.0237718f, 0.0414386f, 0.0482904f, 0.0395639f,
-                          0.0540978f, 0.0683364f, 0.0540687f, 0.0673417f, 0.0114135f, 0.0304133f};
+const float *const kBg = msvgb_detail::kAminoBg;
 
 // Mersenne twister MT19937 as Easel seeds it (a Knuth LCG fills the table).
 struct Mersenne {

@@ -78,8 +78,7 @@ __global__ void __launch_bounds__(512) msv_serve_kernel(ServeArgs a) {
   __shared__ long long item_sh;
   __shared__ ServeItem it_sh;
   __shared__ int loaded_slot, loaded_gen;
-  __shared__ unsigned long long next_seq;
-  const int lane = threadIdx.x & 31;
+  __shared__ ChunkShared cs;
   if (threadIdx.x == 0) { loaded_slot = -1; loaded_gen = -1; atomicAdd_system(&a.ctl->live, 1); }
   for (;;) {
     __syncthreads();
@@ -105,11 +104,11 @@ __global__ void __launch_bounds__(512) msv_serve_kernel(ServeArgs a) {
         if (h < t && !ld_volatile_i32(&a.ctl->stop)) { atomicAdd_system(&a.ctl->live, 1); got = -2; }
       }
       if (got >= 0) {
-        const volatile ServeItem *src = a.ring + (got % a.cap);
+        const volatile ServeItem *src = a.ring + (got & (a.cap - 1));   // cap is a power of two
         it_sh.slot = src->slot; it_sh.gen = src->gen; it_sh.s_begin = src->s_begin; it_sh.s_end = src->s_end;
       }
       item_sh = got;
-      next_seq = 0ull;
+      cs.next_seq = 0u; cs.n_und = 0u; cs.next_und = 0u;
     }
     __syncthreads();
     const long long got = item_sh;
@@ -117,23 +116,13 @@ __global__ void __launch_bounds__(512) msv_serve_kernel(ServeArgs a) {
     if (got < 0) break;
     const ServeItem item = it_sh;
     const ProfDev &P = a.slots[item.slot];
-    const int C = P.C;
     if (loaded_slot != item.slot || loaded_gen != item.gen) {
       stage_tables(P, smem);
       __syncthreads();
       if (threadIdx.x == 0) { loaded_slot = item.slot; loaded_gen = item.gen; }
     }
-    const uint32_t *stab = smem;
-    const uint32_t *mtab = smem + NRES * C * 32;
     const SlotOut o = a.outs[item.slot];
-    const int64_t nseq = item.s_end - item.s_begin;
-    for (;;) {
-      unsigned long long k = 0;
-      if (lane == 0) k = atomicAdd(&next_seq, 1ull);
-      k = __shfl_sync(FULL, k, 0);
-      if ((long long) k >= nseq) break;
-      run_seq_any(C, P, stab, mtab, a.db, item.s_begin + (int64_t) k, lane, o.xj, o.flags);
-    }
+    run_chunk(P, smem, smem + ssv_words(P), a.db, item.s_begin, item.s_end - item.s_begin, o.xj, o.flags, cs);
     __syncthreads();
     if (threadIdx.x == 0) {
       __threadfence_system();                           // results visible before the count
@@ -253,11 +242,13 @@ extern "C" int msvgb_server_create(msvgb_ctx *ctx, const msvgb_db *db, double F1
     s->chunk_begin.push_back(i);
     double acc = 0;
     const int64_t i0 = i;
-    while (i < db->n && (acc < per_item || i - i0 < s->threads / 32)) acc += std::max(1, len[i++]);
+    while (i < db->n && i - i0 < kChunkMaxSeqs && (acc < per_item || i - i0 < s->threads / 32))
+      acc += std::max(1, len[i++]);
   }
   s->chunk_begin.push_back(db->n);
   s->items_per_req = (int64_t) s->chunk_begin.size() - 1;
-  s->cap = (long long) s->nslots * std::max<int64_t>(1, s->items_per_req) + 1;
+  s->cap = 1;                                           // a power of two: the kernel masks, no 64-bit modulo
+  while (s->cap < (long long) s->nslots * std::max<int64_t>(1, s->items_per_req) + 1) s->cap <<= 1;
   if (e == cudaSuccess) e = cudaMalloc(&s->d_slot_mem, s->slot_bytes * s->nslots);
   if (e == cudaSuccess) e = cudaMalloc(&s->d_slots, sizeof(ProfDev) * s->nslots);
   if (e == cudaSuccess) e = cudaMalloc(&s->d_outs, sizeof(SlotOut) * s->nslots);
@@ -302,6 +293,10 @@ extern "C" int msvgb_server_submit(msvgb_server *s, const msvgb_om *om, uint64_t
   std::vector<uint32_t> st, mt;
   int rc = msvgb_detail::build_cost_tables(om, 1, C, st, mt);
   if (rc != MSVGB_eslOK) return rc;
+  int G = msvgb_detail::lanes_for(s->ctx, om->M, -1, nullptr);   // lanes per sequence of the SSV pass
+  if (G < 32 && group_C(om->M, G) < 0) G = 32;
+  const int Cg = G < 32 ? group_C(om->M, G) : 0;
+  if (G < 32) st = msvgb_detail::build_group_table(om, Cg, G);
   msvgb_profile tmp;                                   // scalar view for the threshold search
   tmp.M = om->M; tmp.C = C; tmp.tbm = om->tbm_b; tmp.tec = om->tec_b; tmp.base = om->base_b;
   tmp.bias = om->bias_b; tmp.scale = om->scale_b; tmp.mmu = om->mmu; tmp.mlambda = om->mlambda;
@@ -329,7 +324,8 @@ extern "C" int msvgb_server_submit(msvgb_server *s, const msvgb_om *om, uint64_t
   uint8_t *base = s->d_slot_mem + s->slot_bytes * slot;
   ProfDev P;
   P.M = om->M; P.C = C; P.tbm = om->tbm_b; P.tec = om->tec_b; P.base = om->base_b; P.bias = om->bias_b;
-  P.stab = (const uint32_t *) base; P.mtab = (const uint32_t *) (base + (size_t) NRES * C * 32 * 4);
+  P.G = G; P.Cg = Cg;
+  P.stab = (const uint32_t *) base; P.mtab = (const uint32_t *) (base + st.size() * 4);
   P.tjb = base + s->tab_off_tjb; P.xjmin = base + s->tab_off_xjm; P.ssv_f16 = 1;
   __atomic_store_n(&s->h_ctl->done[slot], 0ull, __ATOMIC_SEQ_CST);
   e = cudaMemcpyAsync(base, st.data(), st.size() * 4, cudaMemcpyHostToDevice, s->upload);
@@ -342,7 +338,7 @@ extern "C" int msvgb_server_submit(msvgb_server *s, const msvgb_om *om, uint64_t
   {
     std::lock_guard<std::mutex> lk(s->mu);
     for (int64_t k = 0; k < s->items_per_req; ++k) {
-      ServeItem &it = s->h_ring[(s->tail + k) % s->cap];
+      ServeItem &it = s->h_ring[(s->tail + k) & (s->cap - 1)];
       it.slot = slot; it.gen = s->gen[slot];
       it.s_begin = s->chunk_begin[k]; it.s_end = s->chunk_begin[k + 1];
     }

@@ -27,9 +27,13 @@ extern "C" {
 #define MSVGB_eslOK      0
 #define MSVGB_eslFAIL    1
 #define MSVGB_eslEMEM    5
+#define MSVGB_eslENOTFOUND 6
+#define MSVGB_eslEFORMAT 7
+#define MSVGB_eslEINCOMPAT 10
 #define MSVGB_eslEINVAL 11
 #define MSVGB_eslESYS   12
 #define MSVGB_eslERANGE 16
+#define MSVGB_eslEWRITE 27
 
 /* Per-(profile, sequence) result flags written by the search entry points. */
 #define MSVGB_FLAG_ERANGE 0x01  /* score overflowed: +inf (eslERANGE)                      */
@@ -103,6 +107,27 @@ int msvgb_profile_variant(const msvgb_profile *prof);
  * M < 64 * G and, for G < 32, M >= 2 * G. Chosen by msvgb_autotune. */
 int msvgb_profile_set_lanes(msvgb_profile *prof, const msvgb_om *om, int lanes);
 int msvgb_profile_lanes(const msvgb_profile *prof);
+
+/* ---- lane-count autotuner (no reference counterpart: the SSE filter has one
+ * layout) ------------------------------------------------------------------
+ * Times the SSV pass at 32 lanes per sequence (f16 and int8 cost tables), 16
+ * and 8 lanes on this context's GPU for a ladder of model lengths (24..1000)
+ * and four target-length bins ([0,150) [150,600) [600,2400) [2400,inf)), on
+ * synthetic sequences, within about budget_s seconds (<= 0: 30 s); keeps the
+ * fastest choice per (M, bin) and over the mix of bins in the context.
+ * Afterwards msvgb_profile_create, msvgb_batch_create and the server take
+ * their lane counts from it; before, a fixed rule applies (8 lanes for
+ * 16 <= M < 512, 16 for M < 1024, else 32). */
+int msvgb_autotune(msvgb_ctx *ctx, double budget_s);
+/* Text form of the context's table (device name and SM count in the header). */
+int msvgb_tune_save(msvgb_ctx *ctx, const char *path);
+/* eslENOTFOUND: no file; eslEFORMAT: not a table; eslEINCOMPAT: measured on
+ * another GPU model. */
+int msvgb_tune_load(msvgb_ctx *ctx, const char *path);
+/* Lanes per sequence the context chooses for model length M and target length
+ * L (L < 0: the whole length mix); *ret_variant (may be NULL) gets the SSV
+ * table type for 32 lanes (1 f16, 0 int8). */
+int msvgb_tune_lanes(msvgb_ctx *ctx, int M, int L, int *ret_variant);
 int msvgb_profile_destroy(msvgb_profile *prof);
 int msvgb_profile_M(const msvgb_profile *prof);
 

@@ -171,6 +171,11 @@ def test_kernel_launch_counter_advances(ctx):
     prof, db = api.DeviceProfile(ctx, p), api.DeviceDB(ctx, s)
     before = api.kernel_launches()
     api.search(ctx, prof, db)
+    # one fused launch at 32 lanes; the lane-group SSV pass plus the full-MSV pass otherwise
+    assert api.kernel_launches() == before + (1 if prof.lanes == 32 else 2)
+    prof.set_lanes(32)
+    before = api.kernel_launches()
+    api.search(ctx, prof, db)
     assert api.kernel_launches() == before + 1
 
 
