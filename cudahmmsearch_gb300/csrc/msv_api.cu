@@ -178,7 +178,10 @@ extern "C" int msvgb_ctx_create(int device, msvgb_ctx **ret_ctx) {
   if (e == cudaSuccess) e = cudaMalloc(&c->d_meta, 4 * sizeof(int64_t));
   if (e == cudaSuccess) e = cudaMalloc(&c->d_out, 64);
   if (e == cudaSuccess) e = cudaMalloc(&c->d_bad, sizeof(int));
-  if (e == cudaSuccess) e = cudaMalloc(&c->d_aux, 2 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_aux, 4 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
   if (e != cudaSuccess) {
     msvgb_ctx_destroy(c);
     return fail(MSVGB_eslESYS, std::string("context setup: ") + cudaGetErrorString(e));
@@ -198,6 +201,9 @@ extern "C" int msvgb_ctx_destroy(msvgb_ctx *c) {
   cudaFree(c->d_seq); cudaFree(c->d_tab); cudaFree(c->d_bad); cudaFree(c->d_aux); cudaFree(c->d_list);
   if (c->h_stage) cudaFreeHost(c->h_stage);
   if (c->own) cudaStreamDestroy(c->own);
+  if (c->side) { cudaStreamSynchronize(c->side); cudaStreamDestroy(c->side); }
+  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+  if (c->ev_join) cudaEventDestroy(c->ev_join);
   msvgb_detail::tune_free(c);
   delete c;
   return MSVGB_eslOK;
@@ -614,6 +620,7 @@ extern "C" int msvgb_db_create(msvgb_ctx *ctx, const uint8_t *codes, const int64
   db->ctx = ctx; db->device = ctx->device; db->n = n; db->residues = total; db->Lmax = Lmax;
   db->serial = g_db_serial.fetch_add(1);
   db->distinct_len = std::move(distinct);
+  db->n_long = std::partition_point(h_len, h_len + n, [](int32_t L) { return L >= kLongTarget; }) - h_len;
   int64_t *d_src = nullptr;
   int bad = 0;
   cudaError_t e = cudaMalloc(&db->d_codes, bytes);
@@ -691,7 +698,10 @@ extern "C" int msvgb_search_device(msvgb_ctx *c, const msvgb_profile *pc, const 
   DbDev dbv{db->d_codes, db->d_start, db->d_len, db->d_orig, db->n};
   if (p->G == 32 || !p->d_stab_g)
     return launch_one(c, p, dbv, t->d_tjb, t->d_xjmin, (uint8_t *) d_xj, (uint8_t *) d_flags);
-  // G-lane SSV pass, then the full MSV on the sequences it left undecided
+  // Long targets (they sort first) on the 32-lane kernel in a side stream;
+  // the rest: the G-lane SSV pass, then the full MSV on the sequences it left
+  // undecided. The side stream forks from and joins back into the context's.
+  const int64_t n_long = std::min(db->n_long, db->n);
   if (c->list_cap < (size_t) db->n) {
     CUDA_TRY(cudaStreamSynchronize(c->stream));            // the old list may still be read
     cudaFree(c->d_list); c->d_list = nullptr; c->list_cap = 0;
@@ -704,10 +714,26 @@ extern "C" int msvgb_search_device(msvgb_ctx *c, const msvgb_profile *pc, const 
   GroupArgs g;
   g.P = P; g.db = dbv; g.out_xj = (uint8_t *) d_xj; g.out_flags = (uint8_t *) d_flags;
   g.ticket = c->d_ticket; g.undecided = c->d_list; g.n_undecided = c->d_aux + 1; g.stream = c->stream;
+  g.s_begin = n_long;
   CUDA_TRY(cudaMemsetAsync(c->d_ticket, 0, sizeof(unsigned long long), c->stream));
-  CUDA_TRY(cudaMemsetAsync(c->d_aux, 0, 2 * sizeof(unsigned long long), c->stream));
-  CUDA_TRY(dispatch_group(p->Cg, p->G, g, c->num_sms));
-  count_launch();
+  CUDA_TRY(cudaMemsetAsync(c->d_aux, 0, 3 * sizeof(unsigned long long), c->stream));
+  if (n_long > 0) {
+    LaunchArgs l;
+    l.P = ProfDev{};
+    l.P.M = p->M; l.P.C = p->C; l.P.tbm = p->tbm; l.P.tec = p->tec; l.P.base = p->base; l.P.bias = p->bias;
+    l.P.stab = p->d_stab; l.P.mtab = p->d_mtab; l.P.tjb = t->d_tjb; l.P.xjmin = t->d_xjmin; l.P.ssv_f16 = p->f16;
+    l.db = dbv; l.out_xj = (uint8_t *) d_xj; l.out_flags = (uint8_t *) d_flags; l.ticket = c->d_aux + 2;
+    l.stream = c->side; l.grid = 0; l.skip_empty = 1; l.range_end = n_long;
+    CUDA_TRY(cudaEventRecord(c->ev_fork, c->stream));
+    CUDA_TRY(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
+    CUDA_TRY(dispatch(p->C, p->f16 != 0, l, c->num_sms));
+    count_launch();
+    CUDA_TRY(cudaEventRecord(c->ev_join, c->side));
+  }
+  if (n_long < db->n) {
+    CUDA_TRY(dispatch_group(p->Cg, p->G, g, c->num_sms));
+    count_launch();
+  }
   ProfDev Pb;
   Pb.M = p->M; Pb.C = p->C; Pb.tbm = p->tbm; Pb.tec = p->tec; Pb.base = p->base; Pb.bias = p->bias;
   Pb.stab = p->d_stab; Pb.mtab = p->d_mtab; Pb.tjb = t->d_tjb; Pb.xjmin = t->d_xjmin; Pb.ssv_f16 = p->f16;
@@ -716,6 +742,7 @@ extern "C" int msvgb_search_device(msvgb_ctx *c, const msvgb_profile *pc, const 
   a.stream = c->stream; a.grid = 0; a.skip_empty = 1; a.list = c->d_list; a.list_count = c->d_aux + 1;
   CUDA_TRY(dispatch(p->C, p->f16 != 0, a, c->num_sms));
   count_launch();
+  if (n_long > 0) CUDA_TRY(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
   return MSVGB_eslOK;
 }
 

@@ -56,6 +56,7 @@ struct GroupArgs {
   unsigned long long *ticket;
   int64_t *undecided;              // sorted indices left for the full MSV pass
   unsigned long long *n_undecided;
+  int64_t s_begin = 0;             // first sorted sequence of the pass (the rest of the database follows)
   cudaStream_t stream;
 };
 
@@ -145,13 +146,13 @@ __device__ __forceinline__ void ssv_group_loop(const ProfDev &P, const uint32_t 
   }
 }
 
-// Stand-alone SSV pass over the whole database (sorted order, global ticket);
-// undecided sequences go to a global list for the full-MSV launch.
+// Stand-alone SSV pass over the sorted sequences [s_begin, n) (global
+// ticket); undecided sequences go to a global list for the full-MSV launch.
 template <int C, int G>
 __global__ void __launch_bounds__(256)
 msv_ssv_group_kernel(ProfDev P, DbDev db, uint8_t *__restrict__ out_xj, uint8_t *__restrict__ out_flags,
                      unsigned long long *__restrict__ ticket, int64_t *__restrict__ undecided,
-                     unsigned long long *__restrict__ n_undecided) {
+                     unsigned long long *__restrict__ n_undecided, int64_t s_begin) {
   extern __shared__ __align__(16) uint32_t smem[];
   using Lay = GroupLayout<C, G>;
   {
@@ -164,7 +165,7 @@ msv_ssv_group_kernel(ProfDev P, DbDev db, uint8_t *__restrict__ out_xj, uint8_t 
   ssv_group_loop<C, G>(
       P, smem, db, out_xj, out_flags,
       [&]() -> long long {
-        const unsigned long long t = atomicAdd(ticket, 1ull);
+        const unsigned long long t = atomicAdd(ticket, 1ull) + (unsigned long long) s_begin;
         return t < n ? (long long) t : -1ll;
       },
       [&](int64_t s) { undecided[atomicAdd(n_undecided, 1ull)] = s; });
@@ -200,10 +201,11 @@ cudaError_t launch_ssv_group(const GroupArgs &a, int num_sms) {
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem);
   if (e != cudaSuccess) return e;
   int grid = std::max(1, per_sm) * num_sms;
-  const long long need = (a.db.n * G + 255) / 256;        // 256 threads hold 256/G sequences
+  const long long need = ((a.db.n - a.s_begin) * G + 255) / 256;   // 256 threads hold 256/G sequences
   if (need < grid) grid = (int) std::max(1LL, need);
   (void) cudaGetLastError();
-  kern<<<grid, 256, smem, a.stream>>>(a.P, a.db, a.out_xj, a.out_flags, a.ticket, a.undecided, a.n_undecided);
+  kern<<<grid, 256, smem, a.stream>>>(a.P, a.db, a.out_xj, a.out_flags, a.ticket, a.undecided, a.n_undecided,
+                                      a.s_begin);
   return cudaGetLastError();
 }
 

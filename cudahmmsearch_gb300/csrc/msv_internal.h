@@ -30,7 +30,9 @@ struct msvgb_ctx {
   uint8_t *d_out = nullptr;
   int *d_bad = nullptr;                                 // database packing: invalid-code flag
   int64_t *d_list = nullptr; size_t list_cap = 0;       // G-lane search: sequences left for the full MSV
-  unsigned long long *d_aux = nullptr;                  // [0] second ticket, [1] list count
+  unsigned long long *d_aux = nullptr;                  // [0] second ticket, [1] list count, [2] third ticket
+  cudaStream_t side = nullptr;                          // long targets of the lane-group search
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   void *h_stage = nullptr; size_t h_stage_cap = 0;      // pinned staging for database metadata
   TuneTable *tune = nullptr;                            // lane counts measured by msvgb_autotune
   std::mutex tune_mu;
@@ -74,7 +76,13 @@ struct msvgb_db {
   int32_t *d_len = nullptr;
   std::vector<int32_t> distinct_len;  // sorted ascending
   uint64_t serial = 0;
+  int64_t n_long = 0;                 // sequences of length >= kLongTarget (they sort first)
 };
+
+// Targets this long are scored with 32 lanes per sequence even when the
+// profile's SSV pass runs on lane groups: at 8 or 16 lanes one sequence takes
+// 2-4x longer, and a single long target would set the length of the launch.
+constexpr int kLongTarget = 2400;
 
 namespace msvgb_detail {
 // HMMER's amino background frequencies, Easel code order A..Y (msv_sample.cu).

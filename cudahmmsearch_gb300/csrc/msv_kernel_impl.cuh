@@ -19,6 +19,8 @@ struct LaunchArgs {
   // full MSV recurrence (they are the ones the G-lane SSV pass left undecided).
   const int64_t            *list = nullptr;
   const unsigned long long *list_count = nullptr;
+  // Range mode (range_end > 0): only the sorted sequences [0, range_end).
+  int64_t                   range_end = 0;
 };
 
 constexpr int WARPS_PER_CTA = 8;
@@ -40,7 +42,8 @@ template <int C, bool F16>
 __global__ void __launch_bounds__(cta_threads<C, F16>())
 msv_search_kernel(ProfDev P, DbDev db, uint8_t *__restrict__ out_xj, uint8_t *__restrict__ out_flags,
                   unsigned long long *__restrict__ ticket, int skip_empty,
-                  const int64_t *__restrict__ list, const unsigned long long *__restrict__ list_count) {
+                  const int64_t *__restrict__ list, const unsigned long long *__restrict__ list_count,
+                  int64_t range_end) {
   extern __shared__ __align__(16) uint32_t smem[];
   constexpr int SW = F16 ? NRES * C * 32 : NRES * (C / 2) * 32;   // words of the SSV table
   constexpr int MW = NRES * ((C + 1) / 2) * 32;                    // words of the MSV table
@@ -57,7 +60,7 @@ msv_search_kernel(ProfDev P, DbDev db, uint8_t *__restrict__ out_xj, uint8_t *__
   __syncthreads();
 
   const int lane = threadIdx.x & 31;
-  const unsigned long long nitems = list ? *list_count : (unsigned long long) db.n;
+  const unsigned long long nitems = list ? *list_count : (unsigned long long) (range_end > 0 ? range_end : db.n);
   for (;;) {
     unsigned long long s = 0;
     if (lane == 0) s = atomicAdd(ticket, 1ull);
@@ -101,12 +104,12 @@ cudaError_t launch_search(const LaunchArgs &a, int num_sms) {
     if (per_sm < 1) per_sm = 1;
     grid = per_sm * num_sms;
     const int warps = threads / 32;
-    const long long need = (a.db.n + warps - 1) / warps;
+    const long long need = ((a.range_end > 0 ? a.range_end : a.db.n) + warps - 1) / warps;
     if (!a.list && need < grid) grid = (int) (need > 0 ? need : 1);
   }
   (void) cudaGetLastError();   // clear a stale error left by an unrelated call
   kern<<<grid, threads, smem, a.stream>>>(a.P, a.db, a.out_xj, a.out_flags, a.ticket, a.skip_empty,
-                                               a.list, a.list_count);
+                                               a.list, a.list_count, a.range_end);
   return cudaGetLastError();
 }
 

@@ -10,11 +10,12 @@
 //     that applies per-bin choices), on a batch of 8 copies of one sampled
 //     profile against that bin's synthetic sequences, so that work items of
 //     the copies interleave and the timing is throughput, not one long tail;
-//   - each choice (int8 table included) on the single-query path against the
-//     four bins together: the choice for a whole length mix.
+//   - each choice (int8 table included) on the single-query path against a
+//     database with the usual protein length law (lognormal, median 300,
+//     sigma 0.7): the choice for a whole length mix.
 // It keeps the fastest per (M, bin) and for the mix, and can save / load the
-// table. Without a table the choice is a fixed rule (8 lanes for
-// 16 <= M < 512, 16 below 1024, else 32) that measurements on GB300 support.
+// table. Without a table the choice is a fixed rule (default_lanes) that
+// measurements on GB300 support.
 // The reference has no counterpart: its SSE filter has one layout.
 #include <algorithm>
 #include <chrono>
@@ -46,9 +47,12 @@ constexpr Cand kCand[] = {{32, 1}, {32, 0}, {16, 1}, {8, 1}};
 constexpr int kNC = sizeof(kCand) / sizeof(kCand[0]);
 constexpr int kNV = kNB + 1;                                // values per candidate: bins, then the mix
 
-int default_lanes(int M) {
-  if (M >= 16 && M < 512) return 8;
-  if (M >= 32 && M < 1024) return 16;
+// The rule used without a measured table (from measurements on GB300): 8
+// lanes up to M = 479; above, 16 lanes for short targets in the batched
+// kernel, else 32.
+int default_lanes(int M, int lbin) {
+  if (M >= 16 && M < 480) return 8;
+  if (M >= 32 && M < 1024 && lbin == 0) return 16;
   return 32;
 }
 
@@ -88,6 +92,33 @@ void synth_bin(int b, std::vector<uint8_t> &codes, std::vector<int64_t> &off) {
   codes.clear(); off.assign(1, 0);
   while ((int64_t) codes.size() < kBinResidues[b]) {
     const int L = kBinLo[b] + (int) ((next() % 64) * (uint64_t) (kBinHi[b] - kBinLo[b]) / 64);
+    for (int i = 0; i < L; ++i) codes.push_back(lut[next() >> 52]);
+    off.push_back((int64_t) codes.size());
+  }
+}
+
+// The length mix: lognormal(ln 300, 0.7) lengths clipped to [10, 35000],
+// residues from the background, about 192M residues (larger than L2, and
+// long enough that launch overheads do not decide the choice).
+void synth_mix(std::vector<uint8_t> &codes, std::vector<int64_t> &off) {
+  uint64_t x = 0xD1B54A32D192ED03ull;
+  auto next = [&]() { x ^= x << 13; x ^= x >> 7; x ^= x << 17; return x; };
+  auto unif = [&]() { return ((next() >> 11) + 0.5) * (1.0 / 9007199254740992.0); };
+  uint8_t lut[4096];
+  {
+    double sum = 0, tot = 0;
+    for (int a = 0; a < 20; ++a) tot += msvgb_detail::kAminoBg[a];
+    int a = 0;
+    for (int i = 0; i < 4096; ++i) {
+      const double u = (i + 0.5) / 4096.0 * tot;
+      while (a < 19 && sum + msvgb_detail::kAminoBg[a] <= u) sum += msvgb_detail::kAminoBg[a++];
+      lut[i] = (uint8_t) a;
+    }
+  }
+  codes.clear(); off.assign(1, 0);
+  while ((int64_t) codes.size() < (192 << 20)) {
+    const double z = std::sqrt(-2.0 * std::log(unif())) * std::cos(6.283185307179586 * unif());
+    const int L = (int) std::min(35000.0, std::max(10.0, std::exp(std::log(300.0) + 0.7 * z)));
     for (int i = 0; i < L; ++i) codes.push_back(lut[next() >> 52]);
     off.push_back((int64_t) codes.size());
   }
@@ -149,7 +180,7 @@ int msvgb_detail::lanes_for(msvgb_ctx *c, int M, int lbin, int *variant) {
       return kCand[ci].lanes;
     }
   }
-  return default_lanes(M);
+  return default_lanes(M, lbin);
 }
 
 void msvgb_detail::tune_free(msvgb_ctx *c) {
@@ -159,7 +190,7 @@ void msvgb_detail::tune_free(msvgb_ctx *c) {
 
 extern "C" int msvgb_autotune(msvgb_ctx *ctx, double budget_s) {
   if (!ctx) return fail(MSVGB_eslEINVAL, "ctx is NULL");
-  if (budget_s <= 0) budget_s = 30.0;
+  if (budget_s <= 0) budget_s = 60.0;
   cudaError_t e = cudaSetDevice(ctx->device);
   if (e != cudaSuccess) return fail(MSVGB_eslESYS, cudaGetErrorString(e));
   const auto t0 = std::chrono::steady_clock::now();
@@ -174,22 +205,19 @@ extern "C" int msvgb_autotune(msvgb_ctx *ctx, double budget_s) {
   int st = MSVGB_eslOK;
   int64_t nmax = 0;
   {
-    std::vector<uint8_t> all;
-    std::vector<int64_t> all_off(1, 0);
+    std::vector<uint8_t> codes;
+    std::vector<int64_t> off;
     for (int b = 0; b < kNB && st == MSVGB_eslOK; ++b) {
-      std::vector<uint8_t> codes;
-      std::vector<int64_t> off;
       synth_bin(b, codes, off);
       const int64_t n = (int64_t) off.size() - 1;
       st = msvgb_db_create(ctx, codes.data(), off.data(), n, &db[b]);
       residues[b] = (int64_t) codes.size();
       nmax = std::max(nmax, kCopies * n);
-      for (int64_t i = 1; i <= n; ++i) all_off.push_back((int64_t) all.size() + off[i]);
-      all.insert(all.end(), codes.begin(), codes.end());
     }
-    if (st == MSVGB_eslOK) st = msvgb_db_create(ctx, all.data(), all_off.data(), (int64_t) all_off.size() - 1, &mix);
-    mix_res = (int64_t) all.size();
-    nmax = std::max(nmax, (int64_t) all_off.size() - 1);
+    synth_mix(codes, off);
+    if (st == MSVGB_eslOK) st = msvgb_db_create(ctx, codes.data(), off.data(), (int64_t) off.size() - 1, &mix);
+    mix_res = (int64_t) codes.size();
+    nmax = std::max(nmax, (int64_t) off.size() - 1);
   }
   if (st == MSVGB_eslOK) {
     e = cudaMalloc(&d_out, 2 * (size_t) nmax);

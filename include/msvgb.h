@@ -113,11 +113,13 @@ int msvgb_profile_lanes(const msvgb_profile *prof);
  * Times the SSV pass at 32 lanes per sequence (f16 and int8 cost tables), 16
  * and 8 lanes on this context's GPU for a ladder of model lengths (24..1000)
  * and four target-length bins ([0,150) [150,600) [600,2400) [2400,inf)), on
- * synthetic sequences, within about budget_s seconds (<= 0: 30 s); keeps the
- * fastest choice per (M, bin) and over the mix of bins in the context.
+ * synthetic sequences, within about budget_s seconds (<= 0: 60 s); keeps the
+ * fastest choice per (M, bin) (timed in the batched kernel) and for a
+ * lognormal length mix (timed on the single-query path) in the context.
  * Afterwards msvgb_profile_create, msvgb_batch_create and the server take
  * their lane counts from it; before, a fixed rule applies (8 lanes for
- * 16 <= M < 512, 16 for M < 1024, else 32). */
+ * 16 <= M < 480; 16 for M < 1024 on targets shorter than 150 in the batched
+ * kernel; else 32). */
 int msvgb_autotune(msvgb_ctx *ctx, double budget_s);
 /* Text form of the context's table (device name and SM count in the header). */
 int msvgb_tune_save(msvgb_ctx *ctx, const char *path);

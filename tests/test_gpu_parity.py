@@ -130,7 +130,7 @@ def test_model_size_corners(ctx, M):
     seqs += [np.full(50, F.CODE_X, np.uint8), np.zeros(0, np.uint8), rng.integers(0, 29, size=77).astype(np.uint8)]
     s = F.SeqSet.from_list(seqs)
     o = O.msv_batch(p, s)
-    for variant in (0, 1):
+    for variant in (0, 1, None):          # None: the lane count the context picks (lane groups + long targets)
         xj, fl = api.search(ctx, api.DeviceProfile(ctx, p, variant), api.DeviceDB(ctx, s))
         check_against_oracle(p, s, xj, fl, o)
 
@@ -148,7 +148,7 @@ def test_extreme_scalar_costs(ctx, bias, tbm, base):
     s = F.SeqSet.concat([F.synth_sequences(300, seed=bias + 7, lmax=3000),
                          F.SeqSet.from_list([rng.integers(0, 20, size=L).astype(np.uint8) for L in (1, 2, 9, 40000)])])
     o = O.msv_batch(p, s)
-    for variant in (0, 1):
+    for variant in (0, 1, None):          # None: the lane count the context picks (lane groups + long targets)
         xj, fl = api.search(ctx, api.DeviceProfile(ctx, p, variant), api.DeviceDB(ctx, s))
         check_against_oracle(p, s, xj, fl, o)
 
@@ -171,8 +171,10 @@ def test_kernel_launch_counter_advances(ctx):
     prof, db = api.DeviceProfile(ctx, p), api.DeviceDB(ctx, s)
     before = api.kernel_launches()
     api.search(ctx, prof, db)
-    # one fused launch at 32 lanes; the lane-group SSV pass plus the full-MSV pass otherwise
-    assert api.kernel_launches() == before + (1 if prof.lanes == 32 else 2)
+    # one fused launch at 32 lanes; otherwise the lane-group SSV pass and the
+    # full-MSV pass, plus a 32-lane launch for targets of 2400 residues or more
+    want = 1 if prof.lanes == 32 else 2 + int((s.lengths >= 2400).any())
+    assert api.kernel_launches() == before + want
     prof.set_lanes(32)
     before = api.kernel_launches()
     api.search(ctx, prof, db)

@@ -22,8 +22,10 @@ def valid(M, lanes):
 def test_rule_before_tuning():
     ctx = api.Context(0)
     try:
-        for M, want in ((1, 32), (15, 32), (16, 8), (100, 8), (511, 8), (512, 16), (1023, 16), (1024, 32), (3000, 32)):
+        for M, want in ((1, 32), (15, 32), (16, 8), (100, 8), (479, 8), (480, 32), (1023, 32), (3000, 32)):
             assert ctx.tune_lanes(M)[0] == want, M
+        for M, L, want in ((100, 50, 8), (100, 5000, 8), (600, 50, 16), (600, 300, 32), (1023, 149, 16), (1024, 50, 32)):
+            assert ctx.tune_lanes(M, L)[0] == want, (M, L)
     finally:
         ctx.close()
 
@@ -115,6 +117,8 @@ def test_forced_choices_are_what_the_context_reports(mixed_ctx):
     assert mixed_ctx.tune_lanes(100, 5000) == (32, 0)
     assert mixed_ctx.tune_lanes(100)[0] == 8
     assert mixed_ctx.tune_lanes(700, 50)[0] == 16     # 8 lanes cannot hold M = 700: the rule's choice
+    assert mixed_ctx.tune_lanes(700, 300)[0] == 16     # the forced table's [150, 600) choice
+    assert mixed_ctx.tune_lanes(700, 1000) == (32, 1)
 
 
 def test_batch_with_per_bin_lanes_matches_oracle(mixed_ctx):
