@@ -19,7 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libmsvgb.so")
 
 eslOK, eslEMEM, eslEINVAL, eslESYS, eslERANGE = 0, 5, 11, 12, 16
-eslENOTFOUND, eslEFORMAT, eslEINCOMPAT, eslEWRITE = 6, 7, 10, 27
+eslEOF, eslENOTFOUND, eslEFORMAT, eslEINCOMPAT, eslEWRITE = 3, 6, 7, 10, 27
 FLAG_ERANGE, FLAG_PASS, FLAG_FULL, FLAG_EMPTY = 0x01, 0x02, 0x04, 0x08
 
 # Every function declared in include/msvgb.h.
@@ -34,6 +34,9 @@ EXPORTS = [
     "msvgb_server_create", "msvgb_server_slots", "msvgb_server_submit", "msvgb_server_wait",
     "msvgb_server_launches", "msvgb_server_destroy", "msvgb_pipeline_run",
     "msvgb_autotune", "msvgb_tune_save", "msvgb_tune_load", "msvgb_tune_lanes",
+    "msvgb_h3f_open", "msvgb_h3f_read", "msvgb_h3f_close", "msvgb_h3f_write", "msvgb_fasta_read",
+    "msvgb_seqs_n", "msvgb_seqs_codes", "msvgb_seqs_offsets", "msvgb_seqs_name", "msvgb_seqs_free",
+    "msvgb_db_save", "msvgb_db_load", "msvgb_db_lengths",
 ]
 
 
@@ -82,6 +85,19 @@ def lib():
         "msvgb_tune_save": (i32, [vp, ctypes.c_char_p]),
         "msvgb_tune_load": (i32, [vp, ctypes.c_char_p]),
         "msvgb_tune_lanes": (i32, [vp, i32, i32, ctypes.POINTER(i32)]),
+        "msvgb_h3f_open": (i32, [ctypes.c_char_p, ctypes.POINTER(vp)]),
+        "msvgb_h3f_read": (i32, [vp, ctypes.POINTER(_Om), ctypes.c_char_p, i32]),
+        "msvgb_h3f_close": (i32, [vp]),
+        "msvgb_h3f_write": (i32, [ctypes.c_char_p, ctypes.POINTER(_Om), ctypes.c_char_p, i32]),
+        "msvgb_fasta_read": (i32, [ctypes.c_char_p, ctypes.POINTER(vp)]),
+        "msvgb_seqs_n": (ctypes.c_int64, [vp]),
+        "msvgb_seqs_codes": (vp, [vp]),
+        "msvgb_seqs_offsets": (vp, [vp]),
+        "msvgb_seqs_name": (ctypes.c_char_p, [vp, ctypes.c_int64]),
+        "msvgb_seqs_free": (i32, [vp]),
+        "msvgb_db_save": (i32, [vp, ctypes.c_char_p]),
+        "msvgb_db_load": (i32, [vp, ctypes.c_char_p, ctypes.POINTER(vp)]),
+        "msvgb_db_lengths": (i32, [vp, vp]),
         "msvgb_profile_lanes": (i32, [vp]),
         "msvgb_profile_destroy": (i32, [vp]),
         "msvgb_profile_M": (i32, [vp]),
@@ -247,6 +263,24 @@ class DeviceDB:
         self.h, self.ctx, self.n, self.lengths = h, ctx, seqs.n, seqs.lengths.copy()
         self.residues = int(seqs.total)
 
+    def save(self, path: str):
+        """Writes the packed layout (msvgb_db_save)."""
+        _check(lib().msvgb_db_save(self.h, path.encode()))
+
+    @classmethod
+    def load(cls, ctx: Context, path: str) -> "DeviceDB":
+        """A database from a packed file (msvgb_db_load)."""
+        h = ctypes.c_void_p()
+        _check(lib().msvgb_db_load(ctx.h, path.encode(), ctypes.byref(h)))
+        self = cls.__new__(cls)
+        self.h, self.ctx = h, ctx
+        self.n = int(lib().msvgb_db_nseq(h))
+        self.residues = int(lib().msvgb_db_residues(h))
+        self.lengths = np.zeros(self.n, np.int32)
+        if self.n:
+            _check(lib().msvgb_db_lengths(h, self.lengths.ctypes.data))
+        return self
+
     def close(self):
         if self.h:
             lib().msvgb_db_destroy(self.h)
@@ -257,6 +291,54 @@ class DeviceDB:
             self.close()
         except Exception:
             pass
+
+
+def read_h3f(path: str):
+    """Every record of a pressed MSV profile file: [(name, Profile)]."""
+    h = ctypes.c_void_p()
+    _check(lib().msvgb_h3f_open(path.encode(), ctypes.byref(h)))
+    out = []
+    try:
+        name = ctypes.create_string_buffer(1024)
+        while True:
+            o = _Om()
+            st = lib().msvgb_h3f_read(h, ctypes.byref(o), name, 1024)
+            if st == eslEOF:
+                break
+            _check(st)
+            Q = F.nqb(o.M)
+            rbv = np.ctypeslib.as_array(ctypes.cast(o.rbv, ctypes.POINTER(ctypes.c_uint8)),
+                                        shape=(o.Kp * Q * 16,)).reshape(o.Kp, Q, 16).copy()
+            out.append((name.value.decode(), F.Profile(M=o.M, rbv=rbv, tbm_b=o.tbm_b, tec_b=o.tec_b,
+                                                        base_b=o.base_b, bias_b=o.bias_b, scale_b=o.scale_b,
+                                                        mmu=o.mmu, mlambda=o.mlambda, tjb_cfg=o.tjb_b)))
+    finally:
+        lib().msvgb_h3f_close(h)
+    return out
+
+
+def write_h3f(path: str, named_profiles):
+    """Writes [(name, Profile)] as a pressed MSV profile file."""
+    for i, (name, p) in enumerate(named_profiles):
+        o, keep = _om_struct(p, p.tjb_cfg)
+        _check(lib().msvgb_h3f_write(path.encode(), ctypes.byref(o), name.encode(), 1 if i else 0))
+
+
+def read_fasta(path: str):
+    """(SeqSet of digital amino codes, names) of a FASTA file."""
+    h = ctypes.c_void_p()
+    _check(lib().msvgb_fasta_read(path.encode(), ctypes.byref(h)))
+    try:
+        n = int(lib().msvgb_seqs_n(h))
+        off = np.ctypeslib.as_array(ctypes.cast(lib().msvgb_seqs_offsets(h), ctypes.POINTER(ctypes.c_int64)),
+                                    shape=(n + 1,)).copy()
+        total = int(off[-1])
+        codes = (np.ctypeslib.as_array(ctypes.cast(lib().msvgb_seqs_codes(h), ctypes.POINTER(ctypes.c_uint8)),
+                                       shape=(total,)).copy() if total else np.zeros(0, np.uint8))
+        names = [lib().msvgb_seqs_name(h, i).decode() for i in range(n)]
+    finally:
+        lib().msvgb_seqs_free(h)
+    return F.SeqSet(codes, off), names
 
 
 def search(ctx: Context, prof: DeviceProfile, db: DeviceDB, F1: float = 0.02):

@@ -97,6 +97,7 @@ extern "C" int msvgb_f1_pass(float usc, int L, float mmu, float mlambda, double 
 // objects
 
 static std::atomic<uint64_t> g_db_serial{1};
+uint64_t msvgb_detail::next_db_serial() { return g_db_serial.fetch_add(1); }
 
 // DP widths (32-bit words per lane; the warp spans 64*C nodes). f16 tables:
 // every C up to 32. int8 tables: even C (two DP words per table word).
@@ -619,6 +620,7 @@ extern "C" int msvgb_db_create(msvgb_ctx *ctx, const uint8_t *codes, const int64
   msvgb_db *db = new msvgb_db();
   db->ctx = ctx; db->device = ctx->device; db->n = n; db->residues = total; db->Lmax = Lmax;
   db->serial = g_db_serial.fetch_add(1);
+  db->packed_bytes = bytes;
   db->distinct_len = std::move(distinct);
   db->n_long = std::partition_point(h_len, h_len + n, [](int32_t L) { return L >= kLongTarget; }) - h_len;
   int64_t *d_src = nullptr;

@@ -77,6 +77,7 @@ struct msvgb_db {
   std::vector<int32_t> distinct_len;  // sorted ascending
   uint64_t serial = 0;
   int64_t n_long = 0;                 // sequences of length >= kLongTarget (they sort first)
+  int64_t packed_bytes = 0;           // size of d_codes
 };
 
 // Targets this long are scored with 32 lanes per sequence even when the
@@ -118,6 +119,8 @@ void tune_free(msvgb_ctx *c);
 // where the model length allows it (0: the context's choice).
 int batch_create(msvgb_ctx *ctx, const msvgb_om *const *oms, int nprof, const msvgb_db *db, double F1,
                  void *d_xj, void *d_flags, int force_lanes, msvgb_batch **ret);
+// A fresh database serial (keys the per-length table caches).
+uint64_t next_db_serial();
 // Adds one to the count msvgb_kernel_launches() reports.
 void count_launch();
 // Scatters raw residues into the packed database layout (msv_pack.cu); sets

@@ -1,8 +1,9 @@
 /* msvgb.h -- C ABI of the GB300 MSV filter (HMMER3 hmmsearch stage 1).
  *
  * Plain C: pointers, sizes and status codes only. Status codes are Easel's
- * (easel/easel.h:95-114): eslOK 0, eslEMEM 5, eslEINVAL 11, eslESYS 12,
- * eslERANGE 16. No function calls exit(); a CUDA failure returns eslESYS and
+ * (easel/easel.h:95-114): eslOK 0, eslEOF 3, eslEMEM 5, eslENOTFOUND 6,
+ * eslEFORMAT 7, eslEINCOMPAT 10, eslEINVAL 11, eslESYS 12, eslERANGE 16,
+ * eslEWRITE 27. No function calls exit(); a CUDA failure returns eslESYS and
  * msvgb_last_error() describes it.
  *
  * Residues are Easel digital codes 0..28 for the amino alphabet
@@ -26,6 +27,7 @@ extern "C" {
 
 #define MSVGB_eslOK      0
 #define MSVGB_eslFAIL    1
+#define MSVGB_eslEOF     3
 #define MSVGB_eslEMEM    5
 #define MSVGB_eslENOTFOUND 6
 #define MSVGB_eslEFORMAT 7
@@ -91,20 +93,24 @@ int msvgb_MSVFilter(msvgb_ctx *ctx, const uint8_t *dsq, int L, const msvgb_om *o
  * (src/impl_sse/p7_oprofile.c:601-640, mf_conversion; sf_conversion :549-590):
  * the striped rbv bytes are re-laid for the kernels. om->tjb_b is ignored here:
  * the search recomputes it per target length (p7_oprofile_ReconfigMSVLength,
- * p7_oprofile.c:920-925). */
+ * p7_oprofile.c:920-925). The SSV table type and lanes per sequence are the
+ * context's choice for M (msvgb_tune_lanes; see msvgb_autotune). */
 int msvgb_profile_create(msvgb_ctx *ctx, const msvgb_om *om, msvgb_profile **ret_prof);
-/* Same with an explicit SSV arithmetic variant: 0 = int8 cost table, packed
- * 16-bit integer cells (default); 1 = f16 cost table, f16x2 cells (exact on
- * these integers; used where its 2x larger table fits in shared memory,
- * otherwise variant 0 is used). msvgb_profile_variant() tells which. */
+/* Same with an explicit SSV arithmetic variant and 32 lanes per sequence:
+ * 0 = int8 cost table, packed 16-bit integer cells; 1 = f16 cost table, f16x2
+ * cells (exact on these integers; used where its 2x larger table fits in
+ * shared memory, otherwise variant 0 is used). msvgb_profile_variant() tells
+ * which. */
 int msvgb_profile_create_ex(msvgb_ctx *ctx, const msvgb_om *om, int ssv_variant, msvgb_profile **ret_prof);
 int msvgb_profile_variant(const msvgb_profile *prof);
-/* Lanes per sequence of the SSV pass: 32 (default; one warp per sequence, SSV
+/* Lanes per sequence of the SSV pass: 32 (one warp per sequence, SSV
  * and full MSV in one kernel), or 16 / 8 (2 / 4 sequences per warp in
  * lockstep, for small models: each lane then holds more DP words per row);
  * with 16 or 8 the sequences SSV leaves undecided are finished by the full
- * MSV in a second launch. om must be the profile's own MSV fields. Needs
- * M < 64 * G and, for G < 32, M >= 2 * G. Chosen by msvgb_autotune. */
+ * MSV in a second launch, and targets of 2400 residues or more run at 32
+ * lanes in a concurrent launch (one long target must not set the length of
+ * the search). om must be the profile's own MSV fields. Needs M < 64 * G and,
+ * for G < 32, M >= 2 * G. */
 int msvgb_profile_set_lanes(msvgb_profile *prof, const msvgb_om *om, int lanes);
 int msvgb_profile_lanes(const msvgb_profile *prof);
 
@@ -130,6 +136,47 @@ int msvgb_tune_load(msvgb_ctx *ctx, const char *path);
  * L (L < 0: the whole length mix); *ret_variant (may be NULL) gets the SSV
  * table type for 32 lanes (1 f16, 0 int8). */
 int msvgb_tune_lanes(msvgb_ctx *ctx, int M, int L, int *ret_variant);
+
+/* ---- on-disk formats ------------------------------------------------------------
+ * Pressed MSV profiles (.h3f, the MSV file hmmpress writes: HMMER 3/f binary,
+ * x86-64 little-endian). Replaces p7_oprofile_ReadMSV (src/impl_sse/io.c:233)
+ * for an hmmscan-style many-profile batch. Amino profiles only. */
+typedef struct msvgb_h3f msvgb_h3f;
+int msvgb_h3f_open(const char *path, msvgb_h3f **ret);
+/* The next record's MSV fields: om->rbv points at storage owned by the reader
+ * until the next read or close; mmu, mlambda come from the record's evparam;
+ * name (may be NULL) receives up to name_cap - 1 bytes of the model name.
+ * Returns 3 (eslEOF) after the last record; eslEFORMAT on a corrupted or
+ * older-format record; eslEINCOMPAT for a non-amino model. */
+int msvgb_h3f_read(msvgb_h3f *f, msvgb_om *om, char *name, int name_cap);
+int msvgb_h3f_close(msvgb_h3f *f);
+/* Writes (append != 0: appends) one record in the same format, as
+ * p7_oprofile_Write does (io.c:89); the SSV table is derived from rbv
+ * (sf_conversion, p7_oprofile.c:549-590); evparam holds mmu and mlambda only. */
+int msvgb_h3f_write(const char *path, const msvgb_om *om, const char *name, int append);
+
+/* FASTA files read into digital amino codes, as Easel's FASTA reader
+ * (easel/esl_sqio_ascii.c) digitizes them: letters of
+ * "ACDEFGHIKLMNPQRSTVWY-BJZOUX*~" in either case, '_' and '.' as gaps, blanks
+ * skipped; any other character is eslEFORMAT. Replaces esl_sqio_ReadBlock
+ * (easel/esl_sqio.c:1040) as the feed of msvgb_db_create. */
+typedef struct msvgb_seqs msvgb_seqs;
+int            msvgb_fasta_read(const char *path, msvgb_seqs **ret);
+int64_t        msvgb_seqs_n(const msvgb_seqs *s);
+const uint8_t *msvgb_seqs_codes(const msvgb_seqs *s);     /* concatenated codes */
+const int64_t *msvgb_seqs_offsets(const msvgb_seqs *s);   /* n + 1 offsets into the codes */
+const char    *msvgb_seqs_name(const msvgb_seqs *s, int64_t i);
+int            msvgb_seqs_free(msvgb_seqs *s);
+
+/* The packed database (length-sorted, 16-byte-aligned residues, as
+ * msvgb_db_create lays it out in HBM) saved to a file and loaded back with
+ * plain copies: a database is packed once, replacing the fork's offline
+ * dbsort step. Loading checks every index a kernel uses; a file that fails is
+ * eslEFORMAT. */
+int msvgb_db_save(const msvgb_db *db, const char *path);
+int msvgb_db_load(msvgb_ctx *ctx, const char *path, msvgb_db **ret);
+/* Sequence lengths in the caller's original order (out: n entries). */
+int msvgb_db_lengths(const msvgb_db *db, int32_t *out);
 int msvgb_profile_destroy(msvgb_profile *prof);
 int msvgb_profile_M(const msvgb_profile *prof);
 

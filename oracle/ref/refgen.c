@@ -15,6 +15,14 @@
  *              p7_bg_SetLength, p7_oprofile_ReconfigLength, p7_bg_NullOne,
  *              p7_MSVFilter (impl_sse/msvfilter.c:78), esl_gumbel_surv, F1 gate.
  *
+ *   hmmfile  : the hmmsearch path for a model read from an HMM file
+ *              (p7_hmmfile_OpenE / p7_hmmfile_Read, src/p7_hmmfile.c:127, 1181;
+ *              p7_ProfileConfig(hmm, bg, gm, 100, p7_LOCAL) + p7_oprofile_Convert
+ *              as src/hmmsearch.c:502-503 does), or the pressed MSV part read back
+ *              with p7_oprofile_ReadMSV (src/impl_sse/io.c:233).
+ *   seqfile  : any sequence file Easel reads (esl_sqfile_OpenDigital, format
+ *              autodetected, easel/esl_sqio.c:300), digitized with the amino alphabet.
+ *
  * File formats (little-endian, written and read by this project only):
  *   profile "MSVPROF1": int32 M, Q, Kp, Lcfg; uint8 tbm,tec,tjb,base,bias,pad[3];
  *                       float scale; double mmu, mlambda; uint8 rbv[Kp*Q*16]
@@ -34,6 +42,7 @@
 #include "esl_random.h"
 #include "esl_randomseq.h"
 #include "esl_sq.h"
+#include "esl_sqio.h"
 #include "esl_gumbel.h"
 #include "hmmer.h"
 
@@ -71,6 +80,36 @@ static void write_profile(const model_t *m, int Lcfg, const char *path)
   fwrite(hdr, 4, 4, fp); fwrite(b, 1, 8, fp); fwrite(&scale, 4, 1, fp); fwrite(ev, 8, 2, fp);
   for (int x = 0; x < m->abc->Kp; x++) fwrite(m->om->rbv[x], 16, Q, fp);
   fclose(fp);
+}
+
+/* The idx-th model of an HMM file, configured and converted as hmmsearch
+ * does; with pressed=1 the MSV part is instead read from the .h3f file. */
+static void file_model(model_t *m, const char *hmmfile, int idx, int pressed)
+{
+  char errbuf[eslERRBUFSIZE];
+  P7_HMMFILE *hfp = NULL;
+  m->abc = NULL; m->hmm = NULL; m->gm = NULL; m->om = NULL;
+  if (p7_hmmfile_OpenE((char *) hmmfile, NULL, &hfp, errbuf) != eslOK) die(errbuf);
+  if (pressed) {
+    for (int i = 0; i <= idx; i++) {
+      if (m->om) p7_oprofile_Destroy(m->om);
+      m->om = NULL;
+      if (p7_oprofile_ReadMSV(hfp, &m->abc, &m->om) != eslOK) die("p7_oprofile_ReadMSV");
+    }
+  } else {
+    for (int i = 0; i <= idx; i++) {
+      if (m->hmm) p7_hmm_Destroy(m->hmm);
+      m->hmm = NULL;
+      if (p7_hmmfile_Read(hfp, &m->abc, &m->hmm) != eslOK) die("p7_hmmfile_Read");
+    }
+    m->bg = p7_bg_Create(m->abc);
+    m->gm = p7_profile_Create(m->hmm->M, m->abc);
+    m->om = p7_oprofile_Create(m->hmm->M, m->abc);
+    if (p7_ProfileConfig(m->hmm, m->bg, m->gm, 100, p7_LOCAL) != eslOK) die("p7_ProfileConfig");
+    if (p7_oprofile_Convert(m->gm, m->om) != eslOK) die("p7_oprofile_Convert");
+  }
+  m->bg = p7_bg_Create(m->abc);
+  p7_hmmfile_Close(hfp);
 }
 
 typedef struct { int64_t n, total; int64_t *off; uint8_t *dsq; } seqs_t;
@@ -155,11 +194,61 @@ int main(int argc, char **argv)
     write_seqs(&s, argv[5]);
     return 0;
   }
-  if (!strcmp(cmd, "score")) {              /* score M seed Lcfg mode seqs out */
-    if (argc != 8) die("score M seed Lcfg mode seqs out");
-    model_t m; int M = atoi(argv[2]), Lcfg = atoi(argv[4]);
-    make_model(&m, M, (uint32_t) atol(argv[3]), Lcfg, atoi(argv[5]));
-    seqs_t s; read_seqs(&s, argv[6]);
+  if (!strcmp(cmd, "hmmfile")) {            /* hmmfile path idx pressed(0/1) out */
+    if (argc != 6) die("hmmfile path idx pressed out");
+    model_t m;
+    file_model(&m, argv[2], atoi(argv[3]), atoi(argv[4]));
+    write_profile(&m, 100, argv[5]);
+    return 0;
+  }
+  if (!strcmp(cmd, "seqfile")) {            /* seqfile path out */
+    if (argc != 4) die("seqfile path out");
+    ESL_ALPHABET *abc = esl_alphabet_Create(eslAMINO);
+    ESL_SQFILE *sqfp = NULL;
+    if (esl_sqfile_OpenDigital(abc, argv[2], eslSQFILE_UNKNOWN, NULL, &sqfp) != eslOK) die("esl_sqfile_OpenDigital");
+    ESL_SQ *sq = esl_sq_CreateDigital(abc);
+    seqs_t s = {0, 0, NULL, NULL}; int64_t cap = 0;
+    s.off = malloc(8); s.off[0] = 0;
+    int st;
+    while ((st = esl_sqio_Read(sqfp, sq)) == eslOK) { push_seq(&s, &cap, sq->dsq, (int) sq->n); esl_sq_Reuse(sq); }
+    if (st != eslEOF) die("esl_sqio_Read");
+    write_seqs(&s, argv[3]);
+    return 0;
+  }
+  if (!strcmp(cmd, "emitfile")) {           /* emitfile hmmfile idx n emitseed out */
+    if (argc != 7) die("emitfile hmmfile idx n emitseed out");
+    model_t m;
+    file_model(&m, argv[2], atoi(argv[3]), 0);
+    int n = atoi(argv[4]);
+    ESL_RANDOMNESS *r = esl_randomness_Create((uint32_t) atol(argv[5]));
+    ESL_SQ *sq = esl_sq_CreateDigital(m.abc);
+    seqs_t s = {0, 0, NULL, NULL}; int64_t cap = 0;
+    s.off = malloc(8); s.off[0] = 0;
+    for (int i = 0; i < n; i++) {
+      esl_sq_Reuse(sq);
+      if (p7_ProfileEmit(r, m.hmm, m.gm, m.bg, sq, NULL) != eslOK) die("p7_ProfileEmit");
+      push_seq(&s, &cap, sq->dsq, (int) sq->n);
+    }
+    write_seqs(&s, argv[6]);
+    return 0;
+  }
+  if (!strcmp(cmd, "score") || !strcmp(cmd, "scorefile")) {  /* score M seed Lcfg mode seqs out | scorefile hmmfile idx seqs out */
+    model_t m; int M;
+    seqs_t s;
+    const char *outpath;
+    if (!strcmp(cmd, "score")) {
+      if (argc != 8) die("score M seed Lcfg mode seqs out");
+      M = atoi(argv[2]);
+      make_model(&m, M, (uint32_t) atol(argv[3]), atoi(argv[4]), atoi(argv[5]));
+      read_seqs(&s, argv[6]);
+      outpath = argv[7];
+    } else {
+      if (argc != 6) die("scorefile hmmfile idx seqs out");
+      file_model(&m, argv[2], atoi(argv[3]), 0);
+      M = m.om->M;
+      read_seqs(&s, argv[4]);
+      outpath = argv[5];
+    }
     int64_t maxL = 1;
     for (int64_t i = 0; i < s.n; i++) if (s.off[i+1] - s.off[i] > maxL) maxL = s.off[i+1] - s.off[i];
     P7_OMX *ox = p7_omx_Create(M, 0, 0);
@@ -181,7 +270,7 @@ int main(int argc, char **argv)
       P[i] = esl_gumbel_surv(seq_score, m.om->evparam[p7_MMU], m.om->evparam[p7_MLAMBDA]);
       pass[i] = (P[i] > F1) ? 0 : 1;
     }
-    FILE *fp = fopen(argv[7], "wb"); if (!fp) die("open result out");
+    FILE *fp = fopen(outpath, "wb"); if (!fp) die("open result out");
     fwrite("MSVRES01", 1, 8, fp); fwrite(&s.n, 8, 1, fp);
     fwrite(st, 4, s.n, fp); fwrite(sc, 4, s.n, fp); fwrite(ns, 8, s.n, fp);
     fwrite(P, 8, s.n, fp); fwrite(pass, 1, s.n, fp);

@@ -15,7 +15,15 @@ SSE2 code). For every case it
      p7_Pipeline MSV stage (``refgen score``).
 
 Files per case NAME: NAME.prof (MSVPROF1), NAME.seqs (MSVSEQS1), NAME.res (MSVRES01).
-Run:  python tests/golden/make_golden.py
+
+The tut_* cases use the reference's tutorial models and sequences instead
+(the Pfam models globins4, fn3 and Pkinase of tutorial/minifam, configured and
+converted as hmmsearch does, ``refgen hmmfile``; tutorial/globins45.fa,
+HBB_HUMAN and 7LESS_DROME read by Easel's sequence reader, ``refgen seqfile``;
+p7_ProfileEmit homologs and saturation repeats of each model; background
+sequences), so the fixtures pin the path on real profiles, including the
+fn3 / 7LESS_DROME search of tutorial/fn3.out.
+Run:  python tests/golden/make_golden.py [reference code dir]
 """
 import os
 import subprocess
@@ -80,11 +88,44 @@ def make_case(name, M, seed, n_ln, lmax, n_hom, n_sat, rep):
           f"pass={int(r.passed.sum())}")
 
 
+# tutorial models: (name, index in tutorial/minifam)
+TUT_MODELS = [("tut_globins4", 0), ("tut_fn3", 1), ("tut_pkinase", 2)]
+TUT_SEQFILES = ["globins45.fa", "HBB_HUMAN", "7LESS_DROME"]
+
+
+def make_tutorial(tut):
+    minifam = os.path.join(tut, "minifam")
+    tmp = os.path.join(HERE, "_tmp.seqs")
+    common = []
+    for f in TUT_SEQFILES:
+        run("seqfile", os.path.join(tut, f), tmp)
+        common.append(F.read_seqs(tmp))
+    run("randseq", 60, 300, 7, tmp)
+    common.append(F.read_seqs(tmp))
+    for k, (name, idx) in enumerate(TUT_MODELS):
+        prof = os.path.join(HERE, name + ".prof")
+        seqs = os.path.join(HERE, name + ".seqs")
+        res = os.path.join(HERE, name + ".res")
+        run("hmmfile", minifam, idx, 0, prof)
+        run("emitfile", minifam, idx, 30, 100 + k, tmp)
+        hom = F.read_seqs(tmp)
+        sat = F.SeqSet.from_list([np.tile(hom.seq(i), 20) for i in range(3)])   # saturation repeats
+        s = F.SeqSet.concat(common + [hom, sat])
+        F.write_seqs(s, seqs)
+        run("scorefile", minifam, idx, seqs, res)
+        r = F.read_results(res)
+        print(f"{name}: M={F.read_profile(prof).M} n={s.n} residues={s.total} "
+              f"erange={(r.status == 16).sum()} pass={int(r.passed.sum())}")
+    os.remove(tmp)
+
+
 def main():
     if not os.path.exists(REFGEN):
         sys.exit("oracle/_ref/refgen missing: make -C oracle/ref REF=<reference>/code")
+    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/code"
     for c in CASES:
         make_case(*c)
+    make_tutorial(os.path.join(ref, "tutorial"))
 
 
 if __name__ == "__main__":
