@@ -36,10 +36,13 @@ sys.path.insert(0, ROOT)
 from cudahmmsearch_gb300 import formats as F  # noqa: E402
 
 INT_LANE_OPS_PER_CLK_PER_SM = 128   # 4 SM sub-partitions x 32 lanes: nominal issue width
-# DRAM bytes per residue per search launch, from the ncu capture summarised in
-# profiles/msv_search_kernel_f16_m400_400k.md (169.4 MB for 154.56 M residues);
-# the launch reads each residue once, so traffic scales with the residue count.
-DRAM_BYTES_PER_RESIDUE = 169.4e6 / 154.56e6
+# DRAM bytes per residue of the hot kernel (the lane-group SSV pass), from the
+# ncu capture summarised in profiles/msv_ssv_group_kernel_m400_400k.md
+# (168.8 MB for 154.56 M residues); the pass reads each residue once, so
+# traffic scales with the residue count.
+DRAM_BYTES_PER_RESIDUE = 168.8e6 / 154.56e6
+SMEM_BYTES_PER_CLK_PER_SM = 128     # one 128-byte shared-memory wavefront per clock
+SSV_TABLE_BYTES_PER_CELL = 2        # f16 cost per DP cell read from shared memory
 
 
 def workload(name, rank=0, args=None):
@@ -343,7 +346,7 @@ def main():
     ap.add_argument("--lanes", type=int, default=None, help="lanes per sequence of the SSV pass (32, 16, 8)")
     ap.add_argument("--M", type=int, default=100, help="sampled workload: model length")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--nprof", type=int, default=256, help="batch workload: number of profiles")
     ap.add_argument("--nseq", type=int, default=1_000_000, help="batch/serve workload: database size")
     ap.add_argument("--loads", default="10:3,50:3,500:0.5", help="serve workload: rate:seconds,...")
@@ -426,23 +429,30 @@ def main():
     codes_pin = torch.from_numpy(s.codes).pin_memory()
     off_np = s.off
     e2e_times, e2e_parts = [], []
+    seqset = F.SeqSet(codes_pin.numpy(), off_np)
     for i in range(args.e2e_steps + 1 if args.e2e_steps > 0 else 0):
         torch.cuda.synchronize()
         t = time.perf_counter()
-        seqset = F.SeqSet(codes_pin.numpy(), off_np)
-        db2 = api.DeviceDB(ctx, seqset)
-        t_db = time.perf_counter()
-        xj, fl = api.search(ctx, prof, db2)
-        t_search = time.perf_counter()
-        db2.close()
+        xj, fl = api.search_host(ctx, prof, seqset)          # chunked upload + packing under the search
         dt = time.perf_counter() - t
-        e2e_parts.append({"db_create_ms": (t_db - t) * 1e3, "search_ms": (t_search - t_db) * 1e3,
-                          "destroy_ms": (t + dt - t_search) * 1e3})
         if i > 0:
             e2e_times.append(dt)
     if e2e_times:
         assert np.array_equal(xj, xj_all) and np.array_equal(fl, fl_all)
-    e2e_val = cells / float(np.mean(e2e_times)) / 1e9 if e2e_times else None
+        # the same work as two separate calls (database upload, then search), for the breakdown
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        db2 = api.DeviceDB(ctx, seqset)
+        t_db = time.perf_counter()
+        xj2, fl2 = api.search(ctx, prof, db2)
+        t_search = time.perf_counter()
+        db2.close()
+        dt2 = time.perf_counter() - t
+        assert np.array_equal(xj2, xj_all) and np.array_equal(fl2, fl_all)
+        e2e_parts.append({"db_create_ms": (t_db - t) * 1e3, "search_ms": (t_search - t_db) * 1e3,
+                          "destroy_ms": (t + dt2 - t_search) * 1e3,
+                          "separate_calls_gcups": cells / dt2 / 1e9})
+    e2e_val = cells / float(np.median(e2e_times)) / 1e9 if e2e_times else None
 
     clocks = clk.summary()
     sm_mhz = clocks["sm_mhz"] or 2070.0
@@ -453,11 +463,17 @@ def main():
     roofline = {"bound": "int32-pipe", "achieved": achieved_tops, "peak": peak_tops, "unit": "Tops/s",
                 "frac": achieved_tops / peak_tops,
                 "traffic": DRAM_BYTES_PER_RESIDUE * s.total,
-                "traffic_note": "DRAM bytes per launch scaled by residues from an ncu capture of the same kernel "
-                                "on 400,000 sequences (profiles/msv_search_kernel_f16_m400_400k.md)",
+                "traffic_note": "DRAM bytes of the SSV pass scaled by residues from an ncu capture of the same "
+                                "kernel on 400,000 sequences (profiles/msv_ssv_group_kernel_m400_400k.md)",
                 "peak_note": f"measured: msvgb_measure_int_peak (independent max.s32/xor over {nsm} SMs); "
                              f"nominal {nsm} SMs x {INT_LANE_OPS_PER_CLK_PER_SM} lane-ops/clk x {sm_mhz:.0f} MHz = "
                              f"{nsm * INT_LANE_OPS_PER_CLK_PER_SM * sm_mhz * 1e6 / 1e12:.1f} Tops/s",
+                "smem": {"achieved": SSV_TABLE_BYTES_PER_CELL * cells / (kern_ms * 1e-3) / 1e9,
+                         "peak": nsm * SMEM_BYTES_PER_CLK_PER_SM * sm_mhz * 1e6 / 1e9, "unit": "GB/s",
+                         "frac": SSV_TABLE_BYTES_PER_CELL * cells / (kern_ms * 1e-3)
+                                 / (nsm * SMEM_BYTES_PER_CLK_PER_SM * sm_mhz * 1e6),
+                         "peak_note": f"nominal: {nsm} SMs x 128 B/clk x {sm_mhz:.0f} MHz (median SM clock "
+                                      "under load); 2 B of f16 SSV cost per cell, the bound of the SSV pass"},
                 "hbm": {"achieved": (s.total + 2 * s.n) / (kern_ms * 1e-3) / 1e9, "peak": 6783.5,
                         "unit": "GB/s", "frac": (s.total + 2 * s.n) / (kern_ms * 1e-3) / 1e9 / 6783.5,
                         "peak_note": "of measured (MEASURED_PEAKS.json hbm_gbs)"}}
@@ -467,9 +483,12 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
             "config": dict(cfg, variant=prof.variant, lanes=prof.lanes, full_msv_fraction=fullfrac,
                            pass_fraction=float(((fl_all & api.FLAG_PASS) != 0).mean())),
-            "e2e": {"value": e2e_val, "unit": "GCUPS", "h2d_bytes_per_step": int(s.total + 8 * (s.n + 1)),
-                    "breakdown_last_step": e2e_parts[-1] if e2e_parts else None,
-                    "d2h_bytes_per_step": int(2 * s.n), "path": "msvgb_db_create + msvgb_search from pinned host memory"},
+            "e2e": {"value": e2e_val, "unit": "GCUPS", "h2d_bytes_per_step": int(s.total + 28 * s.n),
+                    "d2h_bytes_per_step": int(2 * s.n),
+                    "path": "msvgb_search_host from pinned host memory: residues and per-sequence start/orig/"
+                            "src/len metadata uploaded and packed in chunks on a second stream under the search",
+                    "separate_calls": e2e_parts[-1] if e2e_parts else None,
+                    "steps_ms": [round(t * 1e3, 2) for t in e2e_times], "statistic": "median of the timed steps"},
             "gpu_launches": int(launches), "clocks": clocks, "roofline": roofline}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(p, s)

@@ -36,7 +36,7 @@ EXPORTS = [
     "msvgb_autotune", "msvgb_tune_save", "msvgb_tune_load", "msvgb_tune_lanes",
     "msvgb_h3f_open", "msvgb_h3f_read", "msvgb_h3f_close", "msvgb_h3f_write", "msvgb_fasta_read",
     "msvgb_seqs_n", "msvgb_seqs_codes", "msvgb_seqs_offsets", "msvgb_seqs_name", "msvgb_seqs_free",
-    "msvgb_db_save", "msvgb_db_load", "msvgb_db_lengths",
+    "msvgb_db_save", "msvgb_db_load", "msvgb_db_lengths", "msvgb_search_host",
 ]
 
 
@@ -98,6 +98,7 @@ def lib():
         "msvgb_db_save": (i32, [vp, ctypes.c_char_p]),
         "msvgb_db_load": (i32, [vp, ctypes.c_char_p, ctypes.POINTER(vp)]),
         "msvgb_db_lengths": (i32, [vp, vp]),
+        "msvgb_search_host": (i32, [vp, vp, vp, vp, ctypes.c_int64, ctypes.c_double, ctypes.c_int64, vp, vp]),
         "msvgb_profile_lanes": (i32, [vp]),
         "msvgb_profile_destroy": (i32, [vp]),
         "msvgb_profile_M": (i32, [vp]),
@@ -339,6 +340,20 @@ def read_fasta(path: str):
     finally:
         lib().msvgb_seqs_free(h)
     return F.SeqSet(codes, off), names
+
+
+def search_host(ctx: Context, prof: DeviceProfile, seqs: F.SeqSet, F1: float = 0.02, chunk_residues: int = 0):
+    """End to end from host buffers (msvgb_search_host): chunked upload and
+    packing overlapped with the search. Returns (xj, flags) as search()."""
+    codes = np.ascontiguousarray(seqs.codes, dtype=np.uint8)
+    if codes.size == 0:
+        codes = np.zeros(1, np.uint8)
+    off = np.ascontiguousarray(seqs.off, dtype=np.int64)
+    xj = np.zeros(seqs.n, np.uint8)
+    fl = np.zeros(seqs.n, np.uint8)
+    _check(lib().msvgb_search_host(ctx.h, prof.h, codes.ctypes.data, off.ctypes.data, seqs.n, F1,
+                                   chunk_residues, xj.ctypes.data, fl.ctypes.data))
+    return xj, fl
 
 
 def search(ctx: Context, prof: DeviceProfile, db: DeviceDB, F1: float = 0.02):

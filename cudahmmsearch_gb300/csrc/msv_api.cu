@@ -16,7 +16,6 @@
 #include <cstring>
 #include <mutex>
 #include <string>
-#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -181,6 +180,8 @@ extern "C" int msvgb_ctx_create(int device, msvgb_ctx **ret_ctx) {
   if (e == cudaSuccess) e = cudaMalloc(&c->d_bad, sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc(&c->d_aux, 4 * sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->upload, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->dma, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
   if (e != cudaSuccess) {
@@ -200,12 +201,14 @@ extern "C" int msvgb_ctx_destroy(msvgb_ctx *c) {
   if (c->own) cudaStreamSynchronize(c->own);
   cudaFree(c->d_ticket); cudaFree(c->d_meta); cudaFree(c->d_out);
   cudaFree(c->d_seq); cudaFree(c->d_tab); cudaFree(c->d_bad); cudaFree(c->d_aux); cudaFree(c->d_list);
-  if (c->h_stage) cudaFreeHost(c->h_stage);
   if (c->own) cudaStreamDestroy(c->own);
   if (c->side) { cudaStreamSynchronize(c->side); cudaStreamDestroy(c->side); }
+  if (c->upload) { cudaStreamSynchronize(c->upload); cudaStreamDestroy(c->upload); }
+  if (c->dma) { cudaStreamSynchronize(c->dma); cudaStreamDestroy(c->dma); }
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
   msvgb_detail::tune_free(c);
+  if (c->h_pin) cudaFreeHost(c->h_pin);
   delete c;
   return MSVGB_eslOK;
 }
@@ -471,10 +474,13 @@ int msvgb_detail::ensure_tables(msvgb_profile *p, const msvgb_db *db, double F1,
   if (dirty) {
     std::vector<uint8_t> x(t->cap);
     for (int L = 0; L < t->cap; ++L) x[L] = t->xjm[L] < 0 ? 255 : (uint8_t) t->xjm[L];
-    // ordered on the context's stream before the searches that read them
-    cudaError_t e = cudaMemcpyAsync(t->d_tjb, t->tjb.data(), t->cap, cudaMemcpyHostToDevice, p->ctx->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(t->d_xjmin, x.data(), t->cap, cudaMemcpyHostToDevice, p->ctx->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(p->ctx->stream);
+    // Complete before this returns, i.e. before any later search is launched,
+    // without waiting behind searches still running on the context's stream:
+    // entries those may read are rewritten with the bytes they already hold
+    // (or live in retired buffers), so they read consistent values.
+    cudaError_t e = cudaMemcpyAsync(t->d_tjb, t->tjb.data(), t->cap, cudaMemcpyHostToDevice, p->ctx->upload);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(t->d_xjmin, x.data(), t->cap, cudaMemcpyHostToDevice, p->ctx->upload);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(p->ctx->upload);
     if (e != cudaSuccess) return fail(MSVGB_eslESYS, std::string("length tables: ") + cudaGetErrorString(e));
   }
   *out = t;
@@ -502,6 +508,54 @@ struct PhaseTimer {
 
 extern "C" int msvgb_db_create(msvgb_ctx *ctx, const uint8_t *codes, const int64_t *off, int64_t n,
                                msvgb_db **ret) {
+  if (!ctx) return fail(MSVGB_eslEINVAL, "NULL argument");
+  return msvgb_detail::db_create_on(ctx, codes, off, n, ctx->stream, ret);
+}
+
+// Grows the context's small pinned scratch (no copy into it may be pending).
+static cudaError_t grow_pinned(msvgb_ctx *ctx, size_t need) {
+  if (ctx->h_pin) cudaFreeHost(ctx->h_pin);
+  ctx->h_pin = nullptr; ctx->h_pin_cap = 0;
+  need = std::max<size_t>(need, 1 << 16);
+  cudaError_t e = cudaMallocHost(&ctx->h_pin, need);
+  if (e == cudaSuccess) ctx->h_pin_cap = need;
+  return e;
+}
+
+cudaMemPool_t msvgb_detail::scratch_pool(int device) {
+  static std::mutex mu;
+  static std::unordered_map<int, cudaMemPool_t> pools;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = pools.find(device);
+  if (it != pools.end()) return it->second;
+  cudaMemPoolProps props = {};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = device;
+  cudaMemPool_t pool = nullptr;
+  if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) return nullptr;
+  uint64_t keep = (uint64_t) 4 << 30;
+  cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  pools[device] = pool;
+  return pool;
+}
+
+// msvgb_db_create with its copies and packing on stream st. Without an
+// AsyncPack it returns when the database is complete on the device. With one,
+// it returns once everything is enqueued: invalid codes are OR-ed into
+// a->d_bad (checked by the caller) and db->ready completes when the database
+// is on the device.
+//
+// The offsets go up first, then the raw residues in one DMA on the context's
+// dma stream. Meanwhile the lengths are sorted on the device: lengths and
+// their maximum (the only value the host waits for before the end), per-length
+// counts, a scan of the counts by descending length (first sorted slot and
+// first packed byte of every length), placement; then the residues are
+// scattered into the packed layout. The counts come back to the host at the
+// end, for the distinct lengths the per-length tables need. Databases with
+// sequences longer than 4M residues are sorted on the host instead.
+int msvgb_detail::db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64_t *off, int64_t n,
+                               cudaStream_t st, msvgb_db **ret, const AsyncPack *a) {
   if (!ctx || !ret || (n > 0 && (!off || !codes))) return fail(MSVGB_eslEINVAL, "NULL argument");
   PhaseTimer pt;
   *ret = nullptr;
@@ -509,150 +563,149 @@ extern "C" int msvgb_db_create(msvgb_ctx *ctx, const uint8_t *codes, const int64
   const int64_t total = n ? off[n] - off[0] : 0;
   if (total < 0) return fail(MSVGB_eslEINVAL, "bad sequence offsets");
   CUDA_TRY(cudaSetDevice(ctx->device));
-  cudaStream_t st = ctx->stream;
-
-  // The residues go first: their DMA runs while the host sorts the lengths.
+  const int64_t n1 = std::max<int64_t>(n, 1);
+  cudaMemPool_t pool = scratch_pool(ctx->device);
+  if (!pool) return fail(MSVGB_eslESYS, "database upload: no memory pool");
+  std::vector<void *> scratch;                                // freed on st at the end
+  auto alloc = [&](void **ptr, size_t bytes, cudaStream_t s2) {
+    cudaError_t r = cudaMallocFromPoolAsync(ptr, std::max<size_t>(bytes, 16), pool, s2);
+    if (r == cudaSuccess) scratch.push_back(*ptr);
+    return r;
+  };
+  int64_t *d_off = nullptr, *d_scal = nullptr;                // d_scal: [0] Lmax | bad << 32, [1] packed size
+  int32_t *d_len_in = nullptr;
   uint8_t *d_raw = nullptr;
-  CUDA_TRY(cudaMallocAsync((void **) &d_raw, std::max<int64_t>(total, 1), st));
-  if (total) {
-    cudaError_t e = cudaMemcpyAsync(d_raw, codes + off[0], total, cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) { cudaFreeAsync(d_raw, st); return fail(MSVGB_eslESYS, cudaGetErrorString(e)); }
-  }
-
-  // Lengths: validation, Lmax and per-thread histograms, in parallel.
-  const int T = (int) std::max<int64_t>(1, std::min<int64_t>(std::max(1u, std::thread::hardware_concurrency()),
-                                                             std::min<int64_t>(32, n / 65536 + 1)));
-  std::vector<int> lmax_t(T, 0), bad_t(T, 0);
-  auto range = [&](int t) { return std::make_pair(n * t / T, n * (t + 1) / T); };
-  auto par = [&](auto &&fn) {
-    std::vector<std::thread> th;
-    for (int t = 1; t < T; ++t) th.emplace_back(fn, t);
-    fn(0);
-    for (auto &x : th) x.join();
+  cudaEvent_t ev_raw = nullptr;
+  CUDA_TRY(cudaEventCreateWithFlags(&ev_raw, cudaEventDisableTiming));
+  cudaError_t e = alloc((void **) &d_off, (size_t) (n + 1) * 8, st);
+  if (e == cudaSuccess) e = alloc((void **) &d_len_in, (size_t) n1 * 4, st);
+  if (e == cudaSuccess) e = alloc((void **) &d_scal, 16, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_off, off, (size_t) (n + 1) * 8, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaEventRecord(ev_raw, st);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->dma, ev_raw, 0);
+  if (e == cudaSuccess) e = alloc((void **) &d_raw, (size_t) total, ctx->dma);
+  if (e == cudaSuccess && total) e = cudaMemcpyAsync(d_raw, codes + off[0], total, cudaMemcpyHostToDevice, ctx->dma);
+  if (e == cudaSuccess) e = cudaEventRecord(ev_raw, ctx->dma);
+  pt.mark("copies issued");
+  if (e == cudaSuccess && ctx->h_pin_cap < 64) e = grow_pinned(ctx, 64);
+  unsigned *misc = (unsigned *) ctx->h_pin;
+  if (e == cudaSuccess) { misc[0] = misc[1] = 0; e = cudaMemsetAsync(d_scal, 0, 16, st); }
+  if (e == cudaSuccess) e = launch_lengths(d_off, n, d_len_in, (unsigned *) d_scal, (int *) d_scal + 1,
+                                           ctx->num_sms, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(misc, d_scal, 8, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  pt.mark("lengths");
+  const bool bad_len = e == cudaSuccess && misc[1] != 0;
+  const int Lmax = e == cudaSuccess ? (int) misc[0] : 0;
+  auto finish = [&]() {                                       // scratch frees, ordered after all use
+    cudaStreamWaitEvent(st, ev_raw, 0);
+    for (void *q : scratch) cudaFreeAsync(q, st);
+    scratch.clear();
+    cudaEventDestroy(ev_raw);
   };
-  par([&](int t) {
-    auto [lo, hi] = range(t);
-    int m = 0, bad = 0;
-    for (int64_t i = lo; i < hi; ++i) {
-      const int64_t L = off[i + 1] - off[i];
-      if (L < 0 || L > (int64_t) 100000000) bad = 1; else if (L > m) m = (int) L;
-    }
-    lmax_t[t] = m; bad_t[t] = bad;
-  });
-  int Lmax = 0;
-  for (int t = 0; t < T; ++t) {
-    if (bad_t[t]) { cudaFreeAsync(d_raw, st); cudaStreamSynchronize(st); return fail(MSVGB_eslEINVAL, "bad sequence offsets"); }
-    Lmax = std::max(Lmax, lmax_t[t]);
+  if (e != cudaSuccess || bad_len) {
+    finish();
+    cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return fail(MSVGB_eslESYS, std::string("database upload: ") + cudaGetErrorString(e));
+    return fail(MSVGB_eslEINVAL, "bad sequence offsets");
   }
-  // stable counting sort by descending length: per-thread counts, then each
-  // thread's first slot for each length (lengths are ranked first when they
-  // are too large for a direct table)
-  std::vector<int32_t> rank_of;                  // length -> dense rank, only for huge Lmax
-  int R = Lmax;
-  if (Lmax > (1 << 20)) {
-    std::vector<int32_t> ls(n);
-    for (int64_t i = 0; i < n; ++i) ls[i] = (int32_t) (off[i + 1] - off[i]);
-    std::sort(ls.begin(), ls.end());
-    ls.erase(std::unique(ls.begin(), ls.end()), ls.end());
-    rank_of = std::move(ls);                     // sorted distinct lengths
-    R = (int) rank_of.size() - 1;
-  }
-  auto key = [&](int64_t L) -> int64_t {
-    if (rank_of.empty()) return L;
-    return std::lower_bound(rank_of.begin(), rank_of.end(), (int32_t) L) - rank_of.begin();
-  };
-  std::vector<std::vector<int64_t>> cnt(T, std::vector<int64_t>(R + 1, 0));
-  par([&](int t) {
-    auto [lo, hi] = range(t);
-    int64_t *c = cnt[t].data();
-    for (int64_t i = lo; i < hi; ++i) c[key(off[i + 1] - off[i])]++;
-  });
-  std::vector<int32_t> distinct;
-  {
-    int64_t acc = 0;
-    for (int k = R; k >= 0; --k) {
-      int64_t tot = 0;
-      for (int t = 0; t < T; ++t) { const int64_t c = cnt[t][k]; cnt[t][k] = acc + tot; tot += c; }
-      acc += tot;
-      if (tot) distinct.push_back(rank_of.empty() ? k : rank_of[k]);
-    }
-    std::reverse(distinct.begin(), distinct.end());
-  }
-  pt.mark("length scan + histograms");
-  // metadata in pinned staging: start, orig, src (int64) and len (int32) per sorted slot
-  const size_t need = (size_t) std::max<int64_t>(n, 1) * (3 * 8 + 4);
-  if (ctx->h_stage_cap < need) {
-    cudaStreamSynchronize(st);                          // the old staging may still feed a copy
-    if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
-    ctx->h_stage = nullptr; ctx->h_stage_cap = 0;
-    cudaError_t e = cudaMallocHost(&ctx->h_stage, need);
-    if (e != cudaSuccess) { cudaFreeAsync(d_raw, st); return fail(MSVGB_eslEMEM, cudaGetErrorString(e)); }
-    ctx->h_stage_cap = need;
-  }
-  int64_t *h_start = (int64_t *) ctx->h_stage, *h_orig = h_start + n, *h_src = h_orig + n;
-  int32_t *h_len = (int32_t *) (h_src + n);
-  par([&](int t) {
-    auto [lo, hi] = range(t);
-    int64_t *slot = cnt[t].data();
-    for (int64_t i = lo; i < hi; ++i) {
-      const int64_t L = off[i + 1] - off[i], s = slot[key(L)]++;
-      h_orig[s] = i; h_len[s] = (int32_t) L; h_src[s] = off[i] - off[0];
-    }
-  });
-  // padded start offsets: per-thread partial sums, then an exclusive scan
-  std::vector<int64_t> part(T + 1, 0);
-  par([&](int t) {
-    auto [lo, hi] = range(t);
-    int64_t sum = 0;
-    for (int64_t s = lo; s < hi; ++s) sum += ((int64_t) h_len[s] + 15) / 16 * 16;
-    part[t + 1] = sum;
-  });
-  for (int t = 0; t < T; ++t) part[t + 1] += part[t];
-  par([&](int t) {
-    auto [lo, hi] = range(t);
-    int64_t pos = part[t];
-    for (int64_t s = lo; s < hi; ++s) { h_start[s] = pos; pos += ((int64_t) h_len[s] + 15) / 16 * 16; }
-  });
-  const int64_t pos = part[T];
-  pt.mark("placement + offsets");
-  const int64_t bytes = pos + 64;                 // tail so a 16-byte over-read stays inside
 
   msvgb_db *db = new msvgb_db();
   db->ctx = ctx; db->device = ctx->device; db->n = n; db->residues = total; db->Lmax = Lmax;
   db->serial = g_db_serial.fetch_add(1);
-  db->packed_bytes = bytes;
-  db->distinct_len = std::move(distinct);
-  db->n_long = std::partition_point(h_len, h_len + n, [](int32_t L) { return L >= kLongTarget; }) - h_len;
+  const bool gpu_sort = Lmax <= (1 << 22);
+  const size_t nb = (size_t) Lmax + 1;
+  // packed size: exact after a host sort, an upper bound before the device scan
+  int64_t pos = 0;
+  const int64_t bound = gpu_sort ? total + 15 * n : 0;
+  // The database's own arrays come from the pool too: cudaMalloc would wait for
+  // kernels still running (a search of an earlier chunk). msvgb_db_destroy's
+  // cudaFree synchronizes before it frees them.
+  auto keep = [&](void **ptr, size_t bytes) {
+    return cudaMallocFromPoolAsync(ptr, std::max<size_t>(bytes, 16), pool, st);
+  };
   int64_t *d_src = nullptr;
-  int bad = 0;
-  cudaError_t e = cudaMalloc(&db->d_codes, bytes);
-  if (e == cudaSuccess) e = cudaMalloc(&db->d_start, std::max<int64_t>(n, 1) * 8);
-  if (e == cudaSuccess) e = cudaMalloc(&db->d_orig, std::max<int64_t>(n, 1) * 8);
-  if (e == cudaSuccess) e = cudaMalloc(&db->d_len, std::max<int64_t>(n, 1) * 4);
-  if (e == cudaSuccess) e = cudaMallocAsync((void **) &d_src, std::max<int64_t>(n, 1) * 8, st);
-  pt.mark("device allocations");
-  if (e == cudaSuccess && n) e = cudaMemcpyAsync(db->d_start, h_start, n * 8, cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess && n) e = cudaMemcpyAsync(db->d_orig, h_orig, n * 8, cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess && n) e = cudaMemcpyAsync(d_src, h_src, n * 8, cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess && n) e = cudaMemcpyAsync(db->d_len, h_len, n * 4, cudaMemcpyHostToDevice, st);
-  if (trace_on() && e == cudaSuccess) { e = cudaStreamSynchronize(st); pt.mark("uploads (rest of raw + metadata)"); }
-  if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_bad, 0, sizeof(int), st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(db->d_codes + pos, PAD_CODE, 64, st);
-  if (e == cudaSuccess) e = launch_pack(d_raw, d_src, db->d_start, db->d_len, n, db->d_codes, ctx->d_bad,
+  e = alloc((void **) &d_src, (size_t) n1 * 8, st);
+  if (e == cudaSuccess) e = keep((void **) &db->d_start, (size_t) n1 * 8);
+  if (e == cudaSuccess) e = keep((void **) &db->d_orig, (size_t) n1 * 8);
+  if (e == cudaSuccess) e = keep((void **) &db->d_len, (size_t) n1 * 4);
+  unsigned long long *d_hist = nullptr;
+  if (e == cudaSuccess && gpu_sort) {
+    int64_t *d_bins = nullptr;                                // [0, Lmax] first slot, then first byte
+    e = keep((void **) &db->d_codes, bound + 64);
+    if (e == cudaSuccess) e = alloc((void **) &d_hist, nb * 8, st);
+    if (e == cudaSuccess) e = alloc((void **) &d_bins, 2 * nb * 8, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_hist, 0, nb * 8, st);
+    if (e == cudaSuccess) e = launch_histogram(d_len_in, n, d_hist, ctx->num_sms, st);
+    if (e == cudaSuccess) e = launch_bins(d_hist, Lmax, d_bins, d_bins + nb, d_scal + 1, db->d_codes, st);
+    unsigned long long *cursor = nullptr;
+    if (e == cudaSuccess) e = alloc((void **) &cursor, nb * 8, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(cursor, d_bins, nb * 8, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = launch_place(d_off, d_len_in, n, cursor, d_bins, d_bins + nb, db->d_start,
+                                           db->d_orig, db->d_len, d_src, ctx->num_sms, st);
+    pt.mark("sort enqueued");
+  } else if (e == cudaSuccess) {
+    // host fallback for very long sequences: stable sort by descending length
+    std::vector<int64_t> idx(n);
+    for (int64_t i = 0; i < n; ++i) idx[i] = i;
+    std::stable_sort(idx.begin(), idx.end(),
+                     [&](int64_t x, int64_t y) { return off[x + 1] - off[x] > off[y + 1] - off[y]; });
+    std::vector<int64_t> h_start(n), h_orig(n), h_src(n);
+    std::vector<int32_t> h_len(n);
+    for (int64_t s = 0; s < n; ++s) {
+      const int64_t i = idx[s], L = off[i + 1] - off[i];
+      h_orig[s] = i; h_len[s] = (int32_t) L; h_src[s] = off[i] - off[0]; h_start[s] = pos;
+      pos += (L + 15) / 16 * 16;
+      if (L >= kLongTarget) db->n_long++;
+      if (s == 0 || h_len[s - 1] != L) db->distinct_len.push_back((int32_t) L);
+    }
+    std::reverse(db->distinct_len.begin(), db->distinct_len.end());
+    e = keep((void **) &db->d_codes, pos + 64);
+    if (e == cudaSuccess) e = cudaMemsetAsync(db->d_codes + pos, PAD_CODE, 64, st);
+    if (e == cudaSuccess && n) e = cudaMemcpyAsync(db->d_start, h_start.data(), n * 8, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && n) e = cudaMemcpyAsync(db->d_orig, h_orig.data(), n * 8, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && n) e = cudaMemcpyAsync(d_src, h_src.data(), n * 8, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && n) e = cudaMemcpyAsync(db->d_len, h_len.data(), n * 4, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);      // the vectors above feed the copies
+    pt.mark("host sort");
+  }
+  // scatter the residues once they are up; then the counts and flags come back
+  if (e == cudaSuccess && ctx->h_pin_cap < 16 + nb * 8) e = grow_pinned(ctx, 16 + nb * 8);
+  int *d_bad = a ? a->d_bad : ctx->d_bad;
+  int64_t *h_scal = (int64_t *) ctx->h_pin;                   // [0] bad flag, [1] packed size, then counts
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev_raw, 0);
+  if (trace_on() && e == cudaSuccess) { e = cudaStreamSynchronize(st); pt.mark("residues up"); }
+  if (e == cudaSuccess && !a) e = cudaMemsetAsync(d_bad, 0, sizeof(int), st);
+  if (e == cudaSuccess) e = launch_pack(d_raw, d_src, db->d_start, db->d_len, n, db->d_codes, d_bad,
                                         ctx->num_sms, st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, ctx->d_bad, sizeof(int), cudaMemcpyDeviceToHost, st);
-  cudaFreeAsync(d_raw, st);
-  if (d_src) cudaFreeAsync(d_src, st);
+  if (e == cudaSuccess) { h_scal[0] = 0; h_scal[1] = pos; }
+  if (e == cudaSuccess && !a) e = cudaMemcpyAsync(h_scal, d_bad, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && gpu_sort) e = cudaMemcpyAsync(h_scal + 1, d_scal + 1, 8, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && gpu_sort) e = cudaMemcpyAsync(h_scal + 2, d_hist, nb * 8, cudaMemcpyDeviceToHost, st);
+  finish();
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  pt.mark("pack kernel + frees");
+  pt.mark("pack");
+  if (e == cudaSuccess && gpu_sort) {
+    pos = h_scal[1];
+    const unsigned long long *hist = (const unsigned long long *) (h_scal + 2);
+    for (int L = 0; L <= Lmax; ++L)
+      if (hist[L]) {
+        db->distinct_len.push_back(L);
+        if (L >= kLongTarget) db->n_long += (int64_t) hist[L];
+      }
+  }
+  db->packed_bytes = pos + 64;
+  if (e == cudaSuccess && a) e = cudaEventCreateWithFlags(&db->ready, cudaEventDisableTiming);
+  if (e == cudaSuccess && a) e = cudaEventRecord(db->ready, st);
   if (e == cudaSuccess && n) count_launch();
   if (e != cudaSuccess) {
     cudaStreamSynchronize(st);
+    cudaStreamSynchronize(ctx->dma);
     msvgb_db_destroy(db);
     return fail(e == cudaErrorMemoryAllocation ? MSVGB_eslEMEM : MSVGB_eslESYS,
                 std::string("database upload: ") + cudaGetErrorString(e));
   }
-  if (bad) {
+  if (!a && h_scal[0]) {
     msvgb_db_destroy(db);
     return fail(MSVGB_eslEINVAL, "residue code >= 29 (Kp)");
   }
@@ -664,6 +717,7 @@ extern "C" int msvgb_db_destroy(msvgb_db *db) {
   if (!db) return MSVGB_eslOK;
   cudaSetDevice(db->device);
   cudaFree(db->d_codes); cudaFree(db->d_start); cudaFree(db->d_orig); cudaFree(db->d_len);
+  if (db->ready) cudaEventDestroy(db->ready);
   delete db;
   return MSVGB_eslOK;
 }
@@ -697,6 +751,7 @@ extern "C" int msvgb_search_device(msvgb_ctx *c, const msvgb_profile *pc, const 
   LenTables *t = nullptr;
   int st = ensure_tables(p, db, F1, &t);
   if (st != MSVGB_eslOK) return st;
+  if (db->ready) CUDA_TRY(cudaStreamWaitEvent(c->stream, db->ready, 0));   // still being packed
   DbDev dbv{db->d_codes, db->d_start, db->d_len, db->d_orig, db->n};
   if (p->G == 32 || !p->d_stab_g)
     return launch_one(c, p, dbv, t->d_tjb, t->d_xjmin, (uint8_t *) d_xj, (uint8_t *) d_flags);
@@ -764,6 +819,69 @@ extern "C" int msvgb_search(msvgb_ctx *c, const msvgb_profile *p, const msvgb_db
   }
   cudaFreeAsync(d, c->stream);
   if (st == MSVGB_eslOK) CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return st;
+}
+
+// End to end from host buffers. The sequences are cut into chunks by residue
+// count (a quarter of chunk_residues first, doubling up to chunk_residues, so
+// the GPU starts early); while the GPU searches chunk k on the context's
+// stream, the host sorts chunk k+1 and its residues go up and are packed on
+// the upload stream. Results of all chunks land in one device buffer and come
+// back in one copy at the end.
+extern "C" int msvgb_search_host(msvgb_ctx *c, const msvgb_profile *p, const uint8_t *codes, const int64_t *off,
+                                 int64_t n, double F1, int64_t chunk_residues, uint8_t *out_xj,
+                                 uint8_t *out_flags) {
+  if (!c || !p || n < 0 || (n && (!codes || !off || !out_xj || !out_flags)))
+    return fail(MSVGB_eslEINVAL, "NULL argument");
+  if (n == 0) return MSVGB_eslOK;
+  CUDA_TRY(cudaSetDevice(c->device));
+  // chunk boundaries [cut[k], cut[k+1]): by default a quarter of the residues,
+  // then the rest (whose upload hides under the first search; every further
+  // chunk would add a launch tail); with chunk_residues, chunks growing from
+  // a quarter of it to it
+  std::vector<int64_t> cut(1, 0);
+  const int64_t total = off[n] - off[0];
+  for (int64_t want = chunk_residues > 0 ? std::max<int64_t>(1, chunk_residues / 4) : total / 4 + 1, b0 = 0; b0 < n;) {
+    int64_t b1 = b0 + 1;
+    while (b1 < n && off[b1] - off[b0] < want) ++b1;
+    cut.push_back(b1);
+    b0 = b1;
+    want = chunk_residues > 0 ? std::min(chunk_residues, 2 * want) : total;
+  }
+  uint8_t *d = nullptr;
+  CUDA_TRY(cudaMallocAsync((void **) &d, 2 * (size_t) n + 64, c->stream));
+  int *d_bad = (int *) (d + ((2 * (size_t) n + 15) / 16) * 16);
+  CUDA_TRY(cudaMemsetAsync(d_bad, 0, sizeof(int), c->stream));
+  CUDA_TRY(cudaEventRecord(c->ev_fork, c->stream));
+  CUDA_TRY(cudaStreamWaitEvent(c->upload, c->ev_fork, 0));     // the flag is zero before any pack
+  std::vector<msvgb_db *> dbs;
+  int st = MSVGB_eslOK;
+  PhaseTimer pt;
+  for (size_t k = 0; k + 1 < cut.size() && st == MSVGB_eslOK; ++k) {
+    const int64_t b0 = cut[k], b1 = cut[k + 1];
+    msvgb_db *db = nullptr;
+    const AsyncPack a{d_bad};
+    st = db_create_on(c, codes, off + b0, b1 - b0, c->upload, &db, &a);
+    pt.mark("search_host: chunk enqueued");
+    if (st == MSVGB_eslOK) {
+      dbs.push_back(db);
+      st = msvgb_search_device(c, p, db, F1, d + b0, d + n + b0);
+    }
+  }
+  int bad = 0;
+  if (st == MSVGB_eslOK) {
+    cudaError_t e = cudaMemcpyAsync(out_xj, d, n, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out_flags, d + n, n, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+    if (e != cudaSuccess) st = fail(MSVGB_eslESYS, std::string("search: ") + cudaGetErrorString(e));
+  }
+  cudaStreamSynchronize(c->upload);
+  cudaFreeAsync(d, c->stream);
+  const cudaError_t e = cudaStreamSynchronize(c->stream);
+  pt.mark("search_host: last search done");
+  for (auto *db : dbs) msvgb_db_destroy(db);
+  if (st == MSVGB_eslOK && e != cudaSuccess) st = fail(MSVGB_eslESYS, std::string("search: ") + cudaGetErrorString(e));
+  if (st == MSVGB_eslOK && bad) st = fail(MSVGB_eslEINVAL, "residue code >= 29 (Kp)");
   return st;
 }
 

@@ -32,8 +32,10 @@ struct msvgb_ctx {
   int64_t *d_list = nullptr; size_t list_cap = 0;       // G-lane search: sequences left for the full MSV
   unsigned long long *d_aux = nullptr;                  // [0] second ticket, [1] list count, [2] third ticket
   cudaStream_t side = nullptr;                          // long targets of the lane-group search
+  cudaStream_t upload = nullptr;                        // chunk uploads of msvgb_search_host
+  cudaStream_t dma = nullptr;                           // raw residue copies of database creation
+  void *h_pin = nullptr; size_t h_pin_cap = 0;          // small pinned scratch (length counts, flags)
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-  void *h_stage = nullptr; size_t h_stage_cap = 0;      // pinned staging for database metadata
   TuneTable *tune = nullptr;                            // lane counts measured by msvgb_autotune
   std::mutex tune_mu;
 };
@@ -78,6 +80,7 @@ struct msvgb_db {
   uint64_t serial = 0;
   int64_t n_long = 0;                 // sequences of length >= kLongTarget (they sort first)
   int64_t packed_bytes = 0;           // size of d_codes
+  cudaEvent_t ready = nullptr;        // set when packed asynchronously: completes when the data is in place
 };
 
 // Targets this long are scored with 32 lanes per sequence even when the
@@ -119,6 +122,13 @@ void tune_free(msvgb_ctx *c);
 // where the model length allows it (0: the context's choice).
 int batch_create(msvgb_ctx *ctx, const msvgb_om *const *oms, int nprof, const msvgb_db *db, double F1,
                  void *d_xj, void *d_flags, int force_lanes, msvgb_batch **ret);
+// Asynchronous packing of one chunk (db_create_on).
+struct AsyncPack {
+  int *d_bad;      // device flag: set if a residue code is >= 29
+};
+// msvgb_db_create on stream st; with a, asynchronous (see msv_api.cu).
+int db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64_t *off, int64_t n, cudaStream_t st,
+                 msvgb_db **ret, const AsyncPack *a = nullptr);
 // A fresh database serial (keys the per-length table caches).
 uint64_t next_db_serial();
 // Adds one to the count msvgb_kernel_launches() reports.
@@ -127,4 +137,19 @@ void count_launch();
 // *bad to nonzero if any code is >= 29.
 cudaError_t launch_pack(const uint8_t *raw, const int64_t *src, const int64_t *start, const int32_t *len,
                         int64_t n, uint8_t *packed, int *bad, int num_sms, cudaStream_t stream);
+// Device-side length sort (msv_pack.cu): lengths, their maximum and a
+// validity flag; per-length counts; sorted placement.
+cudaError_t launch_lengths(const int64_t *off, int64_t n, int32_t *len, unsigned *lmax, int *bad, int num_sms,
+                           cudaStream_t stream);
+cudaError_t launch_histogram(const int32_t *len, int64_t n, unsigned long long *hist, int num_sms,
+                             cudaStream_t stream);
+cudaError_t launch_bins(const unsigned long long *hist, int Lmax, int64_t *bin_slot, int64_t *bin_byte, int64_t *pos,
+                        uint8_t *codes, cudaStream_t stream);
+// Stream-ordered scratch allocations of database creation come from this
+// pool, which keeps up to 4 GiB mapped between calls (the default pool would
+// unmap and map again every time).
+cudaMemPool_t scratch_pool(int device);
+cudaError_t launch_place(const int64_t *off, const int32_t *len_in, int64_t n, unsigned long long *cursor,
+                         const int64_t *bin_slot, const int64_t *bin_byte, int64_t *start, int64_t *orig,
+                         int32_t *len, int64_t *src, int num_sms, cudaStream_t stream);
 }  // namespace msvgb_detail

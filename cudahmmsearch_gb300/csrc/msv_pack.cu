@@ -1,9 +1,15 @@
 // msv_pack.cu -- device-side database packing.
 //
 // The GB300 replacement of the fork's host packing loops (loadDBQuad,
-// code/src/GPUFunction.cu:219-255): the raw residues arrive in one DMA and a
-// kernel scatters them into the length-sorted, 16-byte-padded layout the
-// search kernels read, checking every code on the way.
+// code/src/GPUFunction.cu:219-255) and of its offline length sort (dbsort):
+// the raw residues arrive in one DMA; kernels compute the lengths, count them
+// per length, place every sequence in descending-length order (its slot and
+// 16-byte-aligned start follow from the per-length counts, which the host
+// scans) and scatter the residues into the padded layout the search kernels
+// read, checking every code on the way. Sequences of equal length may land in
+// any order among themselves: each result is written to its original index.
+#include <algorithm>
+
 #include <cuda_runtime.h>
 
 #include "msv_internal.h"
@@ -34,7 +40,145 @@ pack_kernel(const uint8_t *__restrict__ raw, const int64_t *__restrict__ src, co
   if (__any_sync(0xffffffffu, badl) && lane == 0) atomicOr(bad, 1);
 }
 
+constexpr int64_t kMaxLen = 100000000;
+
+// len[i] = off[i+1] - off[i]; the maximum into *lmax; *bad = 1 for a negative
+// or absurd length (then len[i] = 0).
+__global__ void __launch_bounds__(256)
+len_kernel(const int64_t *__restrict__ off, int64_t n, int32_t *__restrict__ len, unsigned *lmax, int *bad) {
+  unsigned m = 0;
+  int b = 0;
+  for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t) gridDim.x * blockDim.x) {
+    int64_t L = off[i + 1] - off[i];
+    if (L < 0 || L > kMaxLen) { b = 1; L = 0; }
+    len[i] = (int32_t) L;
+    m = max(m, (unsigned) L);
+  }
+  m = __reduce_max_sync(0xffffffffu, m);
+  if ((threadIdx.x & 31) == 0) atomicMax(lmax, m);
+  if (__any_sync(0xffffffffu, b) && (threadIdx.x & 31) == 0) atomicOr(bad, 1);
+}
+
+// hist[L] = number of sequences of length L (warp-aggregated atomics).
+__global__ void __launch_bounds__(256)
+hist_kernel(const int32_t *__restrict__ len, int64_t n, unsigned long long *__restrict__ hist) {
+  const int64_t stride = (int64_t) gridDim.x * blockDim.x;
+  for (int64_t i0 = (int64_t) blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
+    const int64_t i = i0 + threadIdx.x;
+    const bool in = i < n;
+    const unsigned act = __ballot_sync(0xffffffffu, in);
+    if (!in) continue;
+    const int L = len[i];
+    const unsigned peers = __match_any_sync(act, L);
+    if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&hist[L], (unsigned long long) __popc(peers));
+  }
+}
+
+// Sorted slot of every sequence: the next free slot of its length
+// (cursor[L] starts at the first slot of length L); its padded start follows
+// from the slot's rank within the length.
+__global__ void __launch_bounds__(256)
+place_kernel(const int64_t *__restrict__ off, const int32_t *__restrict__ len_in, int64_t n,
+             unsigned long long *__restrict__ cursor, const int64_t *__restrict__ bin_slot,
+             const int64_t *__restrict__ bin_byte, int64_t *__restrict__ start, int64_t *__restrict__ orig,
+             int32_t *__restrict__ len, int64_t *__restrict__ src) {
+  const int64_t stride = (int64_t) gridDim.x * blockDim.x;
+  for (int64_t i0 = (int64_t) blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
+    const int64_t i = i0 + threadIdx.x;
+    const bool in = i < n;
+    const unsigned act = __ballot_sync(0xffffffffu, in);
+    if (!in) continue;
+    const int L = len_in[i];
+    const unsigned peers = __match_any_sync(act, L);
+    const int leader = __ffs(peers) - 1, lane = threadIdx.x & 31;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(&cursor[L], (unsigned long long) __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    const int64_t s = (int64_t) base + __popc(peers & ((1u << lane) - 1u));
+    const int64_t padded = ((int64_t) L + 15) / 16 * 16;
+    start[s] = bin_byte[L] + (s - bin_slot[L]) * padded;
+    orig[s] = i;
+    len[s] = L;
+    src[s] = off[i] - off[0];
+  }
+}
+
+// Descending-length exclusive scans of the per-length counts: the first
+// sorted slot and first packed byte of every length, the packed size *pos,
+// and the padding tail after it in the packed buffer. One block of 1024.
+__global__ void __launch_bounds__(1024)
+bins_kernel(const unsigned long long *__restrict__ hist, int Lmax, int64_t *__restrict__ bin_slot,
+            int64_t *__restrict__ bin_byte, int64_t *__restrict__ pos_out, uint8_t *__restrict__ codes) {
+  __shared__ int64_t s_cnt[1024], s_byt[1024];
+  const int T = blockDim.x, t = threadIdx.x;
+  const int nb = Lmax + 1, per = (nb + T - 1) / T;
+  const int r0 = min(nb, t * per), r1 = min(nb, (t + 1) * per);   // descending ranks: L = Lmax - r
+  int64_t c = 0, b = 0;
+  for (int r = r0; r < r1; ++r) {
+    const int L = Lmax - r;
+    c += (int64_t) hist[L];
+    b += (int64_t) hist[L] * (((int64_t) L + 15) / 16 * 16);
+  }
+  s_cnt[t] = c; s_byt[t] = b;
+  __syncthreads();
+  for (int d = 1; d < T; d <<= 1) {                 // inclusive scan
+    const int64_t vc = t >= d ? s_cnt[t - d] : 0, vb = t >= d ? s_byt[t - d] : 0;
+    __syncthreads();
+    s_cnt[t] += vc; s_byt[t] += vb;
+    __syncthreads();
+  }
+  int64_t slot = t ? s_cnt[t - 1] : 0, byte = t ? s_byt[t - 1] : 0;
+  for (int r = r0; r < r1; ++r) {
+    const int L = Lmax - r;
+    bin_slot[L] = slot; bin_byte[L] = byte;
+    slot += (int64_t) hist[L];
+    byte += (int64_t) hist[L] * (((int64_t) L + 15) / 16 * 16);
+  }
+  const int64_t pos = s_byt[T - 1];
+  if (t == 0) *pos_out = pos;
+  if (t < 64) codes[pos + t] = (uint8_t) msvgb::PAD_CODE;
+}
+
+int grid_for(int64_t n, int num_sms) {
+  const long long blocks = std::min<long long>((n + 255) / 256, (long long) num_sms * 8);
+  return (int) std::max<long long>(1, blocks);
+}
+
 }  // namespace
+
+cudaError_t msvgb_detail::launch_lengths(const int64_t *off, int64_t n, int32_t *len, unsigned *lmax, int *bad,
+                                         int num_sms, cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  (void) cudaGetLastError();
+  len_kernel<<<grid_for(n, num_sms), 256, 0, stream>>>(off, n, len, lmax, bad);
+  return cudaGetLastError();
+}
+
+cudaError_t msvgb_detail::launch_histogram(const int32_t *len, int64_t n, unsigned long long *hist, int num_sms,
+                                           cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  (void) cudaGetLastError();
+  hist_kernel<<<grid_for(n, num_sms), 256, 0, stream>>>(len, n, hist);
+  return cudaGetLastError();
+}
+
+cudaError_t msvgb_detail::launch_bins(const unsigned long long *hist, int Lmax, int64_t *bin_slot, int64_t *bin_byte,
+                                      int64_t *pos, uint8_t *codes, cudaStream_t stream) {
+  (void) cudaGetLastError();
+  bins_kernel<<<1, 1024, 0, stream>>>(hist, Lmax, bin_slot, bin_byte, pos, codes);
+  return cudaGetLastError();
+}
+
+cudaError_t msvgb_detail::launch_place(const int64_t *off, const int32_t *len_in, int64_t n,
+                                       unsigned long long *cursor, const int64_t *bin_slot, const int64_t *bin_byte,
+                                       int64_t *start, int64_t *orig, int32_t *len, int64_t *src, int num_sms,
+                                       cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  (void) cudaGetLastError();
+  place_kernel<<<grid_for(n, num_sms), 256, 0, stream>>>(off, len_in, n, cursor, bin_slot, bin_byte, start, orig,
+                                                         len, src);
+  return cudaGetLastError();
+}
 
 cudaError_t msvgb_detail::launch_pack(const uint8_t *raw, const int64_t *src, const int64_t *start,
                                       const int32_t *len, int64_t n, uint8_t *packed, int *bad,

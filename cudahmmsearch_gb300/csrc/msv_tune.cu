@@ -47,12 +47,13 @@ constexpr Cand kCand[] = {{32, 1}, {32, 0}, {16, 1}, {8, 1}};
 constexpr int kNC = sizeof(kCand) / sizeof(kCand[0]);
 constexpr int kNV = kNB + 1;                                // values per candidate: bins, then the mix
 
-// The rule used without a measured table (from measurements on GB300): 8
-// lanes up to M = 479; above, 16 lanes for short targets in the batched
-// kernel, else 32.
+// The rule used without a measured table (from the tuner's measurements on
+// GB300): 8 lanes up to M = 479; up to M = 1023, 16 lanes for the length mix
+// and for targets shorter than 600 in the batched kernel, 32 for longer ones;
+// 32 above.
 int default_lanes(int M, int lbin) {
   if (M >= 16 && M < 480) return 8;
-  if (M >= 32 && M < 1024 && lbin == 0) return 16;
+  if (M >= 32 && M < 1024 && lbin <= 1) return 16;
   return 32;
 }
 

@@ -124,8 +124,8 @@ int msvgb_profile_lanes(const msvgb_profile *prof);
  * lognormal length mix (timed on the single-query path) in the context.
  * Afterwards msvgb_profile_create, msvgb_batch_create and the server take
  * their lane counts from it; before, a fixed rule applies (8 lanes for
- * 16 <= M < 480; 16 for M < 1024 on targets shorter than 150 in the batched
- * kernel; else 32). */
+ * 16 <= M < 480; for M < 1024, 16 on the length mix and on targets shorter
+ * than 600 in the batched kernel; else 32). */
 int msvgb_autotune(msvgb_ctx *ctx, double budget_s);
 /* Text form of the context's table (device name and SM count in the header). */
 int msvgb_tune_save(msvgb_ctx *ctx, const char *path);
@@ -202,6 +202,15 @@ int msvgb_search(msvgb_ctx *ctx, const msvgb_profile *prof, const msvgb_db *db, 
  * pointers), asynchronous on the context's stream. */
 int msvgb_search_device(msvgb_ctx *ctx, const msvgb_profile *prof, const msvgb_db *db, double F1,
                         void *d_xj, void *d_flags);
+
+/* End to end from host buffers, for a database that is not kept resident:
+ * sequences codes[off[i] .. off[i+1]) (as msvgb_db_create takes them) are
+ * uploaded and packed in chunks while earlier chunks are searched (by default
+ * a quarter of the residues, then the rest; with chunk_residues > 0, chunks
+ * growing to that size); results as msvgb_search. The batched pre-pass the fork's p7_PipelineShort consumed
+ * (src/p7_pipeline.c:887-929), with the upload hidden behind the search. */
+int msvgb_search_host(msvgb_ctx *ctx, const msvgb_profile *prof, const uint8_t *codes, const int64_t *off,
+                      int64_t n, double F1, int64_t chunk_residues, uint8_t *out_xj, uint8_t *out_flags);
 
 /* ---- profile preparation ----------------------------------------------------------
  * Sample a random profile HMM of M nodes exactly as HMMER's p7_hmm_Sample does

@@ -194,3 +194,21 @@ def test_profile_reused_across_databases_at_the_same_address(ctx):
         o = O.msv_batch(p, s)
         check_against_oracle(p, s, xj, fl, o)
         db.close()
+
+
+@pytest.mark.parametrize("chunk", [0, 1000, 60000])
+def test_search_host_equals_resident_search(ctx, chunk):
+    """msvgb_search_host (chunked upload and packing under the search) gives
+    the resident path's results for any chunking, lane count and length mix."""
+    p, _, _ = load_case("m400_s1")
+    s = F.SeqSet.concat([F.synth_sequences(3000, seed=5, lmax=9000), F.emit_homologs(p, 50, seed=6),
+                         F.SeqSet.from_list([np.zeros(0, np.uint8), np.array([7], np.uint8)])])
+    o = O.msv_batch(p, s)
+    for variant in (None, 1):
+        dp = api.DeviceProfile(ctx, p, variant)
+        a = api.search(ctx, dp, api.DeviceDB(ctx, s))
+        b = api.search_host(ctx, dp, s, chunk_residues=chunk)
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+        check_against_oracle(p, s, b[0], b[1], o)
+    e = api.search_host(ctx, api.DeviceProfile(ctx, p), F.SeqSet.from_list([]))
+    assert e[0].size == 0 and e[1].size == 0
