@@ -340,6 +340,7 @@ extern "C" int msvgb_profile_create(msvgb_ctx *ctx, const msvgb_om *om, msvgb_pr
     st = msvgb_profile_set_lanes(*ret, om, G);
     if (st != MSVGB_eslOK) { msvgb_profile_destroy(*ret); *ret = nullptr; }
   }
+  if (st == MSVGB_eslOK) (*ret)->lanes_auto = true;
   return st;
 }
 
@@ -398,6 +399,7 @@ std::vector<uint32_t> msvgb_detail::build_group_table(const msvgb_om *om, int C,
 extern "C" int msvgb_profile_set_lanes(msvgb_profile *p, const msvgb_om *om, int G) {
   if (!p || !om) return fail(MSVGB_eslEINVAL, "NULL argument");
   if (om->M != p->M) return fail(MSVGB_eslEINVAL, "om does not match the profile");
+  p->lanes_auto = false;                                  // set by the caller: applies at any size
   if (G == 32) { p->G = 32; return MSVGB_eslOK; }
   if (G != 16 && G != 8) return fail(MSVGB_eslEINVAL, "lanes per sequence must be 32, 16 or 8");
   const int C = p->M / (2 * G) + 1;                       // 2*C*G > M: the last node is padding
@@ -753,7 +755,11 @@ extern "C" int msvgb_search_device(msvgb_ctx *c, const msvgb_profile *pc, const 
   if (st != MSVGB_eslOK) return st;
   if (db->ready) CUDA_TRY(cudaStreamWaitEvent(c->stream, db->ready, 0));   // still being packed
   DbDev dbv{db->d_codes, db->d_start, db->d_len, db->d_orig, db->n};
-  if (p->G == 32 || !p->d_stab_g)
+  // Lane groups lengthen each sequence's latency (2-4x): below ~40 G cells the
+  // launch tail they add outweighs their throughput, unless lanes were set
+  // explicitly.
+  const bool small = p->lanes_auto && (double) p->M * (double) db->residues < 4e10;
+  if (p->G == 32 || !p->d_stab_g || small)
     return launch_one(c, p, dbv, t->d_tjb, t->d_xjmin, (uint8_t *) d_xj, (uint8_t *) d_flags);
   // Long targets (they sort first) on the 32-lane kernel in a side stream;
   // the rest: the G-lane SSV pass, then the full MSV on the sequences it left

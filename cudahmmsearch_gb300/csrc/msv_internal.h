@@ -62,6 +62,7 @@ struct msvgb_profile {
   float scale = 0.f, mmu = 0.f, mlambda = 0.f;
   uint32_t *d_stab = nullptr, *d_mtab = nullptr;
   int G = 32;                         // lanes per sequence in the SSV pass (32: fused kernel)
+  bool lanes_auto = false;            // G chosen by msvgb_profile_create (small searches then use 32)
   int Cg = 0;                         // DP words per lane of the G-lane table
   uint32_t *d_stab_g = nullptr;       // f16 SSV table in the G-lane layout
   std::vector<LenTables *> tables;    // one per F1 value used

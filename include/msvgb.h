@@ -110,7 +110,10 @@ int msvgb_profile_variant(const msvgb_profile *prof);
  * MSV in a second launch, and targets of 2400 residues or more run at 32
  * lanes in a concurrent launch (one long target must not set the length of
  * the search). om must be the profile's own MSV fields. Needs M < 64 * G and,
- * for G < 32, M >= 2 * G. */
+ * for G < 32, M >= 2 * G. Lanes chosen by msvgb_profile_create apply to
+ * searches of at least ~40e9 cells (M x residues); smaller ones run at 32
+ * lanes, where the shorter per-sequence latency wins; lanes set here always
+ * apply. */
 int msvgb_profile_set_lanes(msvgb_profile *prof, const msvgb_om *om, int lanes);
 int msvgb_profile_lanes(const msvgb_profile *prof);
 

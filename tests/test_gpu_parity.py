@@ -130,8 +130,11 @@ def test_model_size_corners(ctx, M):
     seqs += [np.full(50, F.CODE_X, np.uint8), np.zeros(0, np.uint8), rng.integers(0, 29, size=77).astype(np.uint8)]
     s = F.SeqSet.from_list(seqs)
     o = O.msv_batch(p, s)
-    for variant in (0, 1, None):          # None: the lane count the context picks (lane groups + long targets)
-        xj, fl = api.search(ctx, api.DeviceProfile(ctx, p, variant), api.DeviceDB(ctx, s))
+    for variant, lanes in ((0, None), (1, None), (None, None), (None, 8), (None, 16)):
+        dp = api.DeviceProfile(ctx, p, variant)
+        if lanes and 2 * lanes <= p.M < 64 * lanes:
+            dp.set_lanes(lanes)                       # lane groups, long targets at 32 lanes beside them
+        xj, fl = api.search(ctx, dp, api.DeviceDB(ctx, s))
         check_against_oracle(p, s, xj, fl, o)
 
 
@@ -148,8 +151,11 @@ def test_extreme_scalar_costs(ctx, bias, tbm, base):
     s = F.SeqSet.concat([F.synth_sequences(300, seed=bias + 7, lmax=3000),
                          F.SeqSet.from_list([rng.integers(0, 20, size=L).astype(np.uint8) for L in (1, 2, 9, 40000)])])
     o = O.msv_batch(p, s)
-    for variant in (0, 1, None):          # None: the lane count the context picks (lane groups + long targets)
-        xj, fl = api.search(ctx, api.DeviceProfile(ctx, p, variant), api.DeviceDB(ctx, s))
+    for variant, lanes in ((0, None), (1, None), (None, None), (None, 8), (None, 16)):
+        dp = api.DeviceProfile(ctx, p, variant)
+        if lanes and 2 * lanes <= p.M < 64 * lanes:
+            dp.set_lanes(lanes)                       # lane groups, long targets at 32 lanes beside them
+        xj, fl = api.search(ctx, dp, api.DeviceDB(ctx, s))
         check_against_oracle(p, s, xj, fl, o)
 
 
@@ -171,10 +177,13 @@ def test_kernel_launch_counter_advances(ctx):
     prof, db = api.DeviceProfile(ctx, p), api.DeviceDB(ctx, s)
     before = api.kernel_launches()
     api.search(ctx, prof, db)
-    # one fused launch at 32 lanes; otherwise the lane-group SSV pass and the
+    assert api.kernel_launches() == before + 1      # a small search runs fused at 32 lanes, whatever the lane choice
+    # lanes set explicitly apply at any size: the lane-group SSV pass and the
     # full-MSV pass, plus a 32-lane launch for targets of 2400 residues or more
-    want = 1 if prof.lanes == 32 else 2 + int((s.lengths >= 2400).any())
-    assert api.kernel_launches() == before + want
+    prof.set_lanes(8)
+    before = api.kernel_launches()
+    api.search(ctx, prof, db)
+    assert api.kernel_launches() == before + 2 + int((s.lengths >= 2400).any())
     prof.set_lanes(32)
     before = api.kernel_launches()
     api.search(ctx, prof, db)
@@ -204,8 +213,10 @@ def test_search_host_equals_resident_search(ctx, chunk):
     s = F.SeqSet.concat([F.synth_sequences(3000, seed=5, lmax=9000), F.emit_homologs(p, 50, seed=6),
                          F.SeqSet.from_list([np.zeros(0, np.uint8), np.array([7], np.uint8)])])
     o = O.msv_batch(p, s)
-    for variant in (None, 1):
+    for variant, lanes in ((None, None), (1, None), (None, 8)):
         dp = api.DeviceProfile(ctx, p, variant)
+        if lanes:
+            dp.set_lanes(lanes)
         a = api.search(ctx, dp, api.DeviceDB(ctx, s))
         b = api.search_host(ctx, dp, s, chunk_residues=chunk)
         assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
