@@ -102,8 +102,9 @@ uint64_t msvgb_detail::next_db_serial() { return g_db_serial.fetch_add(1); }
 // every C up to 32. int8 tables: even C (two DP words per table word).
 static const int kI8C[] = {2, 4, 6, 8, 10, 12, 14, 16, 18, 20, 22, 24, 26, 28, 30, 32, 34, 36, 40, 44, 48, 50};
 static const int kF16C[] = {1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 17, 18, 19, 20, 21, 22,
-                            23, 24, 25, 26, 27, 28, 29, 30, 31, 32, 34, 36, 38, 40};
-static const int kMaxF16C = 40;
+                            23, 24, 25, 26, 27, 28, 29, 30, 31, 32, 34, 36, 38, 40,
+                            44, 48, 52, 56, 60, 64};   // above 40: tables stay in global memory
+static const int kMaxF16C = 64;
 
 // Smallest C whose warp spans more than M nodes: node 64*C must be padding
 // (the kernels rely on it for the begin value of node 1).
@@ -126,6 +127,7 @@ cudaError_t msvgb_detail::dispatch(int C, bool f16, const LaunchArgs &a, int sms
       CASE_F16(17) CASE_F16(18) CASE_F16(19) CASE_F16(20) CASE_F16(21) CASE_F16(22) CASE_F16(23) CASE_F16(24)
       CASE_F16(25) CASE_F16(26) CASE_F16(27) CASE_F16(28) CASE_F16(29) CASE_F16(30) CASE_F16(31) CASE_F16(32)
       CASE_F16(34) CASE_F16(36) CASE_F16(38) CASE_F16(40)
+      CASE_F16(44) CASE_F16(48) CASE_F16(52) CASE_F16(56) CASE_F16(60) CASE_F16(64)
     }
   } else {
     switch (C) {
@@ -294,10 +296,11 @@ int msvgb_detail::profile_build_width(msvgb_ctx *ctx, const msvgb_om *om, int wa
   if (om->M < 1) return fail(MSVGB_eslEINVAL, "profile M must be >= 1");
   if (om->Kp != 29) return fail(MSVGB_eslEINVAL, "only the amino alphabet (Kp = 29) is supported");
   if (!om->rbv) return fail(MSVGB_eslEINVAL, "rbv is NULL");
-  const bool f16 = want_f16 && (force_C > 0 ? force_C : choose_C(om->M, true)) > 0 &&
-                   (force_C > 0 ? force_C : choose_C(om->M, true)) <= kMaxF16C;
+  // f16 when asked for and possible, and whenever the int8 layout cannot hold M
+  const int c16 = force_C > 0 ? force_C : choose_C(om->M, true);
+  const bool f16 = c16 > 0 && c16 <= kMaxF16C && (want_f16 || (force_C <= 0 && choose_C(om->M, false) < 0));
   const int C = force_C > 0 ? force_C : choose_C(om->M, f16);
-  if (C < 0) return fail(MSVGB_eslEINVAL, "profile M exceeds the supported maximum (3199 nodes)");
+  if (C < 0) return fail(MSVGB_eslEINVAL, "profile M exceeds the supported maximum (4095 nodes)");
   if (C < need_C(om->M) || (!f16 && (C & 1))) return fail(MSVGB_eslEINVAL, "DP width too small for M");
   std::vector<uint32_t> st, mt;
   build_cost_tables(om, f16 ? 1 : 0, C, st, mt);
@@ -841,18 +844,19 @@ extern "C" int msvgb_search_host(msvgb_ctx *c, const msvgb_profile *p, const uin
     return fail(MSVGB_eslEINVAL, "NULL argument");
   if (n == 0) return MSVGB_eslOK;
   CUDA_TRY(cudaSetDevice(c->device));
-  // chunk boundaries [cut[k], cut[k+1]): by default a quarter of the residues,
-  // then the rest (whose upload hides under the first search; every further
-  // chunk would add a launch tail); with chunk_residues, chunks growing from
-  // a quarter of it to it
+  // chunk boundaries [cut[k], cut[k+1]): by default an eighth of the residues,
+  // a quarter, then the rest (each chunk's upload and sort hide under the
+  // search of the one before; every further chunk would add a launch tail);
+  // with chunk_residues, chunks growing from a quarter of it to it
   std::vector<int64_t> cut(1, 0);
   const int64_t total = off[n] - off[0];
-  for (int64_t want = chunk_residues > 0 ? std::max<int64_t>(1, chunk_residues / 4) : total / 4 + 1, b0 = 0; b0 < n;) {
+  int64_t want = chunk_residues > 0 ? std::max<int64_t>(1, chunk_residues / 4) : total / 8 + 1;
+  for (int64_t b0 = 0, k = 0; b0 < n; ++k) {
     int64_t b1 = b0 + 1;
     while (b1 < n && off[b1] - off[b0] < want) ++b1;
     cut.push_back(b1);
     b0 = b1;
-    want = chunk_residues > 0 ? std::min(chunk_residues, 2 * want) : total;
+    want = chunk_residues > 0 ? std::min(chunk_residues, 2 * want) : (k == 0 ? 2 * want : total);
   }
   uint8_t *d = nullptr;
   CUDA_TRY(cudaMallocAsync((void **) &d, 2 * (size_t) n + 64, c->stream));

@@ -26,8 +26,16 @@ struct LaunchArgs {
 constexpr int WARPS_PER_CTA = 8;
 constexpr int MAX_WARPS_PER_CTA = 16;   // used when the tables leave room for one CTA per SM
 
+// f16 tables wider than 40 words per lane (M >= 2560: 154 KB of SSV costs
+// and up) do not fit in shared memory beside the MSV table: such profiles keep
+// both tables in global memory, where they stream through L1 and L2 (a few
+// hundred KB, resident in the 129 MB L2 for the whole launch).
+template <int C, bool F16>
+__host__ __device__ constexpr bool tables_in_global() { return F16 && C > 40; }
+
 template <int C, bool F16>
 constexpr size_t smem_bytes() {   // SSV table + MSV table
+  if (tables_in_global<C, F16>()) return 0;
   return ((size_t) (F16 ? NRES * C * 32 : NRES * (C / 2) * 32) + (size_t) NRES * ((C + 1) / 2) * 32) * 4;
 }
 
@@ -47,17 +55,18 @@ msv_search_kernel(ProfDev P, DbDev db, uint8_t *__restrict__ out_xj, uint8_t *__
   extern __shared__ __align__(16) uint32_t smem[];
   constexpr int SW = F16 ? NRES * C * 32 : NRES * (C / 2) * 32;   // words of the SSV table
   constexpr int MW = NRES * ((C + 1) / 2) * 32;                    // words of the MSV table
-  uint32_t *stab = smem;
-  uint32_t *mtab = smem + SW;
-  {
+  const uint32_t *stab = P.stab, *mtab = P.mtab;
+  if constexpr (!tables_in_global<C, F16>()) {
     const uint4 *gs = reinterpret_cast<const uint4 *>(P.stab);
     const uint4 *gm = reinterpret_cast<const uint4 *>(P.mtab);
-    uint4 *ss = reinterpret_cast<uint4 *>(stab);
-    uint4 *sm = reinterpret_cast<uint4 *>(mtab);
+    uint4 *ss = reinterpret_cast<uint4 *>(smem);
+    uint4 *sm = reinterpret_cast<uint4 *>(smem + SW);
     for (int i = threadIdx.x; i < SW / 4; i += blockDim.x) ss[i] = __ldg(gs + i);
     for (int i = threadIdx.x; i < MW / 4; i += blockDim.x) sm[i] = __ldg(gm + i);
+    stab = smem;
+    mtab = smem + SW;
+    __syncthreads();
   }
-  __syncthreads();
 
   const int lane = threadIdx.x & 31;
   const unsigned long long nitems = list ? *list_count : (unsigned long long) (range_end > 0 ? range_end : db.n);
