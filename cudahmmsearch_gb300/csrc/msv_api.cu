@@ -103,8 +103,8 @@ uint64_t msvgb_detail::next_db_serial() { return g_db_serial.fetch_add(1); }
 static const int kI8C[] = {2, 4, 6, 8, 10, 12, 14, 16, 18, 20, 22, 24, 26, 28, 30, 32, 34, 36, 40, 44, 48, 50};
 static const int kF16C[] = {1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 17, 18, 19, 20, 21, 22,
                             23, 24, 25, 26, 27, 28, 29, 30, 31, 32, 34, 36, 38, 40,
-                            44, 48, 52, 56, 60, 64};   // above 40: tables stay in global memory
-static const int kMaxF16C = 64;
+                            44, 48, 52, 56, 60, 64, 72, 80, 88, 96, 112, 128};   // above 40: tables in global memory
+static const int kMaxF16C = 128;
 
 // Smallest C whose warp spans more than M nodes: node 64*C must be padding
 // (the kernels rely on it for the begin value of node 1).
@@ -128,6 +128,7 @@ cudaError_t msvgb_detail::dispatch(int C, bool f16, const LaunchArgs &a, int sms
       CASE_F16(25) CASE_F16(26) CASE_F16(27) CASE_F16(28) CASE_F16(29) CASE_F16(30) CASE_F16(31) CASE_F16(32)
       CASE_F16(34) CASE_F16(36) CASE_F16(38) CASE_F16(40)
       CASE_F16(44) CASE_F16(48) CASE_F16(52) CASE_F16(56) CASE_F16(60) CASE_F16(64)
+      CASE_F16(72) CASE_F16(80) CASE_F16(88) CASE_F16(96) CASE_F16(112) CASE_F16(128)
     }
   } else {
     switch (C) {
@@ -300,7 +301,7 @@ int msvgb_detail::profile_build_width(msvgb_ctx *ctx, const msvgb_om *om, int wa
   const int c16 = force_C > 0 ? force_C : choose_C(om->M, true);
   const bool f16 = c16 > 0 && c16 <= kMaxF16C && (want_f16 || (force_C <= 0 && choose_C(om->M, false) < 0));
   const int C = force_C > 0 ? force_C : choose_C(om->M, f16);
-  if (C < 0) return fail(MSVGB_eslEINVAL, "profile M exceeds the supported maximum (4095 nodes)");
+  if (C < 0) return fail(MSVGB_eslEINVAL, "profile M exceeds the supported maximum (8191 nodes)");
   if (C < need_C(om->M) || (!f16 && (C & 1))) return fail(MSVGB_eslEINVAL, "DP width too small for M");
   std::vector<uint32_t> st, mt;
   build_cost_tables(om, f16 ? 1 : 0, C, st, mt);

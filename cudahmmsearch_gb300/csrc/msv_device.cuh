@@ -131,22 +131,45 @@ __device__ __forceinline__ void ssv_row_f16(uint32_t (&dp)[C], uint32_t &acc0, u
                                             const uint32_t *__restrict__ tab, int x, int lane, int src_lane) {
   using Lay = F16Layout<C>;
   constexpr uint32_t one2 = 0x3C003C00u;        // f16x2 (1.0, 1.0)
-  uint32_t s[C];
+  auto cell = [&](int w, uint32_t sw, uint32_t pred0) {
+    dp[w] = fma_relu_f16x2(w ? dp[w - 1] : pred0, one2, sw);
+    if (w & 1) acc1 = max_f16x2(acc1, dp[w]); else acc0 = max_f16x2(acc0, dp[w]);
+  };
+  if constexpr (C <= 64) {
+    // all of the row's costs are loaded first (latency hidden behind the row)
+    uint32_t s[C];
 #pragma unroll
-  for (int q = 0; q < Lay::Q4; ++q) {
-    const uint4 v = *reinterpret_cast<const uint4 *>(tab + ((x * Lay::Q4 + q) * 32 + lane) * 4);
-    s[4 * q] = v.x; s[4 * q + 1] = v.y; s[4 * q + 2] = v.z; s[4 * q + 3] = v.w;
+    for (int q = 0; q < Lay::Q4; ++q) {
+      const uint4 v = *reinterpret_cast<const uint4 *>(tab + ((x * Lay::Q4 + q) * 32 + lane) * 4);
+      s[4 * q] = v.x; s[4 * q + 1] = v.y; s[4 * q + 2] = v.z; s[4 * q + 3] = v.w;
+    }
+    if constexpr (Lay::R >= 2) {
+      const uint2 v = *reinterpret_cast<const uint2 *>(tab + Lay::A_WORDS + (x * 32 + lane) * 2);
+      s[4 * Lay::Q4] = v.x; s[4 * Lay::Q4 + 1] = v.y;
+    }
+    if constexpr (Lay::R & 1) s[C - 1] = tab[Lay::A_WORDS + Lay::B_WORDS + x * 32 + lane];
+    const uint32_t pred0 = pred_word0(dp[C - 1], src_lane);
+#pragma unroll
+    for (int w = C - 1; w >= 0; --w) cell(w, s[w], pred0);
+    return;
   }
+  // rows wider than 64 words: words are updated from the highest down (dp[w]
+  // reads the old dp[w-1]) and each table region is loaded just before its
+  // words, so only the DP row and one quad of costs are live (no spills)
+  const uint32_t pred0 = pred_word0(dp[C - 1], src_lane);
+  if constexpr (Lay::R & 1) cell(C - 1, tab[Lay::A_WORDS + Lay::B_WORDS + x * 32 + lane], pred0);
   if constexpr (Lay::R >= 2) {
     const uint2 v = *reinterpret_cast<const uint2 *>(tab + Lay::A_WORDS + (x * 32 + lane) * 2);
-    s[4 * Lay::Q4] = v.x; s[4 * Lay::Q4 + 1] = v.y;
+    cell(4 * Lay::Q4 + 1, v.y, pred0);
+    cell(4 * Lay::Q4, v.x, pred0);
   }
-  if constexpr (Lay::R & 1) s[C - 1] = tab[Lay::A_WORDS + Lay::B_WORDS + x * 32 + lane];
-  const uint32_t pred0 = pred_word0(dp[C - 1], src_lane);
 #pragma unroll
-  for (int w = C - 1; w >= 0; --w) {
-    dp[w] = fma_relu_f16x2(w ? dp[w - 1] : pred0, one2, s[w]);
-    if (w & 1) acc1 = max_f16x2(acc1, dp[w]); else acc0 = max_f16x2(acc0, dp[w]);
+  for (int q = Lay::Q4 - 1; q >= 0; --q) {
+    const uint4 v = *reinterpret_cast<const uint4 *>(tab + ((x * Lay::Q4 + q) * 32 + lane) * 4);
+    cell(4 * q + 3, v.w, pred0);
+    cell(4 * q + 2, v.z, pred0);
+    cell(4 * q + 1, v.y, pred0);
+    cell(4 * q, v.x, pred0);
   }
 }
 

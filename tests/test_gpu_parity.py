@@ -117,7 +117,7 @@ def test_m2400_length_extremes_and_saturation(ctx):
 
 
 @pytest.mark.parametrize("M", [1, 2, 3, 15, 16, 17, 63, 64, 65, 127, 128, 129, 1000, 2559, 2560, 3072, 3199, 3200,
-                               3583, 4095])
+                               3583, 4095, 4096, 6000, 8191])
 def test_model_size_corners(ctx, M):
     """Node counts around the striping and lane boundaries, random profiles
     built directly from cost tables, tiny and all-X sequences."""
@@ -166,7 +166,7 @@ def test_invalid_inputs_rejected(ctx):
     with pytest.raises(api.MSVError) as e:
         api.DeviceDB(ctx, bad)
     assert e.value.code == api.eslEINVAL
-    big = F.profile_from_node_costs(np.zeros((29, 4096), np.uint8), tbm_b=10, tec_b=3, base_b=190,
+    big = F.profile_from_node_costs(np.zeros((29, 8192), np.uint8), tbm_b=10, tec_b=3, base_b=190,
                                     bias_b=10, scale_b=4.328085, mmu=-9.0, mlambda=0.69)
     with pytest.raises(api.MSVError) as e:
         api.DeviceProfile(ctx, big)
@@ -226,7 +226,7 @@ def test_search_host_equals_resident_search(ctx, chunk):
     assert e[0].size == 0 and e[1].size == 0
 
 
-@pytest.mark.parametrize("M", [2700, 3500, 4095])
+@pytest.mark.parametrize("M", [2700, 3500, 4095, 5500, 8000])
 def test_models_with_tables_in_global_memory(ctx, M):
     """Sampled models too large for shared-memory tables (M >= 2560): both
     tables stream from global memory; homologs, overflow repeats and long
