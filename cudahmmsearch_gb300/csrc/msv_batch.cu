@@ -108,6 +108,8 @@ extern "C" int msvgb_batch_destroy(msvgb_batch *b) {
   return MSVGB_eslOK;
 }
 
+// Profiles above 2047 nodes (up to the single-query maximum) are scored by
+// their own launches, captured in the same graph after the persistent kernel.
 // Work items: for each profile (largest models first), for each target-length
 // bin of the sorted database (longest first), chunks of about per_item
 // residues -- at most kChunkMaxSeqs sequences when the bin's lane count is
@@ -144,12 +146,20 @@ int msvgb_detail::batch_create(msvgb_ctx *ctx, const msvgb_om *const *oms, int n
   // lane-group tables its bins ask for
   std::vector<ProfDev> vars;
   std::vector<std::array<int, msvgb_detail::kNLBins>> var_of(nprof);
+  std::vector<std::pair<int, msvgb_profile *>> large;          // M > 2047: own launches in the graph
   size_t smem = 0;
   for (int i = 0; i < nprof; ++i) {
     if (!oms[i]) return bail(MSVGB_eslEINVAL, "NULL profile");
     const int M = oms[i]->M;
     const int C = multi_C(M);
-    if (C < 0) return bail(MSVGB_eslEINVAL, "batched profiles are limited to M <= 2047");
+    if (C < 0) {
+      msvgb_profile *p = nullptr;
+      int st = msvgb_detail::profile_build_width(ctx, oms[i], 1, 0, &p);
+      if (st != MSVGB_eslOK) { msvgb_batch_destroy(b); return st; }
+      b->own.push_back(p);
+      large.emplace_back(i, p);
+      continue;
+    }
     msvgb_profile *p = nullptr;
     int st = msvgb_detail::profile_build_width(ctx, oms[i], 1, C, &p);
     if (st != MSVGB_eslOK) { msvgb_batch_destroy(b); return st; }
@@ -186,8 +196,15 @@ int msvgb_detail::batch_create(msvgb_ctx *ctx, const msvgb_om *const *oms, int n
     }
   }
   b->nvars = (int) vars.size();
-  std::vector<int> order(nprof);
-  for (int i = 0; i < nprof; ++i) order[i] = i;
+  std::vector<LenTables *> large_tables;
+  for (auto &lp : large) {
+    LenTables *t = nullptr;
+    const int st = msvgb_detail::ensure_tables(lp.second, db, F1, &t);
+    if (st != MSVGB_eslOK) { msvgb_batch_destroy(b); return st; }
+    large_tables.push_back(t);
+  }
+  std::vector<int> order;
+  for (int i = 0; i < nprof; ++i) if (multi_C(oms[i]->M) > 0) order.push_back(i);
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return oms[x]->M > oms[y]->M; });
 
   b->smem = smem;
@@ -202,7 +219,7 @@ int msvgb_detail::batch_create(msvgb_ctx *ctx, const msvgb_om *const *oms, int n
   const double per_item = std::max(4096.0, (double) db->residues * nprof / want_items);
   const int64_t min_seqs = b->threads / 32;
   std::vector<BatchItem> items;
-  for (int oi = 0; oi < nprof; ++oi) {
+  for (size_t oi = 0; oi < order.size(); ++oi) {
     const int pi = order[oi];
     for (const Range &r : ranges) {
       const int v = var_of[pi][r.bin];
@@ -219,7 +236,7 @@ int msvgb_detail::batch_create(msvgb_ctx *ctx, const msvgb_om *const *oms, int n
   b->nitems = (int64_t) items.size();
   e = cudaMalloc(&b->d_vars, sizeof(ProfDev) * std::max(1, b->nvars));
   if (e == cudaSuccess) e = cudaMalloc(&b->d_items, sizeof(BatchItem) * std::max<int64_t>(1, b->nitems));
-  if (e == cudaSuccess) e = cudaMalloc(&b->d_ticket, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_ticket, sizeof(unsigned long long) * (1 + large.size()));
   if (e == cudaSuccess) e = cudaMemcpy(b->d_vars, vars.data(), sizeof(ProfDev) * b->nvars, cudaMemcpyHostToDevice);
   if (e == cudaSuccess && b->nitems)
     e = cudaMemcpy(b->d_items, items.data(), sizeof(BatchItem) * b->nitems, cudaMemcpyHostToDevice);
@@ -234,9 +251,29 @@ int msvgb_detail::batch_create(msvgb_ctx *ctx, const msvgb_om *const *oms, int n
   e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
-    cudaMemsetAsync(b->d_ticket, 0, sizeof(unsigned long long), cs);
-    msv_batch_kernel<<<b->grid, b->threads, b->smem, cs>>>(a);
-    cudaError_t e1 = cudaGetLastError();
+    cudaError_t e1 = cudaSuccess;
+    cudaMemsetAsync(b->d_ticket, 0, sizeof(unsigned long long) * (1 + large.size()), cs);
+    if (b->nitems) {
+      msv_batch_kernel<<<b->grid, b->threads, b->smem, cs>>>(a);
+      e1 = cudaGetLastError();
+    }
+    // models above 2047 nodes: one single-query launch each (32 lanes, tables
+    // in shared or global memory), in the same graph
+    for (size_t j = 0; j < large.size() && e1 == cudaSuccess; ++j) {
+      const msvgb_profile *p = large[j].second;
+      const LenTables *t = large_tables[j];
+      LaunchArgs la;
+      la.P = ProfDev{};
+      la.P.M = p->M; la.P.C = p->C; la.P.tbm = p->tbm; la.P.tec = p->tec; la.P.base = p->base; la.P.bias = p->bias;
+      la.P.stab = p->d_stab; la.P.mtab = p->d_mtab; la.P.tjb = t->d_tjb; la.P.xjmin = t->d_xjmin;
+      la.P.ssv_f16 = p->f16;
+      la.db = a.db;
+      la.out_xj = (uint8_t *) d_xj + (int64_t) large[j].first * db->n;
+      la.out_flags = (uint8_t *) d_flags + (int64_t) large[j].first * db->n;
+      la.ticket = b->d_ticket + 1 + j;
+      la.stream = cs; la.grid = 0; la.skip_empty = 1;
+      e1 = msvgb_detail::dispatch(p->C, p->f16 != 0, la, ctx->num_sms);
+    }
     e = cudaStreamEndCapture(cs, &b->graph);
     if (e == cudaSuccess) e = e1;
   }

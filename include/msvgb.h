@@ -259,8 +259,9 @@ int msvgb_search_static(const msvgb_profile *prof, const msvgb_db *db, double F1
                         void *d_xj, void *d_flags, void *cuda_stream);
 
 /* ---- batched search: many profiles, one persistent launch ------------------------
- * All nprof profiles (M <= 2047 each) against db in a single persistent kernel
- * over a (profile, sequence-chunk) work queue, captured once as a CUDA graph;
+ * All nprof profiles against db in a single persistent kernel over a
+ * (profile, sequence-chunk) work queue (profiles above 2047 nodes, up to
+ * 8191, get their own launches in the same graph), captured once as a CUDA graph;
  * each msvgb_batch_run replays it asynchronously on the context's stream.
  * Outputs are device buffers of nprof * n bytes, profile-major:
  * d_xj[p * n + i], d_flags[p * n + i] as msvgb_search writes them.

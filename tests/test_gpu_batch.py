@@ -36,7 +36,7 @@ def make_profiles(ctx, Ms, seed0=100):
 
 
 def test_batch_equals_single_query_and_oracle(ctx):
-    Ms = [1, 17, 50, 64, 120, 200, 333, 400, 650, 777, 1000, 1500, 2000, 2047]
+    Ms = [1, 17, 50, 64, 120, 200, 333, 400, 650, 777, 1000, 1500, 2000, 2047, 2048, 3000]
     profs = make_profiles(ctx, Ms)
     s = F.SeqSet.concat([F.synth_sequences(2500, seed=41, lmax=8000),
                          F.emit_homologs(profs[5], 30, seed=42), F.emit_homologs(profs[9], 30, seed=43),
@@ -79,7 +79,7 @@ def test_batch_graph_replays_identically(ctx):
 
 
 def test_batch_rejects_oversize_profiles(ctx):
-    big = F.profile_from_node_costs(np.zeros((29, 2048), np.uint8), tbm_b=10, tec_b=3, base_b=190,
+    big = F.profile_from_node_costs(np.zeros((29, 8192), np.uint8), tbm_b=10, tec_b=3, base_b=190,
                                     bias_b=10, scale_b=4.328085, mmu=-9.0, mlambda=0.69)
     db = api.DeviceDB(ctx, F.synth_sequences(10, seed=1))
     with pytest.raises(api.MSVError) as e:
