@@ -115,3 +115,22 @@ def test_packed_database_rejects_corruption(ctx, tmp_path):
     with pytest.raises(api.MSVError) as e:
         api.DeviceDB.load(ctx, str(tmp_path / "missing.msvdb"))
     assert e.value.code == api.eslENOTFOUND
+
+
+def test_database_memory_is_returned(ctx):
+    """Databases come from a stream-ordered pool that keeps at most 4 GiB
+    mapped: creating and destroying a database many times does not grow the
+    device memory in use beyond that."""
+    import torch
+    s = F.synth_sequences(400_000, seed=3, lmax=4000)        # ~150 MB packed
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(25):
+        db = api.DeviceDB(ctx, s)
+        db.close()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free0 - free1 < (4 << 30) + (256 << 20)
+    for _ in range(25):
+        db = api.DeviceDB(ctx, s)
+        db.close()
+    free2, _ = torch.cuda.mem_get_info()
+    assert abs(free1 - free2) < (64 << 20)                    # steady state: nothing leaks

@@ -51,3 +51,61 @@ def test_pipeline_continuation_can_stop_the_run(ctx):
     with pytest.raises(api.MSVError) as e:
         api.pipeline_run(ctx, p, s, lambda i, usc, xj, fl: True, block_size=100, n_workers=2)
     assert e.value.code == 1
+
+
+@pytest.mark.parametrize("name", ["tut_globins4", "tut_fn3", "tut_pkinase"])
+def test_pipeline_on_tutorial_models_equals_reference_msv_stage(ctx, name):
+    """The driver on a real Pfam model (the reference's tutorial library) and
+    its golden targets: n_past_msv and every survivor's score equal the
+    reference's own MSV stage (the golden fixtures came from its
+    p7_MSVFilter and F1 gate)."""
+    p = F.read_profile(os.path.join(GOLDEN, name + ".prof"))
+    s = F.read_seqs(os.path.join(GOLDEN, name + ".seqs"))
+    r = F.read_results(os.path.join(GOLDEN, name + ".res"))
+    got = {}
+    lock = threading.Lock()
+
+    def on_survivor(i, usc, xj, fl):
+        with lock:
+            got[i] = usc
+        return False
+
+    n_past = api.pipeline_run(ctx, p, s, on_survivor, block_size=50, n_workers=3)
+    want = np.nonzero(r.passed == 1)[0]
+    assert n_past == len(want) == len(got) and sorted(got) == list(want)
+    for i in want:
+        assert np.float32(got[i]).view(np.uint32) == r.sc[i].view(np.uint32)
+
+
+def test_dropin_from_many_threads(ctx):
+    """p7_MSVFilter is called from hmmsearch's worker threads: concurrent
+    drop-in calls on one context (serialised inside) and on per-thread
+    contexts give the reference's results."""
+    p = F.read_profile(os.path.join(GOLDEN, "tut_pkinase.prof"))
+    s = F.read_seqs(os.path.join(GOLDEN, "tut_pkinase.seqs"))
+    r = F.read_results(os.path.join(GOLDEN, "tut_pkinase.res"))
+    errors = []
+
+    def work(c, idx):
+        try:
+            for i in idx:
+                L = int(s.lengths[i])
+                dsq = np.concatenate([[255], s.seq(i), [255]]).astype(np.uint8)
+                st, sc = c.MSVFilter(dsq, L, p, api.tjb_b(p.scale_b, L))
+                if st != r.status[i] or np.float32(sc).view(np.uint32) != r.sc[i].view(np.uint32):
+                    errors.append(i)
+        except Exception as e:                      # surfaced below
+            errors.append(repr(e))
+
+    own = [api.Context(0) for _ in range(2)]
+    try:
+        threads = [threading.Thread(target=work, args=(ctx if t < 3 else own[t - 3], range(t, s.n, 5)))
+                   for t in range(5)]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+    finally:
+        for c in own:
+            c.close()
+    assert not errors
