@@ -204,6 +204,63 @@ def read_results(path) -> Results:
     return Results(st, sc, ns, P, ps)
 
 
+@dataclasses.dataclass
+class VProfile:
+    """The ViterbiFilter part of a P7_OPROFILE (src/impl_sse/impl_sse.h:88-96),
+    striped as the reference stores it: Q8 = max(2, ceil(M/8)); twv
+    [8*Q8, 8] int16 (per vector q the 7 vectors BM MM IM DM MD MI II, then the
+    Q8 DD vectors), rwv [Kp, Q8, 8] int16; element z of vector q is node
+    q+1+z*Q8. xw [4, 2] int16 (E N J C x MOVE LOOP) as configured; the
+    N/J/C MOVE costs are recomputed per target length."""
+    M: int
+    twv: np.ndarray
+    rwv: np.ndarray
+    xw: np.ndarray
+    scale_w: float
+    nj: float
+    base_w: int
+    ddbound_w: int
+    vmu: float = 0.0
+    vlambda: float = 0.0
+
+    @property
+    def Q8(self) -> int:
+        return max(2, (self.M - 1) // 8 + 1)
+
+    @property
+    def Kp(self) -> int:
+        return int(self.rwv.shape[0])
+
+
+def read_vprofile(path) -> VProfile:
+    """VITPROF1: int32 M, Q8, Kp; float scale_w, nj; int16 base_w, ddbound_w;
+    int16 xw[4][2]; float vmu, vlambda; int16 twv[8*Q8][8]; int16 rwv[Kp][Q8][8]."""
+    b = open(path, "rb").read()
+    if b[:8] != b"VITPROF1":
+        raise ValueError(f"{path}: not a VITPROF1 file")
+    M, Q8, Kp = struct.unpack_from("<3i", b, 8)
+    scale_w, nj = struct.unpack_from("<2f", b, 20)
+    base_w, ddbound_w = struct.unpack_from("<2h", b, 28)
+    xw = np.frombuffer(b, np.int16, 8, 32).reshape(4, 2).copy()
+    vmu, vlambda = struct.unpack_from("<2f", b, 48)
+    o = 56
+    twv = np.frombuffer(b, np.int16, 8 * Q8 * 8, o).reshape(8 * Q8, 8).copy(); o += 8 * Q8 * 16
+    rwv = np.frombuffer(b, np.int16, Kp * Q8 * 8, o).reshape(Kp, Q8, 8).copy()
+    return VProfile(M=M, twv=twv, rwv=rwv, xw=xw, scale_w=scale_w, nj=nj, base_w=base_w, ddbound_w=ddbound_w,
+                    vmu=vmu, vlambda=vlambda)
+
+
+def read_vresults(path):
+    """VITRES01: int64 n; int32 status[n] (-1: empty); float sc[n]."""
+    b = open(path, "rb").read()
+    if b[:8] != b"VITRES01":
+        raise ValueError(f"{path}: not a VITRES01 file")
+    (n,) = struct.unpack_from("<q", b, 8)
+    st = np.frombuffer(b, np.int32, n, 16).copy()
+    sc = np.frombuffer(b, np.float32, n, 16 + 4 * n).copy()
+    return st, sc
+
+
 def synth_sequences(n: int, *, seed: int, median: float = 300.0, sigma: float = 0.7,
                     lmin: int = 10, lmax: int = 5000, x_frac: float = 0.005,
                     uniform_frac: float = 0.0, uniform_range=(5000, 35000)) -> SeqSet:

@@ -2,8 +2,9 @@
 
 Loads oracle/libmsvoracle.so, the scalar C restatement of HMMER 3.1b1's
 p7_MSVFilter (src/impl_sse/msvfilter.c:77-213, with the SSV fast path of
-src/impl_sse/ssvfilter.c:1364-1413) and of the MSV stage of p7_Pipeline
-(src/p7_pipeline.c:662-677). Only tests/, __graft_entry__.smoke() and the
+src/impl_sse/ssvfilter.c:1364-1413), of the MSV stage of p7_Pipeline
+(src/p7_pipeline.c:662-677) and of p7_ViterbiFilter
+(src/impl_sse/vitfilter.c:84-250). Only tests/, __graft_entry__.smoke() and the
 CPU-baseline leg of bench.py may import this module.
 """
 from __future__ import annotations
@@ -21,10 +22,10 @@ LIB_PATH = os.path.join(HERE, "libmsvoracle.so")
 def build(force: bool = False) -> str:
     """Compiles the scalar oracle (msv_oracle.c) and the vectorized port used
     as the timed CPU baseline (msv_port.c) into one library."""
-    srcs = [os.path.join(HERE, "msv_oracle.c"), os.path.join(HERE, "msv_port.c")]
-    hdr = os.path.join(HERE, "msv_oracle.h")
+    srcs = [os.path.join(HERE, "msv_oracle.c"), os.path.join(HERE, "msv_port.c"), os.path.join(HERE, "vit_oracle.c")]
+    hdrs = [os.path.join(HERE, "msv_oracle.h"), os.path.join(HERE, "vit_oracle.h")]
     if force or not os.path.exists(LIB_PATH) or any(os.path.getmtime(LIB_PATH) < os.path.getmtime(f)
-                                                    for f in srcs + [hdr]):
+                                                    for f in srcs + hdrs):
         subprocess.check_call(["cc", "-O3", "-std=gnu99", "-ffp-contract=off", "-fPIC", "-shared",
                                "-pthread"] + srcs + ["-o", LIB_PATH, "-lm"])
     return LIB_PATH
@@ -36,6 +37,13 @@ class _Prof(ctypes.Structure):
                 ("tbm_b", ctypes.c_uint8), ("tec_b", ctypes.c_uint8),
                 ("base_b", ctypes.c_uint8), ("bias_b", ctypes.c_uint8),
                 ("scale_b", ctypes.c_float), ("mmu", ctypes.c_double), ("mlambda", ctypes.c_double)]
+
+
+class _VProf(ctypes.Structure):
+    _fields_ = [("M", ctypes.c_int), ("Q8", ctypes.c_int), ("Kp", ctypes.c_int),
+                ("scale_w", ctypes.c_float), ("nj", ctypes.c_float),
+                ("base_w", ctypes.c_int16), ("ddbound_w", ctypes.c_int16),
+                ("xw", ctypes.c_int16 * 8), ("twv", ctypes.c_void_p), ("rwv", ctypes.c_void_p)]
 
 
 _lib = None
@@ -59,6 +67,9 @@ def lib():
         _lib.port_msv_batch.argtypes = [ctypes.POINTER(_Prof), ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_int64, ctypes.c_double, ctypes.c_int,
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        _lib.orc_vit_filter.restype = ctypes.c_int
+        _lib.orc_vit_filter.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(_VProf),
+                                        ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int)]
         _lib.orc_msv_batch.restype = ctypes.c_int
         _lib.orc_msv_batch.argtypes = [ctypes.POINTER(_Prof), ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_int64, ctypes.c_double, ctypes.c_int,
@@ -144,3 +155,37 @@ def port_batch(p, seqs, *, F1: float = 0.02, nthreads: int = 0):
                                 out["status"].ctypes.data, out["xj"].ctypes.data, out["sc"].ctypes.data,
                                 out["pass"].ctypes.data)
     return out, used
+
+
+def _vprof(vp):
+    twv = np.ascontiguousarray(vp.twv, dtype=np.int16)
+    rwv = np.ascontiguousarray(vp.rwv, dtype=np.int16)
+    xw = (ctypes.c_int16 * 8)(*[int(v) for v in np.asarray(vp.xw).reshape(-1)])
+    s = _VProf(vp.M, vp.Q8, vp.Kp, vp.scale_w, vp.nj, vp.base_w, vp.ddbound_w, xw,
+               twv.ctypes.data, rwv.ctypes.data)
+    return s, (twv, rwv)
+
+
+def vit_filter(vp, dsq_codes):
+    """p7_ViterbiFilter on one sequence (codes without sentinels). Returns (status, sc, xC)."""
+    L = len(dsq_codes)
+    dsq = np.empty(L + 2, np.uint8)
+    dsq[0] = dsq[-1] = 255
+    dsq[1:L + 1] = dsq_codes
+    s, keep = _vprof(vp)
+    sc = ctypes.c_float()
+    xc = ctypes.c_int()
+    st = lib().orc_vit_filter(dsq.ctypes.data, L, ctypes.byref(s), ctypes.byref(sc), ctypes.byref(xc))
+    return int(st), float(sc.value), int(xc.value)
+
+
+def vit_batch(vp, seqs):
+    """vit_filter over a SeqSet: status (int32, -1 for empty), sc (float32), xc (int32)."""
+    st = np.full(seqs.n, -1, np.int32)
+    sc = np.zeros(seqs.n, np.float32)
+    xc = np.zeros(seqs.n, np.int32)
+    for i in range(seqs.n):
+        if seqs.lengths[i] == 0:
+            continue
+        st[i], sc[i], xc[i] = vit_filter(vp, seqs.seq(i))
+    return {"status": st, "sc": sc, "xc": xc}

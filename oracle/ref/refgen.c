@@ -23,12 +23,21 @@
  *   seqfile  : any sequence file Easel reads (esl_sqfile_OpenDigital, format
  *              autodetected, easel/esl_sqio.c:300), digitized with the amino alphabet.
  *
+ *   vit      : the ViterbiFilter stage (src/impl_sse/vitfilter.c:84-250) on the same
+ *              configured model: its int16 profile part (vf_conversion,
+ *              src/impl_sse/p7_oprofile.c:653-760) dumped, and per sequence
+ *              p7_oprofile_ReconfigLength + p7_ViterbiFilter status and score.
+ *
  * File formats (little-endian, written and read by this project only):
  *   profile "MSVPROF1": int32 M, Q, Kp, Lcfg; uint8 tbm,tec,tjb,base,bias,pad[3];
  *                       float scale; double mmu, mlambda; uint8 rbv[Kp*Q*16]
  *   seqs    "MSVSEQS1": int64 n, total; int64 off[n+1]; uint8 dsq[total]   (codes, no sentinels)
  *   result  "MSVRES01": int64 n; int32 status[n]; float sc[n]; double nullsc[n];
  *                       double P[n]; uint8 pass[n]
+ *   vprof   "VITPROF1": int32 M, Q8, Kp; float scale_w, nj; int16 base_w, ddbound_w;
+ *                       int16 xw[4][2] (E,N,J,C x MOVE,LOOP, as configured);
+ *                       float vmu, vlambda; int16 twv[8*Q8][8]; int16 rwv[Kp][Q8][8]
+ *   vres    "VITRES01": int64 n; int32 status[n]; float sc[n]
  */
 #include "p7_config.h"
 #include <stdio.h>
@@ -110,6 +119,24 @@ static void file_model(model_t *m, const char *hmmfile, int idx, int pressed)
   }
   m->bg = p7_bg_Create(m->abc);
   p7_hmmfile_Close(hfp);
+}
+
+static void write_vprofile(const model_t *m, const char *path)
+{
+  FILE *fp = fopen(path, "wb"); if (!fp) die("open vprofile out");
+  const P7_OPROFILE *om = m->om;
+  int32_t hdr[3]; int Q8 = p7O_NQW(om->M);
+  hdr[0] = om->M; hdr[1] = Q8; hdr[2] = m->abc->Kp;
+  fwrite("VITPROF1", 1, 8, fp);
+  fwrite(hdr, 4, 3, fp);
+  fwrite(&om->scale_w, 4, 1, fp); fwrite(&om->nj, 4, 1, fp);
+  fwrite(&om->base_w, 2, 1, fp); fwrite(&om->ddbound_w, 2, 1, fp);
+  fwrite(om->xw, 2, 8, fp);
+  float ev[2] = { om->evparam[p7_VMU], om->evparam[p7_VLAMBDA] };
+  fwrite(ev, 4, 2, fp);
+  fwrite(om->twv, 16, 8 * Q8, fp);
+  for (int x = 0; x < m->abc->Kp; x++) fwrite(om->rwv[x], 16, Q8, fp);
+  fclose(fp);
 }
 
 typedef struct { int64_t n, total; int64_t *off; uint8_t *dsq; } seqs_t;
@@ -230,6 +257,36 @@ int main(int argc, char **argv)
       push_seq(&s, &cap, sq->dsq, (int) sq->n);
     }
     write_seqs(&s, argv[6]);
+    return 0;
+  }
+  if (!strcmp(cmd, "vit") || !strcmp(cmd, "vitfile")) {  /* vit M seed prof res seqs | vitfile hmmfile idx prof res seqs */
+    model_t m;
+    seqs_t s;
+    if (!strcmp(cmd, "vit")) {
+      if (argc != 7) die("vit M seed vprof vres seqs");
+      make_model(&m, atoi(argv[2]), (uint32_t) atol(argv[3]), 100, p7_LOCAL);
+    } else {
+      if (argc != 7) die("vitfile hmmfile idx vprof vres seqs");
+      file_model(&m, argv[2], atoi(argv[3]), 0);
+    }
+    write_vprofile(&m, argv[4]);
+    read_seqs(&s, argv[6]);
+    int64_t maxL = 1;
+    for (int64_t i = 0; i < s.n; i++) if (s.off[i+1] - s.off[i] > maxL) maxL = s.off[i+1] - s.off[i];
+    P7_OMX *ox = p7_omx_Create(m.om->M, 0, 0);
+    ESL_DSQ *dsq = malloc(maxL + 2);
+    int32_t *st = calloc(s.n, 4); float *sc = calloc(s.n, 4);
+    for (int64_t i = 0; i < s.n; i++) {
+      int L = (int) (s.off[i+1] - s.off[i]);
+      if (L == 0) { st[i] = -1; continue; }
+      dsq[0] = eslDSQ_SENTINEL; memcpy(dsq + 1, s.dsq + s.off[i], L); dsq[L+1] = eslDSQ_SENTINEL;
+      p7_oprofile_ReconfigLength(m.om, L);
+      st[i] = p7_ViterbiFilter(dsq, L, m.om, ox, &sc[i]);
+    }
+    FILE *fp = fopen(argv[5], "wb"); if (!fp) die("open vres out");
+    fwrite("VITRES01", 1, 8, fp); fwrite(&s.n, 8, 1, fp);
+    fwrite(st, 4, s.n, fp); fwrite(sc, 4, s.n, fp);
+    fclose(fp);
     return 0;
   }
   if (!strcmp(cmd, "score") || !strcmp(cmd, "scorefile")) {  /* score M seed Lcfg mode seqs out | scorefile hmmfile idx seqs out */

@@ -23,6 +23,9 @@ HBB_HUMAN and 7LESS_DROME read by Easel's sequence reader, ``refgen seqfile``;
 p7_ProfileEmit homologs and saturation repeats of each model; background
 sequences), so the fixtures pin the path on real profiles, including the
 fn3 / 7LESS_DROME search of tutorial/fn3.out.
+The vit_* files pin the ViterbiFilter stage (vit_NAME.vprof: the model's
+int16 ViterbiFilter profile; vit_NAME.vres: p7_ViterbiFilter status and score
+for every sequence of NAME.seqs).
 Run:  python tests/golden/make_golden.py [reference code dir]
 """
 import os
@@ -119,6 +122,24 @@ def make_tutorial(tut):
     os.remove(tmp)
 
 
+# ViterbiFilter goldens (vit_NAME.vprof / .vres over NAME.seqs): the sampled
+# cases in hmmsearch's local mode, and the tutorial models as hmmsearch
+# configures them
+VIT_SAMPLED = ["m1_s1", "m2_s1", "m16_s1", "m17_s2", "m33_s3", "m50_s1", "m200_s1", "m400_s1", "m777_s3",
+               "m1500_s2", "m2400_s1"]
+
+
+def make_vit(tut):
+    for name in VIT_SAMPLED:
+        M, seed = name[1:].split("_s")
+        run("vit", M, seed, os.path.join(HERE, "vit_" + name + ".vprof"), os.path.join(HERE, "vit_" + name + ".vres"),
+            os.path.join(HERE, name + ".seqs"))
+    for name, idx in TUT_MODELS:
+        run("vitfile", os.path.join(tut, "minifam"), idx, os.path.join(HERE, "vit_" + name + ".vprof"),
+            os.path.join(HERE, "vit_" + name + ".vres"), os.path.join(HERE, name + ".seqs"))
+    print("vit goldens:", len(VIT_SAMPLED) + len(TUT_MODELS))
+
+
 def main():
     if not os.path.exists(REFGEN):
         sys.exit("oracle/_ref/refgen missing: make -C oracle/ref REF=<reference>/code")
@@ -126,6 +147,7 @@ def main():
     for c in CASES:
         make_case(*c)
     make_tutorial(os.path.join(ref, "tutorial"))
+    make_vit(os.path.join(ref, "tutorial"))
 
 
 if __name__ == "__main__":
