@@ -37,6 +37,7 @@ EXPORTS = [
     "msvgb_h3f_open", "msvgb_h3f_read", "msvgb_h3f_close", "msvgb_h3f_write", "msvgb_fasta_read",
     "msvgb_seqs_n", "msvgb_seqs_codes", "msvgb_seqs_offsets", "msvgb_seqs_name", "msvgb_seqs_free",
     "msvgb_db_save", "msvgb_db_load", "msvgb_db_lengths", "msvgb_search_host",
+    "msvgb_vprofile_create", "msvgb_vprofile_destroy", "msvgb_vitfilter", "msvgb_vit_score", "msvgb_vit_move_cost",
 ]
 
 
@@ -51,6 +52,19 @@ class _Om(ctypes.Structure):
                 ("tbm_b", ctypes.c_uint8), ("tec_b", ctypes.c_uint8), ("tjb_b", ctypes.c_uint8),
                 ("base_b", ctypes.c_uint8), ("bias_b", ctypes.c_uint8),
                 ("scale_b", ctypes.c_float), ("mmu", ctypes.c_float), ("mlambda", ctypes.c_float)]
+
+
+class _VOm(ctypes.Structure):
+    _fields_ = [("M", ctypes.c_int), ("Kp", ctypes.c_int), ("twv", ctypes.c_void_p), ("rwv", ctypes.c_void_p),
+                ("xw", ctypes.c_int16 * 8), ("scale_w", ctypes.c_float), ("nj", ctypes.c_float),
+                ("base_w", ctypes.c_int16), ("ddbound_w", ctypes.c_int16)]
+
+
+def _vom_struct(vp: F.VProfile):
+    twv = np.ascontiguousarray(vp.twv, dtype=np.int16)
+    rwv = np.ascontiguousarray(vp.rwv, dtype=np.int16)
+    xw = (ctypes.c_int16 * 8)(*[int(v) for v in np.asarray(vp.xw).reshape(-1)])
+    return _VOm(vp.M, vp.Kp, twv.ctypes.data, rwv.ctypes.data, xw, vp.scale_w, vp.nj, vp.base_w, vp.ddbound_w), (twv, rwv)
 
 
 class _Omx(ctypes.Structure):
@@ -99,6 +113,11 @@ def lib():
         "msvgb_db_load": (i32, [vp, ctypes.c_char_p, ctypes.POINTER(vp)]),
         "msvgb_db_lengths": (i32, [vp, vp]),
         "msvgb_search_host": (i32, [vp, vp, vp, vp, ctypes.c_int64, ctypes.c_double, ctypes.c_int64, vp, vp]),
+        "msvgb_vprofile_create": (i32, [vp, ctypes.POINTER(_VOm), ctypes.POINTER(vp)]),
+        "msvgb_vprofile_destroy": (i32, [vp]),
+        "msvgb_vitfilter": (i32, [vp, vp, vp, vp, ctypes.c_int64, vp, vp]),
+        "msvgb_vit_score": (ctypes.c_float, [i32, i32, i32, ctypes.POINTER(_VOm)]),
+        "msvgb_vit_move_cost": (ctypes.c_int16, [ctypes.c_float, ctypes.c_float, i32]),
         "msvgb_profile_lanes": (i32, [vp]),
         "msvgb_profile_destroy": (i32, [vp]),
         "msvgb_profile_M": (i32, [vp]),
@@ -354,6 +373,42 @@ def search_host(ctx: Context, prof: DeviceProfile, seqs: F.SeqSet, F1: float = 0
     _check(lib().msvgb_search_host(ctx.h, prof.h, codes.ctypes.data, off.ctypes.data, seqs.n, F1,
                                    chunk_residues, xj.ctypes.data, fl.ctypes.data))
     return xj, fl
+
+
+class DeviceVProfile:
+    """The ViterbiFilter part of a profile resident on the GPU (msvgb_vprofile)."""
+
+    def __init__(self, ctx: Context, vp: F.VProfile):
+        o, keep = _vom_struct(vp)
+        h = ctypes.c_void_p()
+        _check(lib().msvgb_vprofile_create(ctx.h, ctypes.byref(o), ctypes.byref(h)))
+        self.h, self.ctx, self.vp = h, ctx, vp
+
+    def close(self):
+        if self.h:
+            lib().msvgb_vprofile_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def vitfilter(ctx: Context, vprof: DeviceVProfile, db: DeviceDB, ids=None):
+    """p7_ViterbiFilter on the listed sequences (original indices; all by
+    default). Returns (status uint8 [0 ok, 1 overflow, 2 empty], score
+    float32 nats) per listed sequence."""
+    ids = np.arange(db.n, dtype=np.int64) if ids is None else np.ascontiguousarray(ids, dtype=np.int64)
+    xc = np.zeros(ids.size, np.int32)
+    st = np.zeros(ids.size, np.uint8)
+    _check(lib().msvgb_vitfilter(ctx.h, vprof.h, db.h, ids.ctypes.data if ids.size else None, ids.size,
+                                 xc.ctypes.data, st.ctypes.data))
+    o, keep = _vom_struct(vprof.vp)
+    sc = np.array([lib().msvgb_vit_score(int(xc[j]), int(st[j]), int(db.lengths[ids[j]]), ctypes.byref(o))
+                   for j in range(ids.size)], np.float32)
+    return st, sc
 
 
 def search(ctx: Context, prof: DeviceProfile, db: DeviceDB, F1: float = 0.02):

@@ -42,12 +42,6 @@ static std::atomic<uint64_t> g_launches{0};
 namespace msvgb_detail {
 int fail(int code, const std::string &msg) { g_err = msg; return code; }
 }  // namespace msvgb_detail
-#define CUDA_TRY(expr)                                                                       \
-  do {                                                                                       \
-    cudaError_t _e = (expr);                                                                 \
-    if (_e != cudaSuccess)                                                                   \
-      return fail(MSVGB_eslESYS, std::string(#expr) + ": " + cudaGetErrorString(_e));         \
-  } while (0)
 
 extern "C" const char *msvgb_last_error(void) { return g_err.c_str(); }
 extern "C" uint64_t msvgb_kernel_launches(void) { return g_launches.load(); }
@@ -724,6 +718,7 @@ extern "C" int msvgb_db_destroy(msvgb_db *db) {
   cudaSetDevice(db->device);
   cudaFree(db->d_codes); cudaFree(db->d_start); cudaFree(db->d_orig); cudaFree(db->d_len);
   if (db->ready) cudaEventDestroy(db->ready);
+  cudaFree(db->d_inv);
   delete db;
   return MSVGB_eslOK;
 }

@@ -82,6 +82,7 @@ struct msvgb_db {
   int64_t n_long = 0;                 // sequences of length >= kLongTarget (they sort first)
   int64_t packed_bytes = 0;           // size of d_codes
   cudaEvent_t ready = nullptr;        // set when packed asynchronously: completes when the data is in place
+  int64_t *d_inv = nullptr;           // original index -> sorted slot, built on first use
 };
 
 // Targets this long are scored with 32 lanes per sequence even when the
@@ -144,6 +145,9 @@ cudaError_t launch_lengths(const int64_t *off, int64_t n, int32_t *len, unsigned
                            cudaStream_t stream);
 cudaError_t launch_histogram(const int32_t *len, int64_t n, unsigned long long *hist, int num_sms,
                              cudaStream_t stream);
+// inv[orig[s]] = s (original index -> sorted slot); ids[j] = inv[ids[j]].
+cudaError_t launch_invert(const int64_t *orig, int64_t n, int64_t *inv, int num_sms, cudaStream_t stream);
+cudaError_t launch_gather_ids(int64_t *ids, int64_t n, const int64_t *inv, int num_sms, cudaStream_t stream);
 cudaError_t launch_bins(const unsigned long long *hist, int Lmax, int64_t *bin_slot, int64_t *bin_byte, int64_t *pos,
                         uint8_t *codes, cudaStream_t stream);
 // Stream-ordered scratch allocations of database creation come from this
@@ -154,3 +158,13 @@ cudaError_t launch_place(const int64_t *off, const int32_t *len_in, int64_t n, u
                          const int64_t *bin_slot, const int64_t *bin_byte, int64_t *start, int64_t *orig,
                          int32_t *len, int64_t *src, int num_sms, cudaStream_t stream);
 }  // namespace msvgb_detail
+
+// Returns eslESYS (with the failing call in the message) from the enclosing
+// function when a CUDA call fails.
+#define CUDA_TRY(expr)                                                                       \
+  do {                                                                                       \
+    cudaError_t _e = (expr);                                                                 \
+    if (_e != cudaSuccess)                                                                   \
+      return fail(MSVGB_eslESYS, std::string(#expr) + ": " + cudaGetErrorString(_e));         \
+  } while (0)
+

@@ -139,6 +139,20 @@ bins_kernel(const unsigned long long *__restrict__ hist, int Lmax, int64_t *__re
   if (t < 64) codes[pos + t] = (uint8_t) msvgb::PAD_CODE;
 }
 
+// inv[orig[s]] = s: original index -> sorted slot
+__global__ void __launch_bounds__(256)
+invert_kernel(const int64_t *__restrict__ orig, int64_t n, int64_t *__restrict__ inv) {
+  for (int64_t s = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (int64_t) gridDim.x * blockDim.x)
+    inv[orig[s]] = s;
+}
+
+// ids[j] = inv[ids[j]]
+__global__ void __launch_bounds__(256)
+gather_ids_kernel(int64_t *__restrict__ ids, int64_t n, const int64_t *__restrict__ inv) {
+  for (int64_t j = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t) gridDim.x * blockDim.x)
+    ids[j] = inv[ids[j]];
+}
+
 int grid_for(int64_t n, int num_sms) {
   const long long blocks = std::min<long long>((n + 255) / 256, (long long) num_sms * 8);
   return (int) std::max<long long>(1, blocks);
@@ -159,6 +173,22 @@ cudaError_t msvgb_detail::launch_histogram(const int32_t *len, int64_t n, unsign
   if (n == 0) return cudaSuccess;
   (void) cudaGetLastError();
   hist_kernel<<<grid_for(n, num_sms), 256, 0, stream>>>(len, n, hist);
+  return cudaGetLastError();
+}
+
+cudaError_t msvgb_detail::launch_invert(const int64_t *orig, int64_t n, int64_t *inv, int num_sms,
+                                        cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  (void) cudaGetLastError();
+  invert_kernel<<<grid_for(n, num_sms), 256, 0, stream>>>(orig, n, inv);
+  return cudaGetLastError();
+}
+
+cudaError_t msvgb_detail::launch_gather_ids(int64_t *ids, int64_t n, const int64_t *inv, int num_sms,
+                                            cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  (void) cudaGetLastError();
+  gather_ids_kernel<<<grid_for(n, num_sms), 256, 0, stream>>>(ids, n, inv);
   return cudaGetLastError();
 }
 

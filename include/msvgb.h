@@ -140,6 +140,37 @@ int msvgb_tune_load(msvgb_ctx *ctx, const char *path);
  * table type for 32 lanes (1 f16, 0 int8). */
 int msvgb_tune_lanes(msvgb_ctx *ctx, int M, int L, int *ret_variant);
 
+/* ---- the stage after MSV: p7_ViterbiFilter (src/impl_sse/vitfilter.c:84-250) ------
+ * The ViterbiFilter part of a P7_OPROFILE (src/impl_sse/impl_sse.h:88-96) as
+ * vf_conversion stores it (src/impl_sse/p7_oprofile.c:653-760): Q8 =
+ * max(2, ceil(M/8)); twv = 8*Q8 vectors of 8 int16 (per q: BM MM IM DM MD MI
+ * II, then the Q8 DD vectors), rwv = Kp*Q8 vectors; element z of vector q is
+ * node q+1+z*Q8; xw[E,N,J,C][MOVE,LOOP] as configured (the N/J/C move cost is
+ * recomputed per target length, p7_oprofile_ReconfigRestLength). */
+typedef struct {
+  int            M;
+  int            Kp;                 /* 29 (amino) */
+  const int16_t *twv;
+  const int16_t *rwv;
+  int16_t        xw[4][2];
+  float          scale_w, nj;
+  int16_t        base_w, ddbound_w;
+} msvgb_vom;
+typedef struct msvgb_vprofile msvgb_vprofile;
+/* Models up to 1536 nodes. */
+int msvgb_vprofile_create(msvgb_ctx *ctx, const msvgb_vom *vom, msvgb_vprofile **ret);
+int msvgb_vprofile_destroy(msvgb_vprofile *vp);
+/* p7_ViterbiFilter on the listed sequences of db (ids: original indices, e.g.
+ * the MSV survivors): out_xc[j] the final xC, out_status[j] 0 ok, 1 overflow
+ * (eslERANGE: +inf), 2 empty. One warp per sequence; bit-exact with the
+ * reference's int16 saturating filter, lazy F included. */
+int msvgb_vitfilter(msvgb_ctx *ctx, msvgb_vprofile *vp, const msvgb_db *db, const int64_t *ids, int64_t nids,
+                    int *out_xc, uint8_t *out_status);
+/* The filter score in nats from xC (vitfilter.c:240-247, exact float
+ * expressions) and the per-length N/J/C move cost. */
+float   msvgb_vit_score(int xc, int status, int L, const msvgb_vom *vom);
+int16_t msvgb_vit_move_cost(float scale_w, float nj, int L);
+
 /* ---- on-disk formats ------------------------------------------------------------
  * Pressed MSV profiles (.h3f, the MSV file hmmpress writes: HMMER 3/f binary,
  * x86-64 little-endian). Replaces p7_oprofile_ReadMSV (src/impl_sse/io.c:233)

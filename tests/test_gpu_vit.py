@@ -1,0 +1,76 @@
+"""The ViterbiFilter stage on the GPU (msvgb_vitfilter) against
+p7_ViterbiFilter's own golden results and the oracle: statuses and score bit
+patterns, for sampled models in hmmsearch's local mode and the tutorial Pfam
+models, over all sequences and over survivor lists."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from cudahmmsearch_gb300 import api
+from cudahmmsearch_gb300 import formats as F
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+VIT = sorted(os.path.basename(p)[4:-6] for p in glob.glob(os.path.join(GOLDEN, "vit_*.vprof")))
+MAX_M = 1536
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = api.Context(0)
+    yield c
+    c.close()
+
+
+def expected(st_ref):
+    """Golden statuses (eslOK 0, eslERANGE 16, -1 empty) as msvgb_vitfilter reports them."""
+    return np.where(st_ref == 16, 1, np.where(st_ref < 0, 2, 0)).astype(np.uint8)
+
+
+@pytest.mark.parametrize("name", VIT)
+def test_vitfilter_matches_reference_golden(ctx, name):
+    vp = F.read_vprofile(os.path.join(GOLDEN, "vit_" + name + ".vprof"))
+    s = F.read_seqs(os.path.join(GOLDEN, name + ".seqs"))
+    st_ref, sc_ref = F.read_vresults(os.path.join(GOLDEN, "vit_" + name + ".vres"))
+    if vp.M > MAX_M:
+        with pytest.raises(api.MSVError) as e:
+            api.DeviceVProfile(ctx, vp)
+        assert e.value.code == api.eslEINVAL
+        return
+    dvp = api.DeviceVProfile(ctx, vp)
+    db = api.DeviceDB(ctx, s)
+    st, sc = api.vitfilter(ctx, dvp, db)
+    assert np.array_equal(st, expected(st_ref))
+    ok = st_ref == 0
+    assert np.array_equal(sc[ok].view(np.uint32), sc_ref[ok].view(np.uint32))
+    # a survivor-style list: every other sequence, in reverse order
+    ids = np.arange(s.n - 1, -1, -2)
+    st2, sc2 = api.vitfilter(ctx, dvp, db, ids)
+    assert np.array_equal(st2, st[ids]) and np.array_equal(sc2.view(np.uint32), sc[ids].view(np.uint32))
+
+
+@pytest.mark.parametrize("name", ["m200_s1", "m400_s1", "tut_pkinase", "m777_s3"])
+def test_vitfilter_matches_oracle_on_homologs_and_long_targets(ctx, name):
+    vp = F.read_vprofile(os.path.join(GOLDEN, "vit_" + name + ".vprof"))
+    p = F.read_profile(os.path.join(GOLDEN, name + ".prof"))
+    s = F.SeqSet.concat([F.synth_sequences(400, seed=vp.M, lmax=6000), F.emit_homologs(p, 60, seed=vp.M + 1),
+                         F.emit_homologs(p, 10, seed=vp.M + 2, repeat=5)])
+    o = O.vit_batch(vp, s)
+    st, sc = api.vitfilter(ctx, api.DeviceVProfile(ctx, vp), api.DeviceDB(ctx, s))
+    assert np.array_equal(st, expected(o["status"]))
+    ok = o["status"] == 0
+    assert np.array_equal(sc[ok].view(np.uint32), o["sc"][ok].view(np.uint32))
+    assert (st == 0).sum() >= 300
+    if name == "tut_pkinase":                # Pfam homologs saturate the 16-bit range
+        assert (st[400:] == 1).sum() == 70
+
+
+def test_vitfilter_rejects_bad_indices(ctx):
+    vp = F.read_vprofile(os.path.join(GOLDEN, "vit_m50_s1.vprof"))
+    db = api.DeviceDB(ctx, F.synth_sequences(10, seed=2))
+    with pytest.raises(api.MSVError) as e:
+        api.vitfilter(ctx, api.DeviceVProfile(ctx, vp), db, np.array([3, 10]))
+    assert e.value.code == api.eslEINVAL
