@@ -261,6 +261,42 @@ def read_vresults(path):
     return st, sc
 
 
+@dataclasses.dataclass
+class PipeResults:
+    """The filter stages of p7_Pipeline on a sequence set (PIPERES1)."""
+    M: int
+    compo: np.ndarray          # float32[20], the model composition (P7_OPROFILE compo)
+    mmu: float
+    mlambda: float
+    vmu: float
+    vlambda: float
+    F1: float
+    F2: float
+    nullsc: np.ndarray         # float32[n]
+    usc: np.ndarray            # float32[n], MSV score
+    fsc: np.ndarray            # float32[n], bias-filter score (every sequence)
+    vfsc: np.ndarray           # float32[n], ViterbiFilter score (NaN where not run)
+    stage: np.ndarray          # uint8[n]: 0 rejected by MSV, 1 by the bias filter, 2 by Viterbi, 3 passed, 255 empty
+
+
+def read_pipe(path) -> PipeResults:
+    """PIPERES1: int32 M; float compo[20]; float mmu, mlambda, vmu, vlambda;
+    double F1, F2; int64 n; float nullsc[n], usc[n], fsc[n], vfsc[n]; uint8 stage[n]."""
+    b = open(path, "rb").read()
+    if b[:8] != b"PIPERES1":
+        raise ValueError(f"{path}: not a PIPERES1 file")
+    M = int(np.frombuffer(b, np.int32, 1, 8)[0])
+    compo = np.frombuffer(b, np.float32, 20, 12).copy()
+    ev = np.frombuffer(b, np.float32, 4, 92)
+    F = np.frombuffer(b, np.float64, 2, 108)
+    n = int(np.frombuffer(b, np.int64, 1, 124)[0])
+    o = 132
+    arr = [np.frombuffer(b, np.float32, n, o + 4 * n * k).copy() for k in range(4)]
+    stage = np.frombuffer(b, np.uint8, n, o + 16 * n).copy()
+    return PipeResults(M, compo, float(ev[0]), float(ev[1]), float(ev[2]), float(ev[3]), float(F[0]), float(F[1]),
+                       arr[0], arr[1], arr[2], arr[3], stage)
+
+
 def synth_sequences(n: int, *, seed: int, median: float = 300.0, sigma: float = 0.7,
                     lmin: int = 10, lmax: int = 5000, x_frac: float = 0.005,
                     uniform_frac: float = 0.0, uniform_range=(5000, 35000)) -> SeqSet:

@@ -3,8 +3,10 @@
 Loads oracle/libmsvoracle.so, the scalar C restatement of HMMER 3.1b1's
 p7_MSVFilter (src/impl_sse/msvfilter.c:77-213, with the SSV fast path of
 src/impl_sse/ssvfilter.c:1364-1413), of the MSV stage of p7_Pipeline
-(src/p7_pipeline.c:662-677) and of p7_ViterbiFilter
-(src/impl_sse/vitfilter.c:84-250). Only tests/, __graft_entry__.smoke() and the
+(src/p7_pipeline.c:662-677), of p7_ViterbiFilter
+(src/impl_sse/vitfilter.c:84-250), of the bias filter p7_bg_FilterScore
+(src/p7_bg.c:473) and of the filter-stage gates of p7_Pipeline
+(src/p7_pipeline.c:666-705). Only tests/, __graft_entry__.smoke() and the
 CPU-baseline leg of bench.py may import this module.
 """
 from __future__ import annotations
@@ -22,8 +24,9 @@ LIB_PATH = os.path.join(HERE, "libmsvoracle.so")
 def build(force: bool = False) -> str:
     """Compiles the scalar oracle (msv_oracle.c) and the vectorized port used
     as the timed CPU baseline (msv_port.c) into one library."""
-    srcs = [os.path.join(HERE, "msv_oracle.c"), os.path.join(HERE, "msv_port.c"), os.path.join(HERE, "vit_oracle.c")]
-    hdrs = [os.path.join(HERE, "msv_oracle.h"), os.path.join(HERE, "vit_oracle.h")]
+    srcs = [os.path.join(HERE, "msv_oracle.c"), os.path.join(HERE, "msv_port.c"), os.path.join(HERE, "vit_oracle.c"),
+            os.path.join(HERE, "bias_oracle.c")]
+    hdrs = [os.path.join(HERE, "msv_oracle.h"), os.path.join(HERE, "vit_oracle.h"), os.path.join(HERE, "bias_oracle.h")]
     if force or not os.path.exists(LIB_PATH) or any(os.path.getmtime(LIB_PATH) < os.path.getmtime(f)
                                                     for f in srcs + hdrs):
         subprocess.check_call(["cc", "-O3", "-std=gnu99", "-ffp-contract=off", "-fPIC", "-shared",
@@ -44,6 +47,11 @@ class _VProf(ctypes.Structure):
                 ("scale_w", ctypes.c_float), ("nj", ctypes.c_float),
                 ("base_w", ctypes.c_int16), ("ddbound_w", ctypes.c_int16),
                 ("xw", ctypes.c_int16 * 8), ("twv", ctypes.c_void_p), ("rwv", ctypes.c_void_p)]
+
+
+class _PipeRes(ctypes.Structure):
+    _fields_ = [("usc", ctypes.c_float), ("nullsc", ctypes.c_float), ("filtersc", ctypes.c_float),
+                ("vfsc", ctypes.c_float), ("stage", ctypes.c_int)]
 
 
 _lib = None
@@ -70,6 +78,14 @@ def lib():
         _lib.orc_vit_filter.restype = ctypes.c_int
         _lib.orc_vit_filter.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(_VProf),
                                         ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int)]
+        _lib.orc_bias_filter.restype = ctypes.c_float
+        _lib.orc_bias_filter.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
+        _lib.orc_gumbel_P.restype = ctypes.c_double
+        _lib.orc_gumbel_P.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_double, ctypes.c_double]
+        _lib.orc_pipe_stages.restype = None
+        _lib.orc_pipe_stages.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_void_p, ctypes.c_int,
+                                         ctypes.POINTER(_VProf), ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                         ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.POINTER(_PipeRes)]
         _lib.orc_msv_batch.restype = ctypes.c_int
         _lib.orc_msv_batch.argtypes = [ctypes.POINTER(_Prof), ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_int64, ctypes.c_double, ctypes.c_int,
@@ -189,3 +205,50 @@ def vit_batch(vp, seqs):
             continue
         st[i], sc[i], xc[i] = vit_filter(vp, seqs.seq(i))
     return {"status": st, "sc": sc, "xc": xc}
+
+
+def _dsq(codes):
+    L = len(codes)
+    dsq = np.empty(L + 2, np.uint8)
+    dsq[0] = dsq[-1] = 255
+    dsq[1:L + 1] = codes
+    return dsq
+
+
+def bias_filter(compo, M: int, dsq_codes) -> float:
+    """p7_bg_FilterScore of one sequence with the filter HMM of the model
+    composition compo[20] and length M."""
+    c = np.ascontiguousarray(compo, dtype=np.float32)
+    dsq = _dsq(dsq_codes)
+    return float(lib().orc_bias_filter(c.ctypes.data, M, dsq.ctypes.data, len(dsq_codes)))
+
+
+def bias_batch(compo, M: int, seqs):
+    """bias_filter over a SeqSet (0 for empty sequences)."""
+    out = np.zeros(seqs.n, np.float32)
+    for i in range(seqs.n):
+        if seqs.lengths[i]:
+            out[i] = bias_filter(compo, M, seqs.seq(i))
+    return out
+
+
+def gumbel_P(sc: float, base: float, mu: float, lam: float) -> float:
+    return float(lib().orc_gumbel_P(sc, base, mu, lam))
+
+
+def pipe_batch(vp, seqs, usc, compo, *, mmu, mlambda, vmu, vlambda, F1=0.02, F2=1e-3, do_bias=True):
+    """The filter stages of p7_Pipeline after the MSV score usc[i] of every
+    sequence: dict of stage (uint8: 0 MSV, 1 bias, 2 Viterbi rejected, 3 passed,
+    255 empty), nullsc, filtersc, vfsc (NaN where Viterbi did not run)."""
+    s, keep = _vprof(vp)
+    c = np.ascontiguousarray(compo, dtype=np.float32)
+    out = {k: np.zeros(seqs.n, np.float32) for k in ("nullsc", "filtersc", "vfsc")}
+    out["stage"] = np.zeros(seqs.n, np.uint8)
+    r = _PipeRes()
+    for i in range(seqs.n):
+        dsq = _dsq(seqs.seq(i))
+        lib().orc_pipe_stages(dsq.ctypes.data, int(seqs.lengths[i]), float(usc[i]), c.ctypes.data, int(do_bias),
+                              ctypes.byref(s), mmu, mlambda, vmu, vlambda, F1, F2, ctypes.byref(r))
+        out["stage"][i] = r.stage
+        out["nullsc"][i], out["filtersc"][i], out["vfsc"][i] = r.nullsc, r.filtersc, r.vfsc
+    return out

@@ -23,6 +23,13 @@
  *   seqfile  : any sequence file Easel reads (esl_sqfile_OpenDigital, format
  *              autodetected, easel/esl_sqio.c:300), digitized with the amino alphabet.
  *
+ *   pipe     : the filter stages of p7_Pipeline (src/p7_pipeline.c:646-705) per sequence,
+ *              after p7_pli_NewModel's p7_bg_SetFilter (src/p7_pipeline.c:480) and
+ *              p7_pli_NewSeq's p7_bg_SetLength: NullOne, MSVFilter and the F1 gate,
+ *              p7_bg_FilterScore (src/p7_bg.c:473) and the F1 gate on it, then
+ *              p7_ViterbiFilter when P > F2 and the F2 gate. Also the bias-filter
+ *              score of every sequence, gated or not. Optionally the MSV
+ *              profile (MSVPROF1) of the model as configured there.
  *   vit      : the ViterbiFilter stage (src/impl_sse/vitfilter.c:84-250) on the same
  *              configured model: its int16 profile part (vf_conversion,
  *              src/impl_sse/p7_oprofile.c:653-760) dumped, and per sequence
@@ -38,6 +45,11 @@
  *                       int16 xw[4][2] (E,N,J,C x MOVE,LOOP, as configured);
  *                       float vmu, vlambda; int16 twv[8*Q8][8]; int16 rwv[Kp][Q8][8]
  *   vres    "VITRES01": int64 n; int32 status[n]; float sc[n]
+ *   pres    "PIPERES1": int32 M; float compo[20]; float mmu, mlambda, vmu, vlambda;
+ *                       double F1, F2; int64 n; float nullsc[n], usc[n], fsc[n] (bias
+ *                       filter score, every sequence), vfsc[n] (NaN where not run);
+ *                       uint8 stage[n] (0 rejected by MSV, 1 by the bias filter,
+ *                       2 by Viterbi, 3 passed Viterbi, 255 empty)
  */
 #include "p7_config.h"
 #include <stdio.h>
@@ -286,6 +298,67 @@ int main(int argc, char **argv)
     FILE *fp = fopen(argv[5], "wb"); if (!fp) die("open vres out");
     fwrite("VITRES01", 1, 8, fp); fwrite(&s.n, 8, 1, fp);
     fwrite(st, 4, s.n, fp); fwrite(sc, 4, s.n, fp);
+    fclose(fp);
+    return 0;
+  }
+  if (!strcmp(cmd, "pipe") || !strcmp(cmd, "pipefile")) {  /* pipe M seed pres seqs [prof] | pipefile hmmfile idx pres seqs [prof] */
+    model_t m;
+    seqs_t s;
+    if (argc != 6 && argc != 7) die("pipe M seed pres seqs [prof] | pipefile hmmfile idx pres seqs [prof]");
+    if (!strcmp(cmd, "pipe")) {
+      make_model(&m, atoi(argv[2]), (uint32_t) atol(argv[3]), 100, p7_LOCAL);
+      /* a sampled HMM has no composition; give it the one hmmbuild would
+       * (p7_hmm_SetComposition, src/p7_hmm.c:625), copied as p7_ProfileConfig
+       * and p7_oprofile_Convert copy it (modelconfig.c:84, p7_oprofile.c:870) */
+      if (p7_hmm_SetComposition(m.hmm) != eslOK) die("p7_hmm_SetComposition");
+      for (int z = 0; z < p7_MAXABET; z++) m.gm->compo[z] = m.om->compo[z] = m.hmm->compo[z];
+    } else file_model(&m, argv[2], atoi(argv[3]), 0);
+    if (argc == 7) write_profile(&m, 100, argv[6]);       /* the MSV part of the same configured model */
+    read_seqs(&s, argv[5]);
+    const double F1 = 0.02, F2 = 1e-3;      /* p7_pipeline.c:210-211 defaults */
+    p7_bg_SetFilter(m.bg, m.om->M, m.om->compo);
+    int64_t maxL = 1;
+    for (int64_t i = 0; i < s.n; i++) if (s.off[i+1] - s.off[i] > maxL) maxL = s.off[i+1] - s.off[i];
+    P7_OMX *ox = p7_omx_Create(m.om->M, 0, 0);
+    ESL_DSQ *dsq = malloc(maxL + 2);
+    float *ns = calloc(s.n, 4), *us = calloc(s.n, 4), *fs = calloc(s.n, 4), *vs = calloc(s.n, 4);
+    uint8_t *stage = calloc(s.n, 1);
+    for (int64_t i = 0; i < s.n; i++) {
+      int L = (int) (s.off[i+1] - s.off[i]);
+      float usc, nullsc, filtersc, vfsc, seq_score;
+      double P;
+      vs[i] = NAN;
+      if (L == 0) { stage[i] = 255; continue; }
+      dsq[0] = eslDSQ_SENTINEL; memcpy(dsq + 1, s.dsq + s.off[i], L); dsq[L+1] = eslDSQ_SENTINEL;
+      p7_bg_SetLength(m.bg, L);
+      p7_oprofile_ReconfigLength(m.om, L);
+      p7_bg_NullOne(m.bg, dsq, L, &nullsc);
+      p7_MSVFilter(dsq, L, m.om, ox, &usc);
+      p7_bg_FilterScore(m.bg, dsq, L, &filtersc);
+      ns[i] = nullsc; us[i] = usc; fs[i] = filtersc;
+      seq_score = (usc - nullsc) / eslCONST_LOG2;
+      P = esl_gumbel_surv(seq_score, m.om->evparam[p7_MMU], m.om->evparam[p7_MLAMBDA]);
+      if (P > F1) { stage[i] = 0; continue; }
+      seq_score = (usc - filtersc) / eslCONST_LOG2;
+      P = esl_gumbel_surv(seq_score, m.om->evparam[p7_MMU], m.om->evparam[p7_MLAMBDA]);
+      if (P > F1) { stage[i] = 1; continue; }
+      if (P > F2) {
+        p7_ViterbiFilter(dsq, L, m.om, ox, &vfsc);
+        vs[i] = vfsc;
+        seq_score = (vfsc - filtersc) / eslCONST_LOG2;
+        P = esl_gumbel_surv(seq_score, m.om->evparam[p7_VMU], m.om->evparam[p7_VLAMBDA]);
+        if (P > F2) { stage[i] = 2; continue; }
+      }
+      stage[i] = 3;
+    }
+    FILE *fp = fopen(argv[4], "wb"); if (!fp) die("open pres out");
+    int32_t M = m.om->M;
+    float ev[4] = { m.om->evparam[p7_MMU], m.om->evparam[p7_MLAMBDA], m.om->evparam[p7_VMU], m.om->evparam[p7_VLAMBDA] };
+    double F[2] = { F1, F2 };
+    fwrite("PIPERES1", 1, 8, fp); fwrite(&M, 4, 1, fp); fwrite(m.om->compo, 4, 20, fp);
+    fwrite(ev, 4, 4, fp); fwrite(F, 8, 2, fp); fwrite(&s.n, 8, 1, fp);
+    fwrite(ns, 4, s.n, fp); fwrite(us, 4, s.n, fp); fwrite(fs, 4, s.n, fp); fwrite(vs, 4, s.n, fp);
+    fwrite(stage, 1, s.n, fp);
     fclose(fp);
     return 0;
   }

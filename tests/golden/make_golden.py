@@ -26,6 +26,17 @@ fn3 / 7LESS_DROME search of tutorial/fn3.out.
 The vit_* files pin the ViterbiFilter stage (vit_NAME.vprof: the model's
 int16 ViterbiFilter profile; vit_NAME.vres: p7_ViterbiFilter status and score
 for every sequence of NAME.seqs).
+The pipe_* files pin the bias filter and the gates of p7_Pipeline around it
+and around the ViterbiFilter (pipe_NAME.seqs: NAME.seqs plus sequences that
+reach the later stages -- local-mode homologs, their shuffles (the model's
+composition without its order), background sequences carrying a short homolog
+fragment, and i.i.d. draws from a homolog's composition; pipe_NAME.pres: the
+reference's p7_bg_FilterScore for every sequence and the stage each one
+reached, ``refgen pipe`` / ``refgen pipefile``; for the sampled models also
+pipe_NAME.prof, the MSV part of the model in hmmsearch's local configuration,
+and the composition hmmbuild would give the model). Sequences drawn from the
+model's commonest residues, or a homolog fragment in model-composition
+flanks, are what the bias filter rejects.
 Run:  python tests/golden/make_golden.py [reference code dir]
 """
 import os
@@ -140,6 +151,70 @@ def make_vit(tut):
     print("vit goldens:", len(VIT_SAMPLED) + len(TUT_MODELS))
 
 
+# pipeline goldens: sampled models in hmmsearch's local mode, and the tutorial models
+PIPE_SAMPLED = ["m50_s1", "m200_s1", "m400_s1", "m777_s3"]
+MODE_LOCAL = 1
+
+
+def pipe_extras(hom, seed, compo):
+    """Sequences for the later filter stages, built from homologs hom and the
+    model composition compo."""
+    rng = np.random.default_rng(seed)
+    out = [hom.seq(i) for i in range(hom.n)]
+    for i in range(hom.n):                                       # shuffles: composition only
+        h = hom.seq(i)
+        out.append(rng.permutation(np.tile(h, 1 + (i % 3))))
+    bg = F.synth_sequences(hom.n, seed=seed + 1, lmax=3000)
+    for i in range(hom.n):                                       # a short homolog fragment in background
+        h, b = hom.seq(i), bg.seq(i)
+        w = int(rng.integers(8, 48))
+        a = int(rng.integers(0, max(1, len(h) - w)))
+        c = int(rng.integers(0, len(b) + 1))
+        out.append(np.concatenate([b[:c], h[a:a + w], b[c:]]))
+    for i in range(hom.n // 2):                                  # i.i.d. draws from a homolog's composition
+        h = hom.seq(i)
+        out.append(rng.choice(h, size=int(rng.integers(50, 1500))).astype(np.uint8))
+    top = np.argsort(-compo)
+    for k in (2, 3, 5):                                          # the model's k commonest residues: bias-filter rejects
+        pr = compo[top[:k]] / compo[top[:k]].sum()
+        for _ in range(8):
+            out.append(rng.choice(top[:k], size=int(rng.integers(100, 2000)), p=pr).astype(np.uint8))
+    pr = compo / compo.sum()
+    for i in range(hom.n // 2):                                  # a homolog fragment in model-composition flanks
+        h = hom.seq(i)
+        f = rng.choice(20, size=int(rng.integers(200, 1500)), p=pr).astype(np.uint8)
+        c = int(rng.integers(0, len(f)))
+        w = int(rng.integers(10, 30))
+        a = int(rng.integers(0, max(1, len(h) - w)))
+        out.append(np.concatenate([f[:c], h[a:a + w], f[c:]]))
+    return F.SeqSet.from_list(out)
+
+
+def make_pipe(tut):
+    tmp = os.path.join(HERE, "_tmp.seqs")
+    jobs = []
+    for k, name in enumerate(PIPE_SAMPLED):
+        M, seed = name[1:].split("_s")
+        run("emit", M, seed, 100, MODE_LOCAL, 24, 500 + k, 1, tmp)
+        jobs.append((name, ("pipe", M, seed), F.read_seqs(tmp)))
+    for k, (name, idx) in enumerate(TUT_MODELS):
+        run("emitfile", os.path.join(tut, "minifam"), idx, 24, 600 + k, tmp)
+        jobs.append((name, ("pipefile", os.path.join(tut, "minifam"), idx), F.read_seqs(tmp)))
+    os.remove(tmp)
+    for k, (name, cmd, hom) in enumerate(jobs):
+        base = os.path.join(HERE, name + ".seqs")
+        seqs = os.path.join(HERE, "pipe_" + name + ".seqs")
+        pres = os.path.join(HERE, "pipe_" + name + ".pres")
+        prof = [os.path.join(HERE, "pipe_" + name + ".prof")] if cmd[0] == "pipe" else []
+        run(*cmd, pres, base, *prof)                             # first pass: the model's composition
+        s = F.SeqSet.concat([F.read_seqs(base), pipe_extras(hom, 700 + 10 * k, F.read_pipe(pres).compo)])
+        F.write_seqs(s, seqs)
+        run(*cmd, pres, seqs, *prof)
+        r = F.read_pipe(pres)
+        print(f"pipe_{name}: n={s.n} stages={np.bincount(r.stage[r.stage < 4], minlength=4).tolist()} "
+              f"vit_run={int(np.isfinite(r.vfsc).sum())}")
+
+
 def main():
     if not os.path.exists(REFGEN):
         sys.exit("oracle/_ref/refgen missing: make -C oracle/ref REF=<reference>/code")
@@ -148,6 +223,7 @@ def main():
         make_case(*c)
     make_tutorial(os.path.join(ref, "tutorial"))
     make_vit(os.path.join(ref, "tutorial"))
+    make_pipe(os.path.join(ref, "tutorial"))
 
 
 if __name__ == "__main__":
