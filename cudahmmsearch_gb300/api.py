@@ -18,7 +18,7 @@ from . import formats as F
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libmsvgb.so")
 
-eslOK, eslEMEM, eslEINVAL, eslESYS, eslERANGE = 0, 5, 11, 12, 16
+eslOK, eslFAIL, eslEMEM, eslEINVAL, eslESYS, eslERANGE = 0, 1, 5, 11, 12, 16
 eslEOF, eslENOTFOUND, eslEFORMAT, eslEINCOMPAT, eslEWRITE = 3, 6, 7, 10, 27
 FLAG_ERANGE, FLAG_PASS, FLAG_FULL, FLAG_EMPTY = 0x01, 0x02, 0x04, 0x08
 
@@ -38,6 +38,7 @@ EXPORTS = [
     "msvgb_seqs_n", "msvgb_seqs_codes", "msvgb_seqs_offsets", "msvgb_seqs_name", "msvgb_seqs_free",
     "msvgb_db_save", "msvgb_db_load", "msvgb_db_lengths", "msvgb_search_host",
     "msvgb_vprofile_create", "msvgb_vprofile_destroy", "msvgb_vitfilter", "msvgb_vit_score", "msvgb_vit_move_cost",
+    "msvgb_biasfilter", "msvgb_bias_length_term", "msvgb_null_score", "msvgb_stage_pass", "msvgb_pipeline_filters",
 ]
 
 
@@ -65,6 +66,21 @@ def _vom_struct(vp: F.VProfile):
     rwv = np.ascontiguousarray(vp.rwv, dtype=np.int16)
     xw = (ctypes.c_int16 * 8)(*[int(v) for v in np.asarray(vp.xw).reshape(-1)])
     return _VOm(vp.M, vp.Kp, twv.ctypes.data, rwv.ctypes.data, xw, vp.scale_w, vp.nj, vp.base_w, vp.ddbound_w), (twv, rwv)
+
+
+class _Filters(ctypes.Structure):
+    _fields_ = [("om", ctypes.POINTER(_Om)), ("vom", ctypes.POINTER(_VOm)), ("compo", ctypes.c_void_p),
+                ("vmu", ctypes.c_float), ("vlambda", ctypes.c_float), ("F1", ctypes.c_double), ("F2", ctypes.c_double)]
+
+
+class FilterHit(ctypes.Structure):
+    _fields_ = [("seq_index", ctypes.c_int64), ("usc", ctypes.c_float), ("nullsc", ctypes.c_float),
+                ("filtersc", ctypes.c_float), ("vfsc", ctypes.c_float)]
+
+
+class FilterStats(ctypes.Structure):
+    _fields_ = [("nseqs", ctypes.c_int64), ("nres", ctypes.c_int64), ("n_past_msv", ctypes.c_int64),
+                ("n_past_bias", ctypes.c_int64), ("n_past_vit", ctypes.c_int64)]
 
 
 class _Omx(ctypes.Structure):
@@ -147,6 +163,12 @@ def lib():
         "msvgb_server_destroy": (i32, [vp]),
         "msvgb_pipeline_run": (i32, [vp, ctypes.POINTER(_Om), vp, vp, i64, i64, f64, i32, vp, vp,
                                      ctypes.POINTER(i64)]),
+        "msvgb_biasfilter": (i32, [vp, vp, i32, vp, vp, i64, vp]),
+        "msvgb_bias_length_term": (f32, [f32, i32]),
+        "msvgb_null_score": (f32, [i32]),
+        "msvgb_stage_pass": (i32, [f32, f32, f64, f64, f64, ctypes.POINTER(f64)]),
+        "msvgb_pipeline_filters": (i32, [vp, ctypes.POINTER(_Filters), vp, vp, i64, i64, i32, vp, vp,
+                                         ctypes.POINTER(FilterStats)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -411,6 +433,25 @@ def vitfilter(ctx: Context, vprof: DeviceVProfile, db: DeviceDB, ids=None):
     return st, sc
 
 
+def biasfilter(ctx: Context, compo, M: int, db: DeviceDB, ids=None):
+    """p7_bg_FilterScore on the listed sequences (original indices; all by
+    default) with the filter HMM of model composition compo[20] and length M.
+    Returns float32 scores in nats."""
+    ids = np.arange(db.n, dtype=np.int64) if ids is None else np.ascontiguousarray(ids, dtype=np.int64)
+    c = np.ascontiguousarray(compo, dtype=np.float32)
+    out = np.zeros(ids.size, np.float32)
+    _check(lib().msvgb_biasfilter(ctx.h, c.ctypes.data, M, db.h, ids.ctypes.data if ids.size else None, ids.size,
+                                  out.ctypes.data))
+    return out
+
+
+def stage_pass(sc: float, base: float, mu: float, lam: float, F: float):
+    """The pipeline gate: (passes, P) for P = esl_gumbel_surv((sc - base) / log 2, mu, lambda)."""
+    P = ctypes.c_double()
+    r = lib().msvgb_stage_pass(sc, base, mu, lam, F, ctypes.byref(P))
+    return bool(r), P.value
+
+
 def search(ctx: Context, prof: DeviceProfile, db: DeviceDB, F1: float = 0.02):
     """Plain path: one profile, one launch. Returns (xj uint8[n], flags uint8[n])."""
     xj = np.zeros(db.n, np.uint8)
@@ -558,6 +599,49 @@ def pipeline_run(ctx: Context, p: F.Profile, seqs: F.SeqSet, on_survivor=None, *
                                     block_size, F1, n_workers, ctypes.cast(cb, ctypes.c_void_p) if cb else None,
                                     None, ctypes.byref(n_past)))
     return n_past.value
+
+
+FILTER_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(FilterHit))
+
+
+def pipeline_filters(ctx: Context, p: F.Profile, seqs: F.SeqSet, *, vprof: F.VProfile | None = None, compo=None,
+                     vmu: float = 0.0, vlambda: float = 0.0, on_hit=None, block_size: int = 100_000,
+                     F1: float = 0.02, F2: float = 1e-3, n_workers: int = 4):
+    """The filter stages of p7_Pipeline on the GPU (msvgb_pipeline_filters):
+    MSV, bias filter (when compo is given), ViterbiFilter (when vprof is
+    given). on_hit(seq_index, usc, nullsc, filtersc, vfsc) runs on the worker
+    threads for every sequence past the last stage; without on_hit the hits
+    are collected. Returns (hits: structured array sorted by seq_index,
+    stats: FilterStats)."""
+    o, keep = _om_struct(p)
+    vo, vkeep = _vom_struct(vprof) if vprof is not None else (None, None)
+    c = np.ascontiguousarray(compo, dtype=np.float32) if compo is not None else None
+    f = _Filters(ctypes.pointer(o), ctypes.pointer(vo) if vo is not None else None,
+                 c.ctypes.data if c is not None else None, vmu, vlambda, F1, F2)
+    codes = np.ascontiguousarray(seqs.codes, dtype=np.uint8)
+    if codes.size == 0:
+        codes = np.zeros(1, np.uint8)
+    off = np.ascontiguousarray(seqs.off, dtype=np.int64)
+    got = []
+    import threading
+    lk = threading.Lock()
+
+    def _cb(user, h):
+        h = h.contents
+        if on_hit is not None:
+            return 1 if on_hit(int(h.seq_index), h.usc, h.nullsc, h.filtersc, h.vfsc) else 0
+        with lk:
+            got.append((h.seq_index, h.usc, h.nullsc, h.filtersc, h.vfsc))
+        return 0
+    cb = FILTER_FN(_cb)
+    stats = FilterStats()
+    _check(lib().msvgb_pipeline_filters(ctx.h, ctypes.byref(f), codes.ctypes.data, off.ctypes.data, seqs.n,
+                                        block_size, n_workers, ctypes.cast(cb, ctypes.c_void_p), None,
+                                        ctypes.byref(stats)))
+    dt = np.dtype([("seq_index", np.int64), ("usc", np.float32), ("nullsc", np.float32),
+                   ("filtersc", np.float32), ("vfsc", np.float32)])
+    hits = np.array(sorted(got), dtype=dt)
+    return hits, stats
 
 
 def tjb_b(scale_b: float, L: int) -> int:

@@ -38,6 +38,7 @@ struct msvgb_ctx {
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   TuneTable *tune = nullptr;                            // lane counts measured by msvgb_autotune
   std::mutex tune_mu;
+  std::mutex mu_inv;                                    // builds of a database's inverse order
 };
 
 // Per-length tables of a profile at one F1 threshold: tjb_b(L) and the
@@ -91,6 +92,9 @@ struct msvgb_db {
 constexpr int kLongTarget = 2400;
 
 namespace msvgb_detail {
+// The database's original-index -> sorted-slot table (db->d_inv), built on
+// the context's stream at first use.
+cudaError_t ensure_inverse(msvgb_ctx *c, const msvgb_db *db);
 // HMMER's amino background frequencies, Easel code order A..Y (msv_sample.cu).
 extern const float kAminoBg[20];
 // Records msg as the calling thread's last error and returns code.

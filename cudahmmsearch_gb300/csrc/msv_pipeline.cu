@@ -12,6 +12,7 @@
 // Forward, domain definition). Upload and search of block k+1 overlap the CPU
 // work on block k.
 #include <atomic>
+#include <cmath>
 #include <condition_variable>
 #include <deque>
 #include <mutex>
@@ -105,6 +106,155 @@ extern "C" int msvgb_pipeline_run(msvgb_ctx *ctx, const msvgb_om *om, const uint
   for (Block *b : q) delete b;
   msvgb_profile_destroy(prof);
   if (ret_n_past_msv) *ret_n_past_msv = n_past.load();
+  if (st == MSVGB_eslOK && abort_flag.load()) return fail(MSVGB_eslFAIL, "the continuation asked to stop");
+  return st;
+}
+
+// ---- the filter stages after MSV on the GPU -----------------------------------------
+
+namespace {
+
+struct HitBlock {
+  std::vector<msvgb_filter_hit> hits;
+};
+
+// The bias and Viterbi stages of one block (sequences b0 .. b0 + nb of the
+// caller's arrays, resident as db). keep: local indices and MSV scores of the
+// F1 survivors. Appends the sequences past the last stage to out.
+int filter_block(msvgb_ctx *ctx, const msvgb_filters *f, msvgb_vprofile *vp, const msvgb_db *db, int64_t b0,
+                 const int64_t *off, const std::vector<int64_t> &keep, const std::vector<float> &usc,
+                 msvgb_filter_stats &stats, std::vector<msvgb_filter_hit> &out) {
+  const size_t ns = keep.size();
+  std::vector<float> fsc(ns), nsc(ns);
+  std::vector<double> P(ns);
+  for (size_t j = 0; j < ns; ++j) nsc[j] = msvgb_null_score((int) (off[b0 + keep[j] + 1] - off[b0 + keep[j]]));
+  if (f->compo) {
+    int st = msvgb_biasfilter(ctx, f->compo, f->om->M, db, keep.data(), (int64_t) ns, fsc.data());
+    if (st != MSVGB_eslOK) return st;
+  } else {
+    fsc = nsc;                                                   // --nobias: filtersc = nullsc
+  }
+  std::vector<size_t> past;                                      // indices into keep
+  for (size_t j = 0; j < ns; ++j)
+    if (msvgb_stage_pass(usc[j], fsc[j], f->om->mmu, f->om->mlambda, f->F1, &P[j])) past.push_back(j);
+  stats.n_past_bias += (int64_t) past.size();
+  std::vector<int64_t> vids;
+  std::vector<size_t> vpos;
+  auto hit = [&](size_t j, float vfsc) {
+    msvgb_filter_hit h;
+    h.seq_index = b0 + keep[j];
+    h.usc = usc[j]; h.nullsc = nsc[j]; h.filtersc = fsc[j]; h.vfsc = vfsc;
+    out.push_back(h);
+  };
+  for (size_t j : past) {
+    if (f->vom && P[j] > f->F2) { vids.push_back(keep[j]); vpos.push_back(j); }
+    else hit(j, NAN);                                            // Viterbi skipped: counts as passed
+  }
+  if (!f->vom) return MSVGB_eslOK;
+  int64_t passed = (int64_t) (past.size() - vids.size());
+  if (!vids.empty()) {
+    std::vector<int> xc(vids.size());
+    std::vector<uint8_t> vst(vids.size());
+    int st = msvgb_vitfilter(ctx, vp, db, vids.data(), (int64_t) vids.size(), xc.data(), vst.data());
+    if (st != MSVGB_eslOK) return st;
+    for (size_t t = 0; t < vids.size(); ++t) {
+      const size_t j = vpos[t];
+      const int L = (int) (off[b0 + keep[j] + 1] - off[b0 + keep[j]]);
+      const float vfsc = msvgb_vit_score(xc[t], vst[t], L, f->vom);
+      if (msvgb_stage_pass(vfsc, fsc[j], f->vmu, f->vlambda, f->F2, nullptr)) {
+        hit(j, vfsc);
+        ++passed;
+      }
+    }
+  }
+  stats.n_past_vit += passed;
+  return MSVGB_eslOK;
+}
+
+}  // namespace
+
+extern "C" int msvgb_pipeline_filters(msvgb_ctx *ctx, const msvgb_filters *f, const uint8_t *codes,
+                                      const int64_t *off, int64_t n, int64_t block_size, int n_workers,
+                                      msvgb_filter_fn fn, void *user, msvgb_filter_stats *ret_stats) {
+  if (!ctx || !f || !f->om || (n > 0 && (!codes || !off)) || block_size < 1 || n < 0)
+    return fail(MSVGB_eslEINVAL, "msvgb_pipeline_filters: bad arguments");
+  if (f->vom && f->vom->M != f->om->M) return fail(MSVGB_eslEINVAL, "MSV and Viterbi parts of different models");
+  if (n_workers < 1) n_workers = 1;
+  msvgb_profile *prof = nullptr;
+  msvgb_vprofile *vp = nullptr;
+  int st = msvgb_profile_create(ctx, f->om, &prof);
+  if (st == MSVGB_eslOK && f->vom) st = msvgb_vprofile_create(ctx, f->vom, &vp);
+  if (st != MSVGB_eslOK) { msvgb_profile_destroy(prof); return st; }
+
+  msvgb_filter_stats stats{};
+  std::mutex mu;
+  std::condition_variable cv_push, cv_pop;
+  std::deque<HitBlock *> q;
+  const size_t qcap = 2;
+  bool producing = true;
+  std::atomic<int> abort_flag{0};
+  auto worker = [&]() {
+    for (;;) {
+      HitBlock *b = nullptr;
+      {
+        std::unique_lock<std::mutex> lk(mu);
+        cv_pop.wait(lk, [&] { return !q.empty() || !producing; });
+        if (q.empty()) return;
+        b = q.front();
+        q.pop_front();
+      }
+      cv_push.notify_one();
+      for (const msvgb_filter_hit &h : b->hits) {
+        if (abort_flag.load()) break;
+        if (fn && fn(user, &h) != 0) abort_flag.store(1);
+      }
+      delete b;
+    }
+  };
+  std::vector<std::thread> workers;
+  for (int t = 0; t < n_workers; ++t) workers.emplace_back(worker);
+
+  std::vector<uint8_t> xj, fl;
+  for (int64_t b0 = 0; b0 < n && st == MSVGB_eslOK && !abort_flag.load(); b0 += block_size) {
+    const int64_t b1 = std::min(n, b0 + block_size), nb = b1 - b0;
+    xj.resize(nb); fl.resize(nb);
+    msvgb_db *db = nullptr;
+    st = msvgb_db_create(ctx, codes, off + b0, nb, &db);
+    if (st == MSVGB_eslOK) st = msvgb_search(ctx, prof, db, f->F1, xj.data(), fl.data());
+    HitBlock *blk = new HitBlock();
+    if (st == MSVGB_eslOK) {
+      std::vector<int64_t> keep;
+      std::vector<float> usc;
+      for (int64_t i = 0; i < nb; ++i) {
+        const int L = (int) (off[b0 + i + 1] - off[b0 + i]);
+        stats.nseqs++;
+        stats.nres += L;
+        if (L == 0 || !(fl[i] & MSVGB_FLAG_PASS)) continue;      // empty, or P > F1 at the MSV stage
+        keep.push_back(i);
+        usc.push_back(msvgb_score(xj[i], fl[i], L, f->om->base_b, f->om->scale_b));
+      }
+      stats.n_past_msv += (int64_t) keep.size();
+      st = filter_block(ctx, f, vp, db, b0, off, keep, usc, stats, blk->hits);
+    }
+    msvgb_db_destroy(db);
+    if (st != MSVGB_eslOK) { delete blk; break; }
+    {
+      std::unique_lock<std::mutex> lk(mu);
+      cv_push.wait(lk, [&] { return q.size() < qcap; });
+      q.push_back(blk);
+    }
+    cv_pop.notify_one();
+  }
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    producing = false;
+  }
+  cv_pop.notify_all();
+  for (auto &t : workers) t.join();
+  for (HitBlock *b : q) delete b;
+  msvgb_vprofile_destroy(vp);
+  msvgb_profile_destroy(prof);
+  if (ret_stats) *ret_stats = stats;
   if (st == MSVGB_eslOK && abort_flag.load()) return fail(MSVGB_eslFAIL, "the continuation asked to stop");
   return st;
 }

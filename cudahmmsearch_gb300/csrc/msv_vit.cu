@@ -38,20 +38,35 @@ namespace {
 
 constexpr int kNT = 8;     // per-node transitions: BM MM IM DM (into k), MD MI II (out of k), DD into k
 
+// Cost tables are lane-interleaved 16-byte vectors: vector v of a lane holds
+// the int16 costs of its nodes 8v .. 8v+7, and the 32 lanes' vectors v are
+// adjacent, so one warp load reads 512 contiguous bytes.
 struct VitDev {
   int CV;                  // nodes per lane
   int16_t base_w, ddbound_w;
   int16_t xwE_move, xwE_loop, xwN_loop, xwJ_loop, xwC_loop;
-  const int16_t *trans;    // [kNT][32][CV]
-  const int16_t *emit;     // [NRES][32][CV]
+  const uint4 *trans;      // [kNT][NV][32]
+  const uint4 *emit;       // [NRES][NV][32]
   const int16_t *move;     // [Lmax+1]: N/J/C move cost at target length L
 };
 
+__host__ __device__ constexpr int vit_nv(int CV) { return (CV + 7) / 8; }
+
 __device__ __forceinline__ int sat16(int v) { return min(32767, max(-32768, v)); }
 
+// signed 16-bit element e (0..7) of a vector
+__device__ __forceinline__ int h16(const uint4 &w, int e) {
+  const uint32_t u = e < 2 ? w.x : e < 4 ? w.y : e < 6 ? w.z : w.w;
+  return (e & 1) ? ((int) u >> 16) : (int) (int16_t) (u & 0xffffu);
+}
+
+// Saturation is monotone, so max(sat(a), sat(b)) = sat(max(a, b)); every
+// transition cost is <= 0, so a sum of a stored int16 score and a transition
+// can only leave the range downwards: one clamp per cell value instead of
+// one per sum. Only the emission can raise a score.
 template <int CV>
 __device__ int vit_one(const VitDev &V, const uint8_t *sq, int L, int lane, int &xc_out) {
-  const int stride_t = 32 * CV;
+  constexpr int NV = vit_nv(CV);
   int Mv[CV], Iv[CV], Dv[CV];
 #pragma unroll
   for (int j = 0; j < CV; ++j) Mv[j] = Iv[j] = Dv[j] = -32768;
@@ -60,32 +75,38 @@ __device__ int vit_one(const VitDev &V, const uint8_t *sq, int L, int lane, int 
   int xB = (int16_t) (xN + move), xJ = -32768, xC = -32768;
   for (int i = 0; i < L; ++i) {
     const int x = sq[i];
-    const int16_t *em = V.emit + (x * 32 + lane) * CV;
+    const uint4 *em = V.emit + (size_t) x * NV * 32 + lane;
     // the transition costs are read anew each row (from L1): kept in
     // registers across rows they would crowd out the DP state
     int opaque;
     asm volatile("mov.u32 %0, 0;" : "=r"(opaque));
-    const int16_t *tr = V.trans + lane * CV + opaque;
+    const uint4 *tr = V.trans + lane + opaque;
     // predecessors of this lane's first node: the previous lane's last node (old row)
     int pM = __shfl_up_sync(FULL, Mv[CV - 1], 1), pI = __shfl_up_sync(FULL, Iv[CV - 1], 1),
         pD = __shfl_up_sync(FULL, Dv[CV - 1], 1);
     if (lane == 0) pM = pI = pD = -32768;
     int xe = -32768, dmax = -32768, dc = -32768;
 #pragma unroll
-    for (int j = 0; j < CV; ++j) {
-      const int cM = Mv[j], cI = Iv[j], cD = Dv[j];
-      int sv = sat16(xB + tr[0 * stride_t + j]);
-      sv = max(sv, sat16(pM + tr[1 * stride_t + j]));
-      sv = max(sv, sat16(pI + tr[2 * stride_t + j]));
-      sv = max(sv, sat16(pD + tr[3 * stride_t + j]));
-      sv = sat16(sv + em[j]);
-      xe = max(xe, sv);
-      Mv[j] = sv;
-      Iv[j] = max(sat16(cM + tr[5 * stride_t + j]), sat16(cI + tr[6 * stride_t + j]));
-      Dv[j] = dc;                                   // M->D from node k-1 (the delayed store)
-      dc = sat16(sv + tr[4 * stride_t + j]);
-      dmax = max(dmax, dc);
-      pM = cM; pI = cI; pD = cD;
+    for (int v = 0; v < NV; ++v) {
+      const uint4 e4 = em[v * 32];
+      uint4 t4[7];
+#pragma unroll
+      for (int t = 0; t < 7; ++t) t4[t] = tr[(t * NV + v) * 32];
+#pragma unroll
+      for (int e = 0; e < 8; ++e) {
+        const int j = v * 8 + e;
+        if (j >= CV) break;
+        const int cM = Mv[j], cI = Iv[j], cD = Dv[j];
+        int sv = max(max(xB + h16(t4[0], e), pM + h16(t4[1], e)), max(pI + h16(t4[2], e), pD + h16(t4[3], e)));
+        sv = sat16(max(sv, -32768) + h16(e4, e));
+        xe = max(xe, sv);
+        Mv[j] = sv;
+        Iv[j] = max(max(cM + h16(t4[5], e), cI + h16(t4[6], e)), -32768);
+        Dv[j] = dc;                                 // M->D from node k-1 (the delayed store)
+        dc = max(sv + h16(t4[4], e), -32768);
+        dmax = max(dmax, dc);
+        pM = cM; pI = cI; pD = cD;
+      }
     }
     // the first node's M->D comes from the previous lane's last node
     const int dprev = __shfl_up_sync(FULL, dc, 1);
@@ -99,12 +120,19 @@ __device__ int vit_one(const VitDev &V, const uint8_t *sq, int L, int lane, int 
     xB = (int16_t) max(xJ + move, xN + move);
     if (dmax + V.ddbound_w > xB) {                  // D->D closure over all nodes
       // this lane's block as max(c, v + b) of the incoming value v
+      int tdd[CV];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        const uint4 t7 = tr[(7 * NV + v) * 32];     // D(k-1) -> D(k)
+#pragma unroll
+        for (int e = 0; e < 8; ++e)
+          if (v * 8 + e < CV) tdd[v * 8 + e] = h16(t7, e);
+      }
       int c = -2000000000, b = 0;
 #pragma unroll
       for (int j = 0; j < CV; ++j) {
-        const int t = tr[7 * stride_t + j];         // D(k-1) -> D(k)
-        c = max(Dv[j], c + t);
-        b += t;
+        c = max(Dv[j], c + tdd[j]);
+        b += tdd[j];
         if (b < -2000000) b = -2000000;             // far below any value: keeps the sums in range
       }
       // exclusive warp scan of the blocks: (c1,b1) then (c2,b2) = (max(c2, c1+b2), b1+b2)
@@ -114,12 +142,12 @@ __device__ int vit_one(const VitDev &V, const uint8_t *sq, int L, int lane, int 
         const int oc = __shfl_up_sync(FULL, sc_c, d), ob = __shfl_up_sync(FULL, sc_b, d);
         if (lane >= d) { sc_c = max(sc_c, oc + sc_b); sc_b = max(ob + sc_b, -2000000); }
       }
-      int v = __shfl_up_sync(FULL, sc_c, 1);
-      if (lane == 0) v = -2000000000;
+      int vin = __shfl_up_sync(FULL, sc_c, 1);
+      if (lane == 0) vin = -2000000000;
 #pragma unroll
       for (int j = 0; j < CV; ++j) {
-        Dv[j] = max(Dv[j], v + tr[7 * stride_t + j]);
-        v = Dv[j];
+        Dv[j] = max(Dv[j], vin + tdd[j]);
+        vin = Dv[j];
       }
     }
   }
@@ -127,8 +155,10 @@ __device__ int vit_one(const VitDev &V, const uint8_t *sq, int L, int lane, int 
   return 0;
 }
 
+constexpr int kVitThreads = 64;   // two warps: occupancy in steps of two warps at any register count
+
 template <int CV>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kVitThreads)
 vit_kernel(VitDev V, DbDev db, const int64_t *__restrict__ sorted_ids, int64_t nids, int *__restrict__ out_xc,
            uint8_t *__restrict__ out_st, unsigned long long *__restrict__ ticket) {
   const int lane = threadIdx.x & 31;
@@ -149,24 +179,25 @@ template <int CV>
 cudaError_t launch_vit(const VitDev &V, const DbDev &db, const int64_t *ids, int64_t n, int *xc, uint8_t *st,
                        unsigned long long *ticket, int sms, cudaStream_t stream) {
   int per_sm = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, vit_kernel<CV>, 256, 0);
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, vit_kernel<CV>, kVitThreads, 0);
   if (e != cudaSuccess) return e;
+  constexpr int warps = kVitThreads / 32;
   long long grid = (long long) std::max(1, per_sm) * sms;
-  grid = std::min<long long>(grid, (n + 7) / 8);
+  grid = std::min<long long>(grid, (n + warps - 1) / warps);
   (void) cudaGetLastError();
-  vit_kernel<CV><<<(unsigned) std::max<long long>(1, grid), 256, 0, stream>>>(V, db, ids, n, xc, st, ticket);
+  vit_kernel<CV><<<(unsigned) std::max<long long>(1, grid), kVitThreads, 0, stream>>>(V, db, ids, n, xc, st, ticket);
   return cudaGetLastError();
 }
 
-// nodes per lane compiled (the widths between spill registers: the next
-// larger one runs instead)
-constexpr int kVitCV[] = {1, 2, 3, 4, 6, 8, 12, 32, 48};
+// nodes per lane compiled (none spills; a model runs at the smallest width
+// that holds its 8*Q8 nodes)
+constexpr int kVitCV[] = {1, 2, 3, 4, 6, 8, 12, 16, 24, 32, 40, 48};
 
 cudaError_t dispatch_vit(int CV, const VitDev &V, const DbDev &db, const int64_t *ids, int64_t n, int *xc,
                          uint8_t *st, unsigned long long *ticket, int sms, cudaStream_t stream) {
   switch (CV) {
 #define VCASE(c) case c: return launch_vit<c>(V, db, ids, n, xc, st, ticket, sms, stream);
-    VCASE(1) VCASE(2) VCASE(3) VCASE(4) VCASE(6) VCASE(8) VCASE(12) VCASE(32) VCASE(48)
+    VCASE(1) VCASE(2) VCASE(3) VCASE(4) VCASE(6) VCASE(8) VCASE(12) VCASE(16) VCASE(24) VCASE(32) VCASE(40) VCASE(48)
 #undef VCASE
   }
   return cudaErrorInvalidValue;
@@ -182,6 +213,17 @@ int16_t wordify(float scale_w, float sc) {
 
 }  // namespace
 
+cudaError_t msvgb_detail::ensure_inverse(msvgb_ctx *c, const msvgb_db *db) {
+  std::lock_guard<std::mutex> lk(c->mu_inv);
+  if (db->d_inv) return cudaSuccess;
+  int64_t *inv = nullptr;
+  cudaError_t e = cudaMalloc(&inv, std::max<int64_t>(db->n, 1) * 8);
+  if (e == cudaSuccess) e = launch_invert(db->d_orig, db->n, inv, c->num_sms, c->stream);
+  if (e != cudaSuccess) { cudaFree(inv); return e; }
+  const_cast<msvgb_db *>(db)->d_inv = inv;   // a cache of the database's own order: logically const
+  return cudaSuccess;
+}
+
 struct msvgb_vprofile {
   msvgb_ctx *ctx = nullptr;
   int device = 0;
@@ -189,7 +231,8 @@ struct msvgb_vprofile {
   float scale_w = 0.f, nj = 0.f;
   int16_t base_w = 0, ddbound_w = 0;
   int16_t xw[4][2] = {};
-  int16_t *d_trans = nullptr, *d_emit = nullptr, *d_move = nullptr;
+  uint4 *d_trans = nullptr, *d_emit = nullptr;
+  int16_t *d_move = nullptr;
   int move_cap = 0;
   std::vector<int16_t> h_move;
 };
@@ -216,23 +259,25 @@ extern "C" int msvgb_vprofile_create(msvgb_ctx *ctx, const msvgb_vom *v, msvgb_v
   int CV = -1;
   for (int c : kVitCV) if (32 * c >= Np) { CV = c; break; }
   if (CV < 0) return fail(MSVGB_eslEINVAL, "ViterbiFilter profile: M exceeds the supported maximum (1536 nodes)");
-  // node-order, lane-major tables; nodes past 8*Q8 (and padding inside it) cost -32768 as the reference's do
-  const int N = 32 * CV;
+  // node-order tables, lane-interleaved vectors of 8 nodes; nodes past 8*Q8
+  // (and padding inside it) cost -32768 as the reference's do
+  const int NV = vit_nv(CV);
   auto node_of = [&](int lane, int j) { return lane * CV + j + 1; };
   auto striped = [&](const int16_t *base, int vec_q, int k) {   // element of node k in vector block vec_q
     const int q = (k - 1) % Q8, z = (k - 1) / Q8;
     return base[(vec_q + q) * 8 + z];
   };
-  std::vector<int16_t> trans((size_t) kNT * N, -32768), emit((size_t) NRES * N, -32768);
+  auto at = [&](int table, int lane, int j) { return (((size_t) table * NV + j / 8) * 32 + lane) * 8 + j % 8; };
+  std::vector<int16_t> trans((size_t) kNT * NV * 32 * 8, -32768), emit((size_t) NRES * NV * 32 * 8, -32768);
   for (int lane = 0; lane < 32; ++lane)
     for (int j = 0; j < CV; ++j) {
       const int k = node_of(lane, j);
       if (k > Np) continue;
       const int q = (k - 1) % Q8, z = (k - 1) / Q8;
-      for (int t = 0; t < 7; ++t) trans[((size_t) t * 32 + lane) * CV + j] = v->twv[(q * 7 + t) * 8 + z];
+      for (int t = 0; t < 7; ++t) trans[at(t, lane, j)] = v->twv[(q * 7 + t) * 8 + z];
       // DD into node k is node k-1's DD cost (the Q8 vectors after the 7*Q8 others)
-      trans[((size_t) 7 * 32 + lane) * CV + j] = k > 1 ? striped(v->twv, 7 * Q8, k - 1) : (int16_t) -32768;
-      for (int x = 0; x < v->Kp; ++x) emit[((size_t) x * 32 + lane) * CV + j] = v->rwv[(x * Q8 + q) * 8 + z];
+      trans[at(7, lane, j)] = k > 1 ? striped(v->twv, 7 * Q8, k - 1) : (int16_t) -32768;
+      for (int x = 0; x < v->Kp; ++x) emit[at(x, lane, j)] = v->rwv[(x * Q8 + q) * 8 + z];
     }
   msvgb_vprofile *p = new msvgb_vprofile();
   p->ctx = ctx; p->device = ctx->device; p->M = v->M; p->Q8 = Q8; p->CV = CV;
@@ -281,12 +326,7 @@ extern "C" int msvgb_vitfilter(msvgb_ctx *c, msvgb_vprofile *p, const msvgb_db *
     cudaFree(p->d_move);
     p->d_move = d; p->move_cap = cap;
   }
-  // original -> sorted indices of the database
-  if (!db->d_inv) {
-    msvgb_db *mdb = const_cast<msvgb_db *>(db);
-    CUDA_TRY(cudaMalloc(&mdb->d_inv, std::max<int64_t>(db->n, 1) * 8));
-    CUDA_TRY(msvgb_detail::launch_invert(db->d_orig, db->n, mdb->d_inv, c->num_sms, c->stream));
-  }
+  CUDA_TRY(msvgb_detail::ensure_inverse(c, db));
   int64_t *d_ids = nullptr;
   int *d_xc = nullptr;
   uint8_t *d_st = nullptr;

@@ -171,6 +171,25 @@ int msvgb_vitfilter(msvgb_ctx *ctx, msvgb_vprofile *vp, const msvgb_db *db, cons
 float   msvgb_vit_score(int xc, int status, int L, const msvgb_vom *vom);
 int16_t msvgb_vit_move_cost(float scale_w, float nj, int L);
 
+/* ---- the bias filter: p7_bg_FilterScore (src/p7_bg.c:473-483) -----------------
+ * The composition-bias filter HMM of p7_bg_SetFilter(bg, M, compo)
+ * (src/p7_bg.c:431-453; compo: the model's mean residue composition, the
+ * first 20 floats of P7_OPROFILE compo) with p7_bg_SetLength's per-sequence
+ * transition, scored with esl_hmm_Forward (easel/esl_hmm.c:351-409) on the
+ * listed sequences of db (ids: original indices): out_sc[j] the filter null
+ * score in nats (0 for an empty sequence), bit-exact with the reference's
+ * float arithmetic. One thread per sequence. */
+int   msvgb_biasfilter(msvgb_ctx *ctx, const float *compo, int M, const msvgb_db *db, const int64_t *ids,
+                       int64_t nids, float *out_sc);
+/* The length term p7_bg_FilterScore adds to the Forward score of length L. */
+float msvgb_bias_length_term(float fwd, int L);
+/* p7_bg_NullOne at length L (src/p7_bg.c:359-363). */
+float msvgb_null_score(int L);
+/* The gate of every filter stage of p7_Pipeline (src/p7_pipeline.c:673-675,
+ * 684-686, 699-701): P = esl_gumbel_surv((sc - base) / log(2), mu, lambda),
+ * with the pipeline's float seq_score; 1 if P <= F. */
+int   msvgb_stage_pass(float sc, float base, double mu, double lambda, double F, double *ret_P);
+
 /* ---- on-disk formats ------------------------------------------------------------
  * Pressed MSV profiles (.h3f, the MSV file hmmpress writes: HMMER 3/f binary,
  * x86-64 little-endian). Replaces p7_oprofile_ReadMSV (src/impl_sse/io.c:233)
@@ -347,6 +366,38 @@ typedef int (*msvgb_survivor_fn)(void *user, int64_t seq_index, float usc, uint8
 int msvgb_pipeline_run(msvgb_ctx *ctx, const msvgb_om *om, const uint8_t *codes, const int64_t *off,
                        int64_t n, int64_t block_size, double F1, int n_workers,
                        msvgb_survivor_fn fn, void *user, int64_t *ret_n_past_msv);
+
+/* ---- pipeline driver with the GPU filter stages after MSV ------------------------
+ * The filter stages of p7_Pipeline (src/p7_pipeline.c:662-705; the fork's
+ * p7_PipelineShort :887-946) on the GPU, block by block as
+ * msvgb_pipeline_run streams them: the MSV stage and its F1 gate; the bias
+ * filter on the MSV survivors and F1 on (usc - filtersc) (skipped when compo
+ * is NULL: --nobias, filtersc = nullsc); p7_ViterbiFilter on the survivors
+ * whose bias-stage P > F2 and the F2 gate on (vfsc - filtersc) with the
+ * Viterbi Gumbel parameters (a sequence with P <= F2 already skips Viterbi,
+ * as in the reference). fn is called on the worker threads for every
+ * sequence past the Viterbi stage (past the bias stage when vom is NULL):
+ * where p7_ForwardParser and domain definition would continue. */
+typedef struct {
+  const msvgb_om  *om;        /* MSV part; om->mmu, om->mlambda: evparam MMU, MLAMBDA */
+  const msvgb_vom *vom;       /* ViterbiFilter part; NULL: stop after the bias stage  */
+  const float     *compo;     /* 20 floats of model composition; NULL: no bias filter */
+  float            vmu, vlambda;   /* evparam VMU, VLAMBDA                            */
+  double           F1, F2;    /* 0.02 and 1e-3 by default (p7_pipeline.c:210-211)      */
+} msvgb_filters;
+typedef struct {
+  int64_t seq_index;
+  float   usc, nullsc, filtersc;
+  float   vfsc;               /* NaN where Viterbi did not run (bias-stage P <= F2, or no vom) */
+} msvgb_filter_hit;
+typedef struct {
+  int64_t nseqs, nres;
+  int64_t n_past_msv, n_past_bias, n_past_vit;   /* the pipeline's counters (p7_pipeline.c:1843-1904) */
+} msvgb_filter_stats;
+typedef int (*msvgb_filter_fn)(void *user, const msvgb_filter_hit *hit);
+int msvgb_pipeline_filters(msvgb_ctx *ctx, const msvgb_filters *f, const uint8_t *codes, const int64_t *off,
+                           int64_t n, int64_t block_size, int n_workers, msvgb_filter_fn fn, void *user,
+                           msvgb_filter_stats *stats);
 
 /* ---- host-side score helpers (exact reference expressions) --------------------- */
 /* tjb_b for target length L (p7_oprofile.c:511-519, 920-925). */

@@ -11,7 +11,7 @@ from cudahmmsearch_gb300 import formats as F
 from oracle import oracle as O
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
-CASES = sorted(os.path.basename(p)[:-5] for p in glob.glob(os.path.join(GOLDEN, "*.prof")))
+CASES = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.res")))
 
 
 @pytest.mark.parametrize("name", CASES)
