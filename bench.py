@@ -263,6 +263,85 @@ def run_batch(args, api, torch, ctx, stream, local):
     print(json.dumps(line))
 
 
+def run_filters(args, api, torch, ctx, stream, local):
+    """The filter stages after MSV (p7_Pipeline, src/p7_pipeline.c:662-705) on
+    the GPU. The model is the M=400 sampled HMM (seed 1) in hmmsearch's local
+    configuration with the composition hmmbuild gives it (tests/golden/
+    pipe_m400_s1.*, vit_m400_s1.vprof); the sequences follow m400_2M's law.
+    Timed per step: (a) the ViterbiFilter kernel stage on 200,000 listed
+    sequences (cells = M x residues), (b) the bias filter on the same list,
+    each with CUDA events on the launching stream (the calls include the id
+    upload and the result copy); (c) the whole filter pipeline (database
+    blocks uploaded, MSV, bias, ViterbiFilter, gates) through
+    msvgb_pipeline_filters from host buffers, host wall clock."""
+    G = os.path.join(ROOT, "tests", "golden")
+    p = F.read_profile(os.path.join(G, "pipe_m400_s1.prof"))
+    vp = F.read_vprofile(os.path.join(G, "vit_m400_s1.vprof"))
+    pr = F.read_pipe(os.path.join(G, "pipe_m400_s1.pres"))
+    n_seq = args.nseq
+    n_hom = n_seq // 50
+    s = F.SeqSet.concat([F.synth_sequences(n_seq - n_hom, seed=1000, lmax=35000),
+                         F.emit_homologs(p, n_hom, seed=2000, lmax=35000)])
+    db = api.DeviceDB(ctx, s)
+    dvp = api.DeviceVProfile(ctx, vp)
+    ids = np.arange(min(200_000, s.n), dtype=np.int64)
+    res_ids = float(s.lengths[ids].sum())
+    xc = np.zeros(ids.size, np.int32)
+    vst = np.zeros(ids.size, np.uint8)
+    fsc = np.zeros(ids.size, np.float32)
+    c = np.ascontiguousarray(pr.compo, np.float32)
+    L = api.lib()
+
+    def vit():
+        api._check(L.msvgb_vitfilter(ctx.h, dvp.h, db.h, ids.ctypes.data, ids.size, xc.ctypes.data, vst.ctypes.data))
+
+    def bias():
+        api._check(L.msvgb_biasfilter(ctx.h, c.ctypes.data, vp.M, db.h, ids.ctypes.data, ids.size, fsc.ctypes.data))
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(args.steps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms.append(a.elapsed_time(b))
+        return float(np.median(ms))
+    launches0 = api.kernel_launches()
+    with ClockSampler(local) as clk:
+        vit_ms = timed(vit)
+        bias_ms = timed(bias)
+        pipe_s = []
+        for i in range(args.warmup + args.steps):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            hits, st = api.pipeline_filters(ctx, p, s, vprof=vp, compo=pr.compo, vmu=pr.vmu, vlambda=pr.vlambda,
+                                            block_size=500_000, n_workers=4)
+            if i >= args.warmup:
+                pipe_s.append(time.perf_counter() - t)
+    launches = api.kernel_launches() - launches0
+    cells = float(p.M) * float(s.total)
+    value = cells / float(np.median(pipe_s)) / 1e9
+    line = {"metric": "filter pipeline GCUPS", "value": value, "unit": "GCUPS", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": float(np.median(pipe_s)) * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u8/s16/f32", "data": "synthetic",
+            "config": {"workload": f"p7_Pipeline filter stages (MSV, bias, ViterbiFilter) on the GPU, M=400 local "
+                                   f"(p7_hmm_Sample seed 1) vs {s.n:,} seqs (m400_2M's law), blocks of 500,000",
+                       "M": p.M, "n_seqs": s.n, "residues": s.total,
+                       "n_past_msv": st.n_past_msv, "n_past_bias": st.n_past_bias, "n_past_vit": st.n_past_vit},
+            "stages": {"vitfilter": {"ms": vit_ms, "gcups": vp.M * res_ids / (vit_ms * 1e-3) / 1e9,
+                                     "n_seqs": int(ids.size), "residues": int(res_ids)},
+                       "biasfilter": {"ms": bias_ms, "gres_per_s": res_ids / (bias_ms * 1e-3) / 1e9,
+                                      "n_seqs": int(ids.size)},
+                       "pipeline_s": [round(t, 4) for t in pipe_s]},
+            "gpu_launches": int(launches), "clocks": clk.summary()}
+    print(json.dumps(line))
+
+
 def run_serve(args, api, torch, ctx, local):
     """Serving: a resident database of 2,000,000 sequences receives query
     profiles (p7_hmm_Sample with per-request seeds, M log-uniform in
@@ -373,6 +452,12 @@ def main():
         return run_batch(args, api, torch, ctx, stream, local)
     if args.workload == "serve":
         return run_serve(args, api, torch, api.Context(local), local)
+    if args.workload == "filters":
+        ctx = api.Context(local)
+        stream = torch.cuda.Stream()
+        torch.cuda.set_stream(stream)
+        ctx.set_stream(stream.cuda_stream)
+        return run_filters(args, api, torch, ctx, stream, local)
 
     p, s, cfg = workload(args.workload, rank, args)
     cells = float(p.M) * float(s.total)

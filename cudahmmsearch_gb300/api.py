@@ -39,6 +39,7 @@ EXPORTS = [
     "msvgb_db_save", "msvgb_db_load", "msvgb_db_lengths", "msvgb_search_host",
     "msvgb_vprofile_create", "msvgb_vprofile_destroy", "msvgb_vitfilter", "msvgb_vit_score", "msvgb_vit_move_cost",
     "msvgb_biasfilter", "msvgb_bias_length_term", "msvgb_null_score", "msvgb_stage_pass", "msvgb_pipeline_filters",
+    "msvgb_filter_collect",
 ]
 
 
@@ -76,6 +77,10 @@ class _Filters(ctypes.Structure):
 class FilterHit(ctypes.Structure):
     _fields_ = [("seq_index", ctypes.c_int64), ("usc", ctypes.c_float), ("nullsc", ctypes.c_float),
                 ("filtersc", ctypes.c_float), ("vfsc", ctypes.c_float)]
+
+
+class _FilterSink(ctypes.Structure):
+    _fields_ = [("hits", ctypes.c_void_p), ("cap", ctypes.c_int64), ("n", ctypes.c_int64)]
 
 
 class FilterStats(ctypes.Structure):
@@ -169,6 +174,7 @@ def lib():
         "msvgb_stage_pass": (i32, [f32, f32, f64, f64, f64, ctypes.POINTER(f64)]),
         "msvgb_pipeline_filters": (i32, [vp, ctypes.POINTER(_Filters), vp, vp, i64, i64, i32, vp, vp,
                                          ctypes.POINTER(FilterStats)]),
+        "msvgb_filter_collect": (i32, [vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -611,8 +617,8 @@ def pipeline_filters(ctx: Context, p: F.Profile, seqs: F.SeqSet, *, vprof: F.VPr
     MSV, bias filter (when compo is given), ViterbiFilter (when vprof is
     given). on_hit(seq_index, usc, nullsc, filtersc, vfsc) runs on the worker
     threads for every sequence past the last stage; without on_hit the hits
-    are collected. Returns (hits: structured array sorted by seq_index,
-    stats: FilterStats)."""
+    are collected natively (msvgb_filter_collect). Returns (hits: structured
+    array sorted by seq_index, empty with on_hit; stats: FilterStats)."""
     o, keep = _om_struct(p)
     vo, vkeep = _vom_struct(vprof) if vprof is not None else (None, None)
     c = np.ascontiguousarray(compo, dtype=np.float32) if compo is not None else None
@@ -622,25 +628,27 @@ def pipeline_filters(ctx: Context, p: F.Profile, seqs: F.SeqSet, *, vprof: F.VPr
     if codes.size == 0:
         codes = np.zeros(1, np.uint8)
     off = np.ascontiguousarray(seqs.off, dtype=np.int64)
-    got = []
-    import threading
-    lk = threading.Lock()
-
-    def _cb(user, h):
-        h = h.contents
-        if on_hit is not None:
-            return 1 if on_hit(int(h.seq_index), h.usc, h.nullsc, h.filtersc, h.vfsc) else 0
-        with lk:
-            got.append((h.seq_index, h.usc, h.nullsc, h.filtersc, h.vfsc))
-        return 0
-    cb = FILTER_FN(_cb)
-    stats = FilterStats()
-    _check(lib().msvgb_pipeline_filters(ctx.h, ctypes.byref(f), codes.ctypes.data, off.ctypes.data, seqs.n,
-                                        block_size, n_workers, ctypes.cast(cb, ctypes.c_void_p), None,
-                                        ctypes.byref(stats)))
     dt = np.dtype([("seq_index", np.int64), ("usc", np.float32), ("nullsc", np.float32),
                    ("filtersc", np.float32), ("vfsc", np.float32)])
-    hits = np.array(sorted(got), dtype=dt)
+    stats = FilterStats()
+    args = (ctx.h, ctypes.byref(f), codes.ctypes.data, off.ctypes.data, seqs.n, block_size, n_workers)
+    if on_hit is not None:
+        def _cb(user, h):
+            h = h.contents
+            return 1 if on_hit(int(h.seq_index), h.usc, h.nullsc, h.filtersc, h.vfsc) else 0
+        cb = FILTER_FN(_cb)
+        _check(lib().msvgb_pipeline_filters(*args, ctypes.cast(cb, ctypes.c_void_p), None, ctypes.byref(stats)))
+        return np.zeros(0, dt), stats
+    cap = max(16, seqs.n // 8)
+    while True:                                   # the native collector; rerun larger if it overflowed
+        buf = np.zeros(cap, dt)
+        sink = _FilterSink(buf.ctypes.data, cap, 0)
+        _check(lib().msvgb_pipeline_filters(*args, ctypes.cast(lib().msvgb_filter_collect, ctypes.c_void_p),
+                                            ctypes.byref(sink), ctypes.byref(stats)))
+        if sink.n <= cap:
+            break
+        cap = sink.n
+    hits = np.sort(buf[:sink.n], order="seq_index")
     return hits, stats
 
 

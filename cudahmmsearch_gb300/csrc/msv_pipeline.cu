@@ -173,6 +173,13 @@ int filter_block(msvgb_ctx *ctx, const msvgb_filters *f, msvgb_vprofile *vp, con
 
 }  // namespace
 
+extern "C" int msvgb_filter_collect(void *user, const msvgb_filter_hit *hit) {
+  msvgb_filter_sink *s = static_cast<msvgb_filter_sink *>(user);
+  const int64_t at = __atomic_fetch_add(&s->n, (int64_t) 1, __ATOMIC_RELAXED);
+  if (at < s->cap) s->hits[at] = *hit;
+  return 0;
+}
+
 extern "C" int msvgb_pipeline_filters(msvgb_ctx *ctx, const msvgb_filters *f, const uint8_t *codes,
                                       const int64_t *off, int64_t n, int64_t block_size, int n_workers,
                                       msvgb_filter_fn fn, void *user, msvgb_filter_stats *ret_stats) {

@@ -38,19 +38,29 @@ namespace {
 
 constexpr int kNT = 8;     // per-node transitions: BM MM IM DM (into k), MD MI II (out of k), DD into k
 
-// Cost tables are lane-interleaved 16-byte vectors: vector v of a lane holds
-// the int16 costs of its nodes 8v .. 8v+7, and the 32 lanes' vectors v are
-// adjacent, so one warp load reads 512 contiguous bytes.
+// Cost tables are lane-interleaved 16-byte vectors, the 32 lanes' vectors v
+// adjacent so that one warp load reads 512 contiguous bytes. Emissions are
+// int16 (vector v of a lane: its nodes 8v .. 8v+7), one unpack per cell,
+// which keeps the 29 residue tables of the widest model within L1.
+// Transitions are int32 (nodes 4v .. 4v+3), ready for the adds, up to 32
+// nodes per lane; wider lanes keep them int16 (the unpacked values would
+// spill registers).
 struct VitDev {
   int CV;                  // nodes per lane
   int16_t base_w, ddbound_w;
   int16_t xwE_move, xwE_loop, xwN_loop, xwJ_loop, xwC_loop;
-  const uint4 *trans;      // [kNT][NV][32]
+  const void *trans;       // [kNT][NT][32] vectors of int32 (4 nodes) or int16 (8 nodes)
   const uint4 *emit;       // [NRES][NV][32]
   const int16_t *move;     // [Lmax+1]: N/J/C move cost at target length L
 };
 
 __host__ __device__ constexpr int vit_nv(int CV) { return (CV + 7) / 8; }
+__host__ __device__ constexpr bool vit_t32(int CV) { return CV <= 32; }
+// nodes per transition vector and vectors per lane
+__host__ __device__ constexpr int vit_tnodes(int CV) { return vit_t32(CV) ? 4 : 8; }
+__host__ __device__ constexpr int vit_nt(int CV) { return (CV + vit_tnodes(CV) - 1) / vit_tnodes(CV); }
+
+__device__ __forceinline__ int i32(const int4 &w, int e) { return e == 0 ? w.x : e == 1 ? w.y : e == 2 ? w.z : w.w; }
 
 __device__ __forceinline__ int sat16(int v) { return min(32767, max(-32768, v)); }
 
@@ -66,7 +76,7 @@ __device__ __forceinline__ int h16(const uint4 &w, int e) {
 // one per sum. Only the emission can raise a score.
 template <int CV>
 __device__ int vit_one(const VitDev &V, const uint8_t *sq, int L, int lane, int &xc_out) {
-  constexpr int NV = vit_nv(CV);
+  constexpr int NV = vit_nv(CV), NT = vit_nt(CV), TN = vit_tnodes(CV);
   int Mv[CV], Iv[CV], Dv[CV];
 #pragma unroll
   for (int j = 0; j < CV; ++j) Mv[j] = Iv[j] = Dv[j] = -32768;
@@ -80,30 +90,35 @@ __device__ int vit_one(const VitDev &V, const uint8_t *sq, int L, int lane, int 
     // registers across rows they would crowd out the DP state
     int opaque;
     asm volatile("mov.u32 %0, 0;" : "=r"(opaque));
-    const uint4 *tr = V.trans + lane + opaque;
+    const int4 *tr = static_cast<const int4 *>(V.trans) + lane + opaque;
     // predecessors of this lane's first node: the previous lane's last node (old row)
     int pM = __shfl_up_sync(FULL, Mv[CV - 1], 1), pI = __shfl_up_sync(FULL, Iv[CV - 1], 1),
         pD = __shfl_up_sync(FULL, Dv[CV - 1], 1);
     if (lane == 0) pM = pI = pD = -32768;
     int xe = -32768, dmax = -32768, dc = -32768;
+    uint4 e4;                                       // emission vector of nodes 8*(j/8) ..
 #pragma unroll
-    for (int v = 0; v < NV; ++v) {
-      const uint4 e4 = em[v * 32];
-      uint4 t4[7];
+    for (int q = 0; q < NT; ++q) {                  // transition vector q: nodes TN*q ..
+      int4 t4[7];
 #pragma unroll
-      for (int t = 0; t < 7; ++t) t4[t] = tr[(t * NV + v) * 32];
+      for (int t = 0; t < 7; ++t) t4[t] = tr[(t * NT + q) * 32];
 #pragma unroll
-      for (int e = 0; e < 8; ++e) {
-        const int j = v * 8 + e;
+      for (int e = 0; e < TN; ++e) {
+        const int j = q * TN + e;
         if (j >= CV) break;
+        if (j % 8 == 0) e4 = em[(j / 8) * 32];
+        auto tv = [&](int t) {
+          if constexpr (vit_t32(CV)) return i32(t4[t], e);
+          else return h16(*reinterpret_cast<const uint4 *>(&t4[t]), e);
+        };
         const int cM = Mv[j], cI = Iv[j], cD = Dv[j];
-        int sv = max(max(xB + h16(t4[0], e), pM + h16(t4[1], e)), max(pI + h16(t4[2], e), pD + h16(t4[3], e)));
-        sv = sat16(max(sv, -32768) + h16(e4, e));
+        int sv = max(max(xB + tv(0), pM + tv(1)), max(pI + tv(2), pD + tv(3)));
+        sv = sat16(max(sv, -32768) + h16(e4, j % 8));
         xe = max(xe, sv);
         Mv[j] = sv;
-        Iv[j] = max(max(cM + h16(t4[5], e), cI + h16(t4[6], e)), -32768);
+        Iv[j] = max(max(cM + tv(5), cI + tv(6)), -32768);
         Dv[j] = dc;                                 // M->D from node k-1 (the delayed store)
-        dc = max(sv + h16(t4[4], e), -32768);
+        dc = max(sv + tv(4), -32768);
         dmax = max(dmax, dc);
         pM = cM; pI = cI; pD = cD;
       }
@@ -122,11 +137,14 @@ __device__ int vit_one(const VitDev &V, const uint8_t *sq, int L, int lane, int 
       // this lane's block as max(c, v + b) of the incoming value v
       int tdd[CV];
 #pragma unroll
-      for (int v = 0; v < NV; ++v) {
-        const uint4 t7 = tr[(7 * NV + v) * 32];     // D(k-1) -> D(k)
+      for (int q = 0; q < NT; ++q) {
+        const int4 t7 = tr[(7 * NT + q) * 32];      // D(k-1) -> D(k)
 #pragma unroll
-        for (int e = 0; e < 8; ++e)
-          if (v * 8 + e < CV) tdd[v * 8 + e] = h16(t7, e);
+        for (int e = 0; e < TN; ++e)
+          if (q * TN + e < CV) {
+            if constexpr (vit_t32(CV)) tdd[q * TN + e] = i32(t7, e);
+            else tdd[q * TN + e] = h16(*reinterpret_cast<const uint4 *>(&t7), e);
+          }
       }
       int c = -2000000000, b = 0;
 #pragma unroll
@@ -231,7 +249,8 @@ struct msvgb_vprofile {
   float scale_w = 0.f, nj = 0.f;
   int16_t base_w = 0, ddbound_w = 0;
   int16_t xw[4][2] = {};
-  uint4 *d_trans = nullptr, *d_emit = nullptr;
+  void *d_trans = nullptr;
+  uint4 *d_emit = nullptr;
   int16_t *d_move = nullptr;
   int move_cap = 0;
   std::vector<int16_t> h_move;
@@ -261,32 +280,38 @@ extern "C" int msvgb_vprofile_create(msvgb_ctx *ctx, const msvgb_vom *v, msvgb_v
   if (CV < 0) return fail(MSVGB_eslEINVAL, "ViterbiFilter profile: M exceeds the supported maximum (1536 nodes)");
   // node-order tables, lane-interleaved vectors of 8 nodes; nodes past 8*Q8
   // (and padding inside it) cost -32768 as the reference's do
-  const int NV = vit_nv(CV);
+  const int NV = vit_nv(CV), NT = vit_nt(CV), TN = vit_tnodes(CV);
   auto node_of = [&](int lane, int j) { return lane * CV + j + 1; };
   auto striped = [&](const int16_t *base, int vec_q, int k) {   // element of node k in vector block vec_q
     const int q = (k - 1) % Q8, z = (k - 1) / Q8;
     return base[(vec_q + q) * 8 + z];
   };
-  auto at = [&](int table, int lane, int j) { return (((size_t) table * NV + j / 8) * 32 + lane) * 8 + j % 8; };
-  std::vector<int16_t> trans((size_t) kNT * NV * 32 * 8, -32768), emit((size_t) NRES * NV * 32 * 8, -32768);
+  auto at_t = [&](int table, int lane, int j) { return (((size_t) table * NT + j / TN) * 32 + lane) * TN + j % TN; };
+  auto at_e = [&](int x, int lane, int j) { return (((size_t) x * NV + j / 8) * 32 + lane) * 8 + j % 8; };
+  std::vector<int32_t> trans((size_t) kNT * NT * 32 * TN, -32768);
+  std::vector<int16_t> emit((size_t) NRES * NV * 32 * 8, -32768);
   for (int lane = 0; lane < 32; ++lane)
     for (int j = 0; j < CV; ++j) {
       const int k = node_of(lane, j);
       if (k > Np) continue;
       const int q = (k - 1) % Q8, z = (k - 1) / Q8;
-      for (int t = 0; t < 7; ++t) trans[at(t, lane, j)] = v->twv[(q * 7 + t) * 8 + z];
+      for (int t = 0; t < 7; ++t) trans[at_t(t, lane, j)] = v->twv[(q * 7 + t) * 8 + z];
       // DD into node k is node k-1's DD cost (the Q8 vectors after the 7*Q8 others)
-      trans[at(7, lane, j)] = k > 1 ? striped(v->twv, 7 * Q8, k - 1) : (int16_t) -32768;
-      for (int x = 0; x < v->Kp; ++x) emit[at(x, lane, j)] = v->rwv[(x * Q8 + q) * 8 + z];
+      trans[at_t(7, lane, j)] = k > 1 ? striped(v->twv, 7 * Q8, k - 1) : (int16_t) -32768;
+      for (int x = 0; x < v->Kp; ++x) emit[at_e(x, lane, j)] = v->rwv[(x * Q8 + q) * 8 + z];
     }
+  std::vector<int16_t> trans16;                     // the int16 form for lanes wider than 32 nodes
+  if (!vit_t32(CV)) trans16.assign(trans.begin(), trans.end());
+  const void *tsrc = vit_t32(CV) ? (const void *) trans.data() : (const void *) trans16.data();
+  const size_t tbytes = trans.size() * (vit_t32(CV) ? 4 : 2);
   msvgb_vprofile *p = new msvgb_vprofile();
   p->ctx = ctx; p->device = ctx->device; p->M = v->M; p->Q8 = Q8; p->CV = CV;
   p->scale_w = v->scale_w; p->nj = v->nj; p->base_w = v->base_w; p->ddbound_w = v->ddbound_w;
   memcpy(p->xw, v->xw, sizeof p->xw);
   cudaError_t e = cudaSetDevice(ctx->device);
-  if (e == cudaSuccess) e = cudaMalloc(&p->d_trans, trans.size() * 2);
+  if (e == cudaSuccess) e = cudaMalloc(&p->d_trans, tbytes);
   if (e == cudaSuccess) e = cudaMalloc(&p->d_emit, emit.size() * 2);
-  if (e == cudaSuccess) e = cudaMemcpy(p->d_trans, trans.data(), trans.size() * 2, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(p->d_trans, tsrc, tbytes, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(p->d_emit, emit.data(), emit.size() * 2, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     msvgb_vprofile_destroy(p);

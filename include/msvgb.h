@@ -398,6 +398,15 @@ typedef int (*msvgb_filter_fn)(void *user, const msvgb_filter_hit *hit);
 int msvgb_pipeline_filters(msvgb_ctx *ctx, const msvgb_filters *f, const uint8_t *codes, const int64_t *off,
                            int64_t n, int64_t block_size, int n_workers, msvgb_filter_fn fn, void *user,
                            msvgb_filter_stats *stats);
+/* A continuation that stores the hits: pass msvgb_filter_collect as fn and a
+ * msvgb_filter_sink as user. Hits beyond cap are counted in n but not stored
+ * (the sink never stops the run); the order is that of the worker threads. */
+typedef struct {
+  msvgb_filter_hit *hits;
+  int64_t           cap;
+  int64_t           n;        /* updated atomically */
+} msvgb_filter_sink;
+int msvgb_filter_collect(void *sink, const msvgb_filter_hit *hit);
 
 /* ---- host-side score helpers (exact reference expressions) --------------------- */
 /* tjb_b for target length L (p7_oprofile.c:511-519, 920-925). */
