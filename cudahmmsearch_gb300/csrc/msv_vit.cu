@@ -64,6 +64,15 @@ __device__ __forceinline__ int i32(const int4 &w, int e) { return e == 0 ? w.x :
 
 __device__ __forceinline__ int sat16(int v) { return min(32767, max(-32768, v)); }
 
+// a + b as an integer multiply-add by a register holding 1 (which the
+// compiler cannot fold): it issues on the FMA pipe, leaving the ALU pipe --
+// the one the max/clamp operations saturate -- to the rest
+__device__ __forceinline__ int add_f(int a, int b, int one) {
+  int r;
+  asm("mad.lo.s32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(one), "r"(b));
+  return r;
+}
+
 // signed 16-bit element e (0..7) of a vector
 __device__ __forceinline__ int h16(const uint4 &w, int e) {
   const uint32_t u = e < 2 ? w.x : e < 4 ? w.y : e < 6 ? w.z : w.w;
@@ -88,8 +97,9 @@ __device__ int vit_one(const VitDev &V, const uint8_t *sq, int L, int lane, int 
     const uint4 *em = V.emit + (size_t) x * NV * 32 + lane;
     // the transition costs are read anew each row (from L1): kept in
     // registers across rows they would crowd out the DP state
-    int opaque;
+    int opaque, one;
     asm volatile("mov.u32 %0, 0;" : "=r"(opaque));
+    asm volatile("mov.u32 %0, 1;" : "=r"(one));
     const int4 *tr = static_cast<const int4 *>(V.trans) + lane + opaque;
     // predecessors of this lane's first node: the previous lane's last node (old row)
     int pM = __shfl_up_sync(FULL, Mv[CV - 1], 1), pI = __shfl_up_sync(FULL, Iv[CV - 1], 1),
@@ -112,13 +122,13 @@ __device__ int vit_one(const VitDev &V, const uint8_t *sq, int L, int lane, int 
           else return h16(*reinterpret_cast<const uint4 *>(&t4[t]), e);
         };
         const int cM = Mv[j], cI = Iv[j], cD = Dv[j];
-        int sv = max(max(xB + tv(0), pM + tv(1)), max(pI + tv(2), pD + tv(3)));
+        int sv = max(max(add_f(xB, tv(0), one), pM + tv(1)), max(add_f(pI, tv(2), one), pD + tv(3)));
         sv = sat16(max(sv, -32768) + h16(e4, j % 8));
         xe = max(xe, sv);
         Mv[j] = sv;
-        Iv[j] = max(max(cM + tv(5), cI + tv(6)), -32768);
+        Iv[j] = max(max(cM + tv(5), add_f(cI, tv(6), one)), -32768);
         Dv[j] = dc;                                 // M->D from node k-1 (the delayed store)
-        dc = max(sv + tv(4), -32768);
+        dc = max(add_f(sv, tv(4), one), -32768);
         dmax = max(dmax, dc);
         pM = cM; pI = cI; pD = cD;
       }

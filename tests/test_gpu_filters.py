@@ -110,3 +110,16 @@ def test_pipeline_filters_stop_and_errors(ctx):
     with pytest.raises(api.MSVError) as e:
         api.biasfilter(ctx, r.compo, r.M, api.DeviceDB(ctx, s), np.array([s.n]))
     assert e.value.code == api.eslEINVAL
+
+
+def test_fn3_pipeline_statistics_match_tutorial_output(ctx):
+    """tutorial/fn3.out:106-112: one 86-node query, one target of 2554
+    residues (7LESS_DROME), passed the MSV, bias and Vit filters."""
+    r, s, p, vp = load("tut_fn3")
+    i = 46                                                  # globins45.fa (45), HBB_HUMAN, then 7LESS_DROME
+    one = s.subset(np.array([i]))
+    hits, st = api.pipeline_filters(ctx, p, one, vprof=vp, compo=r.compo, vmu=r.vmu, vlambda=r.vlambda)
+    assert p.M == 86
+    assert (st.nseqs, st.nres) == (1, 2554)
+    assert (st.n_past_msv, st.n_past_bias, st.n_past_vit) == (1, 1, 1)
+    assert hits["seq_index"].tolist() == [0] and r.stage[i] == 3
