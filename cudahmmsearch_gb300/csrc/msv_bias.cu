@@ -9,9 +9,15 @@
 // sequential in the residues and has two states, so one thread scores one
 // listed sequence, with the reference's float operations in its order:
 // round-to-nearest multiplies, adds and divides written as intrinsics (no
-// contraction into FMA), and each row's log taken in double and stored to
-// float as the reference's double log() of a float is. The length term
-// (logf of p1 and 1 - p1) is added on the host with the C library's logf.
+// contraction into FMA), and each row's log taken in double and rounded to
+// float as the reference's double log() of a float is. The double log is a
+// table-driven one (Tang's method, ACM TOMS 15(2), 1989: reduce by a table
+// entry, then a short polynomial; here 128 entries and the Taylor series of
+// log1p to degree 8), about 14 double operations instead of the library
+// log's many more on this part's narrow FP64 pipe; a row whose result lies
+// within 2^-48 (relative) of a float rounding boundary takes the library log
+// instead. The length term (logf of p1 and 1 - p1) is added on the host with
+// the C library's logf.
 #include <algorithm>
 #include <cmath>
 #include <string>
@@ -27,20 +33,62 @@ using msvgb_detail::fail;
 
 namespace {
 
+constexpr int kLogTab = 128;
+
 struct BiasDev {
   float eo[NRES][2];       // emission odds: [x][0] background state, [x][1] model-composition state
   float t10, t11;          // biased-state transitions 1->0, 1->1 (t[1][2] = 1)
   float pi0, pi1;
+  double2 logtab[kLogTab]; // per top-7-mantissa-bit interval: (1/c, log c) of its reduction point c
 };
 
+// float(log((double) m)) for a float m > 0: m = 2^e f, f in [1, 2); the top 7
+// bits of f pick the interval [1 + j/128, 1 + (j+1)/128), whose point c is
+// its midpoint (halved, with e + 1, from sqrt(2) up, so that f/c stays near
+// 1 and no sum cancels); the intervals next to 1 use c = 1 (m near 1: log m
+// = log1p(f - 1) with no table term). log m = e ln2 + log c + log1p(r),
+// r = f (1/c) - 1 by one fused multiply-add; |r| < 2^-7.
+__device__ __forceinline__ float log_row(float m, const double2 *tab) {
+  const uint32_t b = __float_as_uint(m);
+  if (b - 0x00800000u >= 0x7f000000u) return (float) log((double) m);   // 0, subnormal, inf, nan, negative
+  const int j = (b >> 16) & 0x7f;
+  int e = (int) (b >> 23) - 127;
+  double f = (double) __uint_as_float((b & 0x007fffffu) | 0x3f800000u);
+  if (j >= 53) { f *= 0.5; e += 1; }
+  const double2 t = tab[j];
+  const double r = fma(f, t.x, -1.0);
+  double p = -1.0 / 8;
+  p = fma(p, r, 1.0 / 7);
+  p = fma(p, r, -1.0 / 6);
+  p = fma(p, r, 1.0 / 5);
+  p = fma(p, r, -1.0 / 4);
+  p = fma(p, r, 1.0 / 3);
+  p = fma(p, r, -1.0 / 2);
+  p = fma(p, r, 1.0);
+  const double ln2_hi = 6.93147180369123816490e-01, ln2_lo = 1.90821492927058770002e-10;
+  const double de = (double) e;
+  const double y = fma(de, ln2_hi, t.y + fma(de, ln2_lo, p * r));
+  const float lo = __double2float_rn(y * (1.0 - 0x1p-48)), hi = __double2float_rn(y * (1.0 + 0x1p-48));
+  if (lo != hi) return (float) log((double) m);                       // near a float rounding boundary
+  return lo;
+}
+
+// One thread per listed sequence; threads take the list in database order
+// (order[t]: longest first), so a warp's sequences have similar lengths. Rows
+// go 16 at a time: first the 16 rows' recurrence (a serial chain through the
+// divisions), then their 16 logs, independent of one another, then the
+// in-order float sum.
 __global__ void __launch_bounds__(128)
-bias_kernel(BiasDev B, DbDev db, const int64_t *__restrict__ slots, int64_t nids, float *__restrict__ out,
-            int32_t *__restrict__ out_len) {
+bias_kernel(BiasDev B, DbDev db, const int64_t *__restrict__ slots, const int64_t *__restrict__ order, int64_t nids,
+            float *__restrict__ out, int32_t *__restrict__ out_len) {
   __shared__ float s_eo[NRES][2];
+  __shared__ double2 s_log[kLogTab];
   for (int i = threadIdx.x; i < NRES * 2; i += blockDim.x) (&s_eo[0][0])[i] = (&B.eo[0][0])[i];
+  for (int i = threadIdx.x; i < kLogTab; i += blockDim.x) s_log[i] = B.logtab[i];
   __syncthreads();
-  const int64_t j = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= nids) return;
+  const int64_t t = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nids) return;
+  const int64_t j = order[t];
   const int64_t s = slots[j];
   const int L = db.len[s];
   out_len[j] = L;
@@ -52,29 +100,36 @@ bias_kernel(BiasDev B, DbDev db, const int64_t *__restrict__ slots, int64_t nids
   for (int i0 = 0; i0 < L; i0 += 16) {
     const uint4 w = sq[i0 >> 4];
     const uint32_t words[4] = {w.x, w.y, w.z, w.w};
+    float mx[16];
 #pragma unroll
     for (int b = 0; b < 16; ++b) {
-      const int i = i0 + b;
-      if (i >= L) break;
+      mx[b] = 1.0f;
+      if (i0 + b >= L) continue;
       const int x = (words[b >> 2] >> (8 * (b & 3))) & 0xff;
       float n0, n1;
-      if (i == 0) {
+      if (i0 + b == 0) {
         n0 = __fmul_rn(s_eo[x][0], B.pi0);
         n1 = __fmul_rn(s_eo[x][1], B.pi1);
       } else {
         n0 = __fmul_rn(__fadd_rn(__fmul_rn(d0, t00), __fmul_rn(d1, B.t10)), s_eo[x][0]);
         n1 = __fmul_rn(__fadd_rn(__fmul_rn(d0, t01), __fmul_rn(d1, B.t11)), s_eo[x][1]);
       }
-      float mx = 0.0f;                           // ESL_MAX(dp, max) over k = 0, 1
-      mx = n0 > mx ? n0 : mx;
-      mx = n1 > mx ? n1 : mx;
-      d0 = __fdiv_rn(n0, mx);
-      d1 = __fdiv_rn(n1, mx);
-      logsc = __fadd_rn(logsc, (float) log((double) mx));
+      float m = 0.0f;                            // ESL_MAX(dp, max) over k = 0, 1
+      m = n0 > m ? n0 : m;
+      m = n1 > m ? n1 : m;
+      d0 = __fdiv_rn(n0, m);
+      d1 = __fdiv_rn(n1, m);
+      mx[b] = m;
     }
+    float lg[16];
+#pragma unroll
+    for (int b = 0; b < 16; ++b) lg[b] = log_row(mx[b], s_log);
+#pragma unroll
+    for (int b = 0; b < 16; ++b)
+      if (i0 + b < L) logsc = __fadd_rn(logsc, lg[b]);
   }
   const float end = __fadd_rn(d0, d1);           // dp[L][0] * 1 + dp[L][1] * 1
-  out[j] = __fadd_rn(logsc, (float) log((double) end));
+  out[j] = __fadd_rn(logsc, log_row(end, s_log));
 }
 
 // degenerate amino codes 21..26 (B J Z O U X) as sets of canonical codes
@@ -110,6 +165,13 @@ void filter_hmm(const float *compo, int M, BiasDev &B) {
   B.t11 = L1 / (L1 + 1.0f);
   B.pi0 = 0.999f;
   B.pi1 = 0.001f;
+  for (int j = 0; j < kLogTab; ++j) {
+    double c = 1.0 + (j + 0.5) / kLogTab;
+    if (j >= 53) c *= 0.5;                          // f >= 1 + 53/128 > sqrt(2) is halved
+    if (j == 0 || j == kLogTab - 1) c = 1.0;        // the intervals next to 1
+    const double inv = 1.0 / c;
+    B.logtab[j] = make_double2(inv, -std::log(inv));
+  }
 }
 
 }  // namespace
@@ -145,25 +207,32 @@ extern "C" int msvgb_biasfilter(msvgb_ctx *c, const float *compo, int M, const m
   BiasDev B;
   filter_hmm(compo, M, B);
   CUDA_TRY(msvgb_detail::ensure_inverse(c, db));
-  int64_t *d_ids = nullptr;
+  int64_t *d_ids = nullptr, *d_order = nullptr;
+  int32_t *d_cnt = nullptr;
   float *d_out = nullptr;
   int32_t *d_len = nullptr;
   std::vector<int32_t> lens((size_t) nids);
   CUDA_TRY(cudaMallocAsync((void **) &d_ids, nids * 8, c->stream));
+  CUDA_TRY(cudaMallocAsync((void **) &d_order, nids * 8, c->stream));
+  CUDA_TRY(cudaMallocAsync((void **) &d_cnt, std::max<int64_t>(db->n, 1) * 4, c->stream));
   CUDA_TRY(cudaMallocAsync((void **) &d_out, nids * 4, c->stream));
   CUDA_TRY(cudaMallocAsync((void **) &d_len, nids * 4, c->stream));
   cudaError_t e = cudaMemcpyAsync(d_ids, ids, nids * 8, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess) e = msvgb_detail::launch_gather_ids(d_ids, nids, db->d_inv, c->num_sms, c->stream);
+  if (e == cudaSuccess)
+    e = msvgb_detail::launch_order_by_slot(d_ids, nids, db->n, d_cnt, d_order, c->num_sms, c->stream);
   DbDev dbv{db->d_codes, db->d_start, db->d_len, db->d_orig, db->n};
   if (e == cudaSuccess) {
     (void) cudaGetLastError();
-    bias_kernel<<<(unsigned) ((nids + 127) / 128), 128, 0, c->stream>>>(B, dbv, d_ids, nids, d_out, d_len);
+    bias_kernel<<<(unsigned) ((nids + 127) / 128), 128, 0, c->stream>>>(B, dbv, d_ids, d_order, nids, d_out, d_len);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) msvgb_detail::count_launch();
   if (e == cudaSuccess) e = cudaMemcpyAsync(out_sc, d_out, nids * 4, cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(lens.data(), d_len, nids * 4, cudaMemcpyDeviceToHost, c->stream);
   cudaFreeAsync(d_ids, c->stream);
+  cudaFreeAsync(d_order, c->stream);
+  cudaFreeAsync(d_cnt, c->stream);
   cudaFreeAsync(d_out, c->stream);
   cudaFreeAsync(d_len, c->stream);
   const cudaError_t e2 = cudaStreamSynchronize(c->stream);

@@ -183,29 +183,121 @@ __device__ int vit_one(const VitDev &V, const uint8_t *sq, int L, int lane, int 
   return 0;
 }
 
+// Wide models (more than 48 nodes per lane, M > 1536, up to 256 per lane: M
+// <= 8192): the same recurrence with the M, I, D row in shared memory as
+// int16 (node-major, lane-minor: a warp's access to one node is 64
+// contiguous bytes, conflict-free) and a runtime width; transitions int16.
+// Two warps per block; 6 * 32 * CV bytes of shared memory per warp.
+__device__ int vit_one_wide(const VitDev &V, const uint8_t *sq, int L, int lane, int16_t *Ms, int16_t *Is,
+                            int16_t *Ds, int &xc_out) {
+  const int CV = V.CV, NV = vit_nv(CV), NT = NV;    // transition vectors hold 8 nodes, like the emissions
+  for (int j = 0; j < CV; ++j) Ms[j * 32 + lane] = Is[j * 32 + lane] = Ds[j * 32 + lane] = -32768;
+  __syncwarp();
+  const int move = V.move[L];
+  int xN = V.base_w;
+  int xB = (int16_t) (xN + move), xJ = -32768, xC = -32768;
+  const int4 *tr = static_cast<const int4 *>(V.trans) + lane;
+  for (int i = 0; i < L; ++i) {
+    const int x = sq[i];
+    const uint4 *em = V.emit + (size_t) x * NV * 32 + lane;
+    int pM = __shfl_up_sync(FULL, (int) Ms[(CV - 1) * 32 + lane], 1);
+    int pI = __shfl_up_sync(FULL, (int) Is[(CV - 1) * 32 + lane], 1);
+    int pD = __shfl_up_sync(FULL, (int) Ds[(CV - 1) * 32 + lane], 1);
+    if (lane == 0) pM = pI = pD = -32768;
+    int xe = -32768, dmax = -32768, dc = -32768;
+#pragma unroll 1
+    for (int q = 0; q < NT; ++q) {
+      uint4 t4[7];
+#pragma unroll
+      for (int t = 0; t < 7; ++t) t4[t] = *reinterpret_cast<const uint4 *>(&tr[(t * NT + q) * 32]);
+      const uint4 e4 = em[q * 32];
+#pragma unroll
+      for (int e = 0; e < 8; ++e) {
+        const int j = q * 8 + e;
+        const int a = j * 32 + lane;
+        const int cM = Ms[a], cI = Is[a], cD = Ds[a];
+        int sv = max(max(xB + h16(t4[0], e), pM + h16(t4[1], e)), max(pI + h16(t4[2], e), pD + h16(t4[3], e)));
+        sv = sat16(max(sv, -32768) + h16(e4, e));
+        xe = max(xe, sv);
+        Ms[a] = (int16_t) sv;
+        Is[a] = (int16_t) max(max(cM + h16(t4[5], e), cI + h16(t4[6], e)), -32768);
+        Ds[a] = (int16_t) dc;                       // M->D from node k-1 (the delayed store)
+        dc = max(sv + h16(t4[4], e), -32768);
+        dmax = max(dmax, dc);
+        pM = cM; pI = cI; pD = cD;
+      }
+    }
+    const int dprev = __shfl_up_sync(FULL, dc, 1);
+    Ds[lane] = (int16_t) (lane == 0 ? -32768 : dprev);
+    xe = __reduce_max_sync(FULL, xe);
+    dmax = __reduce_max_sync(FULL, dmax);
+    if (xe >= 32767) { xc_out = 32767; return 1; }  // eslERANGE
+    xN = (int16_t) (xN + V.xwN_loop);
+    xC = (int16_t) max(xC + V.xwC_loop, xe + V.xwE_move);
+    xJ = (int16_t) max(xJ + V.xwJ_loop, xe + V.xwE_loop);
+    xB = (int16_t) max(xJ + move, xN + move);
+    if (dmax + V.ddbound_w > xB) {                  // D->D closure over all nodes (as vit_one)
+      int c = -2000000000, b = 0;
+#pragma unroll 1
+      for (int q = 0; q < NT; ++q) {
+        const uint4 t7 = *reinterpret_cast<const uint4 *>(&tr[(7 * NT + q) * 32]);
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+          const int t = h16(t7, e);
+          c = max((int) Ds[(q * 8 + e) * 32 + lane], c + t);
+          b += t;
+          if (b < -2000000) b = -2000000;
+        }
+      }
+      int sc_c = c, sc_b = b;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const int oc = __shfl_up_sync(FULL, sc_c, d), ob = __shfl_up_sync(FULL, sc_b, d);
+        if (lane >= d) { sc_c = max(sc_c, oc + sc_b); sc_b = max(ob + sc_b, -2000000); }
+      }
+      int vin = __shfl_up_sync(FULL, sc_c, 1);
+      if (lane == 0) vin = -2000000000;
+#pragma unroll 1
+      for (int q = 0; q < NT; ++q) {
+        const uint4 t7 = *reinterpret_cast<const uint4 *>(&tr[(7 * NT + q) * 32]);
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+          const int a = (q * 8 + e) * 32 + lane;
+          const int dv = max((int) Ds[a], vin + h16(t7, e));
+          Ds[a] = (int16_t) dv;
+          vin = dv;
+        }
+      }
+    }
+  }
+  xc_out = xC;
+  return 0;
+}
+
 constexpr int kVitThreads = 64;   // two warps: occupancy in steps of two warps at any register count
 
 template <int CV>
 __global__ void __launch_bounds__(kVitThreads)
-vit_kernel(VitDev V, DbDev db, const int64_t *__restrict__ sorted_ids, int64_t nids, int *__restrict__ out_xc,
-           uint8_t *__restrict__ out_st, unsigned long long *__restrict__ ticket) {
+vit_kernel(VitDev V, DbDev db, const int64_t *__restrict__ slots, const int64_t *__restrict__ order, int64_t nids,
+           int *__restrict__ out_xc, uint8_t *__restrict__ out_st, unsigned long long *__restrict__ ticket) {
   const int lane = threadIdx.x & 31;
   for (;;) {
     unsigned long long t = 0;
     if (lane == 0) t = atomicAdd(ticket, 1ull);
     t = __shfl_sync(FULL, t, 0);
     if (t >= (unsigned long long) nids) break;
-    const int64_t s = sorted_ids[t];
+    const int64_t j = order[t];                     // database order: the longest sequences first
+    const int64_t s = slots[j];
     const int L = db.len[s];
     int xc = -32768;
     const int st = L > 0 ? vit_one<CV>(V, db.codes + db.start[s], L, lane, xc) : 0;
-    if (lane == 0) { out_xc[t] = xc; out_st[t] = (uint8_t) (L > 0 ? st : 2); }
+    if (lane == 0) { out_xc[j] = xc; out_st[j] = (uint8_t) (L > 0 ? st : 2); }
   }
 }
 
 template <int CV>
-cudaError_t launch_vit(const VitDev &V, const DbDev &db, const int64_t *ids, int64_t n, int *xc, uint8_t *st,
-                       unsigned long long *ticket, int sms, cudaStream_t stream) {
+cudaError_t launch_vit(const VitDev &V, const DbDev &db, const int64_t *ids, const int64_t *order, int64_t n, int *xc,
+                       uint8_t *st, unsigned long long *ticket, int sms, cudaStream_t stream) {
   int per_sm = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, vit_kernel<CV>, kVitThreads, 0);
   if (e != cudaSuccess) return e;
@@ -213,7 +305,8 @@ cudaError_t launch_vit(const VitDev &V, const DbDev &db, const int64_t *ids, int
   long long grid = (long long) std::max(1, per_sm) * sms;
   grid = std::min<long long>(grid, (n + warps - 1) / warps);
   (void) cudaGetLastError();
-  vit_kernel<CV><<<(unsigned) std::max<long long>(1, grid), kVitThreads, 0, stream>>>(V, db, ids, n, xc, st, ticket);
+  vit_kernel<CV><<<(unsigned) std::max<long long>(1, grid), kVitThreads, 0, stream>>>(V, db, ids, order, n, xc, st,
+                                                                                      ticket);
   return cudaGetLastError();
 }
 
@@ -221,10 +314,53 @@ cudaError_t launch_vit(const VitDev &V, const DbDev &db, const int64_t *ids, int
 // that holds its 8*Q8 nodes)
 constexpr int kVitCV[] = {1, 2, 3, 4, 6, 8, 12, 16, 24, 32, 40, 48};
 
-cudaError_t dispatch_vit(int CV, const VitDev &V, const DbDev &db, const int64_t *ids, int64_t n, int *xc,
-                         uint8_t *st, unsigned long long *ticket, int sms, cudaStream_t stream) {
+__global__ void __launch_bounds__(kVitThreads)
+vit_wide_kernel(VitDev V, DbDev db, const int64_t *__restrict__ slots, const int64_t *__restrict__ order, int64_t nids,
+                int *__restrict__ out_xc, uint8_t *__restrict__ out_st, unsigned long long *__restrict__ ticket) {
+  extern __shared__ int16_t s_row[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int16_t *Ms = s_row + (size_t) w * 3 * 32 * V.CV, *Is = Ms + 32 * V.CV, *Ds = Is + 32 * V.CV;
+  for (;;) {
+    unsigned long long t = 0;
+    if (lane == 0) t = atomicAdd(ticket, 1ull);
+    t = __shfl_sync(FULL, t, 0);
+    if (t >= (unsigned long long) nids) break;
+    const int64_t j = order[t];
+    const int64_t s = slots[j];
+    const int L = db.len[s];
+    int xc = -32768;
+    const int st = L > 0 ? vit_one_wide(V, db.codes + db.start[s], L, lane, Ms, Is, Ds, xc) : 0;
+    if (lane == 0) { out_xc[j] = xc; out_st[j] = (uint8_t) (L > 0 ? st : 2); }
+    __syncwarp();
+  }
+}
+
+constexpr int kVitWideMax = 256;   // nodes per lane of the widest model (M <= 8192)
+
+size_t vit_wide_smem(int CV) { return (size_t) (kVitThreads / 32) * 3 * 32 * CV * sizeof(int16_t); }
+
+cudaError_t launch_vit_wide(const VitDev &V, const DbDev &db, const int64_t *ids, const int64_t *order, int64_t n,
+                            int *xc, uint8_t *st, unsigned long long *ticket, int sms, cudaStream_t stream) {
+  const size_t smem = vit_wide_smem(V.CV);
+  cudaError_t e = cudaFuncSetAttribute(vit_wide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, vit_wide_kernel, kVitThreads, smem);
+  if (e != cudaSuccess) return e;
+  constexpr int warps = kVitThreads / 32;
+  long long grid = (long long) std::max(1, per_sm) * sms;
+  grid = std::min<long long>(grid, (n + warps - 1) / warps);
+  (void) cudaGetLastError();
+  vit_wide_kernel<<<(unsigned) std::max<long long>(1, grid), kVitThreads, smem, stream>>>(V, db, ids, order, n, xc,
+                                                                                          st, ticket);
+  return cudaGetLastError();
+}
+
+cudaError_t dispatch_vit(int CV, const VitDev &V, const DbDev &db, const int64_t *ids, const int64_t *order, int64_t n,
+                         int *xc, uint8_t *st, unsigned long long *ticket, int sms, cudaStream_t stream) {
+  if (CV > 48) return launch_vit_wide(V, db, ids, order, n, xc, st, ticket, sms, stream);
   switch (CV) {
-#define VCASE(c) case c: return launch_vit<c>(V, db, ids, n, xc, st, ticket, sms, stream);
+#define VCASE(c) case c: return launch_vit<c>(V, db, ids, order, n, xc, st, ticket, sms, stream);
     VCASE(1) VCASE(2) VCASE(3) VCASE(4) VCASE(6) VCASE(8) VCASE(12) VCASE(16) VCASE(24) VCASE(32) VCASE(40) VCASE(48)
 #undef VCASE
   }
@@ -287,7 +423,8 @@ extern "C" int msvgb_vprofile_create(msvgb_ctx *ctx, const msvgb_vom *v, msvgb_v
   const int Q8 = std::max(2, (v->M - 1) / 8 + 1), Np = 8 * Q8;
   int CV = -1;
   for (int c : kVitCV) if (32 * c >= Np) { CV = c; break; }
-  if (CV < 0) return fail(MSVGB_eslEINVAL, "ViterbiFilter profile: M exceeds the supported maximum (1536 nodes)");
+  if (CV < 0) CV = ((Np + 31) / 32 + 7) / 8 * 8;   // the shared-memory row, in whole transition vectors
+  if (CV > kVitWideMax) return fail(MSVGB_eslEINVAL, "ViterbiFilter profile: M exceeds the supported maximum (8192 nodes)");
   // node-order tables, lane-interleaved vectors of 8 nodes; nodes past 8*Q8
   // (and padding inside it) cost -32768 as the reference's do
   const int NV = vit_nv(CV), NT = vit_nt(CV), TN = vit_tnodes(CV);
@@ -362,14 +499,19 @@ extern "C" int msvgb_vitfilter(msvgb_ctx *c, msvgb_vprofile *p, const msvgb_db *
     p->d_move = d; p->move_cap = cap;
   }
   CUDA_TRY(msvgb_detail::ensure_inverse(c, db));
-  int64_t *d_ids = nullptr;
+  int64_t *d_ids = nullptr, *d_order = nullptr;
+  int32_t *d_cnt = nullptr;
   int *d_xc = nullptr;
   uint8_t *d_st = nullptr;
   CUDA_TRY(cudaMallocAsync((void **) &d_ids, nids * 8, c->stream));
+  CUDA_TRY(cudaMallocAsync((void **) &d_order, nids * 8, c->stream));
+  CUDA_TRY(cudaMallocAsync((void **) &d_cnt, std::max<int64_t>(db->n, 1) * 4, c->stream));
   CUDA_TRY(cudaMallocAsync((void **) &d_xc, nids * 4, c->stream));
   CUDA_TRY(cudaMallocAsync((void **) &d_st, nids, c->stream));
   cudaError_t e = cudaMemcpyAsync(d_ids, ids, nids * 8, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess) e = msvgb_detail::launch_gather_ids(d_ids, nids, db->d_inv, c->num_sms, c->stream);
+  if (e == cudaSuccess)
+    e = msvgb_detail::launch_order_by_slot(d_ids, nids, db->n, d_cnt, d_order, c->num_sms, c->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(c->d_ticket, 0, sizeof(unsigned long long), c->stream);
   VitDev V;
   V.CV = p->CV; V.base_w = p->base_w; V.ddbound_w = p->ddbound_w;
@@ -377,11 +519,13 @@ extern "C" int msvgb_vitfilter(msvgb_ctx *c, msvgb_vprofile *p, const msvgb_db *
   V.xwN_loop = p->xw[1][1]; V.xwJ_loop = p->xw[2][1]; V.xwC_loop = p->xw[3][1];
   V.trans = p->d_trans; V.emit = p->d_emit; V.move = p->d_move;
   DbDev dbv{db->d_codes, db->d_start, db->d_len, db->d_orig, db->n};
-  if (e == cudaSuccess) e = dispatch_vit(p->CV, V, dbv, d_ids, nids, d_xc, d_st, c->d_ticket, c->num_sms, c->stream);
+  if (e == cudaSuccess)
+    e = dispatch_vit(p->CV, V, dbv, d_ids, d_order, nids, d_xc, d_st, c->d_ticket, c->num_sms, c->stream);
   if (e == cudaSuccess) msvgb_detail::count_launch();
   if (e == cudaSuccess) e = cudaMemcpyAsync(out_xc, d_xc, nids * 4, cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(out_status, d_st, nids, cudaMemcpyDeviceToHost, c->stream);
-  cudaFreeAsync(d_ids, c->stream); cudaFreeAsync(d_xc, c->stream); cudaFreeAsync(d_st, c->stream);
+  cudaFreeAsync(d_ids, c->stream); cudaFreeAsync(d_order, c->stream); cudaFreeAsync(d_cnt, c->stream);
+  cudaFreeAsync(d_xc, c->stream); cudaFreeAsync(d_st, c->stream);
   const cudaError_t e2 = cudaStreamSynchronize(c->stream);
   if (e == cudaSuccess) e = e2;
   if (e != cudaSuccess) return fail(MSVGB_eslESYS, std::string("vitfilter: ") + cudaGetErrorString(e));

@@ -157,7 +157,7 @@ typedef struct {
   int16_t        base_w, ddbound_w;
 } msvgb_vom;
 typedef struct msvgb_vprofile msvgb_vprofile;
-/* Models up to 1536 nodes. */
+/* Models up to 8192 nodes (above 1536 the DP row lives in shared memory). */
 int msvgb_vprofile_create(msvgb_ctx *ctx, const msvgb_vom *vom, msvgb_vprofile **ret);
 int msvgb_vprofile_destroy(msvgb_vprofile *vp);
 /* p7_ViterbiFilter on the listed sequences of db (ids: original indices, e.g.

@@ -123,3 +123,20 @@ def test_fn3_pipeline_statistics_match_tutorial_output(ctx):
     assert (st.nseqs, st.nres) == (1, 2554)
     assert (st.n_past_msv, st.n_past_bias, st.n_past_vit) == (1, 1, 1)
     assert hits["seq_index"].tolist() == [0] and r.stage[i] == 3
+
+
+def test_biasfilter_matches_oracle_at_scale(ctx):
+    """Millions of rows: background sequences, sequences drawn from the
+    model's composition and from its commonest residues, all 29 codes."""
+    r, s0, p, vp = load("tut_pkinase")
+    rng = np.random.default_rng(9)
+    top = np.argsort(-r.compo)[:4]
+    extra = [rng.choice(20, size=int(rng.integers(50, 3000)), p=r.compo / r.compo.sum()).astype(np.uint8)
+             for _ in range(300)]
+    extra += [rng.choice(top, size=int(rng.integers(50, 3000))).astype(np.uint8) for _ in range(300)]
+    extra += [rng.integers(0, 29, size=int(rng.integers(1, 2000)), dtype=np.uint8) for _ in range(300)]
+    s = F.SeqSet.concat([F.synth_sequences(6000, seed=31, lmax=6000), F.SeqSet.from_list(extra)])
+    got = api.biasfilter(ctx, r.compo, r.M, api.DeviceDB(ctx, s))
+    want = O.bias_batch(r.compo, r.M, s)
+    assert s.total > 2_500_000
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))

@@ -1,7 +1,8 @@
 """The ViterbiFilter stage on the GPU (msvgb_vitfilter) against
 p7_ViterbiFilter's own golden results and the oracle: statuses and score bit
-patterns, for sampled models in hmmsearch's local mode and the tutorial Pfam
-models, over all sequences and over survivor lists."""
+patterns, for sampled models in hmmsearch's local mode (M = 1 .. 4000: the
+register row up to 1536 nodes, the shared-memory row above) and the tutorial
+Pfam models, over all sequences and over survivor lists."""
 import glob
 import os
 
@@ -15,7 +16,7 @@ from oracle import oracle as O
 pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 VIT = sorted(os.path.basename(p)[4:-6] for p in glob.glob(os.path.join(GOLDEN, "vit_*.vprof")))
-MAX_M = 1536
+MAX_M = 8192
 
 
 @pytest.fixture(scope="module")
@@ -35,11 +36,7 @@ def test_vitfilter_matches_reference_golden(ctx, name):
     vp = F.read_vprofile(os.path.join(GOLDEN, "vit_" + name + ".vprof"))
     s = F.read_seqs(os.path.join(GOLDEN, name + ".seqs"))
     st_ref, sc_ref = F.read_vresults(os.path.join(GOLDEN, "vit_" + name + ".vres"))
-    if vp.M > MAX_M:
-        with pytest.raises(api.MSVError) as e:
-            api.DeviceVProfile(ctx, vp)
-        assert e.value.code == api.eslEINVAL
-        return
+    assert vp.M <= MAX_M
     dvp = api.DeviceVProfile(ctx, vp)
     db = api.DeviceDB(ctx, s)
     st, sc = api.vitfilter(ctx, dvp, db)
@@ -52,7 +49,7 @@ def test_vitfilter_matches_reference_golden(ctx, name):
     assert np.array_equal(st2, st[ids]) and np.array_equal(sc2.view(np.uint32), sc[ids].view(np.uint32))
 
 
-@pytest.mark.parametrize("name", ["m200_s1", "m400_s1", "tut_pkinase", "m777_s3"])
+@pytest.mark.parametrize("name", ["m200_s1", "m400_s1", "tut_pkinase", "m777_s3", "m2400_s1"])
 def test_vitfilter_matches_oracle_on_homologs_and_long_targets(ctx, name):
     vp = F.read_vprofile(os.path.join(GOLDEN, "vit_" + name + ".vprof"))
     p = F.read_profile(os.path.join(GOLDEN, name + ".prof"))
@@ -74,3 +71,17 @@ def test_vitfilter_rejects_bad_indices(ctx):
     with pytest.raises(api.MSVError) as e:
         api.vitfilter(ctx, api.DeviceVProfile(ctx, vp), db, np.array([3, 10]))
     assert e.value.code == api.eslEINVAL
+
+
+def test_vitfilter_model_size_limit(ctx):
+    vp = F.read_vprofile(os.path.join(GOLDEN, "vit_m50_s1.vprof"))
+    for M, ok in ((8192, True), (8193, False)):
+        Q8 = max(2, (M - 1) // 8 + 1)
+        big = F.VProfile(M, np.full((8 * Q8, 8), -300, np.int16), np.zeros((29, Q8, 8), np.int16), vp.xw,
+                         vp.scale_w, vp.nj, vp.base_w, vp.ddbound_w)
+        if ok:
+            api.DeviceVProfile(ctx, big).close()
+        else:
+            with pytest.raises(api.MSVError) as e:
+                api.DeviceVProfile(ctx, big)
+            assert e.value.code == api.eslEINVAL
