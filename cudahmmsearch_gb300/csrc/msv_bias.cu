@@ -12,11 +12,11 @@
 // contraction into FMA), and each row's log taken in double and rounded to
 // float as the reference's double log() of a float is. The double log is a
 // table-driven one (Tang's method, ACM TOMS 15(2), 1989: reduce by a table
-// entry, then a short polynomial; here 128 entries and the Taylor series of
-// log1p to degree 8), about 14 double operations instead of the library
+// entry, then a short polynomial; here 512 entries and the Taylor series of
+// log1p to degree 6), about 8 double operations instead of the library
 // log's many more on this part's narrow FP64 pipe; a row whose result lies
-// within 2^-48 (relative) of a float rounding boundary takes the library log
-// instead. The length term (logf of p1 and 1 - p1) is added on the host with
+// within 64 units in the last place of a float rounding boundary takes the
+// library log instead. The length term (logf of p1 and 1 - p1) is added on the host with
 // the C library's logf.
 #include <algorithm>
 #include <cmath>
@@ -33,44 +33,51 @@ using msvgb_detail::fail;
 
 namespace {
 
-constexpr int kLogTab = 128;
+constexpr int kLogTab = 512;
 
 struct BiasDev {
   float eo[NRES][2];       // emission odds: [x][0] background state, [x][1] model-composition state
   float t10, t11;          // biased-state transitions 1->0, 1->1 (t[1][2] = 1)
   float pi0, pi1;
-  double2 logtab[kLogTab]; // per top-7-mantissa-bit interval: (1/c, log c) of its reduction point c
+  double2 logtab[kLogTab]; // per top-9-mantissa-bit interval: (1/c, log c) of its reduction point c
 };
 
-// float(log((double) m)) for a float m > 0: m = 2^e f, f in [1, 2); the top 7
-// bits of f pick the interval [1 + j/128, 1 + (j+1)/128), whose point c is
-// its midpoint (halved, with e + 1, from sqrt(2) up, so that f/c stays near
-// 1 and no sum cancels); the intervals next to 1 use c = 1 (m near 1: log m
-// = log1p(f - 1) with no table term). log m = e ln2 + log c + log1p(r),
-// r = f (1/c) - 1 by one fused multiply-add; |r| < 2^-7.
+// float(log((double) m)) for a float m > 0: m = 2^e f, f in [1, 2); the top 9
+// bits of f pick the interval [1 + j/512, 1 + (j+1)/512), whose point c is its
+// midpoint (halved, with e + 1, from j = 212 (f > 1.414) up, so that f/c stays
+// near 1 and no sum cancels); the intervals next to 1 use c = 1 (m near 1:
+// log m = log1p(f - 1), no table term). f, halved or not, is assembled as a
+// double from the float's bits. log m = e ln2 + log c + log1p(r), r = f (1/c)
+// - 1 by one fused multiply-add, |r| < 2^-9; log1p to degree 6 (truncation <
+// 2^-56 relative). The result's distance to the nearest float rounding
+// boundary is read from the low 29 bits of the double: within 64 units of the
+// last place the library log decides instead.
 __device__ __forceinline__ float log_row(float m, const double2 *tab) {
   const uint32_t b = __float_as_uint(m);
   if (b - 0x00800000u >= 0x7f000000u) return (float) log((double) m);   // 0, subnormal, inf, nan, negative
-  const int j = (b >> 16) & 0x7f;
-  int e = (int) (b >> 23) - 127;
-  double f = (double) __uint_as_float((b & 0x007fffffu) | 0x3f800000u);
-  if (j >= 53) { f *= 0.5; e += 1; }
+  const int j = (b >> 14) & 0x1ff;
+  const int half = j >= 212;
+  const int e = (int) (b >> 23) - 127 + half;
+  const double f = __longlong_as_double((long long) (((uint64_t) (b & 0x7fffffu) << 29) |
+                                                     ((uint64_t) (1023 - half) << 52)));
   const double2 t = tab[j];
   const double r = fma(f, t.x, -1.0);
-  double p = -1.0 / 8;
-  p = fma(p, r, 1.0 / 7);
-  p = fma(p, r, -1.0 / 6);
-  p = fma(p, r, 1.0 / 5);
+  double p = fma(-1.0 / 6, r, 1.0 / 5);
   p = fma(p, r, -1.0 / 4);
   p = fma(p, r, 1.0 / 3);
   p = fma(p, r, -1.0 / 2);
   p = fma(p, r, 1.0);
-  const double ln2_hi = 6.93147180369123816490e-01, ln2_lo = 1.90821492927058770002e-10;
-  const double de = (double) e;
-  const double y = fma(de, ln2_hi, t.y + fma(de, ln2_lo, p * r));
-  const float lo = __double2float_rn(y * (1.0 - 0x1p-48)), hi = __double2float_rn(y * (1.0 + 0x1p-48));
-  if (lo != hi) return (float) log((double) m);                       // near a float rounding boundary
-  return lo;
+  double y;
+  if (e == 0) {
+    y = fma(p, r, t.y);
+  } else {
+    const double ln2_hi = 6.93147180369123816490e-01, ln2_lo = 1.90821492927058770002e-10;
+    const double de = (double) e;
+    y = fma(de, ln2_hi, t.y + fma(de, ln2_lo, p * r));
+  }
+  const long long dist = (long long) ((uint64_t) __double_as_longlong(y) & 0x1fffffffull) - 0x10000000ll;
+  if (dist > -64 && dist < 64) return (float) log((double) m);      // near a float rounding boundary
+  return __double2float_rn(y);
 }
 
 // One thread per listed sequence; threads take the list in database order
@@ -167,7 +174,7 @@ void filter_hmm(const float *compo, int M, BiasDev &B) {
   B.pi1 = 0.001f;
   for (int j = 0; j < kLogTab; ++j) {
     double c = 1.0 + (j + 0.5) / kLogTab;
-    if (j >= 53) c *= 0.5;                          // f >= 1 + 53/128 > sqrt(2) is halved
+    if (j >= 212) c *= 0.5;                         // f >= 1 + 212/512 is halved
     if (j == 0 || j == kLogTab - 1) c = 1.0;        // the intervals next to 1
     const double inv = 1.0 / c;
     B.logtab[j] = make_double2(inv, -std::log(inv));
@@ -214,7 +221,7 @@ extern "C" int msvgb_biasfilter(msvgb_ctx *c, const float *compo, int M, const m
   std::vector<int32_t> lens((size_t) nids);
   CUDA_TRY(cudaMallocAsync((void **) &d_ids, nids * 8, c->stream));
   CUDA_TRY(cudaMallocAsync((void **) &d_order, nids * 8, c->stream));
-  CUDA_TRY(cudaMallocAsync((void **) &d_cnt, std::max<int64_t>(db->n, 1) * 4, c->stream));
+  CUDA_TRY(cudaMallocAsync((void **) &d_cnt, 1024 * 4, c->stream));
   CUDA_TRY(cudaMallocAsync((void **) &d_out, nids * 4, c->stream));
   CUDA_TRY(cudaMallocAsync((void **) &d_len, nids * 4, c->stream));
   cudaError_t e = cudaMemcpyAsync(d_ids, ids, nids * 8, cudaMemcpyHostToDevice, c->stream);

@@ -152,8 +152,9 @@ cudaError_t launch_histogram(const int32_t *len, int64_t n, unsigned long long *
 // inv[orig[s]] = s (original index -> sorted slot); ids[j] = inv[ids[j]].
 cudaError_t launch_invert(const int64_t *orig, int64_t n, int64_t *inv, int num_sms, cudaStream_t stream);
 cudaError_t launch_gather_ids(int64_t *ids, int64_t n, const int64_t *inv, int num_sms, cudaStream_t stream);
-// order[k] = the list positions j sorted by slots[j] (database order: longest
-// first; equal slots in any order); cnt: nslots int32 of scratch.
+// order[k] = the list positions j sorted by slots[j] in 1024 buckets of
+// consecutive slots (database order, the longest first, up to the order within
+// a bucket); nslots: the database's size; cnt: 1024 int32 of scratch.
 cudaError_t launch_order_by_slot(const int64_t *slots, int64_t n, int64_t nslots, int32_t *cnt, int64_t *order,
                                  int num_sms, cudaStream_t stream);
 cudaError_t launch_bins(const unsigned long long *hist, int Lmax, int64_t *bin_slot, int64_t *bin_byte, int64_t *pos,

@@ -154,43 +154,44 @@ gather_ids_kernel(int64_t *__restrict__ ids, int64_t n, const int64_t *__restric
 }
 
 // Listed sequences in database order (longest first): a counting sort of the
-// list positions j by slot[j]. cnt[slot] counts, is scanned to the first
-// position of each slot, then hands out positions.
-__global__ void __launch_bounds__(256)
-slot_count_kernel(const int64_t *__restrict__ slots, int64_t n, int32_t *__restrict__ cnt) {
-  for (int64_t j = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t) gridDim.x * blockDim.x)
-    atomicAdd(&cnt[slots[j]], 1);
+// list positions j into kOrderBuckets buckets of consecutive slots (the
+// database is sorted by length, so a bucket holds similar lengths; within one
+// the order is arbitrary). cnt[bucket] counts, is scanned to the first
+// position of each bucket, then hands out positions.
+constexpr int kOrderBuckets = 1024;
+
+__device__ __forceinline__ int slot_bucket(int64_t slot, int64_t nslots) {
+  return (int) ((slot * kOrderBuckets) / nslots);
 }
 
-// exclusive scan of cnt[0 .. m) in place; one block of 1024
-__global__ void __launch_bounds__(1024)
-slot_scan_kernel(int32_t *__restrict__ cnt, int64_t m) {
-  __shared__ int32_t s_sum[1024];
-  const int T = blockDim.x, t = threadIdx.x;
-  const int64_t per = (m + T - 1) / T, r0 = min(m, t * per), r1 = min(m, (t + 1) * per);
-  int32_t c = 0;
-  for (int64_t r = r0; r < r1; ++r) c += cnt[r];
+__global__ void __launch_bounds__(256)
+slot_count_kernel(const int64_t *__restrict__ slots, int64_t n, int64_t nslots, int32_t *__restrict__ cnt) {
+  for (int64_t j = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t) gridDim.x * blockDim.x)
+    atomicAdd(&cnt[slot_bucket(slots[j], nslots)], 1);
+}
+
+// exclusive scan of the kOrderBuckets counts in place; one block, one count per thread
+__global__ void __launch_bounds__(kOrderBuckets)
+slot_scan_kernel(int32_t *__restrict__ cnt) {
+  __shared__ int32_t s_sum[kOrderBuckets];
+  const int t = threadIdx.x;
+  const int32_t c = cnt[t];
   s_sum[t] = c;
   __syncthreads();
-  for (int d = 1; d < T; d <<= 1) {
+  for (int d = 1; d < kOrderBuckets; d <<= 1) {
     const int32_t v = t >= d ? s_sum[t - d] : 0;
     __syncthreads();
     s_sum[t] += v;
     __syncthreads();
   }
-  int32_t run = t ? s_sum[t - 1] : 0;
-  for (int64_t r = r0; r < r1; ++r) {
-    const int32_t x = cnt[r];
-    cnt[r] = run;
-    run += x;
-  }
+  cnt[t] = s_sum[t] - c;
 }
 
 __global__ void __launch_bounds__(256)
-slot_place_kernel(const int64_t *__restrict__ slots, int64_t n, int32_t *__restrict__ cnt,
+slot_place_kernel(const int64_t *__restrict__ slots, int64_t n, int64_t nslots, int32_t *__restrict__ cnt,
                   int64_t *__restrict__ order) {
   for (int64_t j = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t) gridDim.x * blockDim.x)
-    order[atomicAdd(&cnt[slots[j]], 1)] = j;
+    order[atomicAdd(&cnt[slot_bucket(slots[j], nslots)], 1)] = j;
 }
 
 int grid_for(int64_t n, int num_sms) {
@@ -235,12 +236,12 @@ cudaError_t msvgb_detail::launch_gather_ids(int64_t *ids, int64_t n, const int64
 cudaError_t msvgb_detail::launch_order_by_slot(const int64_t *slots, int64_t n, int64_t nslots, int32_t *cnt,
                                                int64_t *order, int num_sms, cudaStream_t stream) {
   if (n == 0) return cudaSuccess;
-  cudaError_t e = cudaMemsetAsync(cnt, 0, (size_t) nslots * 4, stream);
+  cudaError_t e = cudaMemsetAsync(cnt, 0, kOrderBuckets * sizeof(int32_t), stream);
   if (e != cudaSuccess) return e;
   (void) cudaGetLastError();
-  slot_count_kernel<<<grid_for(n, num_sms), 256, 0, stream>>>(slots, n, cnt);
-  slot_scan_kernel<<<1, 1024, 0, stream>>>(cnt, nslots);
-  slot_place_kernel<<<grid_for(n, num_sms), 256, 0, stream>>>(slots, n, cnt, order);
+  slot_count_kernel<<<grid_for(n, num_sms), 256, 0, stream>>>(slots, n, nslots, cnt);
+  slot_scan_kernel<<<1, kOrderBuckets, 0, stream>>>(cnt);
+  slot_place_kernel<<<grid_for(n, num_sms), 256, 0, stream>>>(slots, n, nslots, cnt, order);
   return cudaGetLastError();
 }
 

@@ -180,6 +180,22 @@ extern "C" int msvgb_filter_collect(void *user, const msvgb_filter_hit *hit) {
   return 0;
 }
 
+namespace {
+
+// A block scored by the MSV stage, waiting for the filter stages.
+struct MsvBlock {
+  int64_t b0 = 0, nb = 0;
+  msvgb_db *db = nullptr;
+  std::vector<uint8_t> xj, fl;
+};
+
+}  // namespace
+
+// Three kinds of threads: the caller uploads and MSV-searches block after
+// block on its context; one filter thread runs the bias and Viterbi stages of
+// each scored block on a second context (its own stream), so block k's
+// filter kernels overlap block k+1's upload and search on the GPU; the
+// workers run the continuation on the hits.
 extern "C" int msvgb_pipeline_filters(msvgb_ctx *ctx, const msvgb_filters *f, const uint8_t *codes,
                                       const int64_t *off, int64_t n, int64_t block_size, int n_workers,
                                       msvgb_filter_fn fn, void *user, msvgb_filter_stats *ret_stats) {
@@ -187,30 +203,87 @@ extern "C" int msvgb_pipeline_filters(msvgb_ctx *ctx, const msvgb_filters *f, co
     return fail(MSVGB_eslEINVAL, "msvgb_pipeline_filters: bad arguments");
   if (f->vom && f->vom->M != f->om->M) return fail(MSVGB_eslEINVAL, "MSV and Viterbi parts of different models");
   if (n_workers < 1) n_workers = 1;
+  msvgb_ctx *fctx = nullptr;
   msvgb_profile *prof = nullptr;
   msvgb_vprofile *vp = nullptr;
-  int st = msvgb_profile_create(ctx, f->om, &prof);
-  if (st == MSVGB_eslOK && f->vom) st = msvgb_vprofile_create(ctx, f->vom, &vp);
-  if (st != MSVGB_eslOK) { msvgb_profile_destroy(prof); return st; }
+  int st = msvgb_ctx_create(ctx->device, &fctx);
+  if (st == MSVGB_eslOK) st = msvgb_profile_create(ctx, f->om, &prof);
+  if (st == MSVGB_eslOK && f->vom) st = msvgb_vprofile_create(fctx, f->vom, &vp);
+  if (st != MSVGB_eslOK) {
+    msvgb_profile_destroy(prof);
+    msvgb_ctx_destroy(fctx);
+    return st;
+  }
 
   msvgb_filter_stats stats{};
   std::mutex mu;
-  std::condition_variable cv_push, cv_pop;
-  std::deque<HitBlock *> q;
+  std::condition_variable cv;                 // any change of the two queues or the flags below
+  std::deque<MsvBlock *> scored;              // MSV stage -> filter thread
+  std::deque<HitBlock *> hits;                // filter thread -> workers
   const size_t qcap = 2;
-  bool producing = true;
+  bool msv_done = false, filters_done = false;
   std::atomic<int> abort_flag{0};
+  int fst = MSVGB_eslOK;                      // the filter thread's status and message
+  std::string fmsg;
+
+  auto filter_thread = [&]() {
+    for (;;) {
+      MsvBlock *b = nullptr;
+      {
+        std::unique_lock<std::mutex> lk(mu);
+        cv.wait(lk, [&] { return !scored.empty() || msv_done; });
+        if (scored.empty()) break;
+        b = scored.front();
+        scored.pop_front();
+      }
+      cv.notify_all();
+      HitBlock *hb = new HitBlock();
+      int s2 = MSVGB_eslOK;
+      if (!abort_flag.load()) {
+        std::vector<int64_t> keep;
+        std::vector<float> usc;
+        for (int64_t i = 0; i < b->nb; ++i) {
+          const int L = (int) (off[b->b0 + i + 1] - off[b->b0 + i]);
+          stats.nseqs++;
+          stats.nres += L;
+          if (L == 0 || !(b->fl[i] & MSVGB_FLAG_PASS)) continue;   // empty, or P > F1 at the MSV stage
+          keep.push_back(i);
+          usc.push_back(msvgb_score(b->xj[i], b->fl[i], L, f->om->base_b, f->om->scale_b));
+        }
+        stats.n_past_msv += (int64_t) keep.size();
+        s2 = filter_block(fctx, f, vp, b->db, b->b0, off, keep, usc, stats, hb->hits);
+      }
+      msvgb_db_destroy(b->db);
+      delete b;
+      if (s2 != MSVGB_eslOK) {
+        delete hb;
+        std::lock_guard<std::mutex> lk(mu);
+        fst = s2;
+        fmsg = msvgb_last_error();                                   // thread-local: carried to the caller
+        abort_flag.store(1);
+        cv.notify_all();
+        continue;                                                    // drain the queue
+      }
+      std::unique_lock<std::mutex> lk(mu);
+      cv.wait(lk, [&] { return hits.size() < qcap; });
+      hits.push_back(hb);
+      cv.notify_all();
+    }
+    std::lock_guard<std::mutex> lk(mu);
+    filters_done = true;
+    cv.notify_all();
+  };
   auto worker = [&]() {
     for (;;) {
       HitBlock *b = nullptr;
       {
         std::unique_lock<std::mutex> lk(mu);
-        cv_pop.wait(lk, [&] { return !q.empty() || !producing; });
-        if (q.empty()) return;
-        b = q.front();
-        q.pop_front();
+        cv.wait(lk, [&] { return !hits.empty() || filters_done; });
+        if (hits.empty()) return;
+        b = hits.front();
+        hits.pop_front();
       }
-      cv_push.notify_one();
+      cv.notify_all();
       for (const msvgb_filter_hit &h : b->hits) {
         if (abort_flag.load()) break;
         if (fn && fn(user, &h) != 0) abort_flag.store(1);
@@ -218,50 +291,43 @@ extern "C" int msvgb_pipeline_filters(msvgb_ctx *ctx, const msvgb_filters *f, co
       delete b;
     }
   };
+  std::thread ft(filter_thread);
   std::vector<std::thread> workers;
   for (int t = 0; t < n_workers; ++t) workers.emplace_back(worker);
 
-  std::vector<uint8_t> xj, fl;
+  // MSV stage: upload and score one block after another
   for (int64_t b0 = 0; b0 < n && st == MSVGB_eslOK && !abort_flag.load(); b0 += block_size) {
-    const int64_t b1 = std::min(n, b0 + block_size), nb = b1 - b0;
-    xj.resize(nb); fl.resize(nb);
-    msvgb_db *db = nullptr;
-    st = msvgb_db_create(ctx, codes, off + b0, nb, &db);
-    if (st == MSVGB_eslOK) st = msvgb_search(ctx, prof, db, f->F1, xj.data(), fl.data());
-    HitBlock *blk = new HitBlock();
-    if (st == MSVGB_eslOK) {
-      std::vector<int64_t> keep;
-      std::vector<float> usc;
-      for (int64_t i = 0; i < nb; ++i) {
-        const int L = (int) (off[b0 + i + 1] - off[b0 + i]);
-        stats.nseqs++;
-        stats.nres += L;
-        if (L == 0 || !(fl[i] & MSVGB_FLAG_PASS)) continue;      // empty, or P > F1 at the MSV stage
-        keep.push_back(i);
-        usc.push_back(msvgb_score(xj[i], fl[i], L, f->om->base_b, f->om->scale_b));
-      }
-      stats.n_past_msv += (int64_t) keep.size();
-      st = filter_block(ctx, f, vp, db, b0, off, keep, usc, stats, blk->hits);
+    MsvBlock *b = new MsvBlock();
+    b->b0 = b0;
+    b->nb = std::min(n, b0 + block_size) - b0;
+    b->xj.resize(b->nb);
+    b->fl.resize(b->nb);
+    st = msvgb_db_create(ctx, codes, off + b0, b->nb, &b->db);
+    if (st == MSVGB_eslOK) st = msvgb_search(ctx, prof, b->db, f->F1, b->xj.data(), b->fl.data());
+    if (st != MSVGB_eslOK) {
+      msvgb_db_destroy(b->db);
+      delete b;
+      break;
     }
-    msvgb_db_destroy(db);
-    if (st != MSVGB_eslOK) { delete blk; break; }
-    {
-      std::unique_lock<std::mutex> lk(mu);
-      cv_push.wait(lk, [&] { return q.size() < qcap; });
-      q.push_back(blk);
-    }
-    cv_pop.notify_one();
+    std::unique_lock<std::mutex> lk(mu);
+    cv.wait(lk, [&] { return scored.size() < qcap || abort_flag.load(); });
+    scored.push_back(b);
+    cv.notify_all();
   }
   {
     std::lock_guard<std::mutex> lk(mu);
-    producing = false;
+    msv_done = true;
   }
-  cv_pop.notify_all();
+  cv.notify_all();
+  ft.join();
   for (auto &t : workers) t.join();
-  for (HitBlock *b : q) delete b;
+  for (MsvBlock *b : scored) { msvgb_db_destroy(b->db); delete b; }
+  for (HitBlock *b : hits) delete b;
   msvgb_vprofile_destroy(vp);
   msvgb_profile_destroy(prof);
+  msvgb_ctx_destroy(fctx);
   if (ret_stats) *ret_stats = stats;
+  if (st == MSVGB_eslOK && fst != MSVGB_eslOK) return fail(fst, fmsg);
   if (st == MSVGB_eslOK && abort_flag.load()) return fail(MSVGB_eslFAIL, "the continuation asked to stop");
   return st;
 }

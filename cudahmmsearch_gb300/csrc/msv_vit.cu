@@ -505,7 +505,7 @@ extern "C" int msvgb_vitfilter(msvgb_ctx *c, msvgb_vprofile *p, const msvgb_db *
   uint8_t *d_st = nullptr;
   CUDA_TRY(cudaMallocAsync((void **) &d_ids, nids * 8, c->stream));
   CUDA_TRY(cudaMallocAsync((void **) &d_order, nids * 8, c->stream));
-  CUDA_TRY(cudaMallocAsync((void **) &d_cnt, std::max<int64_t>(db->n, 1) * 4, c->stream));
+  CUDA_TRY(cudaMallocAsync((void **) &d_cnt, 1024 * 4, c->stream));
   CUDA_TRY(cudaMallocAsync((void **) &d_xc, nids * 4, c->stream));
   CUDA_TRY(cudaMallocAsync((void **) &d_st, nids, c->stream));
   cudaError_t e = cudaMemcpyAsync(d_ids, ids, nids * 8, cudaMemcpyHostToDevice, c->stream);
