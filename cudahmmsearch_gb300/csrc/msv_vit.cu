@@ -183,6 +183,148 @@ __device__ int vit_one(const VitDev &V, const uint8_t *sq, int L, int lane, int 
   return 0;
 }
 
+// ---- packed form: two nodes per 32-bit word ------------------------------------
+// Lane l owns nodes l*CV+1 .. (l+1)*CV as W = CV/2 words; word w holds node
+// l*CV + w + 1 in its low half and node l*CV + W + w + 1 in its high half, so
+// the predecessors of word w are word w-1 (both halves) and, for word 0, the
+// previous lane's last node (low half) and this lane's word W-1 low half
+// (high half). Every operation is a 16x2 SIMD instruction on both nodes. A
+// saturating add of a cost t <= 0 is add(max(v, -32768 - t), t) with the bound
+// from a table; the emission add clamps between -32768 - min(e, 0) =
+// ~(min(e, 0) + 32767) and 32767 - max(e, 0) = max(e, 0) ^ 0x7fff.
+// Tables: uint4 vectors of 4 words, [table][NV4][32]: the 7 costs BM MM IM DM
+// MD MI II, their 7 bounds, DD into the node; emissions [NRES][NV4][32].
+constexpr int kPT = 15;
+__host__ __device__ constexpr int vitp_nv4(int CV) { return (CV / 2 + 3) / 4; }
+
+__device__ __forceinline__ uint32_t v2add(uint32_t a, uint32_t b) { return add_s16x2(a, b); }
+__device__ __forceinline__ uint32_t v2max(uint32_t a, uint32_t b) { return max_s16x2(a, b); }
+__device__ __forceinline__ uint32_t v2min(uint32_t a, uint32_t b) { return min_s16x2(a, b); }
+__device__ __forceinline__ uint32_t u4w(const uint4 &v, int e) { return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w; }
+__device__ __forceinline__ int lo16(uint32_t x) { return (int) (int16_t) (x & 0xffffu); }
+__device__ __forceinline__ int hi16(uint32_t x) { return (int) x >> 16; }
+__device__ __forceinline__ uint32_t set_lo(uint32_t x, int v) { return __byte_perm(x, (uint32_t) v, 0x3254); }
+__device__ __forceinline__ uint32_t set_hi(uint32_t x, int v) { return __byte_perm(x, (uint32_t) v, 0x5410); }
+
+template <int CV>
+__device__ int vitp_one(const VitDev &V, const uint8_t *sq, int L, int lane, int &xc_out) {
+  constexpr int W = CV / 2, NV4 = vitp_nv4(CV);
+  constexpr uint32_t FLOOR = 0x80008000u;
+  uint32_t Mv[W], Iv[W], Dv[W];
+#pragma unroll
+  for (int w = 0; w < W; ++w) Mv[w] = Iv[w] = Dv[w] = FLOOR;
+  const int move = V.move[L];
+  int xN = V.base_w;
+  int xB = (int16_t) (xN + move), xJ = -32768, xC = -32768;
+  for (int i = 0; i < L; ++i) {
+    const int x = sq[i];
+    const uint4 *em = V.emit + (size_t) x * NV4 * 32 + lane;
+    int opaque;
+    asm volatile("mov.u32 %0, 0;" : "=r"(opaque));
+    const uint4 *tr = static_cast<const uint4 *>(V.trans) + lane + opaque;
+    const uint32_t xBp = (uint32_t) (xB & 0xffff) * 0x10001u;
+    // predecessors of word 0 (old row): previous lane's last node, this lane's word W-1 low half
+    uint32_t sM = __shfl_up_sync(FULL, Mv[W - 1], 1), sI = __shfl_up_sync(FULL, Iv[W - 1], 1),
+             sD = __shfl_up_sync(FULL, Dv[W - 1], 1);
+    if (lane == 0) sM = sI = sD = FLOOR;
+    uint32_t pM = __byte_perm(sM, Mv[W - 1], 0x5432), pI = __byte_perm(sI, Iv[W - 1], 0x5432),
+             pD = __byte_perm(sD, Dv[W - 1], 0x5432);
+    uint32_t xe = FLOOR, dmax = FLOOR, dc = FLOOR;
+#pragma unroll
+    for (int q = 0; q < NV4; ++q) {
+      // a zero computed from the previous group's result: this group's table
+      // loads cannot be hoisted above it, so one group's 56 words are live at a time
+      int zq;
+      asm volatile("and.b32 %0, %1, 0;" : "=r"(zq) : "r"(dc));
+      uint4 t4[14];
+#pragma unroll
+      for (int t = 0; t < 14; ++t) t4[t] = tr[(t * NV4 + q) * 32 + zq];
+      const uint4 e4 = em[q * 32 + zq];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int w = q * 4 + e;
+        if (w >= W) break;
+        const uint32_t cM = Mv[w], cI = Iv[w], cD = Dv[w];
+        const uint32_t c1 = v2add(v2max(xBp, u4w(t4[7], e)), u4w(t4[0], e));
+        const uint32_t c2 = v2add(v2max(pM, u4w(t4[8], e)), u4w(t4[1], e));
+        const uint32_t c3 = v2add(v2max(pI, u4w(t4[9], e)), u4w(t4[2], e));
+        const uint32_t c4 = v2add(v2max(pD, u4w(t4[10], e)), u4w(t4[3], e));
+        uint32_t sv = v2max(v2max(c1, c2), v2max(c3, c4));
+        const uint32_t ev = u4w(e4, e);
+        const uint32_t en = v2min(ev, 0u), ep = v2max(ev, 0u);
+        sv = v2add(v2min(v2max(sv, ~v2add(en, 0x7fff7fffu)), ep ^ 0x7fff7fffu), ev);
+        xe = v2max(xe, sv);
+        Mv[w] = sv;
+        Iv[w] = v2max(v2add(v2max(cM, u4w(t4[12], e)), u4w(t4[5], e)), v2add(v2max(cI, u4w(t4[13], e)), u4w(t4[6], e)));
+        Dv[w] = dc;                                 // M->D from word w-1 (the delayed store)
+        dc = v2add(v2max(sv, u4w(t4[11], e)), u4w(t4[4], e));
+        dmax = v2max(dmax, dc);
+        pM = cM; pI = cI; pD = cD;
+      }
+    }
+    // word 0's M->D: the previous lane's last node (low half), this lane's word W-1 low half (high half)
+    uint32_t sdc = __shfl_up_sync(FULL, dc, 1);
+    if (lane == 0) sdc = FLOOR;
+    Dv[0] = __byte_perm(sdc, dc, 0x5432);
+    int xes = max(lo16(xe), hi16(xe)), dms = max(lo16(dmax), hi16(dmax));
+    xes = __reduce_max_sync(FULL, xes);
+    dms = __reduce_max_sync(FULL, dms);
+    if (xes >= 32767) { xc_out = 32767; return 1; } // eslERANGE
+    xN = (int16_t) (xN + V.xwN_loop);
+    xC = (int16_t) max(xC + V.xwC_loop, xes + V.xwE_move);
+    xJ = (int16_t) max(xJ + V.xwJ_loop, xes + V.xwE_loop);
+    xB = (int16_t) max(xJ + move, xN + move);
+    if (dms + V.ddbound_w > xB) {                   // D->D closure over all nodes (as vit_one), in node order:
+      // the low halves of words 0 .. W-1, then the high halves; DD costs reread from L1
+      int c = -2000000000, b = 0;
+#pragma unroll
+      for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int q = 0; q < NV4; ++q) {
+          int zq;                                   // loads wait for the running value (no hoisting)
+          asm volatile("and.b32 %0, %1, 0;" : "=r"(zq) : "r"(c));
+          const uint4 t7 = tr[(14 * NV4 + q) * 32 + zq];
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const int w = q * 4 + e;
+            if (w >= W) break;
+            const int t = h ? hi16(u4w(t7, e)) : lo16(u4w(t7, e));
+            c = max(h ? hi16(Dv[w]) : lo16(Dv[w]), c + t);
+            b += t;
+            if (b < -2000000) b = -2000000;
+          }
+        }
+      int sc_c = c, sc_b = b;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const int oc = __shfl_up_sync(FULL, sc_c, d), ob = __shfl_up_sync(FULL, sc_b, d);
+        if (lane >= d) { sc_c = max(sc_c, oc + sc_b); sc_b = max(ob + sc_b, -2000000); }
+      }
+      int vin = __shfl_up_sync(FULL, sc_c, 1);
+      if (lane == 0) vin = -2000000000;
+#pragma unroll
+      for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int q = 0; q < NV4; ++q) {
+          int zq;
+          asm volatile("and.b32 %0, %1, 0;" : "=r"(zq) : "r"(vin));
+          const uint4 t7 = tr[(14 * NV4 + q) * 32 + zq];
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const int w = q * 4 + e;
+            if (w >= W) break;
+            const int t = h ? hi16(u4w(t7, e)) : lo16(u4w(t7, e));
+            const int dv = max(h ? hi16(Dv[w]) : lo16(Dv[w]), vin + t);
+            Dv[w] = h ? set_hi(Dv[w], dv) : set_lo(Dv[w], dv);
+            vin = dv;
+          }
+        }
+    }
+  }
+  xc_out = xC;
+  return 0;
+}
+
 // Wide models (more than 48 nodes per lane, M > 1536, up to 256 per lane: M
 // <= 8192): the same recurrence with the M, I, D row in shared memory as
 // int16 (node-major, lane-minor: a warp's access to one node is 64
@@ -296,6 +438,40 @@ vit_kernel(VitDev V, DbDev db, const int64_t *__restrict__ slots, const int64_t 
 }
 
 template <int CV>
+__global__ void __launch_bounds__(kVitThreads)
+vitp_kernel(VitDev V, DbDev db, const int64_t *__restrict__ slots, const int64_t *__restrict__ order, int64_t nids,
+            int *__restrict__ out_xc, uint8_t *__restrict__ out_st, unsigned long long *__restrict__ ticket) {
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    unsigned long long t = 0;
+    if (lane == 0) t = atomicAdd(ticket, 1ull);
+    t = __shfl_sync(FULL, t, 0);
+    if (t >= (unsigned long long) nids) break;
+    const int64_t j = order[t];                     // database order: the longest sequences first
+    const int64_t s = slots[j];
+    const int L = db.len[s];
+    int xc = -32768;
+    const int st = L > 0 ? vitp_one<CV>(V, db.codes + db.start[s], L, lane, xc) : 0;
+    if (lane == 0) { out_xc[j] = xc; out_st[j] = (uint8_t) (L > 0 ? st : 2); }
+  }
+}
+
+template <int CV>
+cudaError_t launch_vitp(const VitDev &V, const DbDev &db, const int64_t *ids, const int64_t *order, int64_t n, int *xc,
+                        uint8_t *st, unsigned long long *ticket, int sms, cudaStream_t stream) {
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, vitp_kernel<CV>, kVitThreads, 0);
+  if (e != cudaSuccess) return e;
+  constexpr int warps = kVitThreads / 32;
+  long long grid = (long long) std::max(1, per_sm) * sms;
+  grid = std::min<long long>(grid, (n + warps - 1) / warps);
+  (void) cudaGetLastError();
+  vitp_kernel<CV><<<(unsigned) std::max<long long>(1, grid), kVitThreads, 0, stream>>>(V, db, ids, order, n, xc, st,
+                                                                                       ticket);
+  return cudaGetLastError();
+}
+
+template <int CV>
 cudaError_t launch_vit(const VitDev &V, const DbDev &db, const int64_t *ids, const int64_t *order, int64_t n, int *xc,
                        uint8_t *st, unsigned long long *ticket, int sms, cudaStream_t stream) {
   int per_sm = 0;
@@ -311,8 +487,13 @@ cudaError_t launch_vit(const VitDev &V, const DbDev &db, const int64_t *ids, con
 }
 
 // nodes per lane compiled (none spills; a model runs at the smallest width
-// that holds its 8*Q8 nodes)
+// that holds its 8*Q8 nodes): one node per int32 register up to 32 (measured
+// faster there than the packed form: 733 vs 604 GCUPS at M=200, 734 vs 652 at
+// M=400), two per register (the packed form) at 40 and 48, where the int32
+// form would need 16-bit transitions (851 vs 802 GCUPS at M=1500), the
+// shared-memory row above 48
 constexpr int kVitCV[] = {1, 2, 3, 4, 6, 8, 12, 16, 24, 32, 40, 48};
+constexpr bool vit_packed(int CV) { return CV == 40 || CV == 48; }
 
 __global__ void __launch_bounds__(kVitThreads)
 vit_wide_kernel(VitDev V, DbDev db, const int64_t *__restrict__ slots, const int64_t *__restrict__ order, int64_t nids,
@@ -361,8 +542,11 @@ cudaError_t dispatch_vit(int CV, const VitDev &V, const DbDev &db, const int64_t
   if (CV > 48) return launch_vit_wide(V, db, ids, order, n, xc, st, ticket, sms, stream);
   switch (CV) {
 #define VCASE(c) case c: return launch_vit<c>(V, db, ids, order, n, xc, st, ticket, sms, stream);
-    VCASE(1) VCASE(2) VCASE(3) VCASE(4) VCASE(6) VCASE(8) VCASE(12) VCASE(16) VCASE(24) VCASE(32) VCASE(40) VCASE(48)
+    VCASE(1) VCASE(2) VCASE(3) VCASE(4) VCASE(6) VCASE(8) VCASE(12) VCASE(16) VCASE(24) VCASE(32)
 #undef VCASE
+#define PCASE(c) case c: return launch_vitp<c>(V, db, ids, order, n, xc, st, ticket, sms, stream);
+    PCASE(40) PCASE(48)
+#undef PCASE
   }
   return cudaErrorInvalidValue;
 }
@@ -421,6 +605,8 @@ extern "C" int msvgb_vprofile_create(msvgb_ctx *ctx, const msvgb_vom *v, msvgb_v
   *ret = nullptr;
   if (v->M < 1 || v->Kp != 29) return fail(MSVGB_eslEINVAL, "ViterbiFilter profile: M >= 1 and amino (Kp = 29) only");
   const int Q8 = std::max(2, (v->M - 1) / 8 + 1), Np = 8 * Q8;
+  for (int i = 0; i < 8 * Q8 * 8; ++i)
+    if (v->twv[i] > 0) return fail(MSVGB_eslEINVAL, "ViterbiFilter profile: transition costs must be <= 0 (log probabilities)");
   int CV = -1;
   for (int c : kVitCV) if (32 * c >= Np) { CV = c; break; }
   if (CV < 0) CV = ((Np + 31) / 32 + 7) / 8 * 8;   // the shared-memory row, in whole transition vectors
@@ -450,16 +636,47 @@ extern "C" int msvgb_vprofile_create(msvgb_ctx *ctx, const msvgb_vom *v, msvgb_v
   std::vector<int16_t> trans16;                     // the int16 form for lanes wider than 32 nodes
   if (!vit_t32(CV)) trans16.assign(trans.begin(), trans.end());
   const void *tsrc = vit_t32(CV) ? (const void *) trans.data() : (const void *) trans16.data();
-  const size_t tbytes = trans.size() * (vit_t32(CV) ? 4 : 2);
+  size_t tbytes = trans.size() * (vit_t32(CV) ? 4 : 2);
+  const void *esrc = emit.data();
+  size_t ebytes = emit.size() * 2;
+  // the packed form (8 .. 96 nodes per lane): two nodes per word
+  const bool packed = vit_packed(CV);
+  std::vector<uint32_t> ptr, pem;
+  if (packed) {
+    const int W = CV / 2, NV4 = vitp_nv4(CV);
+    auto at_p = [&](int table, int lane, int w) { return (((size_t) table * NV4 + w / 4) * 32 + lane) * 4 + w % 4; };
+    auto put = [](uint32_t &word, int h, int v) {
+      word = h ? (word & 0xffffu) | ((uint32_t) (uint16_t) v << 16) : (word & 0xffff0000u) | (uint16_t) v;
+    };
+    ptr.assign((size_t) kPT * NV4 * 32 * 4, 0);
+    pem.assign((size_t) NRES * NV4 * 32 * 4, 0);
+    for (int lane = 0; lane < 32; ++lane)
+      for (int w = 0; w < W; ++w)
+        for (int h = 0; h < 2; ++h) {
+          const int k = lane * CV + h * W + w + 1;
+          const bool real = k <= Np;
+          const int q = (k - 1) % Q8, z = (k - 1) / Q8;
+          for (int t = 0; t < 7; ++t) {
+            const int c = real ? v->twv[(q * 7 + t) * 8 + z] : -32768;
+            put(ptr[at_p(t, lane, w)], h, c);
+            put(ptr[at_p(7 + t, lane, w)], h, -32768 - c);          // the saturating add's bound
+          }
+          put(ptr[at_p(14, lane, w)], h, real && k > 1 ? striped(v->twv, 7 * Q8, k - 1) : -32768);
+          for (int x = 0; x < NRES; ++x)
+            put(pem[at_p(x, lane, w)], h, real && x < v->Kp ? v->rwv[(x * Q8 + q) * 8 + z] : -32768);
+        }
+    tsrc = ptr.data(); tbytes = ptr.size() * 4;
+    esrc = pem.data(); ebytes = pem.size() * 4;
+  }
   msvgb_vprofile *p = new msvgb_vprofile();
   p->ctx = ctx; p->device = ctx->device; p->M = v->M; p->Q8 = Q8; p->CV = CV;
   p->scale_w = v->scale_w; p->nj = v->nj; p->base_w = v->base_w; p->ddbound_w = v->ddbound_w;
   memcpy(p->xw, v->xw, sizeof p->xw);
   cudaError_t e = cudaSetDevice(ctx->device);
   if (e == cudaSuccess) e = cudaMalloc(&p->d_trans, tbytes);
-  if (e == cudaSuccess) e = cudaMalloc(&p->d_emit, emit.size() * 2);
+  if (e == cudaSuccess) e = cudaMalloc(&p->d_emit, ebytes);
   if (e == cudaSuccess) e = cudaMemcpy(p->d_trans, tsrc, tbytes, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(p->d_emit, emit.data(), emit.size() * 2, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(p->d_emit, esrc, ebytes, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     msvgb_vprofile_destroy(p);
     return fail(MSVGB_eslESYS, std::string("vprofile upload: ") + cudaGetErrorString(e));

@@ -148,18 +148,20 @@ def make_vit(tut):
     for name, idx in TUT_MODELS:
         run("vitfile", os.path.join(tut, "minifam"), idx, os.path.join(HERE, "vit_" + name + ".vprof"),
             os.path.join(HERE, "vit_" + name + ".vres"), os.path.join(HERE, name + ".seqs"))
-    # a wide model (the shared-memory row of the GPU kernel): background, homologs, saturation repeats
+    # models for the GPU kernel's other row forms: M=1100 (40 nodes per lane, two per
+    # register) and M=4000 (the shared-memory row); background, homologs, saturation repeats
     tmp = os.path.join(HERE, "_tmp.seqs")
-    parts = [F.synth_sequences(24, seed=4001, lmax=3000)]
-    run("emit", 4000, 7, 100, MODE_LOCAL, 6, 4002, 1, tmp)
-    parts.append(F.read_seqs(tmp))
-    run("emit", 4000, 7, 20, MODE_LOCAL, 2, 4003, 4, tmp)
-    parts.append(F.read_seqs(tmp))
+    for name, M, seed in (("vitmid_m1100_s4", 1100, 4), ("vitwide_m4000_s7", 4000, 7)):
+        parts = [F.synth_sequences(24, seed=M + 1, lmax=3000)]
+        run("emit", M, seed, 100, MODE_LOCAL, 6, M + 2, 1, tmp)
+        parts.append(F.read_seqs(tmp))
+        run("emit", M, seed, 20, MODE_LOCAL, 2, M + 3, 4, tmp)
+        parts.append(F.read_seqs(tmp))
+        F.write_seqs(F.SeqSet.concat(parts), os.path.join(HERE, name + ".seqs"))
+        run("vit", M, seed, os.path.join(HERE, "vit_" + name + ".vprof"), os.path.join(HERE, "vit_" + name + ".vres"),
+            os.path.join(HERE, name + ".seqs"))
     os.remove(tmp)
-    F.write_seqs(F.SeqSet.concat(parts), os.path.join(HERE, "vitwide_m4000_s7.seqs"))
-    run("vit", 4000, 7, os.path.join(HERE, "vit_vitwide_m4000_s7.vprof"), os.path.join(HERE, "vit_vitwide_m4000_s7.vres"),
-        os.path.join(HERE, "vitwide_m4000_s7.seqs"))
-    print("vit goldens:", len(VIT_SAMPLED) + len(TUT_MODELS) + 1)
+    print("vit goldens:", len(VIT_SAMPLED) + len(TUT_MODELS) + 2)
 
 
 # pipeline goldens: sampled models in hmmsearch's local mode, and the tutorial models
