@@ -11,9 +11,18 @@
  * are pinned to the reference's golden vectors (tests/test_port_golden.py).
  * The product never links it.
  *
- * The few vector operations it needs are wrapped below for NEON (aarch64)
- * and SSE2 (x86-64): unsigned/signed saturating byte arithmetic, byte max,
- * a one-byte lane shift and a horizontal max.
+ * The few vector operations it needs are wrapped below: NEON intrinsics on
+ * aarch64 (the hosts it is timed on), and elsewhere GCC vector extensions
+ * with the saturating byte arithmetic written out (slower; used by the tests
+ * on other hosts): unsigned/signed saturating byte arithmetic, byte max, a
+ * one-byte lane shift and a horizontal max.
+ *
+ * The SSV pass follows the reference's register scheme
+ * (ssvfilter.c:215-330): with no J state the diagonals never meet, so a
+ * register follows 16 diagonals down the whole sequence -- one saturating
+ * subtract, one max and one profile load per row, a byte shift where its
+ * vector index wraps -- and the Q vectors are covered by sweeps of up to 8
+ * registers; no DP row is kept in memory.
  *
  * Build: cc -O3 -ffp-contract=off -fPIC -shared -pthread msv_port.c msv_oracle.c -lm
  */
@@ -37,25 +46,26 @@ static inline v16 v_shl1(v16 a) { return vextq_u8(vdupq_n_u8(0), a, 15); }  /* l
 static inline v16 v_or(v16 a, v16 b) { return vorrq_u8(a, b); }
 static inline uint8_t v_hmax(v16 a) { return vmaxvq_u8(a); }
 static inline v16 v_load(const uint8_t *p) { return vld1q_u8(p); }
-#elif defined(__SSE2__)
-#include <emmintrin.h>
-typedef __m128i v16;
-static inline v16 v_set1(uint8_t x) { return _mm_set1_epi8((char) x); }
-static inline v16 v_subs_u8(v16 a, v16 b) { return _mm_subs_epu8(a, b); }
-static inline v16 v_adds_u8(v16 a, v16 b) { return _mm_adds_epu8(a, b); }
-static inline v16 v_max_u8(v16 a, v16 b) { return _mm_max_epu8(a, b); }
-static inline v16 v_subs_s8(v16 a, v16 b) { return _mm_subs_epi8(a, b); }
-static inline v16 v_shl1(v16 a) { return _mm_slli_si128(a, 1); }
-static inline v16 v_or(v16 a, v16 b) { return _mm_or_si128(a, b); }
-static inline uint8_t v_hmax(v16 a) {
-  uint8_t t[16]; int z; uint8_t m = 0;
-  _mm_storeu_si128((__m128i *) t, a);
-  for (z = 0; z < 16; z++) if (t[z] > m) m = t[z];
-  return m;
-}
-static inline v16 v_load(const uint8_t *p) { return _mm_loadu_si128((const __m128i *) p); }
 #else
-#error "msv_port.c needs NEON or SSE2"
+typedef uint8_t v16 __attribute__((vector_size(16)));
+typedef int8_t v16s __attribute__((vector_size(16)));
+static inline v16 v_set1(uint8_t x) { v16 r; for (int z = 0; z < 16; z++) r[z] = x; return r; }
+static inline v16 v_subs_u8(v16 a, v16 b) { return (v16) ((a - b) & (v16) (a >= b)); }
+static inline v16 v_adds_u8(v16 a, v16 b) { v16 s = a + b; return (v16) (s | (v16) (s < a)); }
+static inline v16 v_max_u8(v16 a, v16 b) { const v16 m = (v16) (a > b); return (a & m) | (b & ~m); }
+static inline v16 v_subs_s8(v16 a, v16 b) {
+  const v16s x = (v16s) a, y = (v16s) b, r = x - y;
+  const v16s ov = ((x ^ y) & (x ^ r)) < 0;                 /* signed overflow lanes */
+  const v16s sat = (x >> 7) ^ (v16s) {127, 127, 127, 127, 127, 127, 127, 127, 127, 127, 127, 127, 127, 127, 127, 127};
+  return (v16) ((ov & sat) | (~ov & r));
+}
+static inline v16 v_shl1(v16 a) {
+  const v16 z = {0};
+  return __builtin_shuffle(z, a, (v16) {0, 16, 17, 18, 19, 20, 21, 22, 23, 24, 25, 26, 27, 28, 29, 30});
+}
+static inline v16 v_or(v16 a, v16 b) { return a | b; }
+static inline uint8_t v_hmax(v16 a) { uint8_t m = 0; for (int z = 0; z < 16; z++) if (a[z] > m) m = a[z]; return m; }
+static inline v16 v_load(const uint8_t *p) { v16 r; memcpy(&r, p, 16); return r; }
 #endif
 
 typedef struct {
@@ -84,10 +94,42 @@ static int port_prepare(const orc_profile *om, port_prof *pp)
   return 0;
 }
 
+/* One sweep of the SSV pass: W registers, register j holding the 16
+ * diagonals that sit in striped vector q0 + j at row 1. Each row a register
+ * moves one vector on (cell (i, q) -> (i+1, q+1)); from the last vector it
+ * wraps to vector 0 with its lanes shifted by one (node k -> k+1 across the
+ * stripe boundary) and the begin value entering lane 0. */
+#define SSV_SWEEP(W)                                                                                   \
+  static v16 ssv_sweep_##W(const uint8_t *dsq, int L, const v16 *sbv, int Q, int q0, v16 xEv,          \
+                           v16 beginv, v16 begin0)                                                      \
+  {                                                                                                    \
+    v16 sv[W], xe[W];                  /* one max accumulator per register: no chain across them */  \
+    int p[W];                                                                                          \
+    for (int j = 0; j < W; j++) { sv[j] = beginv; xe[j] = xEv; p[j] = q0 + j; }                        \
+    for (int i = 1; i <= L;) {                                                                         \
+      /* rows until a register reaches the last vector; none wraps before that */                      \
+      int seg = L - i + 1;                                                                             \
+      for (int j = 0; j < W; j++) if (Q - p[j] < seg) seg = Q - p[j];                                  \
+      for (int t = 0; t < seg; t++, i++) {                                                             \
+        const v16 *sc = sbv + (size_t) dsq[i] * Q + t;                                                 \
+        for (int j = 0; j < W; j++) { sv[j] = v_subs_s8(sv[j], sc[p[j]]); xe[j] = v_max_u8(xe[j], sv[j]); } \
+      }                                                                                                \
+      for (int j = 0; j < W; j++) {                                                                    \
+        p[j] += seg;                                                                                   \
+        if (p[j] == Q) { p[j] = 0; sv[j] = v_or(v_shl1(sv[j]), begin0); }                              \
+      }                                                                                                \
+    }                                                                                                  \
+    for (int j = 0; j < W; j++) xEv = v_max_u8(xEv, xe[j]);                                            \
+    return xEv;                                                                                        \
+  }
+SSV_SWEEP(1) SSV_SWEEP(2) SSV_SWEEP(3) SSV_SWEEP(4) SSV_SWEEP(5) SSV_SWEEP(6) SSV_SWEEP(7) SSV_SWEEP(8)
+#define SSV_WMAX 8
+
 /* SSV filter: the J-free diagonal recurrence in the reference's signed
- * domain (begin = -128 = 0x80), striped; xE is the unsigned max over cells. */
+ * domain (begin = -128 = 0x80); xE is the unsigned max over all cells,
+ * computed by sweeps of up to SSV_WMAX registers of diagonals. */
 static int port_ssv(const uint8_t *dsq, int L, const orc_profile *om, const port_prof *pp, uint8_t tjb,
-                    v16 *dp, uint8_t *ret_xj, float *ret_sc)
+                    uint8_t *ret_xj, float *ret_sc)
 {
   const int Q = pp->Q;
   int tbm = om->tbm_b, tec = om->tec_b, base = om->base_b, bias = om->bias_b;
@@ -96,16 +138,20 @@ static int port_ssv(const uint8_t *dsq, int L, const orc_profile *om, const port
   uint8_t lane0[16] = {128, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   const v16 begin0 = v_load(lane0);
   v16 xEv = beginv;
-  for (int q = 0; q < Q; q++) dp[q] = beginv;
-  for (int i = 1; i <= L; i++) {
-    const v16 *sc = pp->sbv + (size_t) dsq[i] * Q;
-    v16 mpv = v_or(v_shl1(dp[Q - 1]), begin0);     /* node 0 is the begin value */
-    for (int q = 0; q < Q; q++) {
-      v16 sv = v_subs_s8(mpv, sc[q]);
-      xEv = v_max_u8(xEv, sv);
-      mpv = dp[q];
-      dp[q] = sv;
+  const int ns = (Q + SSV_WMAX - 1) / SSV_WMAX;         /* sweeps of balanced widths */
+  for (int k = 0, q0 = 0; k < ns; k++) {
+    const int w = Q / ns + (k < Q % ns ? 1 : 0);
+    switch (w) {
+      case 1: xEv = ssv_sweep_1(dsq, L, pp->sbv, Q, q0, xEv, beginv, begin0); break;
+      case 2: xEv = ssv_sweep_2(dsq, L, pp->sbv, Q, q0, xEv, beginv, begin0); break;
+      case 3: xEv = ssv_sweep_3(dsq, L, pp->sbv, Q, q0, xEv, beginv, begin0); break;
+      case 4: xEv = ssv_sweep_4(dsq, L, pp->sbv, Q, q0, xEv, beginv, begin0); break;
+      case 5: xEv = ssv_sweep_5(dsq, L, pp->sbv, Q, q0, xEv, beginv, begin0); break;
+      case 6: xEv = ssv_sweep_6(dsq, L, pp->sbv, Q, q0, xEv, beginv, begin0); break;
+      case 7: xEv = ssv_sweep_7(dsq, L, pp->sbv, Q, q0, xEv, beginv, begin0); break;
+      default: xEv = ssv_sweep_8(dsq, L, pp->sbv, Q, q0, xEv, beginv, begin0); break;
     }
+    q0 += w;
   }
   uint16_t xE = v_hmax(xEv), xJ;
   if (xE >= 255 - bias) {
@@ -183,7 +229,7 @@ static void *port_worker(void *arg)
       if (L == 0) { if (b->status) b->status[i] = -1; if (b->pass) b->pass[i] = 0; continue; }
       dsq[0] = 255; memcpy(dsq + 1, b->res + b->off[i], (size_t) L); dsq[L + 1] = 255;
       uint8_t tjb = orc_tjb_b(b->om->scale_b, L);
-      st = port_ssv(dsq, L, b->om, b->pp, tjb, dp, &xj, &sc);
+      st = port_ssv(dsq, L, b->om, b->pp, tjb, &xj, &sc);
       if (st == ORC_eslENORESULT) st = port_msv(dsq, L, b->om, b->pp, tjb, dp, &xj, &sc);
       if (b->status) b->status[i] = st;
       if (b->xj) b->xj[i] = xj;
