@@ -214,16 +214,15 @@ extern "C" int msvgb_biasfilter(msvgb_ctx *c, const float *compo, int M, const m
   BiasDev B;
   filter_hmm(compo, M, B);
   CUDA_TRY(msvgb_detail::ensure_inverse(c, db));
-  int64_t *d_ids = nullptr, *d_order = nullptr;
-  int32_t *d_cnt = nullptr;
-  float *d_out = nullptr;
-  int32_t *d_len = nullptr;
   std::vector<int32_t> lens((size_t) nids);
-  CUDA_TRY(cudaMallocAsync((void **) &d_ids, nids * 8, c->stream));
-  CUDA_TRY(cudaMallocAsync((void **) &d_order, nids * 8, c->stream));
-  CUDA_TRY(cudaMallocAsync((void **) &d_cnt, 1024 * 4, c->stream));
-  CUDA_TRY(cudaMallocAsync((void **) &d_out, nids * 4, c->stream));
-  CUDA_TRY(cudaMallocAsync((void **) &d_len, nids * 4, c->stream));
+  // one scratch block: list slots and order (int64), bucket counts, scores and lengths
+  const size_t a8 = ((size_t) nids * 8 + 255) & ~(size_t) 255, a4 = ((size_t) nids * 4 + 255) & ~(size_t) 255;
+  char *d_scr = nullptr;
+  CUDA_TRY(cudaMallocAsync((void **) &d_scr, 2 * a8 + 4096 + 2 * a4, c->stream));
+  int64_t *d_ids = (int64_t *) d_scr, *d_order = (int64_t *) (d_scr + a8);
+  int32_t *d_cnt = (int32_t *) (d_scr + 2 * a8);
+  float *d_out = (float *) (d_scr + 2 * a8 + 4096);
+  int32_t *d_len = (int32_t *) (d_scr + 2 * a8 + 4096 + a4);
   cudaError_t e = cudaMemcpyAsync(d_ids, ids, nids * 8, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess) e = msvgb_detail::launch_gather_ids(d_ids, nids, db->d_inv, c->num_sms, c->stream);
   if (e == cudaSuccess)
@@ -237,11 +236,7 @@ extern "C" int msvgb_biasfilter(msvgb_ctx *c, const float *compo, int M, const m
   if (e == cudaSuccess) msvgb_detail::count_launch();
   if (e == cudaSuccess) e = cudaMemcpyAsync(out_sc, d_out, nids * 4, cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(lens.data(), d_len, nids * 4, cudaMemcpyDeviceToHost, c->stream);
-  cudaFreeAsync(d_ids, c->stream);
-  cudaFreeAsync(d_order, c->stream);
-  cudaFreeAsync(d_cnt, c->stream);
-  cudaFreeAsync(d_out, c->stream);
-  cudaFreeAsync(d_len, c->stream);
+  cudaFreeAsync(d_scr, c->stream);
   const cudaError_t e2 = cudaStreamSynchronize(c->stream);
   if (e == cudaSuccess) e = e2;
   if (e != cudaSuccess) return fail(MSVGB_eslESYS, std::string("biasfilter: ") + cudaGetErrorString(e));

@@ -38,7 +38,6 @@ struct msvgb_ctx {
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   TuneTable *tune = nullptr;                            // lane counts measured by msvgb_autotune
   std::mutex tune_mu;
-  std::mutex mu_inv;                                    // builds of a database's inverse order
 };
 
 // Per-length tables of a profile at one F1 threshold: tjb_b(L) and the

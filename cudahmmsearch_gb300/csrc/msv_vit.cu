@@ -562,7 +562,8 @@ int16_t wordify(float scale_w, float sc) {
 }  // namespace
 
 cudaError_t msvgb_detail::ensure_inverse(msvgb_ctx *c, const msvgb_db *db) {
-  std::lock_guard<std::mutex> lk(c->mu_inv);
+  static std::mutex mu;                      // a database may be listed from several contexts at once
+  std::lock_guard<std::mutex> lk(mu);
   if (db->d_inv) return cudaSuccess;
   int64_t *inv = nullptr;
   cudaError_t e = cudaMalloc(&inv, std::max<int64_t>(db->n, 1) * 8);
@@ -584,6 +585,8 @@ struct msvgb_vprofile {
   int16_t *d_move = nullptr;
   int move_cap = 0;
   std::vector<int16_t> h_move;
+  std::mutex move_mu;                        // the move table grows under concurrent calls
+  std::vector<int16_t *> retired;            // smaller move tables other calls may still read
 };
 
 extern "C" int16_t msvgb_vit_move_cost(float scale_w, float nj, int L) {
@@ -689,6 +692,7 @@ extern "C" int msvgb_vprofile_destroy(msvgb_vprofile *p) {
   if (!p) return MSVGB_eslOK;
   cudaSetDevice(p->device);
   cudaFree(p->d_trans); cudaFree(p->d_emit); cudaFree(p->d_move);
+  for (int16_t *t : p->retired) cudaFree(t);
   delete p;
   return MSVGB_eslOK;
 }
@@ -703,28 +707,33 @@ extern "C" int msvgb_vitfilter(msvgb_ctx *c, msvgb_vprofile *p, const msvgb_db *
   CUDA_TRY(cudaSetDevice(c->device));
   for (int64_t j = 0; j < nids; ++j)
     if (ids[j] < 0 || ids[j] >= db->n) return fail(MSVGB_eslEINVAL, "sequence index out of range");
-  // per-length move costs up to the database's longest sequence
-  if (p->move_cap < db->Lmax + 1) {
-    const int cap = std::max(db->Lmax + 1, 2 * p->move_cap);
-    for (int L = (int) p->h_move.size(); L < cap; ++L) p->h_move.push_back(msvgb_vit_move_cost(p->scale_w, p->nj, L));
-    int16_t *d = nullptr;
-    CUDA_TRY(cudaMalloc(&d, cap * 2));
-    const cudaError_t e = cudaMemcpy(d, p->h_move.data(), cap * 2, cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) { cudaFree(d); return fail(MSVGB_eslESYS, cudaGetErrorString(e)); }
-    CUDA_TRY(cudaStreamSynchronize(c->stream));                // an older table may still be read
-    cudaFree(p->d_move);
-    p->d_move = d; p->move_cap = cap;
+  // per-length move costs up to the database's longest sequence; a smaller
+  // table is retired, not freed, while the profile lives (a call on another
+  // thread may have taken its pointer and not launched yet)
+  const int16_t *d_move = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(p->move_mu);
+    if (p->move_cap < db->Lmax + 1) {
+      const int cap = std::max(db->Lmax + 1, 2 * p->move_cap);
+      for (int L = (int) p->h_move.size(); L < cap; ++L) p->h_move.push_back(msvgb_vit_move_cost(p->scale_w, p->nj, L));
+      int16_t *d = nullptr;
+      CUDA_TRY(cudaMalloc(&d, cap * 2));
+      const cudaError_t e = cudaMemcpy(d, p->h_move.data(), cap * 2, cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) { cudaFree(d); return fail(MSVGB_eslESYS, cudaGetErrorString(e)); }
+      if (p->d_move) p->retired.push_back(p->d_move);
+      p->d_move = d; p->move_cap = cap;
+    }
+    d_move = p->d_move;
   }
   CUDA_TRY(msvgb_detail::ensure_inverse(c, db));
-  int64_t *d_ids = nullptr, *d_order = nullptr;
-  int32_t *d_cnt = nullptr;
-  int *d_xc = nullptr;
-  uint8_t *d_st = nullptr;
-  CUDA_TRY(cudaMallocAsync((void **) &d_ids, nids * 8, c->stream));
-  CUDA_TRY(cudaMallocAsync((void **) &d_order, nids * 8, c->stream));
-  CUDA_TRY(cudaMallocAsync((void **) &d_cnt, 1024 * 4, c->stream));
-  CUDA_TRY(cudaMallocAsync((void **) &d_xc, nids * 4, c->stream));
-  CUDA_TRY(cudaMallocAsync((void **) &d_st, nids, c->stream));
+  // one scratch block: list slots and order (int64), bucket counts, xC and statuses
+  const size_t a8 = ((size_t) nids * 8 + 255) & ~(size_t) 255, a4 = ((size_t) nids * 4 + 255) & ~(size_t) 255;
+  char *d_scr = nullptr;
+  CUDA_TRY(cudaMallocAsync((void **) &d_scr, 2 * a8 + 4096 + a4 + (size_t) nids, c->stream));
+  int64_t *d_ids = (int64_t *) d_scr, *d_order = (int64_t *) (d_scr + a8);
+  int32_t *d_cnt = (int32_t *) (d_scr + 2 * a8);
+  int *d_xc = (int *) (d_scr + 2 * a8 + 4096);
+  uint8_t *d_st = (uint8_t *) (d_scr + 2 * a8 + 4096 + a4);
   cudaError_t e = cudaMemcpyAsync(d_ids, ids, nids * 8, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess) e = msvgb_detail::launch_gather_ids(d_ids, nids, db->d_inv, c->num_sms, c->stream);
   if (e == cudaSuccess)
@@ -734,15 +743,14 @@ extern "C" int msvgb_vitfilter(msvgb_ctx *c, msvgb_vprofile *p, const msvgb_db *
   V.CV = p->CV; V.base_w = p->base_w; V.ddbound_w = p->ddbound_w;
   V.xwE_move = p->xw[0][0]; V.xwE_loop = p->xw[0][1];
   V.xwN_loop = p->xw[1][1]; V.xwJ_loop = p->xw[2][1]; V.xwC_loop = p->xw[3][1];
-  V.trans = p->d_trans; V.emit = p->d_emit; V.move = p->d_move;
+  V.trans = p->d_trans; V.emit = p->d_emit; V.move = d_move;
   DbDev dbv{db->d_codes, db->d_start, db->d_len, db->d_orig, db->n};
   if (e == cudaSuccess)
     e = dispatch_vit(p->CV, V, dbv, d_ids, d_order, nids, d_xc, d_st, c->d_ticket, c->num_sms, c->stream);
   if (e == cudaSuccess) msvgb_detail::count_launch();
   if (e == cudaSuccess) e = cudaMemcpyAsync(out_xc, d_xc, nids * 4, cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(out_status, d_st, nids, cudaMemcpyDeviceToHost, c->stream);
-  cudaFreeAsync(d_ids, c->stream); cudaFreeAsync(d_order, c->stream); cudaFreeAsync(d_cnt, c->stream);
-  cudaFreeAsync(d_xc, c->stream); cudaFreeAsync(d_st, c->stream);
+  cudaFreeAsync(d_scr, c->stream);
   const cudaError_t e2 = cudaStreamSynchronize(c->stream);
   if (e == cudaSuccess) e = e2;
   if (e != cudaSuccess) return fail(MSVGB_eslESYS, std::string("vitfilter: ") + cudaGetErrorString(e));

@@ -85,3 +85,37 @@ def test_vitfilter_model_size_limit(ctx):
             with pytest.raises(api.MSVError) as e:
                 api.DeviceVProfile(ctx, big)
             assert e.value.code == api.eslEINVAL
+
+
+def test_vitfilter_shared_profile_from_threads():
+    """One ViterbiFilter profile used at once from threads on their own
+    contexts, over databases whose longest sequences differ (the per-length
+    move table grows while other calls run): every result equals the
+    sequential one."""
+    import threading
+    vp = F.read_vprofile(os.path.join(GOLDEN, "vit_m200_s1.vprof"))
+    sets = [F.synth_sequences(3000, seed=60 + t, lmax=500 * (t + 1) ** 2) for t in range(4)]
+    ctxs = [api.Context(0) for _ in sets]
+    dvp = api.DeviceVProfile(ctxs[0], vp)
+    dbs = [api.DeviceDB(c, s) for c, s in zip(ctxs, sets)]
+    got = [None] * len(sets)
+
+    def run(t):
+        got[t] = api.vitfilter(ctxs[t], dvp, dbs[t])
+    threads = [threading.Thread(target=run, args=(t,)) for t in range(len(sets))]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    for t, s in enumerate(sets):
+        st, sc = api.vitfilter(ctxs[t], dvp, dbs[t])
+        assert np.array_equal(got[t][0], st) and np.array_equal(got[t][1].view(np.uint32), sc.view(np.uint32))
+    o = O.vit_batch(vp, sets[3].subset(np.arange(0, 3000, 50)))
+    st, sc = got[3]
+    sub = np.arange(0, 3000, 50)
+    assert np.array_equal(sc[sub].view(np.uint32), o["sc"].view(np.uint32))
+    for d in dbs:
+        d.close()
+    dvp.close()
+    for c in ctxs:
+        c.close()
