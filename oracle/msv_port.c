@@ -1,5 +1,5 @@
 /* msv_port.c -- vectorized CPU port of the reference MSV filter
- * (TEST AND BASELINE INFRASTRUCTURE ONLY).
+ * (TEST INFRASTRUCTURE AND CPU BASELINE ONLY).
  *
  * A 16-lane uint8 restatement of HMMER 3.1b1's SSE2 p7_MSVFilter
  * (src/impl_sse/msvfilter.c:77-213) and of the SSV filter it calls first
