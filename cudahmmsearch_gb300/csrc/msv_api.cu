@@ -572,35 +572,20 @@ int msvgb_detail::db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64
     if (r == cudaSuccess) scratch.push_back(*ptr);
     return r;
   };
-  const int64_t *d_off = nullptr;
-  int64_t *d_scal = nullptr;                                  // d_scal: [0] Lmax | bad << 32, [1] packed size
+  int64_t *d_off = nullptr, *d_scal = nullptr;                // d_scal: [0] Lmax | bad << 32, [1] packed size
   int32_t *d_len_in = nullptr;
-  const uint8_t *d_raw = nullptr;
+  uint8_t *d_raw = nullptr;
   cudaEvent_t ev_raw = nullptr;
-  const bool pre = a && a->d_raw;                             // residues already up: the caller's copy
   CUDA_TRY(cudaEventCreateWithFlags(&ev_raw, cudaEventDisableTiming));
-  cudaError_t e = alloc((void **) &d_len_in, (size_t) n1 * 4, st);
+  cudaError_t e = alloc((void **) &d_off, (size_t) (n + 1) * 8, st);
+  if (e == cudaSuccess) e = alloc((void **) &d_len_in, (size_t) n1 * 4, st);
   if (e == cudaSuccess) e = alloc((void **) &d_scal, 16, st);
-  if (a && a->d_off) {                                        // offsets already up: the caller's copy
-    d_off = a->d_off;
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, a->off_ready, 0);
-  } else {
-    int64_t *o = nullptr;
-    if (e == cudaSuccess) e = alloc((void **) &o, (size_t) (n + 1) * 8, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(o, off, (size_t) (n + 1) * 8, cudaMemcpyHostToDevice, st);
-    d_off = o;
-  }
-  if (pre) {
-    d_raw = a->d_raw;                                         // ev_raw stays unrecorded: the pack waits
-  } else {                                                    // on the caller's event instead
-    uint8_t *raw = nullptr;
-    if (e == cudaSuccess) e = cudaEventRecord(ev_raw, st);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->dma, ev_raw, 0);
-    if (e == cudaSuccess) e = alloc((void **) &raw, (size_t) total, ctx->dma);
-    if (e == cudaSuccess && total) e = cudaMemcpyAsync(raw, codes + off[0], total, cudaMemcpyHostToDevice, ctx->dma);
-    if (e == cudaSuccess) e = cudaEventRecord(ev_raw, ctx->dma);
-    d_raw = raw;
-  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_off, off, (size_t) (n + 1) * 8, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaEventRecord(ev_raw, st);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->dma, ev_raw, 0);
+  if (e == cudaSuccess) e = alloc((void **) &d_raw, (size_t) total, ctx->dma);
+  if (e == cudaSuccess && total) e = cudaMemcpyAsync(d_raw, codes + off[0], total, cudaMemcpyHostToDevice, ctx->dma);
+  if (e == cudaSuccess) e = cudaEventRecord(ev_raw, ctx->dma);
   pt.mark("copies issued");
   if (e == cudaSuccess && ctx->h_pin_cap < 64) e = grow_pinned(ctx, 64);
   unsigned *misc = (unsigned *) ctx->h_pin;
@@ -612,9 +597,8 @@ int msvgb_detail::db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64
   pt.mark("lengths");
   const bool bad_len = e == cudaSuccess && misc[1] != 0;
   const int Lmax = e == cudaSuccess ? (int) misc[0] : 0;
-  const cudaEvent_t raw_done = pre ? a->raw_ready : ev_raw;   // the residues are on the device
   auto finish = [&]() {                                       // scratch frees, ordered after all use
-    cudaStreamWaitEvent(st, raw_done, 0);
+    cudaStreamWaitEvent(st, ev_raw, 0);
     for (void *q : scratch) cudaFreeAsync(q, st);
     scratch.clear();
     cudaEventDestroy(ev_raw);
@@ -689,7 +673,7 @@ int msvgb_detail::db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64
   if (e == cudaSuccess && ctx->h_pin_cap < 16 + nb * 8) e = grow_pinned(ctx, 16 + nb * 8);
   int *d_bad = a ? a->d_bad : ctx->d_bad;
   int64_t *h_scal = (int64_t *) ctx->h_pin;                   // [0] bad flag, [1] packed size, then counts
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(st, raw_done, 0);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev_raw, 0);
   if (trace_on() && e == cudaSuccess) { e = cudaStreamSynchronize(st); pt.mark("residues up"); }
   if (e == cudaSuccess && !a) e = cudaMemsetAsync(d_bad, 0, sizeof(int), st);
   if (e == cudaSuccess) e = launch_pack(d_raw, d_src, db->d_start, db->d_len, n, db->d_codes, d_bad,
@@ -880,38 +864,10 @@ extern "C" int msvgb_search_host(msvgb_ctx *c, const msvgb_profile *p, const uin
   std::vector<msvgb_db *> dbs;
   int st = MSVGB_eslOK;
   PhaseTimer pt;
-  // every chunk's residues go up at once, back to back on the copy engine:
-  // a chunk's packing then never waits for a copy issued after the chunk
-  // before it was packed
-  const size_t nchunks = cut.size() - 1;
-  std::vector<uint8_t *> d_raw(nchunks, nullptr);
-  std::vector<cudaEvent_t> raw_ready(nchunks, nullptr);
-  int64_t *d_off_all = nullptr;                               // all offsets first: a small copy the
-  cudaEvent_t off_ready = nullptr;                            // first lengths kernel waits for
-  cudaMemPool_t pool = scratch_pool(c->device);
-  cudaError_t ce = pool ? cudaEventRecord(c->ev_fork, c->stream) : cudaErrorMemoryAllocation;
-  if (ce == cudaSuccess) ce = cudaStreamWaitEvent(c->dma, c->ev_fork, 0);
-  if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&off_ready, cudaEventDisableTiming);
-  if (ce == cudaSuccess) ce = cudaMallocFromPoolAsync((void **) &d_off_all, (size_t) (n + 1) * 8, pool, c->dma);
-  if (ce == cudaSuccess) ce = cudaMemcpyAsync(d_off_all, off, (size_t) (n + 1) * 8, cudaMemcpyHostToDevice, c->dma);
-  if (ce == cudaSuccess) ce = cudaEventRecord(off_ready, c->dma);
-  for (size_t k = 0; k < nchunks && ce == cudaSuccess; ++k) {
-    const int64_t r0 = off[cut[k]], r1 = off[cut[k + 1]];
-    ce = cudaEventCreateWithFlags(&raw_ready[k], cudaEventDisableTiming);
-    if (ce == cudaSuccess)
-      ce = cudaMallocFromPoolAsync((void **) &d_raw[k], std::max<int64_t>(r1 - r0, 16), pool, c->dma);
-    if (ce == cudaSuccess && r1 > r0) ce = cudaMemcpyAsync(d_raw[k], codes + r0, r1 - r0, cudaMemcpyHostToDevice, c->dma);
-    if (ce == cudaSuccess) ce = cudaEventRecord(raw_ready[k], c->dma);
-  }
-  if (ce != cudaSuccess) st = fail(MSVGB_eslESYS, std::string("search: ") + cudaGetErrorString(ce));
   for (size_t k = 0; k + 1 < cut.size() && st == MSVGB_eslOK; ++k) {
     const int64_t b0 = cut[k], b1 = cut[k + 1];
     msvgb_db *db = nullptr;
-    AsyncPack a{d_bad};
-    a.d_raw = d_raw[k];
-    a.raw_ready = raw_ready[k];
-    a.d_off = d_off_all + b0;
-    a.off_ready = off_ready;
+    const AsyncPack a{d_bad};
     st = db_create_on(c, codes, off + b0, b1 - b0, c->upload, &db, &a);
     pt.mark("search_host: chunk enqueued");
     if (st == MSVGB_eslOK) {
@@ -927,14 +883,7 @@ extern "C" int msvgb_search_host(msvgb_ctx *c, const msvgb_profile *p, const uin
     if (e != cudaSuccess) st = fail(MSVGB_eslESYS, std::string("search: ") + cudaGetErrorString(e));
   }
   cudaStreamSynchronize(c->upload);
-  cudaStreamSynchronize(c->dma);
   cudaFreeAsync(d, c->stream);
-  for (size_t k = 0; k < nchunks; ++k) {
-    if (d_raw[k]) cudaFreeAsync(d_raw[k], c->stream);          // the packs that read them are done
-    if (raw_ready[k]) cudaEventDestroy(raw_ready[k]);
-  }
-  if (d_off_all) cudaFreeAsync(d_off_all, c->stream);
-  if (off_ready) cudaEventDestroy(off_ready);
   const cudaError_t e = cudaStreamSynchronize(c->stream);
   pt.mark("search_host: last search done");
   for (auto *db : dbs) msvgb_db_destroy(db);

@@ -129,11 +129,7 @@ int batch_create(msvgb_ctx *ctx, const msvgb_om *const *oms, int nprof, const ms
                  void *d_xj, void *d_flags, int force_lanes, msvgb_batch **ret);
 // Asynchronous packing of one chunk (db_create_on).
 struct AsyncPack {
-  int *d_bad;                      // device flag: set if a residue code is >= 29
-  const uint8_t *d_raw = nullptr;  // the residues already copied up (the caller's), or NULL
-  cudaEvent_t raw_ready = nullptr; // recorded after that copy
-  const int64_t *d_off = nullptr;  // the offsets already copied up (off[0 .. n]), or NULL
-  cudaEvent_t off_ready = nullptr; // recorded after that copy
+  int *d_bad;      // device flag: set if a residue code is >= 29
 };
 // msvgb_db_create on stream st; with a, asynchronous (see msv_api.cu).
 int db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64_t *off, int64_t n, cudaStream_t st,
