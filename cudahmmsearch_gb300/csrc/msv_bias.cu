@@ -20,6 +20,7 @@
 // the C library's logf.
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -80,6 +81,58 @@ __device__ __forceinline__ float log_row(float m, const double2 *tab) {
   return __double2float_rn(y);
 }
 
+// float(log(m)) in float-float arithmetic on the FP32 pipe, for m in
+// [0.707, 1.414) (exponent 0 after the reduction; the row maxima of the
+// filter's scaled Forward lie there): the top 11 mantissa bits pick a
+// reduction point c (2048 intervals; c = 1 next to 1) with 1/c and log c
+// stored as float pairs; d = f - c is exact, r = d/c a float pair by fused
+// multiply-adds, log1p(r) = r - r^2/2 (pairs) + r^3/3 - r^4/4 + r^5/5 (float;
+// |r| < 2^-11.5, truncation < 2^-57), summed with error-free two-sums. The
+// result is returned only when it is at least 2^-42 (relative) away from a
+// float rounding boundary -- every float in [0.25, 4) checked on the host
+// against the C library's double log: 0 differences; otherwise (and for
+// other exponents) the double path decides.
+__device__ float4 g_logff[2048];
+
+__device__ __forceinline__ float fsub(float a, float b) { return __fadd_rn(a, -b); }
+
+__device__ __forceinline__ bool log_ff(float m, float *out) {
+  const uint32_t b = __float_as_uint(m);
+  if (b - 0x00800000u >= 0x7f000000u) return false;
+  const int j = (b >> 12) & 0x7ff;
+  const int half = j >= 849;
+  if ((int) (b >> 23) - 127 + half != 0) return false;
+  const float f = __uint_as_float((b & 0x7fffffu) | ((uint32_t) (127 - half) << 23));
+  const float4 t = g_logff[j];                               // 1/c (hi, lo), log c (hi, lo)
+  const float c = (j == 0 || j == 2047) ? 1.0f : __fmul_rn(half ? 0.5f : 1.0f, 1.0f + ((float) j + 0.5f) / 2048.0f);
+  const float d = fsub(f, c);                                // exact
+  const float rh = __fmul_rn(d, t.x);
+  const float rl = __fadd_rn(__fmaf_rn(d, t.x, -rh), __fmul_rn(d, t.y));
+  const float sh = __fmul_rn(rh, rh);
+  const float sl = __fadd_rn(__fmaf_rn(rh, rh, -sh), __fmul_rn(__fmul_rn(2.0f, rh), rl));
+  const float q3 = __fmul_rn(__fmul_rn(rh, sh),
+                             __fadd_rn(1.0f / 3.0f, __fmul_rn(rh, __fadd_rn(-0.25f, __fmul_rn(rh, 0.2f)))));
+  float H = t.z, L = 0.0f, sm, bb;
+  sm = __fadd_rn(H, rh); bb = fsub(sm, H); L = __fadd_rn(L, __fadd_rn(fsub(H, fsub(sm, bb)), fsub(rh, bb))); H = sm;
+  const float hs = __fmul_rn(-0.5f, sh);
+  sm = __fadd_rn(H, hs); bb = fsub(sm, H); L = __fadd_rn(L, __fadd_rn(fsub(H, fsub(sm, bb)), fsub(hs, bb))); H = sm;
+  L = __fadd_rn(L, __fadd_rn(__fadd_rn(__fadd_rn(t.w, rl), __fmul_rn(-0.5f, sl)), q3));
+  const float res = __fadd_rn(H, L);
+  const float bv = fsub(res, H);
+  const float tr = __fadd_rn(fsub(H, fsub(res, bv)), fsub(L, bv));   // H + L - res, exactly
+  const uint32_t rb = __float_as_uint(res);
+  if ((rb & 0x7fffffffu) < 0x01000000u) return false;
+  const float ulp = __uint_as_float((rb & 0x7f800000u) - (23u << 23));
+  if (fsub(__fmul_rn(0.5f, ulp), fabsf(tr)) < __fmul_rn(fabsf(res), 0x1p-42f)) return false;
+  *out = res;
+  return true;
+}
+
+__device__ __forceinline__ float log_rowf(float m, const double2 *tab) {
+  float r;
+  return log_ff(m, &r) ? r : log_row(m, tab);
+}
+
 // One thread per listed sequence; threads take the list in database order
 // (order[t]: longest first), so a warp's sequences have similar lengths. Rows
 // go 16 at a time: first the 16 rows' recurrence (a serial chain through the
@@ -130,13 +183,13 @@ bias_kernel(BiasDev B, DbDev db, const int64_t *__restrict__ slots, const int64_
     }
     float lg[16];
 #pragma unroll
-    for (int b = 0; b < 16; ++b) lg[b] = log_row(mx[b], s_log);
+    for (int b = 0; b < 16; ++b) lg[b] = log_rowf(mx[b], s_log);
 #pragma unroll
     for (int b = 0; b < 16; ++b)
       if (i0 + b < L) logsc = __fadd_rn(logsc, lg[b]);
   }
   const float end = __fadd_rn(d0, d1);           // dp[L][0] * 1 + dp[L][1] * 1
-  out[j] = __fadd_rn(logsc, log_row(end, s_log));
+  out[j] = __fadd_rn(logsc, log_rowf(end, s_log));
 }
 
 // degenerate amino codes 21..26 (B J Z O U X) as sets of canonical codes
@@ -183,6 +236,26 @@ void filter_hmm(const float *compo, int M, BiasDev &B) {
 
 }  // namespace
 
+// The float-pair table of log_ff, uploaded once per device.
+static cudaError_t ensure_logff(int device) {
+  static std::mutex mu;
+  static std::vector<int> done;
+  std::lock_guard<std::mutex> lk(mu);
+  for (int d : done) if (d == device) return cudaSuccess;
+  std::vector<float4> t(2048);
+  for (int j = 0; j < 2048; ++j) {
+    double c = 1.0 + (j + 0.5) / 2048.0;
+    if (j >= 849) c *= 0.5;
+    if (j == 0 || j == 2047) c = 1.0;
+    const double inv = 1.0 / c, lg = std::log(c);
+    const float ih = (float) inv, th = (float) lg;
+    t[j] = make_float4(ih, (float) (inv - (double) ih), th, (float) (lg - (double) th));
+  }
+  const cudaError_t e = cudaMemcpyToSymbol(g_logff, t.data(), sizeof(float4) * 2048);
+  if (e == cudaSuccess) done.push_back(device);
+  return e;
+}
+
 extern "C" float msvgb_bias_length_term(float fwd, int L) {
   // p7_bg_FilterScore: nullsc + (float) L * logf(bg->p1) + logf(1. - bg->p1)
   const float p1 = (float) L / (float) (L + 1);
@@ -213,6 +286,7 @@ extern "C" int msvgb_biasfilter(msvgb_ctx *c, const float *compo, int M, const m
   CUDA_TRY(cudaSetDevice(c->device));
   BiasDev B;
   filter_hmm(compo, M, B);
+  CUDA_TRY(ensure_logff(c->device));
   CUDA_TRY(msvgb_detail::ensure_inverse(c, db));
   std::vector<int32_t> lens((size_t) nids);
   // one scratch block: list slots and order (int64), bucket counts, scores and lengths
