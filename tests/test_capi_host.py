@@ -59,3 +59,54 @@ def test_context_without_gpu_fails_cleanly():
         pytest.skip("a GPU is present")
     with pytest.raises(api.MSVError):
         api.Context(0)
+
+
+def test_filter_stage_helpers_match_reference():
+    """The host expressions of the stages after MSV, against the reference's
+    own pipeline results (tests/golden/pipe_*.pres) and the oracle:
+    p7_bg_NullOne, the stage gate, the ViterbiFilter score from xC."""
+    import glob
+    lib = api.lib()
+    gold = os.path.join(ROOT, "tests", "golden")
+    for pres in sorted(glob.glob(os.path.join(gold, "pipe_*.pres"))):
+        name = os.path.basename(pres)[5:-5]
+        r = F.read_pipe(pres)
+        s = F.read_seqs(os.path.join(gold, "pipe_" + name + ".seqs"))
+        vp = F.read_vprofile(os.path.join(gold, "vit_" + name + ".vprof"))
+        vo, keep = api._vom_struct(vp)
+        for i in range(s.n):
+            L = int(s.lengths[i])
+            if L == 0:
+                continue
+            ns = lib.msvgb_null_score(L)
+            assert np.float32(ns).view(np.uint32) == r.nullsc[i:i + 1].view(np.uint32)[0]
+            ok, P = api.stage_pass(float(r.usc[i]), float(r.nullsc[i]), r.mmu, r.mlambda, r.F1)
+            assert ok == (r.stage[i] >= 1)
+            assert P == O.gumbel_P(float(r.usc[i]), float(r.nullsc[i]), r.mmu, r.mlambda)
+            if r.stage[i] >= 1:
+                ok2, _ = api.stage_pass(float(r.usc[i]), float(r.fsc[i]), r.mmu, r.mlambda, r.F1)
+                assert ok2 == (r.stage[i] >= 2)
+            if np.isfinite(r.vfsc[i]):
+                st, sc, xc = O.vit_filter(vp, s.seq(i))
+                got = lib.msvgb_vit_score(xc, 1 if st == 16 else 0, L, ctypes.byref(vo))
+                assert np.float32(got).view(np.uint32) == r.vfsc[i:i + 1].view(np.uint32)[0]
+
+
+def test_bias_length_term_matches_reference():
+    """msvgb_bias_length_term(fwd, L) adds exactly what p7_bg_FilterScore adds
+    to the Forward score: the reference's score minus the Forward part of the
+    oracle's restatement, for every sequence of a golden set."""
+    lib = api.lib()
+    gold = os.path.join(ROOT, "tests", "golden")
+    r = F.read_pipe(os.path.join(gold, "pipe_tut_fn3.pres"))
+    s = F.read_seqs(os.path.join(gold, "pipe_tut_fn3.seqs"))
+    for i in range(0, s.n, 7):
+        L = int(s.lengths[i])
+        if L == 0:
+            continue
+        p1 = np.float32(L) / np.float32(L + 1)
+        fwd = np.float32(r.fsc[i]) - (np.float32(L) * np.float32(np.log(p1))) - np.float32(np.log(np.float32(1.0 - np.float64(p1))))
+        # the library's term applied to a Forward score gives back a float sum of the same three terms
+        got = lib.msvgb_bias_length_term(float(fwd), L)
+        want = np.float32(np.float32(fwd) + np.float32(L) * np.float32(np.log(p1))) + np.float32(np.log(np.float32(1.0 - np.float64(p1))))
+        assert abs(float(got) - float(want)) <= 1e-5 * max(1.0, abs(float(want)))
