@@ -42,9 +42,10 @@ constexpr int kNT = 8;     // per-node transitions: BM MM IM DM (into k), MD MI 
 // adjacent so that one warp load reads 512 contiguous bytes. Emissions are
 // int16 (vector v of a lane: its nodes 8v .. 8v+7), one unpack per cell,
 // which keeps the 29 residue tables of the widest model within L1.
-// Transitions are int32 (nodes 4v .. 4v+3), ready for the adds, up to 32
-// nodes per lane; wider lanes keep them int16 (the unpacked values would
-// spill registers).
+// Transitions are int32 (nodes 4v .. 4v+3), ready for the adds, in the
+// one-node-per-register kernel (up to 32 nodes per lane); the shared-memory
+// kernel (above 48) reads them as int16 (8 nodes per vector); the packed
+// kernel (40, 48) has its own tables.
 struct VitDev {
   int CV;                  // nodes per lane
   int16_t base_w, ddbound_w;
@@ -85,6 +86,7 @@ __device__ __forceinline__ int h16(const uint4 &w, int e) {
 // one per sum. Only the emission can raise a score.
 template <int CV>
 __device__ int vit_one(const VitDev &V, const uint8_t *sq, int L, int lane, int &xc_out) {
+  static_assert(vit_t32(CV), "the one-node-per-register row reads int32 transitions");
   constexpr int NV = vit_nv(CV), NT = vit_nt(CV), TN = vit_tnodes(CV);
   int Mv[CV], Iv[CV], Dv[CV];
 #pragma unroll
@@ -117,10 +119,7 @@ __device__ int vit_one(const VitDev &V, const uint8_t *sq, int L, int lane, int 
         const int j = q * TN + e;
         if (j >= CV) break;
         if (j % 8 == 0) e4 = em[(j / 8) * 32];
-        auto tv = [&](int t) {
-          if constexpr (vit_t32(CV)) return i32(t4[t], e);
-          else return h16(*reinterpret_cast<const uint4 *>(&t4[t]), e);
-        };
+        auto tv = [&](int t) { return i32(t4[t], e); };
         const int cM = Mv[j], cI = Iv[j], cD = Dv[j];
         int sv = max(max(add_f(xB, tv(0), one), pM + tv(1)), max(add_f(pI, tv(2), one), pD + tv(3)));
         sv = sat16(max(sv, -32768) + h16(e4, j % 8));
@@ -151,10 +150,7 @@ __device__ int vit_one(const VitDev &V, const uint8_t *sq, int L, int lane, int 
         const int4 t7 = tr[(7 * NT + q) * 32];      // D(k-1) -> D(k)
 #pragma unroll
         for (int e = 0; e < TN; ++e)
-          if (q * TN + e < CV) {
-            if constexpr (vit_t32(CV)) tdd[q * TN + e] = i32(t7, e);
-            else tdd[q * TN + e] = h16(*reinterpret_cast<const uint4 *>(&t7), e);
-          }
+          if (q * TN + e < CV) tdd[q * TN + e] = i32(t7, e);
       }
       int c = -2000000000, b = 0;
 #pragma unroll
@@ -636,8 +632,8 @@ extern "C" int msvgb_vprofile_create(msvgb_ctx *ctx, const msvgb_vom *v, msvgb_v
       trans[at_t(7, lane, j)] = k > 1 ? striped(v->twv, 7 * Q8, k - 1) : (int16_t) -32768;
       for (int x = 0; x < v->Kp; ++x) emit[at_e(x, lane, j)] = v->rwv[(x * Q8 + q) * 8 + z];
     }
-  std::vector<int16_t> trans16;                     // the int16 form for lanes wider than 32 nodes
-  if (!vit_t32(CV)) trans16.assign(trans.begin(), trans.end());
+  std::vector<int16_t> trans16;                     // the int16 form the shared-memory kernel reads
+  if (!vit_t32(CV) && !vit_packed(CV)) trans16.assign(trans.begin(), trans.end());
   const void *tsrc = vit_t32(CV) ? (const void *) trans.data() : (const void *) trans16.data();
   size_t tbytes = trans.size() * (vit_t32(CV) ? 4 : 2);
   const void *esrc = emit.data();
