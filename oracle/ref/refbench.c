@@ -4,8 +4,14 @@
  * one p7_oprofile_Clone (impl_sse/p7_oprofile.c:398) and one private P7_OMX
  * per thread, p7_oprofile_ReconfigLength before every call.
  *
- * Test infrastructure (x86-64 only; the reference's MSV is SSE2 code).
- *   refbench M seed Lcfg mode seqs nthreads reps
+ * With stage "vit" it times p7_ViterbiFilter (impl_sse/vitfilter.c:84) the
+ * same way; with stage "bias", p7_bg_FilterScore (src/p7_bg.c:473) with a
+ * private P7_BG per thread (p7_bg_SetFilter with the model's composition, as
+ * p7_pli_NewModel does, src/p7_pipeline.c:480; p7_bg_SetLength per sequence).
+ * The sampled HMM gets the composition hmmbuild would give it.
+ *
+ * Test infrastructure (x86-64 only; the reference's filters are SSE2 code).
+ *   refbench M seed Lcfg mode seqs nthreads reps [msv|vit|bias]
  * prints one line: "cells=<M*sum L*reps> seconds=<wall> gcups=<...> threads=<n>"
  */
 #include "p7_config.h"
@@ -25,7 +31,7 @@ static void die(const char *m) { fprintf(stderr, "refbench: %s\n", m); exit(1); 
 
 typedef struct {
   const P7_OPROFILE *om0; const int64_t *off; const uint8_t *res;
-  int64_t lo, hi; int reps; double sink;
+  int64_t lo, hi; int reps; double sink; int stage;   /* 0 msv, 1 vit, 2 bias */
 } job_t;
 
 static void *worker(void *arg)
@@ -33,6 +39,8 @@ static void *worker(void *arg)
   job_t *j = (job_t *) arg;
   P7_OPROFILE *om = p7_oprofile_Clone(j->om0);
   P7_OMX *ox = p7_omx_Create(om->M, 0, 0);
+  P7_BG *bg = p7_bg_Create(om->abc);
+  p7_bg_SetFilter(bg, om->M, om->compo);
   int64_t maxL = 1;
   for (int64_t i = j->lo; i < j->hi; i++) if (j->off[i+1] - j->off[i] > maxL) maxL = j->off[i+1] - j->off[i];
   ESL_DSQ *dsq = malloc(maxL + 2);
@@ -42,18 +50,25 @@ static void *worker(void *arg)
       int L = (int) (j->off[i+1] - j->off[i]); float sc;
       if (L == 0) continue;
       dsq[0] = eslDSQ_SENTINEL; memcpy(dsq + 1, j->res + j->off[i], L); dsq[L+1] = eslDSQ_SENTINEL;
-      p7_oprofile_ReconfigLength(om, L);
-      p7_MSVFilter(dsq, L, om, ox, &sc);
+      if (j->stage == 2) {
+        p7_bg_SetLength(bg, L);
+        p7_bg_FilterScore(bg, dsq, L, &sc);
+      } else {
+        p7_oprofile_ReconfigLength(om, L);
+        if (j->stage == 1) p7_ViterbiFilter(dsq, L, om, ox, &sc);
+        else p7_MSVFilter(dsq, L, om, ox, &sc);
+      }
       acc += sc;
     }
   j->sink = acc;
-  free(dsq); p7_omx_Destroy(ox); p7_oprofile_Destroy(om);
+  free(dsq); p7_omx_Destroy(ox); p7_oprofile_Destroy(om); p7_bg_Destroy(bg);
   return NULL;
 }
 
 int main(int argc, char **argv)
 {
-  if (argc != 8) die("usage: refbench M seed Lcfg mode seqs nthreads reps");
+  if (argc != 8 && argc != 9) die("usage: refbench M seed Lcfg mode seqs nthreads reps [msv|vit|bias]");
+  const int stage = argc == 9 ? (!strcmp(argv[8], "vit") ? 1 : !strcmp(argv[8], "bias") ? 2 : 0) : 0;
   int M = atoi(argv[1]), Lcfg = atoi(argv[3]), mode = atoi(argv[4]);
   int nth = atoi(argv[6]), reps = atoi(argv[7]);
   ESL_RANDOMNESS *r = esl_randomness_Create((uint32_t) atol(argv[2]));
@@ -61,6 +76,7 @@ int main(int argc, char **argv)
   P7_BG *bg = p7_bg_Create(abc); P7_HMM *hmm = NULL;
   if (p7_hmm_Sample(r, M, abc, &hmm) != eslOK) die("sample");
   if (p7_Calibrate(hmm, NULL, NULL, &bg, NULL, NULL) != eslOK) die("calibrate");
+  if (p7_hmm_SetComposition(hmm) != eslOK) die("composition");
   P7_PROFILE *gm = p7_profile_Create(M, abc);
   p7_ProfileConfig(hmm, bg, gm, Lcfg, mode);
   P7_OPROFILE *om = p7_oprofile_Create(M, abc);
@@ -80,7 +96,7 @@ int main(int argc, char **argv)
     int64_t target = (total * (t + 1)) / nth, e = s;
     while (e < n && off[e] < target) e++;
     if (t == nth - 1) e = n;
-    jobs[t] = (job_t){ om, off, res, s, e, reps, 0.0 };
+    jobs[t] = (job_t){ om, off, res, s, e, reps, 0.0, stage };
     s = e;
   }
   struct timespec t0, t1;
