@@ -82,16 +82,17 @@ __device__ __forceinline__ float log_row(float m, const double2 *tab) {
 }
 
 // float(log(m)) in float-float arithmetic on the FP32 pipe, for m in
-// [0.707, 1.414) (exponent 0 after the reduction; the row maxima of the
-// filter's scaled Forward lie there): the top 11 mantissa bits pick a
+// [2^-8.5, 2^8.5) (exponents -8 .. 8 after the reduction; the row maxima of
+// the filter's scaled Forward lie there): the top 11 mantissa bits pick a
 // reduction point c (2048 intervals; c = 1 next to 1) with 1/c and log c
 // stored as float pairs; d = f - c is exact, r = d/c a float pair by fused
 // multiply-adds, log1p(r) = r - r^2/2 (pairs) + r^3/3 - r^4/4 + r^5/5 (float;
 // |r| < 2^-11.5, truncation < 2^-57), summed with error-free two-sums. The
 // result is returned only when it is at least 2^-42 (relative) away from a
-// float rounding boundary -- every float in [0.25, 4) checked on the host
-// against the C library's double log: 0 differences; otherwise (and for
-// other exponents) the double path decides.
+// float rounding boundary -- every float in [2^-8, 2^8) checked on the host
+// against the C library's double log: 0 differences, 737 of 134 M left to
+// the double path; otherwise (and for other exponents) the double path
+// decides.
 __device__ float4 g_logff[2048];
 
 __device__ __forceinline__ float fsub(float a, float b) { return __fadd_rn(a, -b); }
@@ -101,7 +102,8 @@ __device__ __forceinline__ bool log_ff(float m, float *out) {
   if (b - 0x00800000u >= 0x7f000000u) return false;
   const int j = (b >> 12) & 0x7ff;
   const int half = j >= 849;
-  if ((int) (b >> 23) - 127 + half != 0) return false;
+  const int e = (int) (b >> 23) - 127 + half;
+  if (e < -8 || e > 8) return false;
   const float f = __uint_as_float((b & 0x7fffffu) | ((uint32_t) (127 - half) << 23));
   const float4 t = g_logff[j];                               // 1/c (hi, lo), log c (hi, lo)
   const float c = (j == 0 || j == 2047) ? 1.0f : __fmul_rn(half ? 0.5f : 1.0f, 1.0f + ((float) j + 0.5f) / 2048.0f);
@@ -112,11 +114,24 @@ __device__ __forceinline__ bool log_ff(float m, float *out) {
   const float sl = __fadd_rn(__fmaf_rn(rh, rh, -sh), __fmul_rn(__fmul_rn(2.0f, rh), rl));
   const float q3 = __fmul_rn(__fmul_rn(rh, sh),
                              __fadd_rn(1.0f / 3.0f, __fmul_rn(rh, __fadd_rn(-0.25f, __fmul_rn(rh, 0.2f)))));
-  float H = t.z, L = 0.0f, sm, bb;
-  sm = __fadd_rn(H, rh); bb = fsub(sm, H); L = __fadd_rn(L, __fadd_rn(fsub(H, fsub(sm, bb)), fsub(rh, bb))); H = sm;
-  const float hs = __fmul_rn(-0.5f, sh);
-  sm = __fadd_rn(H, hs); bb = fsub(sm, H); L = __fadd_rn(L, __fadd_rn(fsub(H, fsub(sm, bb)), fsub(hs, bb))); H = sm;
-  L = __fadd_rn(L, __fadd_rn(__fadd_rn(__fadd_rn(t.w, rl), __fmul_rn(-0.5f, sl)), q3));
+  // e ln2 in three parts: a 16-bit head (e * head exact for |e| <= 8), the
+  // middle as an exact product, the tail
+  const float l2h = 0.693145751953125f, l2m = 0x1.7f7d1cp-20f, l2l = 5.49560397e-14f;
+  const float fe = (float) e;
+  const float A = __fmul_rn(fe, l2h);
+  const float bh = __fmul_rn(fe, l2m), bl = __fmaf_rn(fe, l2m, -bh);
+  float H = A, L = 0.0f, sm, bb;
+  auto two_sum = [&](float x) {                              // H + x = sm + error, the error into L
+    sm = __fadd_rn(H, x); bb = fsub(sm, H);
+    L = __fadd_rn(L, __fadd_rn(fsub(H, fsub(sm, bb)), fsub(x, bb)));
+    H = sm;
+  };
+  two_sum(t.z);
+  two_sum(bh);
+  two_sum(rh);
+  two_sum(__fmul_rn(-0.5f, sh));
+  L = __fadd_rn(L, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(t.w, bl), __fmul_rn(fe, l2l)), rl),
+                                       __fmul_rn(-0.5f, sl)), q3));
   const float res = __fadd_rn(H, L);
   const float bv = fsub(res, H);
   const float tr = __fadd_rn(fsub(H, fsub(res, bv)), fsub(L, bv));   // H + L - res, exactly
