@@ -433,9 +433,17 @@ def vitfilter(ctx: Context, vprof: DeviceVProfile, db: DeviceDB, ids=None):
     st = np.zeros(ids.size, np.uint8)
     _check(lib().msvgb_vitfilter(ctx.h, vprof.h, db.h, ids.ctypes.data if ids.size else None, ids.size,
                                  xc.ctypes.data, st.ctypes.data))
-    o, keep = _vom_struct(vprof.vp)
-    sc = np.array([lib().msvgb_vit_score(int(xc[j]), int(st[j]), int(db.lengths[ids[j]]), ctypes.byref(o))
-                   for j in range(ids.size)], np.float32)
+    # msvgb_vit_score's float expression (vitfilter.c:240-247), vectorized: the
+    # integer sums are exact in float32, the division is IEEE, and subtracting
+    # 3.0 in double then rounding equals the float32 subtraction here
+    vp = vprof.vp
+    L = db.lengths[ids].astype(np.int64)
+    uniq, inv = np.unique(L, return_inverse=True)
+    move = np.array([lib().msvgb_vit_move_cost(vp.scale_w, vp.nj, int(x)) for x in uniq], np.float32)[inv]
+    with np.errstate(over="ignore", invalid="ignore"):
+        sc = (xc.astype(np.float32) + move - np.float32(vp.base_w)) / np.float32(vp.scale_w) - np.float32(3.0)
+    sc = np.where(xc <= -32768, np.float32(-np.inf), sc).astype(np.float32)
+    sc = np.where(st == 1, np.float32(np.inf), sc).astype(np.float32)
     return st, sc
 
 
