@@ -39,7 +39,7 @@ EXPORTS = [
     "msvgb_db_save", "msvgb_db_load", "msvgb_db_lengths", "msvgb_search_host",
     "msvgb_vprofile_create", "msvgb_vprofile_destroy", "msvgb_vitfilter", "msvgb_vit_score", "msvgb_vit_move_cost",
     "msvgb_biasfilter", "msvgb_bias_length_term", "msvgb_null_score", "msvgb_stage_pass", "msvgb_pipeline_filters",
-    "msvgb_filter_collect",
+    "msvgb_filter_collect", "msvgb_h3f_filter_params", "msvgb_h3p_open", "msvgb_h3p_read", "msvgb_h3p_close",
 ]
 
 
@@ -175,6 +175,10 @@ def lib():
         "msvgb_pipeline_filters": (i32, [vp, ctypes.POINTER(_Filters), vp, vp, i64, i64, i32, vp, vp,
                                          ctypes.POINTER(FilterStats)]),
         "msvgb_filter_collect": (i32, [vp, vp]),
+        "msvgb_h3f_filter_params": (i32, [vp, vp, ctypes.POINTER(f32), ctypes.POINTER(f32)]),
+        "msvgb_h3p_open": (i32, [ctypes.c_char_p, ctypes.POINTER(vp)]),
+        "msvgb_h3p_read": (i32, [vp, ctypes.POINTER(_VOm), ctypes.c_char_p, i32]),
+        "msvgb_h3p_close": (i32, [vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -341,8 +345,10 @@ class DeviceDB:
             pass
 
 
-def read_h3f(path: str):
-    """Every record of a pressed MSV profile file: [(name, Profile)]."""
+def read_h3f(path: str, filter_params: bool = False):
+    """Every record of a pressed MSV profile file: [(name, Profile)]; with
+    filter_params, [(name, Profile, compo float32[20], vmu, vlambda)] -- the
+    composition and Viterbi Gumbel parameters the later filter stages use."""
     h = ctypes.c_void_p()
     _check(lib().msvgb_h3f_open(path.encode(), ctypes.byref(h)))
     out = []
@@ -357,11 +363,44 @@ def read_h3f(path: str):
             Q = F.nqb(o.M)
             rbv = np.ctypeslib.as_array(ctypes.cast(o.rbv, ctypes.POINTER(ctypes.c_uint8)),
                                         shape=(o.Kp * Q * 16,)).reshape(o.Kp, Q, 16).copy()
-            out.append((name.value.decode(), F.Profile(M=o.M, rbv=rbv, tbm_b=o.tbm_b, tec_b=o.tec_b,
-                                                        base_b=o.base_b, bias_b=o.bias_b, scale_b=o.scale_b,
-                                                        mmu=o.mmu, mlambda=o.mlambda, tjb_cfg=o.tjb_b)))
+            prof = F.Profile(M=o.M, rbv=rbv, tbm_b=o.tbm_b, tec_b=o.tec_b, base_b=o.base_b, bias_b=o.bias_b,
+                             scale_b=o.scale_b, mmu=o.mmu, mlambda=o.mlambda, tjb_cfg=o.tjb_b)
+            if filter_params:
+                compo = np.zeros(20, np.float32)
+                vmu, vlam = ctypes.c_float(), ctypes.c_float()
+                _check(lib().msvgb_h3f_filter_params(h, compo.ctypes.data, ctypes.byref(vmu), ctypes.byref(vlam)))
+                out.append((name.value.decode(), prof, compo, vmu.value, vlam.value))
+            else:
+                out.append((name.value.decode(), prof))
     finally:
         lib().msvgb_h3f_close(h)
+    return out
+
+
+def read_h3p(path: str):
+    """Every record of a pressed profile's .h3p file, its ViterbiFilter part:
+    [(name, VProfile)]."""
+    h = ctypes.c_void_p()
+    _check(lib().msvgb_h3p_open(path.encode(), ctypes.byref(h)))
+    out = []
+    try:
+        name = ctypes.create_string_buffer(1024)
+        while True:
+            v = _VOm()
+            st = lib().msvgb_h3p_read(h, ctypes.byref(v), name, 1024)
+            if st == eslEOF:
+                break
+            _check(st)
+            Q8 = max(2, (v.M - 1) // 8 + 1)
+            twv = np.ctypeslib.as_array(ctypes.cast(v.twv, ctypes.POINTER(ctypes.c_int16)), shape=(8 * Q8 * 8,))
+            rwv = np.ctypeslib.as_array(ctypes.cast(v.rwv, ctypes.POINTER(ctypes.c_int16)), shape=(v.Kp * Q8 * 8,))
+            xw = np.array(list(v.xw), np.int16).reshape(4, 2)
+            out.append((name.value.decode(), F.VProfile(M=v.M, twv=twv.reshape(8 * Q8, 8).copy(),
+                                                         rwv=rwv.reshape(v.Kp, Q8, 8).copy(), xw=xw,
+                                                         scale_w=v.scale_w, nj=v.nj, base_w=v.base_w,
+                                                         ddbound_w=v.ddbound_w)))
+    finally:
+        lib().msvgb_h3p_close(h)
     return out
 
 

@@ -91,6 +91,9 @@ struct msvgb_h3f {
   std::vector<uint8_t> data;
   size_t pos = 0;
   std::vector<uint8_t> rbv;        // the last record's table (om->rbv points here)
+  float compo[20] = {};            // the last record's composition and evparam VMU, VLAMBDA
+  float vmu = 0.f, vlambda = 0.f;
+  bool have = false;
 };
 
 extern "C" int msvgb_h3f_open(const char *path, msvgb_h3f **ret) {
@@ -127,7 +130,8 @@ extern "C" int msvgb_h3f_read(msvgb_h3f *f, msvgb_om *om, char *name, int name_c
   const uint8_t *rbv = r.take((size_t) kKpAmino * Q * 16);
   float ev[kNEvparam];
   for (float &v : ev) v = r.get<float>();
-  r.take((size_t) kNOffsets * kOffT + (size_t) kMaxAbet * 4);   // hmmpfam offsets, composition
+  r.take((size_t) kNOffsets * kOffT);                           // hmmpfam offsets
+  const uint8_t *compo = r.take((size_t) kMaxAbet * 4);
   const uint32_t tail = r.get<uint32_t>();
   if (!r.ok) return fail(MSVGB_eslEFORMAT, "truncated record");
   if (tail != kMagic3f) return fail(MSVGB_eslEFORMAT, "bad sentinel magic: corrupted .h3f record");
@@ -137,11 +141,105 @@ extern "C" int msvgb_h3f_read(msvgb_h3f *f, msvgb_om *om, char *name, int name_c
   om->tbm_b = tbm; om->tec_b = tec; om->tjb_b = tjb; om->base_b = base; om->bias_b = bias;
   om->scale_b = scale;
   om->mmu = ev[0]; om->mlambda = ev[1];                         // p7_MMU, p7_MLAMBDA
+  memcpy(f->compo, compo, sizeof f->compo);
+  f->vmu = ev[2]; f->vlambda = ev[3];                           // p7_VMU, p7_VLAMBDA
+  f->have = true;
   if (name && name_cap > 0) {
     const size_t k = std::min((size_t) name_cap - 1, (size_t) n);
     memcpy(name, nm, k);
     name[k] = '\0';
   }
+  return MSVGB_eslOK;
+}
+
+extern "C" int msvgb_h3f_filter_params(const msvgb_h3f *f, float *compo, float *vmu, float *vlambda) {
+  if (!f || !f->have) return fail(MSVGB_eslEINVAL, "no record read yet");
+  if (compo) memcpy(compo, f->compo, sizeof f->compo);
+  if (vmu) *vmu = f->vmu;
+  if (vlambda) *vlambda = f->vlambda;
+  return MSVGB_eslOK;
+}
+
+// ------------------------------------------------------------------------------
+// .h3p: the rest of a pressed profile (p7_oprofile_Write's <pfp> part,
+// src/impl_sse/io.c:122-170); the ViterbiFilter fields are returned, the
+// annotation and Forward/Backward fields checked for length and skipped
+
+namespace {
+constexpr uint32_t kMagic3p = 0xb3e6f0f3u;   // "3fps" + 0x80808080 (src/impl_sse/io.c:49)
+constexpr int kNCutoffs = 6;                 // p7_NCUTOFFS
+int nqw(int M) { return std::max(2, (M - 1) / 8 + 1); }   // p7O_NQW
+int nqf(int M) { return std::max(2, (M - 1) / 4 + 1); }   // p7O_NQF
+}  // namespace
+
+struct msvgb_h3p {
+  std::vector<uint8_t> data;
+  size_t pos = 0;
+  std::vector<int16_t> twv, rwv;   // the last record's tables (vom->twv, vom->rwv point here)
+};
+
+extern "C" int msvgb_h3p_open(const char *path, msvgb_h3p **ret) {
+  if (!path || !ret) return fail(MSVGB_eslEINVAL, "NULL argument");
+  *ret = nullptr;
+  msvgb_h3p *f = new msvgb_h3p();
+  int st = read_file(path, f->data);
+  if (st != MSVGB_eslOK) { delete f; return st; }
+  *ret = f;
+  return MSVGB_eslOK;
+}
+
+extern "C" int msvgb_h3p_read(msvgb_h3p *f, msvgb_vom *vom, char *name, int name_cap) {
+  if (!f || !vom) return fail(MSVGB_eslEINVAL, "NULL argument");
+  if (f->pos >= f->data.size()) return MSVGB_eslEOF;
+  Reader r{f->data, f->pos};
+  const uint32_t magic = r.get<uint32_t>();
+  if (!r.ok) return fail(MSVGB_eslEFORMAT, "truncated record");
+  if (magic != kMagic3p) return fail(MSVGB_eslEFORMAT, "bad magic: not a HMMER 3/f profile (.h3p) file");
+  const int32_t M = r.get<int32_t>(), alpha = r.get<int32_t>(), n = r.get<int32_t>();
+  if (!r.ok || M < 1 || M > 100000 || n < 0 || n > (1 << 20)) return fail(MSVGB_eslEFORMAT, "bad record header");
+  if (alpha != kAlphaAmino)
+    return fail(MSVGB_eslEINCOMPAT, "only amino acid profiles are supported (alphabet type " + std::to_string(alpha) + ")");
+  const uint8_t *nm = r.take((size_t) n + 1);
+  for (int k = 0; k < 2; ++k) {                                  // accession, description
+    const int32_t len = r.get<int32_t>();
+    if (!r.ok || len < 0 || len > (1 << 24)) return fail(MSVGB_eslEFORMAT, "bad accession/description length");
+    if (len > 0) r.take((size_t) len + 1);
+  }
+  r.take((size_t) 4 * (M + 2));                                 // rf, mm, cs, consensus
+  const int Q8 = nqw(M), Q4 = nqf(M);
+  const uint8_t *twv = r.take((size_t) 8 * Q8 * 16);
+  const uint8_t *rwv = r.take((size_t) kKpAmino * Q8 * 16);
+  int16_t xw[4][2];
+  for (auto &row : xw) for (int16_t &v : row) v = r.get<int16_t>();
+  const float scale_w = r.get<float>();
+  const int16_t base_w = r.get<int16_t>(), ddbound_w = r.get<int16_t>();
+  r.get<float>();                                               // ncj_roundoff
+  r.take((size_t) 8 * Q4 * 16 + (size_t) kKpAmino * Q4 * 16 + 8 * 4);   // tfv, rfv, xf: the Forward part
+  r.take((size_t) kNCutoffs * 4);
+  const float nj = r.get<float>();
+  r.get<int32_t>(); r.get<int32_t>();                           // mode, L
+  const uint32_t tail = r.get<uint32_t>();
+  if (!r.ok) return fail(MSVGB_eslEFORMAT, "truncated record");
+  if (tail != kMagic3p) return fail(MSVGB_eslEFORMAT, "bad sentinel magic: corrupted .h3p record");
+  f->twv.resize((size_t) 8 * Q8 * 8);
+  f->rwv.resize((size_t) kKpAmino * Q8 * 8);
+  memcpy(f->twv.data(), twv, f->twv.size() * 2);
+  memcpy(f->rwv.data(), rwv, f->rwv.size() * 2);
+  f->pos = r.pos;
+  vom->M = M; vom->Kp = kKpAmino;
+  vom->twv = f->twv.data(); vom->rwv = f->rwv.data();
+  memcpy(vom->xw, xw, sizeof xw);
+  vom->scale_w = scale_w; vom->nj = nj; vom->base_w = base_w; vom->ddbound_w = ddbound_w;
+  if (name && name_cap > 0) {
+    const size_t k = std::min((size_t) name_cap - 1, (size_t) n);
+    memcpy(name, nm, k);
+    name[k] = '\0';
+  }
+  return MSVGB_eslOK;
+}
+
+extern "C" int msvgb_h3p_close(msvgb_h3p *f) {
+  delete f;
   return MSVGB_eslOK;
 }
 

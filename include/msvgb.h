@@ -203,6 +203,20 @@ int msvgb_h3f_open(const char *path, msvgb_h3f **ret);
  * older-format record; eslEINCOMPAT for a non-amino model. */
 int msvgb_h3f_read(msvgb_h3f *f, msvgb_om *om, char *name, int name_cap);
 int msvgb_h3f_close(msvgb_h3f *f);
+/* The record last read: its model composition (20 floats, P7_OPROFILE compo)
+ * and evparam VMU, VLAMBDA -- what the bias filter and the ViterbiFilter gate
+ * need besides the .h3p part (any pointer may be NULL). */
+int msvgb_h3f_filter_params(const msvgb_h3f *f, float *compo, float *vmu, float *vlambda);
+/* The rest of a pressed profile (.h3p, p7_oprofile_Write's second file,
+ * impl_sse/io.c:122-170, read back by p7_oprofile_ReadRest): the next
+ * record's ViterbiFilter part into vom (vom->twv, vom->rwv point at storage
+ * owned by the reader until the next read or close); the annotation and
+ * Forward/Backward fields are checked for length and skipped. eslEOF after
+ * the last record; eslEFORMAT on a corrupted record. */
+typedef struct msvgb_h3p msvgb_h3p;
+int msvgb_h3p_open(const char *path, msvgb_h3p **ret);
+int msvgb_h3p_read(msvgb_h3p *f, msvgb_vom *vom, char *name, int name_cap);
+int msvgb_h3p_close(msvgb_h3p *f);
 /* Writes (append != 0: appends) one record in the same format, as
  * p7_oprofile_Write does (io.c:89); the SSV table is derived from rbv
  * (sf_conversion, p7_oprofile.c:549-590); evparam holds mmu and mlambda only. */

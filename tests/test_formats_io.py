@@ -180,3 +180,36 @@ def test_fasta_errors_and_empty(tmp_path):
     with pytest.raises(api.MSVError) as e:
         api.read_fasta(str(tmp_path / "missing.fa"))
     assert e.value.code == api.eslENOTFOUND
+
+
+@has_tutorial
+def test_reference_pressed_rest_reads_as_the_reference_configures_it():
+    """tutorial/minifam.h3p (hmmpress's second file): the ViterbiFilter part of
+    each model equals the reference's own hmmsearch-configured profile
+    (tests/golden/vit_tut_*.vprof) except the N/J/C move costs (pressed at
+    length 400, configured at 100; recomputed per target length), and the
+    .h3f record's composition and Viterbi Gumbel parameters equal those the
+    reference's pipeline used (tests/golden/pipe_tut_*.pres)."""
+    rest = api.read_h3p(os.path.join(TUTORIAL, "minifam.h3p"))
+    msv = api.read_h3f(os.path.join(TUTORIAL, "minifam.h3f"), filter_params=True)
+    assert [n for n, _ in rest] == ["globins4", "fn3", "Pkinase"] == [r[0] for r in msv]
+    for (name, vp), (_, p, compo, vmu, vlambda), g in zip(rest, msv, ["tut_globins4", "tut_fn3", "tut_pkinase"]):
+        want = F.read_vprofile(os.path.join(GOLDEN, "vit_" + g + ".vprof"))
+        pipe = F.read_pipe(os.path.join(GOLDEN, "pipe_" + g + ".pres"))
+        assert vp.M == want.M == p.M
+        assert np.array_equal(vp.twv, want.twv) and np.array_equal(vp.rwv, want.rwv)
+        assert (vp.scale_w, vp.nj, vp.base_w, vp.ddbound_w) == (want.scale_w, want.nj, want.base_w, want.ddbound_w)
+        assert np.array_equal(vp.xw[0], want.xw[0]) and np.array_equal(vp.xw[1:, 1], want.xw[1:, 1])
+        assert np.array_equal(compo.view(np.uint32), pipe.compo.view(np.uint32))
+        assert (np.float32(vmu), np.float32(vlambda)) == (np.float32(pipe.vmu), np.float32(pipe.vlambda))
+
+
+def test_h3p_errors(tmp_path):
+    with pytest.raises(api.MSVError) as e:
+        api.read_h3p(str(tmp_path / "missing.h3p"))
+    assert e.value.code == api.eslENOTFOUND
+    bad = tmp_path / "bad.h3p"
+    bad.write_bytes(b"\x00" * 64)
+    with pytest.raises(api.MSVError) as e:
+        api.read_h3p(str(bad))
+    assert e.value.code == api.eslEFORMAT
