@@ -37,7 +37,7 @@ from cudahmmsearch_gb300 import formats as F  # noqa: E402
 
 INT_LANE_OPS_PER_CLK_PER_SM = 128   # 4 SM sub-partitions x 32 lanes: nominal issue width
 # DRAM bytes per residue of the hot kernel (the lane-group SSV pass), from the
-# ncu capture summarised in profiles/msv_ssv_group_kernel_m400_400k.md
+# ncu capture of the lane-group SSV kernel on 400,000 sequences (summary under profiles/)
 # (168.8 MB for 154.56 M residues); the pass reads each residue once, so
 # traffic scales with the residue count.
 DRAM_BYTES_PER_RESIDUE = 168.8e6 / 154.56e6
@@ -550,7 +550,7 @@ def main():
                 "frac": achieved_tops / peak_tops,
                 "traffic": DRAM_BYTES_PER_RESIDUE * s.total,
                 "traffic_note": "DRAM bytes of the SSV pass scaled by residues from an ncu capture of the same "
-                                "kernel on 400,000 sequences (profiles/msv_ssv_group_kernel_m400_400k.md)",
+                                "kernel on 400,000 sequences (summary under profiles/)",
                 "peak_note": f"measured: msvgb_measure_int_peak (independent max.s32/xor over {nsm} SMs); "
                              f"nominal {nsm} SMs x {INT_LANE_OPS_PER_CLK_PER_SM} lane-ops/clk x {sm_mhz:.0f} MHz = "
                              f"{nsm * INT_LANE_OPS_PER_CLK_PER_SM * sm_mhz * 1e6 / 1e12:.1f} Tops/s",
