@@ -213,3 +213,31 @@ def test_h3p_errors(tmp_path):
     with pytest.raises(api.MSVError) as e:
         api.read_h3p(str(bad))
     assert e.value.code == api.eslEFORMAT
+
+
+@has_tutorial
+def test_h3p_rejects_corrupted_records(tmp_path):
+    """The reference's minifam.h3p cut or altered at record boundaries and
+    inside fields: every damaged copy is eslEFORMAT, never a wrong profile."""
+    good = open(os.path.join(TUTORIAL, "minifam.h3p"), "rb").read()
+    rest = api.read_h3p(os.path.join(TUTORIAL, "minifam.h3p"))
+    M0 = rest[0][1].M
+
+    def check(name, data):
+        p = tmp_path / (name + ".h3p")
+        p.write_bytes(data)
+        with pytest.raises(api.MSVError) as e:
+            api.read_h3p(str(p))
+        assert e.value.code == api.eslEFORMAT, name
+
+    for cut in (3, 11, 40, len(good) // 3, len(good) // 2, len(good) - 4, len(good) - 1):
+        check(f"cut{cut}", good[:cut])
+    bad = bytearray(good)
+    bad[0] ^= 0xFF                                            # magic
+    check("magic", bytes(bad))
+    bad = bytearray(good)
+    bad[4:8] = np.int32(M0 + 1).tobytes()                     # M: every later field shifts
+    check("M", bytes(bad))
+    bad = bytearray(good)
+    bad[12:16] = np.int32(-5).tobytes()                       # name length
+    check("namelen", bytes(bad))
