@@ -843,11 +843,14 @@ extern "C" int msvgb_search_host(msvgb_ctx *c, const msvgb_profile *p, const uin
   // chunk boundaries [cut[k], cut[k+1]): by default a sixth of the residues,
   // then the rest (the rest's copy, at ~5x the search's residue rate, is up
   // before the first sixth is searched; every further chunk adds a launch
-  // tail and a full-MSV pass, ~0.5 ms each); with chunk_residues, chunks
-  // growing from a quarter of it to it
+  // tail and a full-MSV pass, ~0.5 ms each), and one chunk when the whole
+  // copy takes less than that (kOneChunkResidues); with chunk_residues,
+  // chunks growing from a quarter of it to it
   std::vector<int64_t> cut(1, 0);
   const int64_t total = off[n] - off[0];
-  int64_t want = chunk_residues > 0 ? std::max<int64_t>(1, chunk_residues / 4) : total / 6 + 1;
+  constexpr int64_t kOneChunkResidues = 64 << 20;
+  int64_t want = chunk_residues > 0 ? std::max<int64_t>(1, chunk_residues / 4)
+                                    : (total < kOneChunkResidues ? total : total / 6 + 1);
   for (int64_t b0 = 0; b0 < n;) {
     int64_t b1 = b0 + 1;
     while (b1 < n && off[b1] - off[b0] < want) ++b1;
