@@ -63,7 +63,11 @@ typedef struct {
 } msvgb_omx;
 
 /* Objects created on a context (profiles, databases) may be destroyed before
- * or after it; searches need their context alive. */
+ * or after it; searches need their context alive.
+ * Threads: a context serves one call at a time (its stream and scratch are
+ * shared by its calls), except msvgb_MSVFilter, which serialises itself;
+ * give each thread its own context. Profiles, ViterbiFilter profiles and
+ * databases of one device may be used from several contexts at once. */
 typedef struct msvgb_ctx     msvgb_ctx;      /* one GPU, one stream, device buffers   */
 typedef struct msvgb_profile msvgb_profile;  /* a profile resident in HBM             */
 typedef struct msvgb_db      msvgb_db;       /* a packed sequence database in HBM     */
