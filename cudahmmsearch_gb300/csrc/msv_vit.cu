@@ -488,7 +488,7 @@ cudaError_t launch_vit(const VitDev &V, const DbDev &db, const int64_t *ids, con
 // M=400), two per register (the packed form) at 40 and 48, where the int32
 // form would need 16-bit transitions (851 vs 802 GCUPS at M=1500), the
 // shared-memory row above 48
-constexpr int kVitCV[] = {1, 2, 3, 4, 6, 8, 12, 16, 24, 32, 40, 48};
+constexpr int kVitCV[] = {1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 20, 24, 28, 32, 40, 48};
 constexpr bool vit_packed(int CV) { return CV == 40 || CV == 48; }
 
 __global__ void __launch_bounds__(kVitThreads)
@@ -538,7 +538,8 @@ cudaError_t dispatch_vit(int CV, const VitDev &V, const DbDev &db, const int64_t
   if (CV > 48) return launch_vit_wide(V, db, ids, order, n, xc, st, ticket, sms, stream);
   switch (CV) {
 #define VCASE(c) case c: return launch_vit<c>(V, db, ids, order, n, xc, st, ticket, sms, stream);
-    VCASE(1) VCASE(2) VCASE(3) VCASE(4) VCASE(6) VCASE(8) VCASE(12) VCASE(16) VCASE(24) VCASE(32)
+    VCASE(1) VCASE(2) VCASE(3) VCASE(4) VCASE(5) VCASE(6) VCASE(7) VCASE(8) VCASE(9) VCASE(10) VCASE(11)
+    VCASE(12) VCASE(13) VCASE(14) VCASE(15) VCASE(16) VCASE(20) VCASE(24) VCASE(28) VCASE(32)
 #undef VCASE
 #define PCASE(c) case c: return launch_vitp<c>(V, db, ids, order, n, xc, st, ticket, sms, stream);
     PCASE(40) PCASE(48)
