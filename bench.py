@@ -274,7 +274,7 @@ def run_filters(args, api, torch, ctx, stream, local):
     each with CUDA events on the launching stream (the calls include the id
     upload and the result copy); (c) the whole filter pipeline (database
     blocks uploaded, MSV, bias, ViterbiFilter, gates) through
-    msvgb_pipeline_filters from host buffers, host wall clock."""
+    msvgb_pipeline_filters from pinned host buffers, host wall clock."""
     G = os.path.join(ROOT, "tests", "golden")
     p = F.read_profile(os.path.join(G, "pipe_m400_s1.prof"))
     vp = F.read_vprofile(os.path.join(G, "vit_m400_s1.vprof"))
@@ -312,6 +312,8 @@ def run_filters(args, api, torch, ctx, stream, local):
             torch.cuda.synchronize()
             ms.append(a.elapsed_time(b))
         return float(np.median(ms))
+    # the pipeline reads the residues and offsets from pinned host memory
+    hs = F.SeqSet(torch.from_numpy(s.codes).pin_memory().numpy(), torch.from_numpy(s.off).pin_memory().numpy())
     launches0 = api.kernel_launches()
     with ClockSampler(local) as clk:
         vit_ms = timed(vit)
@@ -320,7 +322,7 @@ def run_filters(args, api, torch, ctx, stream, local):
         for i in range(args.warmup + args.steps):
             torch.cuda.synchronize()
             t = time.perf_counter()
-            hits, st = api.pipeline_filters(ctx, p, s, vprof=vp, compo=pr.compo, vmu=pr.vmu, vlambda=pr.vlambda,
+            hits, st = api.pipeline_filters(ctx, p, hs, vprof=vp, compo=pr.compo, vmu=pr.vmu, vlambda=pr.vlambda,
                                             block_size=500_000, n_workers=4)
             if i >= args.warmup:
                 pipe_s.append(time.perf_counter() - t)
@@ -331,7 +333,8 @@ def run_filters(args, api, torch, ctx, stream, local):
             "warmup": args.warmup, "ms_per_step": float(np.median(pipe_s)) * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u8/s16/f32", "data": "synthetic",
             "config": {"workload": f"p7_Pipeline filter stages (MSV, bias, ViterbiFilter) on the GPU, M=400 local "
-                                   f"(p7_hmm_Sample seed 1) vs {s.n:,} seqs (m400_2M's law), blocks of 500,000",
+                                   f"(p7_hmm_Sample seed 1) vs {s.n:,} seqs (m400_2M's law), blocks of 500,000, "
+                                   f"from pinned host buffers",
                        "M": p.M, "n_seqs": s.n, "residues": s.total,
                        "n_past_msv": st.n_past_msv, "n_past_bias": st.n_past_bias, "n_past_vit": st.n_past_vit},
             "stages": {"vitfilter": {"ms": vit_ms, "gcups": vp.M * res_ids / (vit_ms * 1e-3) / 1e9,
