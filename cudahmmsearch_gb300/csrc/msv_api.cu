@@ -828,8 +828,7 @@ extern "C" int msvgb_search(msvgb_ctx *c, const msvgb_profile *p, const msvgb_db
 }
 
 // End to end from host buffers. The sequences are cut into chunks by residue
-// count (a quarter of chunk_residues first, doubling up to chunk_residues, so
-// the GPU starts early); while the GPU searches chunk k on the context's
+// count (below); while the GPU searches chunk k on the context's
 // stream, the host sorts chunk k+1 and its residues go up and are packed on
 // the upload stream. Results of all chunks land in one device buffer and come
 // back in one copy at the end.

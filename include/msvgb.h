@@ -277,8 +277,9 @@ int msvgb_search_device(msvgb_ctx *ctx, const msvgb_profile *prof, const msvgb_d
 /* End to end from host buffers, for a database that is not kept resident:
  * sequences codes[off[i] .. off[i+1]) (as msvgb_db_create takes them) are
  * uploaded and packed in chunks while earlier chunks are searched (by default
- * an eighth of the residues, a quarter, then the rest; with chunk_residues >
- * 0, chunks growing to that size); results as msvgb_search. The batched pre-pass the fork's p7_PipelineShort consumed
+ * a sixth of the residues, then the rest, or one chunk below 64 M residues;
+ * with chunk_residues > 0, chunks growing from a quarter of that size to it);
+ * results as msvgb_search. The batched pre-pass the fork's p7_PipelineShort consumed
  * (src/p7_pipeline.c:887-929), with the upload hidden behind the search. */
 int msvgb_search_host(msvgb_ctx *ctx, const msvgb_profile *prof, const uint8_t *codes, const int64_t *off,
                       int64_t n, double F1, int64_t chunk_residues, uint8_t *out_xj, uint8_t *out_flags);
