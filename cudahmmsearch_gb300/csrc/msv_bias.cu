@@ -97,13 +97,14 @@ __device__ float4 g_logff[2048];
 
 __device__ __forceinline__ float fsub(float a, float b) { return __fadd_rn(a, -b); }
 
-__device__ __forceinline__ bool log_ff(float m, float *out) {
+// Branch-free: ok says whether the returned value is the result (the
+// arithmetic runs on any input; the table index is always in range).
+__device__ __forceinline__ float log_ff(float m, bool &ok) {
   const uint32_t b = __float_as_uint(m);
-  if (b - 0x00800000u >= 0x7f000000u) return false;
   const int j = (b >> 12) & 0x7ff;
   const int half = j >= 849;
   const int e = (int) (b >> 23) - 127 + half;
-  if (e < -8 || e > 8) return false;
+  const bool in_range = b - 0x00800000u < 0x7f000000u && e >= -8 && e <= 8;
   const float f = __uint_as_float((b & 0x7fffffu) | ((uint32_t) (127 - half) << 23));
   const float4 t = g_logff[j];                               // 1/c (hi, lo), log c (hi, lo)
   const float c = (j == 0 || j == 2047) ? 1.0f : __fmul_rn(half ? 0.5f : 1.0f, 1.0f + ((float) j + 0.5f) / 2048.0f);
@@ -136,23 +137,24 @@ __device__ __forceinline__ bool log_ff(float m, float *out) {
   const float bv = fsub(res, H);
   const float tr = __fadd_rn(fsub(H, fsub(res, bv)), fsub(L, bv));   // H + L - res, exactly
   const uint32_t rb = __float_as_uint(res);
-  if ((rb & 0x7fffffffu) < 0x01000000u) return false;
   const float ulp = __uint_as_float((rb & 0x7f800000u) - (23u << 23));
-  if (fsub(__fmul_rn(0.5f, ulp), fabsf(tr)) < __fmul_rn(fabsf(res), 0x1p-42f)) return false;
-  *out = res;
-  return true;
+  ok = in_range && (rb & 0x7fffffffu) >= 0x01000000u &&
+       !(fsub(__fmul_rn(0.5f, ulp), fabsf(tr)) < __fmul_rn(fabsf(res), 0x1p-42f));
+  return res;
 }
 
 __device__ __forceinline__ float log_rowf(float m, const double2 *tab) {
-  float r;
-  return log_ff(m, &r) ? r : log_row(m, tab);
+  bool ok;
+  const float r = log_ff(m, ok);
+  return ok ? r : log_row(m, tab);
 }
 
 // One thread per listed sequence; threads take the list in database order
 // (order[t]: longest first), so a warp's sequences have similar lengths. Rows
-// go 16 at a time: first the 16 rows' recurrence (a serial chain through the
-// divisions), then their 16 logs, independent of one another, then the
-// in-order float sum.
+// go 16 at a time. The row logs of one batch are taken while the next batch's
+// recurrence runs -- row b's log next to row b's step, in straight-line code,
+// so its instructions fill the latency of the serial chain through the
+// divisions -- and then summed in row order.
 __global__ void __launch_bounds__(128)
 bias_kernel(BiasDev B, DbDev db, const int64_t *__restrict__ slots, const int64_t *__restrict__ order, int64_t nids,
             float *__restrict__ out, int32_t *__restrict__ out_len) {
@@ -172,17 +174,17 @@ bias_kernel(BiasDev B, DbDev db, const int64_t *__restrict__ slots, const int64_
   const float p1 = __fdiv_rn((float) L, (float) (L + 1));
   const float t00 = p1, t01 = __fadd_rn(1.0f, -p1);
   float d0 = 0.0f, d1 = 0.0f, logsc = 0.0f;
-  for (int i0 = 0; i0 < L; i0 += 16) {
-    const uint4 w = sq[i0 >> 4];
+  float mx[16];                                  // row maxima of the last batch, logs not yet taken
+  {                                              // rows 0 .. 15: the first starts from pi
+    const uint4 w = sq[0];
     const uint32_t words[4] = {w.x, w.y, w.z, w.w};
-    float mx[16];
 #pragma unroll
     for (int b = 0; b < 16; ++b) {
       mx[b] = 1.0f;
-      if (i0 + b >= L) continue;
+      if (b >= L) continue;
       const int x = (words[b >> 2] >> (8 * (b & 3))) & 0xff;
       float n0, n1;
-      if (i0 + b == 0) {
+      if (b == 0) {
         n0 = __fmul_rn(s_eo[x][0], B.pi0);
         n1 = __fmul_rn(s_eo[x][1], B.pi1);
       } else {
@@ -196,13 +198,43 @@ bias_kernel(BiasDev B, DbDev db, const int64_t *__restrict__ slots, const int64_
       d1 = __fdiv_rn(n1, m);
       mx[b] = m;
     }
-    float lg[16];
-#pragma unroll
-    for (int b = 0; b < 16; ++b) lg[b] = log_rowf(mx[b], s_log);
-#pragma unroll
-    for (int b = 0; b < 16; ++b)
-      if (i0 + b < L) logsc = __fadd_rn(logsc, lg[b]);
   }
+  for (int i0 = 16; i0 < L; i0 += 16) {          // the previous batch (rows i0-16 .. i0-1) is full
+    const uint4 w = sq[i0 >> 4];
+    const uint32_t words[4] = {w.x, w.y, w.z, w.w};
+    float lg[16], pm[16];
+    uint32_t fail = 0;
+#pragma unroll
+    for (int b = 0; b < 16; ++b) {
+      bool ok;
+      pm[b] = mx[b];
+      lg[b] = log_ff(pm[b], ok);
+      fail |= ok ? 0u : 1u << b;
+      // rows past L are computed from residue 0 and dropped
+      const bool live = i0 + b < L;
+      const int x = live ? (int) ((words[b >> 2] >> (8 * (b & 3))) & 0xff) : 0;
+      const float n0 = __fmul_rn(__fadd_rn(__fmul_rn(d0, t00), __fmul_rn(d1, B.t10)), s_eo[x][0]);
+      const float n1 = __fmul_rn(__fadd_rn(__fmul_rn(d0, t01), __fmul_rn(d1, B.t11)), s_eo[x][1]);
+      float m = 0.0f;
+      m = n0 > m ? n0 : m;
+      m = n1 > m ? n1 : m;
+      const float q0 = __fdiv_rn(n0, m), q1 = __fdiv_rn(n1, m);
+      d0 = live ? q0 : d0;
+      d1 = live ? q1 : d1;
+      mx[b] = live ? m : 1.0f;
+    }
+    if (fail) {
+#pragma unroll
+      for (int b = 0; b < 16; ++b)
+        if (fail >> b & 1u) lg[b] = log_row(pm[b], s_log);
+    }
+#pragma unroll
+    for (int b = 0; b < 16; ++b) logsc = __fadd_rn(logsc, lg[b]);
+  }
+  const int last = ((L - 1) >> 4) << 4;          // first row of the last batch
+#pragma unroll
+  for (int b = 0; b < 16; ++b)
+    if (last + b < L) logsc = __fadd_rn(logsc, log_rowf(mx[b], s_log));
   const float end = __fadd_rn(d0, d1);           // dp[L][0] * 1 + dp[L][1] * 1
   out[j] = __fadd_rn(logsc, log_rowf(end, s_log));
 }
