@@ -35,3 +35,13 @@ def test_golden_covers_overflow_and_the_dd_paths():
         st, _ = F.read_vresults(os.path.join(GOLDEN, "vit_" + name + ".vres"))
         n_erange += int((st == 16).sum())
     assert n_erange >= 5
+
+
+def test_crop_vprofile_keeps_the_nodes():
+    """A profile cut at its own length is the profile (the striping helper
+    the per-width GPU parity cases use)."""
+    from tests.vprofiles import crop_vprofile
+    for name in ("m777_s3", "m2400_s1", "m17_s2"):
+        vp = F.read_vprofile(os.path.join(GOLDEN, "vit_" + name + ".vprof"))
+        same = crop_vprofile(vp, vp.M)
+        assert np.array_equal(same.rwv, vp.rwv) and np.array_equal(same.twv, vp.twv)
