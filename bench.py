@@ -161,7 +161,9 @@ def cpu_baseline(p, s, budget_s=12.0, nthreads=0):
     dt = time.perf_counter() - t0
     return {"value": reps * sub.total * p.M / dt / 1e9, "unit": "GCUPS", "cores": used, "kind": "port",
             "sample": f"{sub.n} random sequences of the workload ({sub.total} residues, M={p.M}) x{reps}, {dt:.1f} s; "
-                      "vectorized port of the reference SSE2 p7_MSVFilter (NEON; SSV in register sweeps of diagonals as the reference), "
+                      f"vectorized port of the reference SSE2 p7_MSVFilter "
+                      f"({'NEON' if os.uname().machine == 'aarch64' else 'GCC vector extensions'}; "
+                      "SSV in register sweeps of diagonals as the reference), "
                       "bit-exact with its golden vectors",
             "seconds": dt}
 
