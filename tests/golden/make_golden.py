@@ -148,10 +148,24 @@ def make_vit(tut):
     for name, idx in TUT_MODELS:
         run("vitfile", os.path.join(tut, "minifam"), idx, os.path.join(HERE, "vit_" + name + ".vprof"),
             os.path.join(HERE, "vit_" + name + ".vres"), os.path.join(HERE, name + ".seqs"))
-    # models for the GPU kernel's other row forms: M=1100 (40 nodes per lane, two per
-    # register) and M=4000 (the shared-memory row); background, homologs, saturation repeats
+    make_vit_widths()
+    print("vit goldens:", len(VIT_SAMPLED) + len(TUT_MODELS) + len(VIT_WIDTHS))
+
+
+# models for the GPU kernel's row forms: M=1100 (40 nodes per lane, two per
+# register), M=4000 (the shared-memory row), and the widest model of several
+# register-row widths (5, 9, 13, 20, 28 nodes per lane); each over background
+# sequences, homologs and saturation repeats
+VIT_WIDTHS = [("vitmid_m1100_s4", 1100, 4), ("vitwide_m4000_s7", 4000, 7), ("vitw5_m157_s5", 157, 5),
+              ("vitw9_m285_s9", 285, 9), ("vitw13_m413_s13", 413, 13), ("vitw20_m637_s20", 637, 20),
+              ("vitw28_m893_s28", 893, 28)]
+
+
+def make_vit_widths(only=None):
     tmp = os.path.join(HERE, "_tmp.seqs")
-    for name, M, seed in (("vitmid_m1100_s4", 1100, 4), ("vitwide_m4000_s7", 4000, 7)):
+    for name, M, seed in VIT_WIDTHS:
+        if only is not None and name not in only:
+            continue
         parts = [F.synth_sequences(24, seed=M + 1, lmax=3000)]
         run("emit", M, seed, 100, MODE_LOCAL, 6, M + 2, 1, tmp)
         parts.append(F.read_seqs(tmp))
@@ -160,8 +174,8 @@ def make_vit(tut):
         F.write_seqs(F.SeqSet.concat(parts), os.path.join(HERE, name + ".seqs"))
         run("vit", M, seed, os.path.join(HERE, "vit_" + name + ".vprof"), os.path.join(HERE, "vit_" + name + ".vres"),
             os.path.join(HERE, name + ".seqs"))
-    os.remove(tmp)
-    print("vit goldens:", len(VIT_SAMPLED) + len(TUT_MODELS) + 2)
+    if os.path.exists(tmp):
+        os.remove(tmp)
 
 
 # pipeline goldens: sampled models in hmmsearch's local mode, and the tutorial models
