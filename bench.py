@@ -16,8 +16,20 @@ the database by the profile. GCUPS = M * residues / seconds.
           vectorized port of its SSE2 code (oracle/msv_port.c, NEON), since
           the reference's own SSE2 build cannot run on the aarch64 host.
 
+The default line also carries, measured after the timed region:
+  parity  : the timed outputs against the oracle on 50,000 random sequences
+          of the timed database (status, xJ, float score bits, pass flag);
+  batched : 256 profiles (M~U[50,1500]) vs 1,000,000 sequences in one
+          persistent launch (CUDA graph) next to 256 single-query launches,
+          with the batched-over-plain ratio and an oracle sample;
+  serving : Poisson query streams at 50 and 500 queries/s on the resident
+          database, with p50/p99 latency and offered vs achieved load.
+
 The database (~770 MB) is larger than L2 (129 MB), so no flush is needed.
-For N>1 (torchrun), every rank searches its own database (weak scaling).
+For N>1 (torchrun), the database is the concatenation of one block per rank
+(each rank's block is its residue-balanced shard, generated by that rank);
+every rank searches its shard (weak scaling: per-GPU work fixed) and the
+per-sequence results are gathered once with a tensor all_gather.
 """
 from __future__ import annotations
 
@@ -89,6 +101,22 @@ def workload(name, rank=0, args=None):
                "l2_flush": "inputs larger than L2 (129 MB)" if s.total > 129e6 else "none (inputs fit in L2)"}
         return p, s, cfg
     raise SystemExit(f"unknown workload {name}")
+
+
+def measure_peak(name, device):
+    """One of the probe library's peaks (include/msvgb_probe.h), measured now
+    on this GPU: msvgb_measure_int_peak (32-bit integer ops/s) or
+    msvgb_measure_smem_peak (shared-memory bytes/s)."""
+    import ctypes
+    L = ctypes.CDLL(os.path.join(ROOT, "cudahmmsearch_gb300", "libmsvgb_probe.so"))
+    fn = getattr(L, name)
+    fn.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    fn.restype = ctypes.c_int
+    L.msvgb_probe_last_error.restype = ctypes.c_char_p
+    v = ctypes.c_double()
+    if fn(device, ctypes.byref(v)) != 0:
+        raise RuntimeError(L.msvgb_probe_last_error().decode())
+    return v.value
 
 
 class ClockSampler:
@@ -187,11 +215,44 @@ def run_reference(args):
     print(json.dumps(line))
 
 
-def run_batch(args, api, torch, ctx, stream, local):
+ORACLE_NOTE = ("oracle/msv_oracle.c: scalar C restatement of p7_MSVFilter (SSV decision, full MSV) and the "
+               "p7_Pipeline F1 gate, pinned bit-exact to the reference's golden vectors")
+
+
+def oracle_parity(api, p, s, xj, fl, n_check=50_000, seed=11):
+    """Compares a GPU search's outputs (xj, flags over the whole SeqSet s) with
+    the oracle on a random sample of s: the status (ERANGE or not), xJ where
+    the status is eslOK, the float score's bit pattern and the F1 pass flag.
+    Runs outside any timed region, on all host cores."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(seed)
+    idx = np.sort(rng.choice(s.n, size=min(n_check, s.n), replace=False))
+    sub = s.subset(idx)
+    t = time.perf_counter()
+    o = O.msv_batch(p, sub)
+    o_s = time.perf_counter() - t
+    gx, gf = xj[idx], fl[idx]
+    nonempty = sub.lengths > 0
+    ok = o["status"] == 0
+    mism = np.zeros(idx.size, bool)
+    mism |= ((gf & api.FLAG_ERANGE) != 0) != (o["status"] == 16)
+    mism[ok] |= gx[ok] != o["xj"][ok]
+    mism[nonempty] |= ((gf & api.FLAG_PASS) != 0)[nonempty] != (o["pass"][nonempty] == 1)
+    mism[~nonempty] |= (gf[~nonempty] & api.FLAG_EMPTY) == 0
+    sc = api.scores(p, sub.lengths, gx, gf)
+    mism[nonempty] |= sc.view(np.uint32)[nonempty] != o["sc"].view(np.uint32)[nonempty]
+    return {"checked": int(idx.size), "mismatches": int(mism.sum()),
+            "erange": int((o["status"] == 16).sum()), "passed": int((o["pass"] == 1).sum()),
+            "compared": "status, xJ, float score bits, F1 pass flag", "oracle": ORACLE_NOTE,
+            "oracle_s": round(o_s, 2)}
+
+
+def batch_record(args, api, torch, ctx, stream, local, steps, warmup):
     """256 profiles (p7_hmm_Sample seeds 1..256, M uniform in [50, 1500],
     calibrated on the GPU) against 1,000,000 sequences in one persistent
     launch (a replayed CUDA graph), next to 256 back-to-back single-query
-    launches on the same GPU."""
+    launches on the same GPU (the reference's one-launch-per-query pattern).
+    Returns (record, clock summary, launches, per-step ms)."""
     rng = np.random.default_rng(4)
     n_prof = args.nprof
     Ms = rng.integers(50, 1501, size=n_prof)
@@ -208,13 +269,13 @@ def run_batch(args, api, torch, ctx, stream, local):
     out = torch.empty(2 * n_prof * s.n, dtype=torch.uint8, device="cuda")
     d_xj, d_fl = out.data_ptr(), out.data_ptr() + n_prof * s.n
     batch = api.Batch(ctx, profs, db, d_xj, d_fl)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         batch.run()
     torch.cuda.synchronize()
     launches0 = api.kernel_launches()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     with ClockSampler(local) as clk:
-        for i in range(args.steps):
+        for i in range(steps):
             ev[i][0].record(stream)
             batch.run()
             ev[i][1].record(stream)
@@ -222,7 +283,7 @@ def run_batch(args, api, torch, ctx, stream, local):
     launches = api.kernel_launches() - launches0
     per = [a.elapsed_time(b) for a, b in ev]
     total_ms = float(sum(per))
-    value = cells * args.steps / (total_ms * 1e-3) / 1e9
+    value = cells * steps / (total_ms * 1e-3) / 1e9
     batched = out.cpu().numpy().copy()
     # the plain path: one single-query launch per profile, back to back
     dprofs = [api.DeviceProfile(ctx, p) for p in profs]
@@ -232,7 +293,6 @@ def run_batch(args, api, torch, ctx, stream, local):
     torch.cuda.synchronize()
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     a.record(stream)
-    mismatches = 0
     for i, dp in enumerate(dprofs):
         api.search_device(ctx, dp, db, plain.data_ptr(), plain.data_ptr() + s.n)
     b.record(stream)
@@ -240,26 +300,55 @@ def run_batch(args, api, torch, ctx, stream, local):
     plain_ms = a.elapsed_time(b)
     plain_value = cells / (plain_ms * 1e-3) / 1e9
     # identical per-pair xJ and flags (checked on a sample of profiles)
+    mismatches, checked = 0, []
     for i in range(0, n_prof, max(1, n_prof // 16)):
         api.search_device(ctx, dprofs[i], db, plain.data_ptr(), plain.data_ptr() + s.n)
         torch.cuda.synchronize()
         pl = plain.cpu().numpy()
         mismatches += int((pl[:s.n] != batched[i * s.n:(i + 1) * s.n]).sum())
         mismatches += int((pl[s.n:] != batched[(n_prof + i) * s.n:(n_prof + i + 1) * s.n]).sum())
-    clocks = clk.summary()
-    peak_tops = api.measure_int_peak(local) / 1e12
+        checked.append(i)
+    # the oracle on a sample of (profile, sequence) pairs: four profiles
+    # spread over the model lengths, 2,000 random sequences each
+    order = np.argsort(Ms)
+    par = {"checked": 0, "mismatches": 0, "oracle": ORACLE_NOTE, "profiles_M": []}
+    for j, pi in enumerate(order[np.linspace(0, n_prof - 1, 4).astype(int)]):
+        r = oracle_parity(api, profs[pi], s, batched[pi * s.n:(pi + 1) * s.n],
+                          batched[(n_prof + pi) * s.n:(n_prof + pi + 1) * s.n], n_check=2000, seed=100 + j)
+        par["checked"] += r["checked"]
+        par["mismatches"] += r["mismatches"]
+        par["profiles_M"].append(int(Ms[pi]))
+    del out, plain
+    db.close()
+    rec = {"workload": f"batched MSV: {n_prof} profiles (p7_hmm_Sample seeds 1..{n_prof}, M~U[50,1500], "
+                       f"GPU-calibrated) vs {s.n} seqs (lognormal median 300, 1% homologs), one persistent "
+                       "launch replayed as a CUDA graph",
+           "value": value, "unit": "GCUPS", "steps": steps, "warmup": warmup, "ms_per_step": total_ms / steps,
+           "n_profiles": n_prof, "n_seqs": s.n, "residues": s.total, "sum_M": int(sum(p.M for p in profs)),
+           "work_items": batch.items, "profile_prep_s": round(prep_s, 2),
+           "plain": {"value": plain_value, "unit": "GCUPS", "ms": plain_ms,
+                     "what": f"{n_prof} back-to-back msvgb_search_device launches, one per profile"},
+           "batched_over_plain": value / plain_value,
+           "mismatches_vs_plain": mismatches, "profiles_checked_vs_plain": len(checked),
+           "parity": par}
+    batch.close()
+    return rec, clk.summary(), launches, per
+
+
+def run_batch(args, api, torch, ctx, stream, local):
+    rec, clocks, launches, per = batch_record(args, api, torch, ctx, stream, local, args.steps, args.warmup)
+    peak_tops = measure_peak("msvgb_measure_int_peak", local) / 1e12
+    cells = float(rec["sum_M"]) * float(rec["residues"])
     achieved = cells / (np.mean(per) * 1e-3) / 1e12
-    line = {"metric": "MSV GCUPS", "value": value, "unit": "GCUPS", "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+    line = {"metric": "MSV GCUPS", "value": rec["value"], "unit": "GCUPS", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": rec["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-            "config": {"workload": f"batched MSV: {n_prof} profiles (p7_hmm_Sample seeds 1..{n_prof}, M~U[50,1500], "
-                                   f"GPU-calibrated) vs {s.n} seqs (lognormal median 300, 1% homologs), one persistent "
-                                   "launch replayed as a CUDA graph", "n_profiles": n_prof, "n_seqs": s.n,
-                       "residues": s.total, "sum_M": int(sum(p.M for p in profs)), "work_items": batch.items,
-                       "profile_prep_s": prep_s},
-            "plain_256_launches": {"value": plain_value, "unit": "GCUPS", "ms": plain_ms},
-            "batched_over_plain": value / plain_value, "mismatches_vs_plain": mismatches,
-            "gpu_launches": int(launches), "clocks": clocks,
+            "config": {"workload": rec["workload"], "n_profiles": rec["n_profiles"], "n_seqs": rec["n_seqs"],
+                       "residues": rec["residues"], "sum_M": rec["sum_M"], "work_items": rec["work_items"],
+                       "profile_prep_s": rec["profile_prep_s"]},
+            "plain_256_launches": rec["plain"],
+            "batched_over_plain": rec["batched_over_plain"], "mismatches_vs_plain": rec["mismatches_vs_plain"],
+            "parity": rec["parity"], "gpu_launches": int(launches), "clocks": clocks,
             "roofline": {"bound": "int32-pipe", "achieved": achieved, "peak": peak_tops, "unit": "Tops/s",
                          "frac": achieved / peak_tops, "traffic": None,
                          "peak_note": "measured: msvgb_measure_int_peak"}}
@@ -348,17 +437,74 @@ def run_filters(args, api, torch, ctx, stream, local):
     print(json.dumps(line))
 
 
-def run_serve(args, api, torch, ctx, local):
-    """Serving: a resident database of 2,000,000 sequences receives query
-    profiles (p7_hmm_Sample with per-request seeds, M log-uniform in
-    [50, 2000], calibrated beforehand) as Poisson streams at several rates;
+def run_dropin(args, api, torch, ctx, local):
+    """Per-call latency of the drop-in msvgb_MSVFilter (one sequence per call,
+    as p7_Pipeline calls p7_MSVFilter, src/p7_pipeline.c:671) at L=300 for
+    M = 200, 400, 2400, beside the reference's per-call cost on one host core
+    (the vectorized port of its SSE2 filter) and the per-sequence cost of the
+    batched search of the same sequences from a resident database. Host wall
+    clock; the drop-in figure includes the ctypes call (its overhead alone,
+    measured on a host-only C ABI function, is reported)."""
+    import ctypes
+    from oracle import oracle as O
+    n = args.dropin_calls
+    L = 300
+    s = F.synth_sequences(n, seed=61, sigma=1e-9, lmin=L, lmax=L)
+    assert int(s.lengths.min()) == L == int(s.lengths.max())
+    f = api.lib().msvgb_tjb_b
+    t = time.perf_counter()
+    for _ in range(n):
+        f(ctypes.c_float(4.328), L)
+    ctypes_us = (time.perf_counter() - t) / n * 1e6
+    rows = []
+    for name in ("m200_s1", "m400_s1", "m2400_s1"):
+        p = F.read_profile(os.path.join(ROOT, "tests", "golden", name + ".prof"))
+        tjb = api.tjb_b(p.scale_b, L)
+        dsqs = [np.concatenate([[255], s.seq(i), [255]]).astype(np.uint8) for i in range(n)]
+        for i in range(min(50, n)):
+            ctx.MSVFilter(dsqs[i], L, p, tjb)
+        got = np.zeros(n, np.float32)
+        t = time.perf_counter()
+        for i in range(n):
+            got[i] = ctx.MSVFilter(dsqs[i], L, p, tjb)[1]
+        gpu_us = (time.perf_counter() - t) / n * 1e6
+        o = O.msv_batch(p, s)
+        mism = int((got.view(np.uint32) != o["sc"].view(np.uint32)).sum())
+        O.port_batch(p, s, nthreads=1)
+        t = time.perf_counter()
+        O.port_batch(p, s, nthreads=1)
+        cpu_us = (time.perf_counter() - t) / n * 1e6
+        dp, db = api.DeviceProfile(ctx, p), api.DeviceDB(ctx, s)
+        api.search(ctx, dp, db)
+        t = time.perf_counter()
+        api.search(ctx, dp, db)
+        batch_us = (time.perf_counter() - t) / n * 1e6
+        dp.close()
+        db.close()
+        rows.append({"M": p.M, "L": L, "dropin_us_per_call": gpu_us, "cpu_port_1core_us_per_call": cpu_us,
+                     "resident_search_us_per_seq": batch_us, "dropin_over_cpu": cpu_us / gpu_us,
+                     "score_mismatches_vs_oracle": mism})
+    line = {"metric": "drop-in p7_MSVFilter latency", "value": rows[1]["dropin_us_per_call"], "unit": "us/call",
+            "n_gpus": 1, "steps": n, "warmup": 50, "ms_per_step": rows[1]["dropin_us_per_call"] / 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            "config": {"workload": f"msvgb_MSVFilter one call per sequence, {n} sequences of L={L}, "
+                                   "M = 200, 400, 2400 (reference-sampled golden profiles)",
+                       "ctypes_call_us": ctypes_us},
+            "rows": rows}
+    print(json.dumps(line))
+
+
+def serve_record(args, api, ctx, s, db, loads):
+    """Serving: a resident database receives query profiles (p7_hmm_Sample
+    with per-request seeds, M log-uniform in [50, 2000], calibrated
+    beforehand) as Poisson streams at the given (rate q/s, window s) loads;
     admission is bounded by a device-memory budget. Latency = completion -
-    arrival (admission wait included)."""
+    arrival (admission wait included). The first two requests of every
+    window are also searched alone on the plain path afterwards: their
+    served results must be identical. Returns (windows, launches, prep s,
+    checks)."""
     import threading
     import concurrent.futures as cf
-    s = F.synth_sequences(args.nseq if args.nseq != 1_000_000 else 2_000_000, seed=8000, lmax=35000)
-    db = api.DeviceDB(ctx, s)
-    loads = [(float(r), float(t)) for r, t in (x.split(":") for x in args.loads.split(","))]
     rng = np.random.default_rng(9)
     n_req_total = sum(int(r * t * 1.5) + 8 for r, t in loads)
     Ms = np.exp(rng.uniform(np.log(50), np.log(2000), size=n_req_total)).astype(int)
@@ -368,25 +514,28 @@ def run_serve(args, api, torch, ctx, local):
     srv = api.Server(ctx, db, max_slots=args.slots, mem_budget=args.mem_budget)
     # warm-up: one query end to end
     srv.wait(srv.submit(profs[0]), want=False)
-    results = []
+    results, kept = [], {}
     used = 1
     for rate, dur in loads:
         arr = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * dur * 1.5) + 8))
         arr = arr[arr < dur]
         reqs = list(range(used, used + len(arr)))
         used += len(arr)
+        keep_ids = set(reqs[:2])
         lat, done_t, cells = [], [], []
         lock = threading.Lock()
         pool = cf.ThreadPoolExecutor(max_workers=max(8, args.slots))
         start = time.perf_counter()
 
         def finish(tk, a_time, pi):
-            srv.wait(tk, want=True)
+            xj, fl = srv.wait(tk, want=True)
             t = time.perf_counter() - start
             with lock:
                 lat.append(t - a_time)
                 done_t.append(t)
                 cells.append(float(profs[pi].M) * s.total)
+                if pi in keep_ids:
+                    kept[pi] = (xj, fl)
 
         futs = []
         for a_time, pi in zip(arr, reqs):
@@ -409,6 +558,21 @@ def run_serve(args, api, torch, ctx, local):
                         "latency_max_ms": float(np.max(lat) * 1e3) if lat else None})
     launches = srv.launches
     srv.close()
+    mism = 0
+    for pi, (xj, fl) in kept.items():                       # served in the mix == searched alone
+        dp = api.DeviceProfile(ctx, profs[pi])
+        xa, fa = api.search(ctx, dp, db)
+        mism += int((xa != xj).sum() + (fa != fl).sum())
+        dp.close()
+    checks = {"requests_checked": len(kept), "mismatches_vs_alone": mism}
+    return results, launches, prep_s, checks
+
+
+def run_serve(args, api, torch, ctx, local):
+    s = F.synth_sequences(args.nseq if args.nseq != 1_000_000 else 2_000_000, seed=8000, lmax=35000)
+    db = api.DeviceDB(ctx, s)
+    loads = [(float(r), float(t)) for r, t in (x.split(":") for x in args.loads.split(","))]
+    results, launches, prep_s, checks = serve_record(args, api, ctx, s, db, loads)
     best = max(r["achieved_gcups"] for r in results)
     line = {"metric": "MSV GCUPS (serving)", "value": best, "unit": "GCUPS", "n_gpus": 1, "steps": len(loads),
             "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
@@ -416,7 +580,7 @@ def run_serve(args, api, torch, ctx, local):
             "config": {"workload": f"serving: resident {s.n} seqs (lognormal median 300, {s.total} residues), "
                                    "Poisson query streams, M log-uniform [50,2000] (p7_hmm_Sample per-request seeds)",
                        "slots": args.slots, "mem_budget_bytes": args.mem_budget, "profile_prep_s": prep_s},
-            "serving": results, "gpu_launches": int(launches)}
+            "serving": results, "checks": checks, "gpu_launches": int(launches)}
     print(json.dumps(line))
 
 
@@ -437,6 +601,14 @@ def main():
     ap.add_argument("--loads", default="10:3,50:3,500:0.5", help="serve workload: rate:seconds,...")
     ap.add_argument("--slots", type=int, default=32, help="serve workload: max concurrent queries")
     ap.add_argument("--mem-budget", type=int, default=1 << 30, help="serve workload: device bytes for slots")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="default workload: skip the batched and serving sub-records")
+    ap.add_argument("--batch-steps", type=int, default=2, help="batched sub-record: timed replays")
+    ap.add_argument("--serve-loads", default="50:2,500:0.4",
+                    help="serving sub-record: rate:seconds,... on the default workload's database")
+    ap.add_argument("--dropin-calls", type=int, default=2000, help="dropin workload: calls per model")
+    ap.add_argument("--parity-seqs", type=int, default=50_000,
+                    help="default workload: random sequences of the timed database checked against the oracle")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -458,6 +630,8 @@ def main():
         return run_batch(args, api, torch, ctx, stream, local)
     if args.workload == "serve":
         return run_serve(args, api, torch, api.Context(local), local)
+    if args.workload == "dropin":
+        return run_dropin(args, api, torch, api.Context(local), local)
     if args.workload == "filters":
         ctx = api.Context(local)
         stream = torch.cuda.Stream()
@@ -512,9 +686,11 @@ def main():
     total_ms = float(t_max.item())
     value = cells * world * args.steps / (total_ms * 1e-3) / 1e9
 
-    # correctness spot-check of the timed outputs against the oracle (outside the timed region)
+    # the timed outputs (the last step's) against the oracle on 50,000 random
+    # sequences of the timed database (outside the timed region)
     xj_all = out[:s.n].cpu().numpy()
     fl_all = out[s.n:].cpu().numpy()
+    parity = oracle_parity(api, p, s, xj_all, fl_all, n_check=args.parity_seqs) if rank == 0 else None
 
     # e2e through the public API from pinned host buffers
     codes_pin = torch.from_numpy(s.codes).pin_memory()
@@ -548,7 +724,14 @@ def main():
     clocks = clk.summary()
     sm_mhz = clocks["sm_mhz"] or 2070.0
     nsm = torch.cuda.get_device_properties(local).multi_processor_count
-    peak_tops = api.measure_int_peak(local) / 1e12        # measured now, same GPU and clock regime
+    peak_tops = measure_peak("msvgb_measure_int_peak", local) / 1e12    # measured now, same GPU and clock regime
+    smem_peak = measure_peak("msvgb_measure_smem_peak", local) / 1e9
+    hbm_peak, hbm_note = 6800.0, "of fallback (6.8 TB/s: no measured peaks file)"
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            hbm_peak, hbm_note = float(json.load(f)["hbm_gbs"]), "of measured (MEASURED_PEAKS.json hbm_gbs)"
+    except (OSError, KeyError, ValueError):
+        pass
     kern_ms = float(np.mean(per))
     achieved_tops = cells / (kern_ms * 1e-3) / 1e12          # 1 cell = 1 packed int32 op (4 uint8 lane-ops)
     roofline = {"bound": "int32-pipe", "achieved": achieved_tops, "peak": peak_tops, "unit": "Tops/s",
@@ -560,14 +743,16 @@ def main():
                              f"nominal {nsm} SMs x {INT_LANE_OPS_PER_CLK_PER_SM} lane-ops/clk x {sm_mhz:.0f} MHz = "
                              f"{nsm * INT_LANE_OPS_PER_CLK_PER_SM * sm_mhz * 1e6 / 1e12:.1f} Tops/s",
                 "smem": {"achieved": SSV_TABLE_BYTES_PER_CELL * cells / (kern_ms * 1e-3) / 1e9,
-                         "peak": nsm * SMEM_BYTES_PER_CLK_PER_SM * sm_mhz * 1e6 / 1e9, "unit": "GB/s",
-                         "frac": SSV_TABLE_BYTES_PER_CELL * cells / (kern_ms * 1e-3)
-                                 / (nsm * SMEM_BYTES_PER_CLK_PER_SM * sm_mhz * 1e6),
-                         "peak_note": f"nominal: {nsm} SMs x 128 B/clk x {sm_mhz:.0f} MHz (median SM clock "
-                                      "under load); 2 B of f16 SSV cost per cell, the bound of the SSV pass"},
-                "hbm": {"achieved": (s.total + 2 * s.n) / (kern_ms * 1e-3) / 1e9, "peak": 6783.5,
-                        "unit": "GB/s", "frac": (s.total + 2 * s.n) / (kern_ms * 1e-3) / 1e9 / 6783.5,
-                        "peak_note": "of measured (MEASURED_PEAKS.json hbm_gbs)"}}
+                         "peak": smem_peak, "unit": "GB/s",
+                         "frac": SSV_TABLE_BYTES_PER_CELL * cells / (kern_ms * 1e-3) / 1e9 / smem_peak,
+                         "nominal": nsm * SMEM_BYTES_PER_CLK_PER_SM * sm_mhz * 1e6 / 1e9,
+                         "peak_note": "measured: msvgb_measure_smem_peak (conflict-free 16-byte loads over "
+                                      f"{nsm} SMs); nominal {nsm} SMs x 128 B/clk x {sm_mhz:.0f} MHz. "
+                                      f"{SSV_TABLE_BYTES_PER_CELL} B of f16 SSV cost per cell: the binding "
+                                      "bound of the SSV pass"},
+                "hbm": {"achieved": (s.total + 2 * s.n) / (kern_ms * 1e-3) / 1e9, "peak": hbm_peak,
+                        "unit": "GB/s", "frac": (s.total + 2 * s.n) / (kern_ms * 1e-3) / 1e9 / hbm_peak,
+                        "peak_note": hbm_note}}
     fullfrac = float(((fl_all & api.FLAG_FULL) != 0).mean())
     line = {"metric": "MSV GCUPS", "value": value, "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -580,7 +765,29 @@ def main():
                             "src/len metadata uploaded and packed in chunks on a second stream under the search",
                     "separate_calls": e2e_parts[-1] if e2e_parts else None,
                     "steps_ms": [round(t * 1e3, 2) for t in e2e_times], "statistic": "median of the timed steps"},
-            "gpu_launches": int(launches), "clocks": clocks, "roofline": roofline}
+            "gpu_launches": int(launches), "clocks": clocks, "roofline": roofline, "parity": parity}
+    if world > 1:
+        # the one exchange of the sharded search: every rank's per-sequence
+        # bytes, concatenated in rank (= database) order on every rank
+        from cudahmmsearch_gb300 import shard as S
+        t = time.perf_counter()
+        gx, gf = S.gather_results(xj_all, fl_all, device=torch.device("cuda", local))
+        line["gather"] = {"seqs": int(gx.size), "ms": (time.perf_counter() - t) * 1e3,
+                          "how": "torch.distributed all_gather of fixed-size uint8 tensors (NCCL)"}
+    if rank == 0 and world == 1 and not args.no_extras:
+        # the metric's other halves: batched vs plain, and serving latency
+        del out
+        torch.cuda.empty_cache()
+        bsteps, bwarm = args.batch_steps, max(3, min(args.warmup, 3))
+        brec, bclk, _, _ = batch_record(args, api, torch, ctx, stream, local, bsteps, bwarm)
+        brec["clocks"] = bclk
+        line["batched"] = brec
+        loads = [(float(r), float(t)) for r, t in (x.split(":") for x in args.serve_loads.split(","))]
+        sres, slaunch, sprep, schecks = serve_record(args, api, ctx, s, db, loads)
+        line["serving"] = {"workload": f"serving: the resident {s.n:,}-sequence database above, Poisson query "
+                                       "streams, M log-uniform [50,2000] (p7_hmm_Sample per-request seeds)",
+                           "windows": sres, "slots": args.slots, "mem_budget_bytes": args.mem_budget,
+                           "profile_prep_s": round(sprep, 2), "kernel_launches": int(slaunch), **schecks}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(p, s)
     if rank == 0:

@@ -29,7 +29,7 @@ EXPORTS = [
     "msvgb_profile_M", "msvgb_profile_create_ex", "msvgb_profile_variant", "msvgb_profile_set_lanes",
     "msvgb_profile_lanes", "msvgb_db_create", "msvgb_db_destroy", "msvgb_db_nseq", "msvgb_db_residues",
     "msvgb_search", "msvgb_search_device", "msvgb_tjb_b", "msvgb_score", "msvgb_f1_pass",
-    "msvgb_search_static", "msvgb_measure_int_peak", "msvgb_sample_om", "msvgb_calibrate",
+    "msvgb_search_static", "msvgb_sample_om", "msvgb_calibrate",
     "msvgb_batch_create", "msvgb_batch_run", "msvgb_batch_items", "msvgb_batch_destroy", "msvgb_search_batch",
     "msvgb_server_create", "msvgb_server_slots", "msvgb_server_submit", "msvgb_server_wait",
     "msvgb_server_launches", "msvgb_server_destroy", "msvgb_pipeline_run",
@@ -152,7 +152,6 @@ def lib():
         "msvgb_score": (f32, [u8, u8, i32, u8, f32]),
         "msvgb_f1_pass": (i32, [f32, i32, f32, f32, f64, ctypes.POINTER(f64)]),
         "msvgb_search_static": (i32, [vp, vp, f64, vp, vp, vp]),
-        "msvgb_measure_int_peak": (i32, [i32, ctypes.POINTER(f64)]),
         "msvgb_sample_om": (i32, [ctypes.c_uint32, i32, vp, ctypes.POINTER(_Om), ctypes.POINTER(f64)]),
         "msvgb_calibrate": (i32, [vp, ctypes.POINTER(_Om), f64]),
         "msvgb_batch_create": (i32, [vp, vp, i32, vp, f64, vp, vp, ctypes.POINTER(vp)]),
@@ -532,13 +531,6 @@ def sample_profile(M: int, seed: int, ctx: "Context | None" = None) -> F.Profile
     return F.Profile(M=M, rbv=rbv, tbm_b=om.tbm_b, tec_b=om.tec_b, base_b=om.base_b, bias_b=om.bias_b,
                      scale_b=float(np.float32(om.scale_b)), mmu=float(np.float32(om.mmu)),
                      mlambda=float(np.float32(om.mlambda)))
-
-
-def measure_int_peak(device: int = 0) -> float:
-    """Sustained 32-bit integer ops/s over all SMs (integer-pipe roofline denominator)."""
-    v = ctypes.c_double()
-    _check(lib().msvgb_measure_int_peak(device, ctypes.byref(v)))
-    return v.value
 
 
 def _om_array(profiles):

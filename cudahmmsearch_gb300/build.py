@@ -16,10 +16,14 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmsvgb.so")
+# the benchmark's peak probes: a library of their own (include/msvgb_probe.h)
+PROBE_SRC = "msv_probe.cu"
+PROBE_LIB = os.path.join(HERE, "libmsvgb_probe.so")
 
-SOURCES = ["msv_batch.cu", "msv_serve.cu", "inst_g16.cu", "inst_g8.cu", "msv_api.cu", "msv_tune.cu", "msv_io.cu", "msv_vit.cu", "msv_noalloc.cu", "msv_probe.cu", "msv_pack.cu", "msv_sample.cu", "msv_pipeline.cu", "msv_bias.cu", "inst_a.cu", "inst_b.cu", "inst_c.cu", "inst_d.cu",
+SOURCES = ["msv_batch.cu", "msv_serve.cu", "inst_g16.cu", "inst_g8.cu", "msv_api.cu", "msv_tune.cu", "msv_io.cu", "msv_vit.cu", "msv_noalloc.cu", "msv_pack.cu", "msv_sample.cu", "msv_pipeline.cu", "msv_bias.cu", "inst_a.cu", "inst_b.cu", "inst_c.cu", "inst_d.cu",
            "inst_e.cu", "inst_f.cu", "inst_h.cu", "inst_i.cu"]
-HEADERS = ["msv_device.cuh", "msv_kernel_impl.cuh", "msv_internal.h", "msv_multi.cuh", "msv_group.cuh", os.path.join("..", "..", "include", "msvgb.h")]
+HEADERS = ["msv_device.cuh", "msv_kernel_impl.cuh", "msv_internal.h", "msv_multi.cuh", "msv_group.cuh",
+           os.path.join("..", "..", "include", "msvgb.h"), os.path.join("..", "..", "include", "msvgb_probe.h")]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
@@ -44,7 +48,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     hdrs = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.abspath(__file__)]
     jobs = []
-    for s in SOURCES:
+    for s in SOURCES + [PROBE_SRC]:
         src = os.path.join(CSRC, s)
         obj = os.path.join(BUILD, s.replace(".cu", ".o"))
         if force or _stale(obj, [src] + hdrs):
@@ -59,12 +63,14 @@ def build(force: bool = False, verbose: bool = False) -> str:
                 if r.returncode != 0:
                     raise RuntimeError(f"nvcc failed: {' '.join(j)}")
     objs = [os.path.join(BUILD, s.replace(".cu", ".o")) for s in SOURCES]
-    if force or jobs or _stale(LIB, objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            sys.stderr.write(r.stdout + r.stderr)
-            raise RuntimeError("link failed")
+    probe_obj = [os.path.join(BUILD, PROBE_SRC.replace(".cu", ".o"))]
+    for lib, o in ((LIB, objs), (PROBE_LIB, probe_obj)):
+        if force or jobs or _stale(lib, o):
+            cmd = [nvcc()] + ARCH + ["-shared", "-o", lib] + o
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                sys.stderr.write(r.stdout + r.stderr)
+                raise RuntimeError("link failed")
     return LIB
 
 

@@ -172,7 +172,6 @@ extern "C" int msvgb_ctx_create(int device, msvgb_ctx **ret_ctx) {
   cudaError_t e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMalloc(&c->d_ticket, sizeof(unsigned long long));
-  if (e == cudaSuccess) e = cudaMalloc(&c->d_meta, 4 * sizeof(int64_t));
   if (e == cudaSuccess) e = cudaMalloc(&c->d_out, 64);
   if (e == cudaSuccess) e = cudaMalloc(&c->d_bad, sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc(&c->d_aux, 4 * sizeof(unsigned long long));
@@ -186,6 +185,12 @@ extern "C" int msvgb_ctx_create(int device, msvgb_ctx **ret_ctx) {
     return fail(MSVGB_eslESYS, std::string("context setup: ") + cudaGetErrorString(e));
   }
   c->stream = c->own;
+  // MSVGB_TEST_HASH_BITS=b keeps only b bits of the drop-in cache's content
+  // hash, so tests can make different profiles collide on purpose.
+  if (const char *hb = getenv("MSVGB_TEST_HASH_BITS")) {
+    const int b = atoi(hb);
+    c->hash_mask = b <= 0 ? 0ull : b >= 64 ? ~0ull : ((1ull << b) - 1ull);
+  }
   *ret_ctx = c;
   return MSVGB_eslOK;
 }
@@ -193,11 +198,11 @@ extern "C" int msvgb_ctx_create(int device, msvgb_ctx **ret_ctx) {
 extern "C" int msvgb_ctx_destroy(msvgb_ctx *c) {
   if (!c) return MSVGB_eslOK;
   cudaSetDevice(c->device);
-  for (auto &kv : c->cache) msvgb_profile_destroy(kv.second);
-  c->cache.clear();
+  for (auto &e : c->dropin) msvgb_profile_destroy(e.p);
+  c->dropin.clear();
   if (c->own) cudaStreamSynchronize(c->own);
-  cudaFree(c->d_ticket); cudaFree(c->d_meta); cudaFree(c->d_out);
-  cudaFree(c->d_seq); cudaFree(c->d_tab); cudaFree(c->d_bad); cudaFree(c->d_aux); cudaFree(c->d_list);
+  cudaFree(c->d_ticket); cudaFree(c->d_out);
+  cudaFree(c->d_one); cudaFree(c->d_bad); cudaFree(c->d_aux); cudaFree(c->d_list);
   if (c->own) cudaStreamDestroy(c->own);
   if (c->side) { cudaStreamSynchronize(c->side); cudaStreamDestroy(c->side); }
   if (c->upload) { cudaStreamSynchronize(c->upload); cudaStreamDestroy(c->upload); }
@@ -206,6 +211,7 @@ extern "C" int msvgb_ctx_destroy(msvgb_ctx *c) {
   if (c->ev_join) cudaEventDestroy(c->ev_join);
   msvgb_detail::tune_free(c);
   if (c->h_pin) cudaFreeHost(c->h_pin);
+  if (c->h_one) cudaFreeHost(c->h_one);
   delete c;
   return MSVGB_eslOK;
 }
@@ -903,28 +909,81 @@ static uint64_t fnv1a(const void *data, size_t n, uint64_t h) {
   return h;
 }
 
-static uint64_t om_key(const msvgb_om *om) {
+// The bytes a drop-in profile's device tables are built from: the scalar MSV
+// fields (tjb_b excluded: the caller rewrites it per target length) and the
+// rbv vectors.
+static void om_image(const msvgb_om *om, std::vector<uint8_t> &img) {
   const int Q = std::max(2, (om->M - 1) / 16 + 1);
-  uint64_t h = 1469598103934665603ull;
-  h = fnv1a(&om->M, sizeof(int), h);
-  h = fnv1a(&om->tbm_b, 1, h); h = fnv1a(&om->tec_b, 1, h);
-  h = fnv1a(&om->base_b, 1, h); h = fnv1a(&om->bias_b, 1, h);
-  h = fnv1a(&om->scale_b, sizeof(float), h);
-  return fnv1a(om->rbv, (size_t) om->Kp * Q * 16, h);
+  const size_t nrbv = (size_t) om->Kp * Q * 16;
+  img.resize(16 + nrbv);
+  uint8_t *b = img.data();
+  memcpy(b, &om->M, 4);
+  memcpy(b + 4, &om->Kp, 4);
+  b[8] = om->tbm_b; b[9] = om->tec_b; b[10] = om->base_b; b[11] = om->bias_b;
+  memcpy(b + 12, &om->scale_b, 4);
+  memcpy(b + 16, om->rbv, nrbv);
 }
 
-static int ensure_cap(uint8_t **ptr, size_t *cap, size_t need) {
-  if (*cap >= need) return MSVGB_eslOK;
-  cudaFree(*ptr); *ptr = nullptr; *cap = 0;
-  size_t n = std::max<size_t>(need, 4096);
-  CUDA_TRY(cudaMalloc(ptr, n));
-  *cap = n;
+// Whether om's bytes equal a cached image (no copy: header then rbv).
+static bool om_equals(const msvgb_om *om, const std::vector<uint8_t> &img) {
+  const int Q = std::max(2, (om->M - 1) / 16 + 1);
+  const size_t nrbv = (size_t) om->Kp * Q * 16;
+  if (img.size() != 16 + nrbv) return false;
+  uint8_t h[16];
+  memcpy(h, &om->M, 4);
+  memcpy(h + 4, &om->Kp, 4);
+  h[8] = om->tbm_b; h[9] = om->tec_b; h[10] = om->base_b; h[11] = om->bias_b;
+  memcpy(h + 12, &om->scale_b, 4);
+  return memcmp(h, img.data(), 16) == 0 && memcmp(om->rbv, img.data() + 16, nrbv) == 0;
+}
+
+// The cached profile for om, or a new one. A cache entry is found by the
+// caller's rbv pointer and M first (the usual case: the same P7_OPROFILE, or
+// clones sharing its vectors), else by content hash; either way its bytes are
+// compared with om's before it is used, so neither a reused pointer nor a hash
+// collision can score om with another profile's tables.
+static int dropin_profile(msvgb_ctx *c, const msvgb_om *om, msvgb_profile **ret) {
+  DropinEntry *hit = nullptr;
+  for (auto &e : c->dropin)
+    if (e.rbv_ptr == om->rbv && e.M == om->M && om_equals(om, e.image)) { hit = &e; break; }
+  if (!hit) {
+    const int Q = std::max(2, (om->M - 1) / 16 + 1);
+    uint64_t h = 1469598103934665603ull;
+    const uint8_t hdr[5] = {om->tbm_b, om->tec_b, om->base_b, om->bias_b, (uint8_t) om->Kp};
+    h = fnv1a(&om->M, sizeof(int), h);
+    h = fnv1a(hdr, sizeof(hdr), h);
+    h = fnv1a(&om->scale_b, sizeof(float), h);
+    h = fnv1a(om->rbv, (size_t) om->Kp * Q * 16, h) & c->hash_mask;
+    for (auto &e : c->dropin)
+      if (e.hash == h && om_equals(om, e.image)) { hit = &e; break; }
+    if (hit) {
+      hit->rbv_ptr = om->rbv;                                  // the fast path finds it next time
+    } else {
+      msvgb_profile *p = nullptr;
+      const int st = profile_build(c, om, default_f16(), &p);
+      if (st != MSVGB_eslOK) return st;
+      if (c->dropin.size() >= 64) {                            // evict the least recently used
+        auto lru = std::min_element(c->dropin.begin(), c->dropin.end(),
+                                    [](const DropinEntry &a, const DropinEntry &b) { return a.last_use < b.last_use; });
+        msvgb_profile_destroy(lru->p);
+        c->dropin.erase(lru);
+      }
+      DropinEntry e;
+      e.rbv_ptr = om->rbv; e.M = om->M; e.hash = h; e.p = p;
+      om_image(om, e.image);
+      c->dropin.push_back(std::move(e));
+      hit = &c->dropin.back();
+    }
+  }
+  hit->last_use = ++c->dropin_clock;
+  *ret = hit->p;
   return MSVGB_eslOK;
 }
 
 extern "C" int msvgb_MSVFilter(msvgb_ctx *c, const uint8_t *dsq, int L, const msvgb_om *om, msvgb_omx *ox,
                                float *ret_sc) {
   if (!c || !dsq || !om || !ox || !ret_sc) return fail(MSVGB_eslEINVAL, "NULL argument");
+  if (om->M < 1 || !om->rbv) return fail(MSVGB_eslEINVAL, "bad profile");
   const int Q = std::max(2, (om->M - 1) / 16 + 1);
   if (Q > ox->allocQ16) return fail(MSVGB_eslEINVAL, "DP matrix allocated too small");   // msvfilter.c:103
   ox->M = om->M;
@@ -933,38 +992,52 @@ extern "C" int msvgb_MSVFilter(msvgb_ctx *c, const uint8_t *dsq, int L, const ms
     if (dsq[i] >= 29) return fail(MSVGB_eslEINVAL, "residue code >= 29 (Kp)");
   std::lock_guard<std::mutex> lock(c->mu);
   CUDA_TRY(cudaSetDevice(c->device));
-  const uint64_t key = om_key(om);
   msvgb_profile *p = nullptr;
-  auto it = c->cache.find(key);
-  if (it != c->cache.end()) p = it->second;
-  else {
-    int st = profile_build(c, om, default_f16(), &p);
-    if (st != MSVGB_eslOK) return st;
-    if (c->cache.size() >= 64) { msvgb_profile_destroy(c->cache.begin()->second); c->cache.erase(c->cache.begin()); }
-    c->cache[key] = p;
-  }
-  // residues padded to 16 bytes with the pad code; the tjb table holds the
-  // caller's om->tjb_b at index L (the reference reads om->tjb_b as set).
+  int st = dropin_profile(c, om, &p);
+  if (st != MSVGB_eslOK) return st;
+  // One block, staged in pinned memory and uploaded in one copy:
+  // [0, 64) ticket (zero) and the one-sequence database arrays (start = 0,
+  // orig = 0, len); [64, 64 + T) the tjb table (the caller's om->tjb_b at
+  // index L, the reference reads om->tjb_b as set) then the xjmin table (255:
+  // the pass flag is unused here); then the residues padded to 16 bytes with
+  // the pad code.
+  const size_t T = ((2 * ((size_t) L + 1)) + 15) / 16 * 16;
   const size_t padded = ((size_t) L + 15) / 16 * 16 + 64;
-  int st = ensure_cap(&c->d_seq, &c->d_seq_cap, padded);
-  if (st != MSVGB_eslOK) return st;
-  st = ensure_cap(&c->d_tab, &c->d_tab_cap, 2 * ((size_t) L + 1));
-  if (st != MSVGB_eslOK) return st;
-  std::vector<uint8_t> h(padded, (uint8_t) PAD_CODE);
-  if (L) memcpy(h.data(), dsq + 1, (size_t) L);
-  std::vector<uint8_t> tab(2 * ((size_t) L + 1), 0);
-  tab[L] = om->tjb_b;                                  // tjb table
-  tab[(size_t) L + 1 + L] = 255;                       // xjmin: pass flag unused here
-  int64_t meta[4] = {0, 0, 0, 0};                      // start = 0, orig = 0, len (int32) in meta[2]
-  int32_t len32 = L;
-  memcpy(&meta[2], &len32, 4);
-  CUDA_TRY(cudaMemcpyAsync(c->d_seq, h.data(), padded, cudaMemcpyHostToDevice, c->stream));
-  CUDA_TRY(cudaMemcpyAsync(c->d_tab, tab.data(), tab.size(), cudaMemcpyHostToDevice, c->stream));
-  CUDA_TRY(cudaMemcpyAsync(c->d_meta, meta, sizeof(meta), cudaMemcpyHostToDevice, c->stream));
-  DbDev dbv{c->d_seq, c->d_meta, (const int32_t *) (c->d_meta + 2), c->d_meta + 1, 1};
-  st = launch_one(c, p, dbv, c->d_tab, c->d_tab + L + 1, c->d_out, c->d_out + 1, 0);
-  if (st != MSVGB_eslOK) return st;
-  uint8_t res[2];
+  const size_t bytes = 64 + T + padded;
+  if (c->h_one_cap < bytes || c->d_one_cap < bytes) {
+    CUDA_TRY(cudaStreamSynchronize(c->stream));               // nothing still reads the old blocks
+    const size_t cap = std::max<size_t>(bytes, 16384);
+    if (c->h_one) cudaFreeHost(c->h_one);
+    cudaFree(c->d_one);
+    c->h_one = nullptr; c->d_one = nullptr; c->h_one_cap = c->d_one_cap = 0;
+    CUDA_TRY(cudaMallocHost((void **) &c->h_one, cap));
+    c->h_one_cap = cap;
+    CUDA_TRY(cudaMalloc((void **) &c->d_one, cap));
+    c->d_one_cap = cap;
+  }
+  uint8_t *h = c->h_one;
+  memset(h, 0, 64);
+  const int32_t len32 = L;
+  memcpy(h + 32, &len32, 4);                                  // [8,16) start = 0, [16,24) orig = 0, [32,36) len
+  memset(h + 64, 0, T);
+  h[64 + L] = om->tjb_b;
+  h[64 + (L + 1) + L] = 255;
+  uint8_t *hs = h + 64 + T;
+  if (L) memcpy(hs, dsq + 1, (size_t) L);
+  memset(hs + L, PAD_CODE, padded - (size_t) L);
+  uint8_t *d = c->d_one;
+  CUDA_TRY(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, c->stream));
+  const DbDev dbv{d + 64 + T, (const int64_t *) (d + 8), (const int32_t *) (d + 32), (const int64_t *) (d + 16), 1};
+  ProfDev P;
+  P.M = p->M; P.C = p->C; P.tbm = p->tbm; P.tec = p->tec; P.base = p->base; P.bias = p->bias;
+  P.stab = p->d_stab; P.mtab = p->d_mtab; P.tjb = d + 64; P.xjmin = d + 64 + L + 1; P.ssv_f16 = p->f16;
+  LaunchArgs a;
+  a.P = P; a.db = dbv; a.out_xj = c->d_out; a.out_flags = c->d_out + 1;
+  a.ticket = (unsigned long long *) d;
+  a.stream = c->stream; a.grid = 1; a.skip_empty = 0;
+  CUDA_TRY(dispatch(p->C, p->f16 != 0, a, c->num_sms));
+  g_launches.fetch_add(1);
+  uint8_t *res = h;                                           // the results come back into the staged block
   CUDA_TRY(cudaMemcpyAsync(res, c->d_out, 2, cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(cudaStreamSynchronize(c->stream));
   if (res[1] & MSVGB_FLAG_ERANGE) { *ret_sc = INFINITY; return MSVGB_eslERANGE; }

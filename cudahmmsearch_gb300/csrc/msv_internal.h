@@ -15,6 +15,18 @@
 
 struct TuneTable;                                       // msv_tune.cu
 
+// A profile of the drop-in msvgb_MSVFilter's per-context cache: the device
+// tables and a copy of the bytes they were built from (the om's scalar MSV
+// fields and its rbv vectors), so a hit is confirmed byte for byte.
+struct DropinEntry {
+  const uint8_t *rbv_ptr = nullptr;   // fast-path key: the caller's vectors and M
+  int M = 0;
+  uint64_t hash = 0;                  // content hash (masked: see msvgb_ctx::hash_mask)
+  std::vector<uint8_t> image;         // M, Kp, tbm, tec, base, bias, scale, then rbv
+  msvgb_profile *p = nullptr;
+  uint64_t last_use = 0;
+};
+
 struct msvgb_ctx {
   int device = 0;
   int num_sms = 0;
@@ -22,11 +34,13 @@ struct msvgb_ctx {
   cudaStream_t stream = nullptr;
   unsigned long long *d_ticket = nullptr;
   std::mutex mu;                                        // serialises the single-call path
-  std::unordered_map<uint64_t, msvgb_profile *> cache;  // single-call profile cache
-  // single-call scratch
-  uint8_t *d_seq = nullptr; size_t d_seq_cap = 0;
-  uint8_t *d_tab = nullptr; size_t d_tab_cap = 0;
-  int64_t *d_meta = nullptr;                            // start, orig (int64), len (int32) for n=1
+  std::vector<DropinEntry> dropin;                      // single-call profile cache (least recently used out)
+  uint64_t dropin_clock = 0;
+  uint64_t hash_mask = ~0ull;                           // content-hash bits kept (tests force collisions)
+  // single-call scratch: one block [ticket | meta | tjb/xjmin table | residues]
+  // staged in pinned host memory and uploaded in one copy
+  uint8_t *d_one = nullptr; size_t d_one_cap = 0;
+  uint8_t *h_one = nullptr; size_t h_one_cap = 0;
   uint8_t *d_out = nullptr;
   int *d_bad = nullptr;                                 // database packing: invalid-code flag
   int64_t *d_list = nullptr; size_t list_cap = 0;       // G-lane search: sequences left for the full MSV

@@ -45,6 +45,9 @@ uint8_t *g_scratch_addr[kMaxDevices] = {};   // device address of g_static_scrat
 
 // Once per device, with that device current: the device address of the
 // array. (Host code cannot use g_static_scratch's own name as an address.)
+// The address is kept for the life of the process: it does not survive a
+// reset of the device's primary context (cudaDeviceReset), after which this
+// entry point must not be called again in the same process.
 int scratch_address(int device, uint8_t **out) {
   if (device < 0 || device >= kMaxDevices) return fail(MSVGB_eslEINVAL, "device index out of range");
   std::lock_guard<std::mutex> lock(g_setup_mu);
@@ -97,16 +100,26 @@ extern "C" int msvgb_search_static(const msvgb_profile *p, const msvgb_db *db, d
   }
 
   cudaStream_t s = cuda_stream ? (cudaStream_t) cuda_stream : c->stream;
+  if (db->ready) {                                   // a database still being packed, as msvgb_search_device waits
+    e = cudaStreamWaitEvent(s, db->ready, 0);
+    if (e != cudaSuccess) return fail(MSVGB_eslESYS, std::string("cudaStreamWaitEvent: ") + cudaGetErrorString(e));
+  }
   uint8_t *d_ticket = scratch;
   uint8_t *d_tjb = scratch + kTicketBytes;
   uint8_t *d_xjmin = scratch + kTicketBytes + kTableBytes;
   // The array keeps the previous call's contents: the ticket must restart at
-  // zero, and both tables are rewritten over [0, Lmax].
+  // zero, and both tables are rewritten over [0, Lmax]. The tables are copied
+  // from pageable host memory (this call allocates no pinned buffer): the
+  // runtime waits for the stream's earlier work before such a copy and
+  // returns once it has taken the bytes, so the vectors may go when it returns.
   e = cudaMemsetAsync(d_ticket, 0, sizeof(unsigned long long), s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(d_tjb, tjb.data(), Lmax + 1, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(d_xjmin, xjm.data(), Lmax + 1, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return fail(MSVGB_eslESYS, std::string("static scratch upload: ") + cudaGetErrorString(e));
 
+  // Always the fused 32-lane kernel, whatever lanes the profile was given:
+  // the lane-group pass needs a list of undecided sequences as long as the
+  // database, which a fixed-size array cannot hold.
   ProfDev P;
   P.M = p->M; P.C = p->C; P.tbm = p->tbm; P.tec = p->tec; P.base = p->base; P.bias = p->bias;
   P.stab = p->d_stab; P.mtab = p->d_mtab; P.tjb = d_tjb; P.xjmin = d_xjmin; P.ssv_f16 = p->f16;

@@ -35,19 +35,41 @@ def shard(seqs: F.SeqSet, rank: int, world: int) -> tuple[F.SeqSet, int, int]:
     return F.SeqSet(codes, off.astype(np.int64)), lo, hi
 
 
-def gather_results(local_xj: np.ndarray, local_flags: np.ndarray, n_total: int, group=None):
-    """Concatenate every rank's per-sequence bytes in rank (= sequence) order
-    with a host-side gather over torch.distributed (any backend); returns the
-    full arrays on every rank."""
+def shard_view(seqs: F.SeqSet, rank: int, world: int):
+    """This rank's shard without a copy, in the argument layout of
+    msvgb_search_host / msvgb_db_create: the whole residue buffer, the
+    rank's slice of the offsets (n+1 absolute offsets into that buffer) and
+    its sequence count. Returns (codes, off, n, begin, end)."""
+    b = shard_bounds(seqs.lengths, world)
+    lo, hi = int(b[rank]), int(b[rank + 1])
+    return seqs.codes, seqs.off[lo:hi + 1], hi - lo, lo, hi
+
+
+def gather_results(local_xj: np.ndarray, local_flags: np.ndarray, n_total: int | None = None, group=None,
+                   device=None):
+    """Concatenates every rank's per-sequence bytes (xj, flags) in rank (=
+    sequence) order on every rank: one all_gather of the shard sizes, then
+    one all_gather of fixed-size uint8 tensors (each rank's bytes padded to
+    the largest shard). device: where the tensors live -- a CUDA device for
+    NCCL, the CPU (default) for gloo. Returns the full (xj, flags) arrays."""
     import torch
     import torch.distributed as dist
     world = dist.get_world_size(group)
-    local = np.concatenate([local_xj, local_flags]).astype(np.uint8)
-    sizes = [None] * world
-    dist.all_gather_object(sizes, int(len(local_xj)), group=group)
-    parts = [None] * world
-    dist.all_gather_object(parts, local.tobytes(), group=group)
-    xj = np.concatenate([np.frombuffer(p, np.uint8)[:sz] for p, sz in zip(parts, sizes)])
-    fl = np.concatenate([np.frombuffer(p, np.uint8)[sz:] for p, sz in zip(parts, sizes)])
-    assert len(xj) == n_total
+    dev = torch.device("cpu") if device is None else torch.device(device)
+    n = int(len(local_xj))
+    sizes_t = [torch.zeros(1, dtype=torch.int64, device=dev) for _ in range(world)]
+    dist.all_gather(sizes_t, torch.tensor([n], dtype=torch.int64, device=dev), group=group)
+    sizes = [int(t.item()) for t in sizes_t]
+    cap = max(max(sizes), 1)
+    local = torch.zeros(2 * cap, dtype=torch.uint8)
+    local[:n] = torch.from_numpy(np.ascontiguousarray(local_xj, dtype=np.uint8))
+    local[cap:cap + n] = torch.from_numpy(np.ascontiguousarray(local_flags, dtype=np.uint8))
+    local = local.to(dev)
+    parts = [torch.empty(2 * cap, dtype=torch.uint8, device=dev) for _ in range(world)]
+    dist.all_gather(parts, local, group=group)
+    parts = [t.cpu().numpy() for t in parts]
+    xj = np.concatenate([pt[:sz] for pt, sz in zip(parts, sizes)])
+    fl = np.concatenate([pt[cap:cap + sz] for pt, sz in zip(parts, sizes)])
+    if n_total is not None and len(xj) != n_total:
+        raise ValueError(f"gathered {len(xj)} sequences, expected {n_total}")
     return xj, fl

@@ -87,8 +87,11 @@ uint64_t    msvgb_kernel_launches(void);
  * om->tjb_b must already hold the value for this L (p7_oprofile_ReconfigLength),
  * as the reference requires. Returns eslOK or eslERANGE (*ret_sc = +inf);
  * eslEINVAL if p7O_NQB(om->M) > ox->allocQ16 (msvfilter.c:103). Sets ox->M = om->M.
- * The profile is uploaded once and cached by content. Thread-safe (serialised
- * per context). */
+ * The profile is uploaded once per context and cached (up to 64 profiles,
+ * least recently used out), found by the caller's rbv pointer and M or by a
+ * content hash and confirmed byte for byte before use. Each call then makes
+ * one host-to-device copy (from pinned staging), one launch and one 2-byte
+ * copy back, and waits for them. Thread-safe (serialised per context). */
 int msvgb_MSVFilter(msvgb_ctx *ctx, const uint8_t *dsq, int L, const msvgb_om *om,
                     msvgb_omx *ox, float *ret_sc);
 
@@ -298,12 +301,6 @@ int msvgb_sample_om(uint32_t seed, int M, uint8_t *rbv, msvgb_om *om, double *re
  * with this library's GPU search and sets om->mmu (and om->mlambda = lambda). */
 int msvgb_calibrate(msvgb_ctx *ctx, msvgb_om *om, double lambda);
 
-/* ---- measurement ------------------------------------------------------------------
- * Sustained rate of independent 32-bit integer operations over all SMs of the
- * device (ops/s), measured by a short kernel: the denominator of the
- * integer-pipe roofline (one DP cell = one packed 32-bit op). No reference
- * counterpart. */
-int msvgb_measure_int_peak(int device, double *ops_per_second);
 
 /* ---- allocation-free search ------------------------------------------------------
  * No counterpart in the reference. For callers that cannot allocate device
@@ -320,9 +317,13 @@ int msvgb_measure_int_peak(int device, double *ops_per_second);
  * array: calls whose work overlaps on the GPU (different streams, or
  * different host threads) race and must be serialised by the caller. The
  * first call on a device looks up the array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture.
- * Asynchronous on cuda_stream (NULL: the context's stream); results equal
- * msvgb_search_device's. */
+ * (cudaGetSymbolAddress) and keeps it for the process: make that first call
+ * before any stream capture, and do not call this again after a
+ * cudaDeviceReset. Work is enqueued on cuda_stream (NULL: the context's
+ * stream); the two per-length tables go up from pageable host memory, so the
+ * call first waits for the stream's earlier work. It always runs the fused
+ * 32-lane search kernel (the lane-group pass that msvgb_search_device may
+ * choose needs a database-sized list); results equal msvgb_search_device's. */
 #define MSVGB_STATIC_MAX_LEN 65535
 int msvgb_search_static(const msvgb_profile *prof, const msvgb_db *db, double F1,
                         void *d_xj, void *d_flags, void *cuda_stream);

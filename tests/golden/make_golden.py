@@ -245,7 +245,9 @@ def make_pipe(tut):
 def main():
     if not os.path.exists(REFGEN):
         sys.exit("oracle/_ref/refgen missing: make -C oracle/ref REF=<reference>/code")
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/code"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MSVGB_REFERENCE_CODE")
+    if not ref or not os.path.isdir(ref):
+        sys.exit("usage: make_golden.py <reference>/code  (or set MSVGB_REFERENCE_CODE)")
     for c in CASES:
         make_case(*c)
     make_tutorial(os.path.join(ref, "tutorial"))

@@ -15,8 +15,8 @@ from oracle import oracle as O
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def header_functions():
-    src = open(os.path.join(ROOT, "include", "msvgb.h")).read()
+def header_functions(header="msvgb.h"):
+    src = open(os.path.join(ROOT, "include", header)).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
     return sorted(set(re.findall(r"\b(msvgb_\w+)\s*\(", src)))
 
@@ -28,6 +28,16 @@ def test_library_exports_every_declared_function():
     for name in declared:
         assert hasattr(lib, name), name
     assert sorted(api.EXPORTS) == declared
+
+
+def test_probe_library_exports_its_header():
+    """The benchmark's peak probes live in a library of their own."""
+    lib = ctypes.CDLL(os.path.join(ROOT, "cudahmmsearch_gb300", "libmsvgb_probe.so"))
+    declared = header_functions("msvgb_probe.h")
+    assert declared == ["msvgb_measure_int_peak", "msvgb_measure_smem_peak", "msvgb_probe_last_error"]
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert not hasattr(api.lib(), "msvgb_measure_int_peak")
 
 
 @pytest.mark.parametrize("L", [0, 1, 2, 3, 10, 100, 300, 1000, 5000, 35000, 100000])

@@ -1,6 +1,9 @@
-"""Multi-GPU sharding logic on CPU: two gloo ranks each score their
+"""Multi-GPU sharding logic on CPU: gloo ranks each score their
 residue-balanced shard (with the oracle standing in for a GPU) and gather the
-per-sequence bytes; the result equals scoring the whole database at once."""
+per-sequence bytes with fixed-size tensor all_gathers; the result equals
+scoring the whole database at once. One case cuts the shard as a copy, the
+other as a view in msvgb_search_host's argument layout (the whole residue
+buffer, the rank's slice of absolute offsets, its count)."""
 import os
 import socket
 
@@ -20,14 +23,19 @@ def _free_port():
         return s.getsockname()[1]
 
 
-def _rank_main(rank, world, port, q):
+def _rank_main(rank, world, port, q, view=False):
     import torch.distributed as dist
     from oracle import oracle as O
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
     dist.init_process_group("gloo", rank=rank, world_size=world)
     p = F.read_profile(os.path.join(GOLDEN, "m200_s1.prof"))
     s = F.synth_sequences(800, seed=3, lmax=3000)
-    local, lo, hi = S.shard(s, rank, world)
+    if view:
+        codes, off, n, lo, hi = S.shard_view(s, rank, world)
+        assert off.size == n + 1 and codes is s.codes
+        local = F.SeqSet(codes, off)        # absolute offsets into the shared buffer
+    else:
+        local, lo, hi = S.shard(s, rank, world)
     o = O.msv_batch(p, local, nthreads=1)
     flags = (o["status"] == 16).astype(np.uint8) | (o["pass"] << 1)
     xj, fl = S.gather_results(o["xj"], flags, s.n)
@@ -39,11 +47,12 @@ def _rank_main(rank, world, port, q):
     dist.destroy_process_group()
 
 
-def test_two_gloo_ranks_gather_equals_whole():
+@pytest.mark.parametrize("world,view", [(2, False), (2, True), (3, True)])
+def test_gloo_ranks_gather_equals_whole(world, view):
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = _free_port()
-    procs = [ctx.Process(target=_rank_main, args=(r, 2, port, q)) for r in range(2)]
+    procs = [ctx.Process(target=_rank_main, args=(r, world, port, q, view)) for r in range(world)]
     for pr in procs:
         pr.start()
     res = q.get(timeout=120)

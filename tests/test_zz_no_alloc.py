@@ -72,3 +72,28 @@ def test_search_static_rejects_sequences_over_its_limit():
     assert _search_static(prof, db, out, 0) == api.eslEINVAL
     assert b"MSVGB_STATIC_MAX_LEN" in api.lib().msvgb_last_error()
     ctx.close()
+
+
+def test_search_static_allocates_nothing_after_its_first_call():
+    """The defining property: once the first call on a device has looked up
+    the static array (and the runtime has loaded the kernel), further calls
+    leave the device's free memory exactly where it was."""
+    import torch
+    ctx = api.Context(0)
+    p = F.read_profile(os.path.join(GOLDEN, "m200_s1.prof"))
+    s = F.SeqSet.concat([F.synth_sequences(4000, seed=95, lmax=3000), F.emit_homologs(p, 40, seed=96)])
+    prof, db = api.DeviceProfile(ctx, p), api.DeviceDB(ctx, s)
+    want = api.search(ctx, prof, db)
+    out = torch.zeros(2 * db.n, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    assert _search_static(prof, db, out, stream.cuda_stream) == api.eslOK
+    torch.cuda.synchronize()      # device-wide: stream-ordered pools give back what earlier calls freed
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(5):
+        assert _search_static(prof, db, out, stream.cuda_stream) == api.eslOK
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert np.array_equal(out.cpu().numpy(), np.concatenate(want))
+    ctx.close()
