@@ -49,6 +49,94 @@ __device__ __forceinline__ void ssv_row_group(uint32_t (&dp)[C], uint32_t &acc0,
   }
 }
 
+// ---- mixed-width SSV table (f16 and 8-bit costs) ------------------------------
+// The f16 row reads 2 bytes of cost per cell from shared memory and is bound
+// by shared-memory bandwidth (one 128-byte wavefront per clock and SM) while
+// the FMA and ALU pipes idle half the time. Here the last CI words of every
+// lane keep their costs as bytes (1 byte per cell) and widen them in
+// registers, trading shared-memory bytes for instructions on the idle pipes.
+//
+// Units: cells and costs are integers times 2^-24, i.e. f16 subnormals (and
+// the smallest normals): an integer n with |n| < 2048 is exact, its bits are
+// sign-magnitude (n < 0: 0x8000 | -n). A byte t is widened to a cost with one
+// PRMT (t as the low byte of a zero high byte: t * 2^-24) and one f16 add of
+// -128 units, so the table stores t = s + 128. Cell updates stay one
+// fma.relu per word as in the f16 row, and they are exact for the same
+// reason (integers below 2048 units; the relu clamps at 0). Non-negative f16
+// bits order like signed 16-bit integers, so the running maximum is taken on
+// the bits with integer instructions (ALU pipe) instead of f16 maxima (FMA
+// pipe).
+//
+// Layout for residue x (CF = C - CI f16 words, CI a multiple of 8): the f16
+// regions of GroupLayout<CF, G> (quads, pair, single), then 16-byte octets
+// [x][o][g][4 words]: word k of octet o of lane g holds the bytes
+// [t(w, h0), t(w+1, h0), t(w, h1), t(w+1, h1)] of DP words w = CF + 8o + 2k
+// and w + 1.
+template <int C, int CI, int G>
+struct HybLayout {
+  static_assert(CI % 8 == 0 && CI >= 8 && CI <= C, "8-bit words come in octets");
+  static constexpr int CF = C - CI;
+  static constexpr int Q4 = CF / 4, R = CF % 4, NO = CI / 8;
+  static constexpr int A_WORDS = NRES * Q4 * G * 4;
+  static constexpr int B_WORDS = (R >= 2) ? NRES * G * 2 : 0;
+  static constexpr int C_WORDS = (R & 1) ? NRES * G : 0;
+  static constexpr int D_WORDS = NRES * NO * G * 4;
+  static constexpr int WORDS = A_WORDS + B_WORDS + C_WORDS + D_WORDS;
+};
+
+__device__ __forceinline__ uint32_t add_f16x2(uint32_t a, uint32_t b) {
+  uint32_t d; asm("add.rn.f16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b)); return d;
+}
+
+template <int C, int CI, int G>
+__device__ __forceinline__ void ssv_row_hyb(uint32_t (&dp)[C], uint32_t &acc,
+                                            const uint32_t *__restrict__ tab, int x, int glane, int src_lane) {
+  using Lay = HybLayout<C, CI, G>;
+  constexpr int CF = Lay::CF;
+  constexpr uint32_t one2 = 0x3C003C00u;        // f16x2 (1.0, 1.0)
+  constexpr uint32_t m128 = 0x80808080u;        // f16x2 (-128, -128) units of 2^-24
+  uint32_t s[C];
+#pragma unroll
+  for (int q = 0; q < Lay::Q4; ++q) {
+    const uint4 v = *reinterpret_cast<const uint4 *>(tab + ((x * Lay::Q4 + q) * G + glane) * 4);
+    s[4 * q] = v.x; s[4 * q + 1] = v.y; s[4 * q + 2] = v.z; s[4 * q + 3] = v.w;
+  }
+  if constexpr (Lay::R >= 2) {
+    const uint2 v = *reinterpret_cast<const uint2 *>(tab + Lay::A_WORDS + (x * G + glane) * 2);
+    s[4 * Lay::Q4] = v.x; s[4 * Lay::Q4 + 1] = v.y;
+  }
+  if constexpr (Lay::R & 1) s[CF - 1] = tab[Lay::A_WORDS + Lay::B_WORDS + x * G + glane];
+  const uint32_t *td = tab + Lay::A_WORDS + Lay::B_WORDS + Lay::C_WORDS;
+#pragma unroll
+  for (int o = 0; o < Lay::NO; ++o) {
+    const uint4 v = *reinterpret_cast<const uint4 *>(td + ((x * Lay::NO + o) * G + glane) * 4);
+    const uint32_t tw[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      s[CF + 8 * o + 2 * k]     = add_f16x2(prmt(tw[k], 0u, 0x4240u), m128);   // bytes 0, 2
+      s[CF + 8 * o + 2 * k + 1] = add_f16x2(prmt(tw[k], 0u, 0x4341u), m128);   // bytes 1, 3
+    }
+  }
+  const uint32_t pred0 = pred_word0(dp[C - 1], src_lane);
+#pragma unroll
+  for (int w = C - 1; w >= 0; --w) dp[w] = fma_relu_f16x2(w ? dp[w - 1] : pred0, one2, s[w]);
+  // running maximum on the bits (signed: a -0 from the relu is the smallest)
+  if constexpr (C & 1) acc = max_s16x2(acc, dp[C - 1]);
+#pragma unroll
+  for (int w = 0; w + 1 < C; w += 2) acc = __vimax3_s16x2(acc, dp[w], dp[w + 1]);
+}
+
+// The group maximum of a hybrid accumulator as a float number of units
+// (capped at 4096: above 2047 units values are not exact, and past the trust
+// bound only "large" matters).
+__device__ __forceinline__ float hyb_units(uint32_t acc) {
+  const int lo = (int) (int16_t) (acc & 0xFFFFu), hi = (int) (int16_t) (acc >> 16);
+  const int b = max(max(lo, hi), 0);
+  if (b >= 0x7C00) return 4096.0f;                         // inf: far past any bound
+  const float f = __half2float(__ushort_as_half((unsigned short) b)) * 16777216.0f;
+  return fminf(f, 4096.0f);
+}
+
 struct GroupArgs {
   ProfDev P;                       // P.stab: the G-lane f16 SSV table
   DbDev db;
@@ -66,7 +154,8 @@ constexpr uint32_t kPadWord = 0x1D1D1D1Du;   // four PAD_CODE residues
 // returns the next sorted sequence index, or a negative value when there is
 // none; undecided(s) (lane 0 of a group) records a sequence that needs the full
 // MSV. Decided sequences (and empty ones) are written to out_xj / out_flags.
-template <int C, int G, class Fetch, class Undecided>
+// CI > 0: the mixed-width table (HybLayout<C, CI, G>, units of 2^-24).
+template <int C, int G, int CI = 0, class Fetch, class Undecided>
 __device__ __forceinline__ void ssv_group_loop(const ProfDev &P, const uint32_t *__restrict__ tab, const DbDev &db,
                                                uint8_t *__restrict__ out_xj, uint8_t *__restrict__ out_flags,
                                                Fetch fetch, Undecided undecided) {
@@ -116,13 +205,21 @@ __device__ __forceinline__ void ssv_group_loop(const ProfDev &P, const uint32_t 
     const uint32_t w4 = active ? nextw : kPadWord;
     if (active && i + 4 < L) nextw = __ldg(sq + (i >> 2) + 1);
 #pragma unroll
-    for (int j = 0; j < 4; ++j) ssv_row_group<C, G>(dp, acc0, acc1, tab, (w4 >> (8 * j)) & 0xFF, glane, src_lane);
+    for (int j = 0; j < 4; ++j) {
+      if constexpr (CI > 0) ssv_row_hyb<C, CI, G>(dp, acc0, tab, (w4 >> (8 * j)) & 0xFF, glane, src_lane);
+      else                  ssv_row_group<C, G>(dp, acc0, acc1, tab, (w4 >> (8 * j)) & 0xFF, glane, src_lane);
+    }
     i += 4;
     const bool fin = active && i >= L;
     if (__any_sync(FULL, fin)) {                      // group maxima (all lanes take part)
-      const __half2 a = __hmax2(*reinterpret_cast<const __half2 *>(&acc0),
-                                *reinterpret_cast<const __half2 *>(&acc1));
-      float f = fminf(fmaxf(__low2float(a), __high2float(a)), 4096.0f);
+      float f;
+      if constexpr (CI > 0) {
+        f = hyb_units(acc0);
+      } else {
+        const __half2 a = __hmax2(*reinterpret_cast<const __half2 *>(&acc0),
+                                  *reinterpret_cast<const __half2 *>(&acc1));
+        f = fminf(fmaxf(__low2float(a), __high2float(a)), 4096.0f);
+      }
 #pragma unroll
       for (int off = G / 2; off >= 1; off >>= 1) f = fmaxf(f, __shfl_xor_sync(FULL, f, off));
       if (fin) {
@@ -148,21 +245,27 @@ __device__ __forceinline__ void ssv_group_loop(const ProfDev &P, const uint32_t 
 
 // Stand-alone SSV pass over the sorted sequences [s_begin, n) (global
 // ticket); undecided sequences go to a global list for the full-MSV launch.
-template <int C, int G>
+// Table words of the lane-group SSV pass: f16 (CI = 0) or mixed width.
+template <int C, int G, int CI>
+constexpr int group_table_words() {
+  if constexpr (CI > 0) return HybLayout<C, CI, G>::WORDS;
+  else return GroupLayout<C, G>::WORDS;
+}
+
+template <int C, int G, int CI = 0>
 __global__ void __launch_bounds__(256)
 msv_ssv_group_kernel(ProfDev P, DbDev db, uint8_t *__restrict__ out_xj, uint8_t *__restrict__ out_flags,
                      unsigned long long *__restrict__ ticket, int64_t *__restrict__ undecided,
                      unsigned long long *__restrict__ n_undecided, int64_t s_begin) {
   extern __shared__ __align__(16) uint32_t smem[];
-  using Lay = GroupLayout<C, G>;
   {
     const uint4 *gs = reinterpret_cast<const uint4 *>(P.stab);
     uint4 *ss = reinterpret_cast<uint4 *>(smem);
-    for (int i = threadIdx.x; i < Lay::WORDS / 4; i += blockDim.x) ss[i] = __ldg(gs + i);
+    for (int i = threadIdx.x; i < group_table_words<C, G, CI>() / 4; i += blockDim.x) ss[i] = __ldg(gs + i);
   }
   __syncthreads();
   const unsigned long long n = (unsigned long long) db.n;
-  ssv_group_loop<C, G>(
+  ssv_group_loop<C, G, CI>(
       P, smem, db, out_xj, out_flags,
       [&]() -> long long {
         const unsigned long long t = atomicAdd(ticket, 1ull) + (unsigned long long) s_begin;
@@ -188,10 +291,10 @@ __device__ __forceinline__ void ssv_group_chunk(const ProfDev &P, const uint32_t
       [&](int64_t s) { und[atomicAdd(n_und, 1u)] = (uint16_t) (s - s0); });
 }
 
-template <int C, int G>
+template <int C, int G, int CI = 0>
 cudaError_t launch_ssv_group(const GroupArgs &a, int num_sms) {
-  auto kern = msv_ssv_group_kernel<C, G>;
-  constexpr size_t smem = (size_t) GroupLayout<C, G>::WORDS * 4;
+  auto kern = msv_ssv_group_kernel<C, G, CI>;
+  constexpr size_t smem = (size_t) group_table_words<C, G, CI>() * 4;
   static std::atomic<unsigned long long> configured{0};
   {
     cudaError_t e = ensure_smem_attr((const void *) kern, smem, configured);
@@ -212,4 +315,6 @@ cudaError_t launch_ssv_group(const GroupArgs &a, int num_sms) {
 }  // namespace msvgb
 
 #define MSVGB_INSTANTIATE_GROUP(C, G) \
-  template cudaError_t msvgb::launch_ssv_group<C, G>(const msvgb::GroupArgs &, int);
+  template cudaError_t msvgb::launch_ssv_group<C, G, 0>(const msvgb::GroupArgs &, int);
+#define MSVGB_INSTANTIATE_HYB(C, G, CI) \
+  template cudaError_t msvgb::launch_ssv_group<C, G, CI>(const msvgb::GroupArgs &, int);
