@@ -593,6 +593,8 @@ def main():
     ap.add_argument("--workload", default="m400_2M")
     ap.add_argument("--variant", type=int, default=None, help="SSV arithmetic: 0 int8 table, 1 f16 table")
     ap.add_argument("--lanes", type=int, default=None, help="lanes per sequence of the SSV pass (32, 16, 8)")
+    ap.add_argument("--int8-words", type=int, default=None,
+                    help="lane-group SSV pass: DP words per lane with 8-bit costs (mixed-width table)")
     ap.add_argument("--M", type=int, default=100, help="sampled workload: model length")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=5)
@@ -650,6 +652,8 @@ def main():
     prof = api.DeviceProfile(ctx, p, args.variant)
     if args.lanes:
         prof.set_lanes(args.lanes)
+    if args.int8_words is not None:
+        prof.set_int8_words(args.int8_words)
     db = api.DeviceDB(ctx, s)
     out = torch.empty(2 * s.n, dtype=torch.uint8, device="cuda")
     d_xj, d_fl = out.data_ptr(), out.data_ptr() + s.n
@@ -757,7 +761,8 @@ def main():
     line = {"metric": "MSV GCUPS", "value": value, "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-            "config": dict(cfg, variant=prof.variant, lanes=prof.lanes, full_msv_fraction=fullfrac,
+            "config": dict(cfg, variant=prof.variant, lanes=prof.lanes, int8_words=prof.int8_words,
+                           full_msv_fraction=fullfrac,
                            pass_fraction=float(((fl_all & api.FLAG_PASS) != 0).mean())),
             "e2e": {"value": e2e_val, "unit": "GCUPS", "h2d_bytes_per_step": int(s.total + 28 * s.n),
                     "d2h_bytes_per_step": int(2 * s.n),

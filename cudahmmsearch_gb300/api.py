@@ -27,7 +27,7 @@ EXPORTS = [
     "msvgb_ctx_create", "msvgb_ctx_destroy", "msvgb_ctx_set_stream", "msvgb_last_error",
     "msvgb_kernel_launches", "msvgb_MSVFilter", "msvgb_profile_create", "msvgb_profile_destroy",
     "msvgb_profile_M", "msvgb_profile_create_ex", "msvgb_profile_variant", "msvgb_profile_set_lanes",
-    "msvgb_profile_lanes", "msvgb_db_create", "msvgb_db_destroy", "msvgb_db_nseq", "msvgb_db_residues",
+    "msvgb_profile_lanes", "msvgb_profile_set_ssv_int8_words", "msvgb_profile_ssv_int8_words", "msvgb_db_create", "msvgb_db_destroy", "msvgb_db_nseq", "msvgb_db_residues",
     "msvgb_search", "msvgb_search_device", "msvgb_tjb_b", "msvgb_score", "msvgb_f1_pass",
     "msvgb_search_static", "msvgb_sample_om", "msvgb_calibrate",
     "msvgb_batch_create", "msvgb_batch_run", "msvgb_batch_items", "msvgb_batch_destroy", "msvgb_search_batch",
@@ -116,6 +116,8 @@ def lib():
         "msvgb_profile_create_ex": (i32, [vp, ctypes.POINTER(_Om), i32, ctypes.POINTER(vp)]),
         "msvgb_profile_variant": (i32, [vp]),
         "msvgb_profile_set_lanes": (i32, [vp, ctypes.POINTER(_Om), i32]),
+        "msvgb_profile_set_ssv_int8_words": (i32, [vp, ctypes.POINTER(_Om), i32]),
+        "msvgb_profile_ssv_int8_words": (i32, [vp]),
         "msvgb_autotune": (i32, [vp, ctypes.c_double]),
         "msvgb_tune_save": (i32, [vp, ctypes.c_char_p]),
         "msvgb_tune_load": (i32, [vp, ctypes.c_char_p]),
@@ -288,6 +290,15 @@ class DeviceProfile:
     @property
     def lanes(self) -> int:
         return int(lib().msvgb_profile_lanes(self.h))
+
+    def set_int8_words(self, words: int):
+        """DP words per lane of the 16/8-lane SSV pass whose costs are bytes (mixed-width table)."""
+        o, keep = _om_struct(self.profile)
+        _check(lib().msvgb_profile_set_ssv_int8_words(self.h, ctypes.byref(o), words))
+
+    @property
+    def int8_words(self) -> int:
+        return int(lib().msvgb_profile_ssv_int8_words(self.h))
 
     def close(self):
         if self.h:

@@ -137,12 +137,39 @@ cudaError_t msvgb_detail::dispatch(int C, bool f16, const LaunchArgs &a, int sms
 }
 
 namespace msvgb {
-template <int C, int G> cudaError_t launch_ssv_group(const GroupArgs &a, int num_sms);
+template <int C, int G, int CI> cudaError_t launch_ssv_group(const GroupArgs &a, int num_sms);
 }
 
-cudaError_t msvgb_detail::dispatch_group(int C, int G, const GroupArgs &a, int sms) {
-#define G16(c) case c: return launch_ssv_group<c, 16>(a, sms);
-#define G8(c)  case c: return launch_ssv_group<c, 8>(a, sms);
+// Mixed-width instantiations (inst_hyb*.cu): (C, G, CI) triples.
+#include "msv_hyb_list.h"
+
+// Default 8-bit words per lane of the G-lane SSV pass at DP width C, from a
+// sweep on GB300 (1,000,000 sequences; M from 120 to 1008): at 8 lanes none
+// below 10 words (4 lost 2.5% at M = 120), 4 up to 17 words (+4 to +7%), 8
+// from 18 words (+7 to +10%; 12 and 16 were slower than 8 everywhere); at 16
+// lanes 4 up to 23 words (+3 to +9%), 8 from 24 (+8%).
+int msvgb_detail::hyb_default_words(int C, int G) {
+  if (G == 8) return C < 10 ? 0 : C < 18 ? 4 : 8;
+  if (G == 16) return C < 13 ? 0 : C < 24 ? 4 : 8;
+  return 0;
+}
+
+bool msvgb_detail::hyb_compiled(int C, int G, int CI) {
+#define MSVGB_HYB_HAS(c, g, ci) if (C == c && G == g && CI == ci) return true;
+  MSVGB_HYB_LIST(MSVGB_HYB_HAS)
+#undef MSVGB_HYB_HAS
+  return false;
+}
+
+cudaError_t msvgb_detail::dispatch_group(int C, int G, int CI, const GroupArgs &a, int sms) {
+  if (CI > 0) {
+#define MSVGB_HYB_CALL(c, g, ci) if (C == c && G == g && CI == ci) return launch_ssv_group<c, g, ci>(a, sms);
+    MSVGB_HYB_LIST(MSVGB_HYB_CALL)
+#undef MSVGB_HYB_CALL
+    return cudaErrorInvalidValue;
+  }
+#define G16(c) case c: return launch_ssv_group<c, 16, 0>(a, sms);
+#define G8(c)  case c: return launch_ssv_group<c, 8, 0>(a, sms);
   if (G == 16) {
     switch (C) { G16(2) G16(3) G16(4) G16(5) G16(6) G16(7) G16(8) G16(9) G16(10) G16(11) G16(12) G16(13)
                  G16(14) G16(15) G16(16) G16(17) G16(18) G16(19) G16(20) G16(21) G16(22) G16(23) G16(24)
@@ -404,23 +431,83 @@ extern "C" int msvgb_profile_set_lanes(msvgb_profile *p, const msvgb_om *om, int
   if (!p || !om) return fail(MSVGB_eslEINVAL, "NULL argument");
   if (om->M != p->M) return fail(MSVGB_eslEINVAL, "om does not match the profile");
   p->lanes_auto = false;                                  // set by the caller: applies at any size
-  if (G == 32) { p->G = 32; return MSVGB_eslOK; }
+  if (G == 32) { p->G = 32; p->CI = 0; return MSVGB_eslOK; }
   if (G != 16 && G != 8) return fail(MSVGB_eslEINVAL, "lanes per sequence must be 32, 16 or 8");
   const int C = p->M / (2 * G) + 1;                       // 2*C*G > M: the last node is padding
   if (C > 32) return fail(MSVGB_eslEINVAL, "model too long for this many lanes per sequence");
   if (C < 2) return fail(MSVGB_eslEINVAL, "model too short for this many lanes per sequence");
-  std::vector<uint32_t> st = build_group_table(om, C, G);
+  int CI = hyb_default_words(C, G);
+  if (CI > 0 && !hyb_compiled(C, G, CI)) CI = 0;
+  std::vector<uint32_t> st = CI ? build_hyb_table(om, C, G, CI) : build_group_table(om, C, G);
   CUDA_TRY(cudaSetDevice(p->device));
   uint32_t *d = nullptr;
   CUDA_TRY(cudaMalloc(&d, st.size() * 4));
   cudaError_t e = cudaMemcpy(d, st.data(), st.size() * 4, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) { cudaFree(d); return fail(MSVGB_eslESYS, cudaGetErrorString(e)); }
   cudaFree(p->d_stab_g);
-  p->d_stab_g = d; p->Cg = C; p->G = G;
+  p->d_stab_g = d; p->Cg = C; p->G = G; p->CI = CI;
   return MSVGB_eslOK;
 }
 
 extern "C" int msvgb_profile_lanes(const msvgb_profile *p) { return p ? p->G : -1; }
+
+// Mixed-width lane-group table: the first C - CI words of every lane as f16
+// bits of s units of 2^-24 (sign-magnitude: s < 0 -> 0x8000 | -s), the last
+// CI words (a multiple of 4) as bytes t = s + 128 (layout HybLayout<C, CI, G>,
+// msv_group.cuh).
+std::vector<uint32_t> msvgb_detail::build_hyb_table(const msvgb_om *om, int C, int G, int CI) {
+  const int M = om->M, Q = std::max(2, (M - 1) / 16 + 1), bias = om->bias_b;
+  auto s_of = [&](int x, int k) -> int {
+    if (x >= 29 || k > M) return -128;
+    return std::min(127, std::max(-128, bias - rbv_at(om, Q, x, k)));
+  };
+  auto sm16 = [](int v) -> uint32_t { return v < 0 ? 0x8000u | (uint32_t) (-v) : (uint32_t) v; };
+  const int CF = C - CI, Q4 = CF / 4, R = CF % 4, NO = CI / 8, HALF = (CI % 8) / 4;
+  const size_t a_words = (size_t) NRES * Q4 * G * 4, b_words = (R >= 2) ? (size_t) NRES * G * 2 : 0;
+  const size_t c_words = (R & 1) ? (size_t) NRES * G : 0, d_words = (size_t) NRES * NO * G * 4;
+  std::vector<uint32_t> st(a_words + b_words + c_words + d_words + (size_t) NRES * HALF * G * 2);
+  for (int x = 0; x < NRES; ++x)
+    for (int g = 0; g < G; ++g) {
+      auto k_of = [&](int w, int h) { return g * 2 * C + h * C + w + 1; };
+      for (int w = 0; w < CF; ++w) {
+        const uint32_t v = sm16(s_of(x, k_of(w, 0))) | (sm16(s_of(x, k_of(w, 1))) << 16);
+        size_t i;
+        if (w < 4 * Q4)                     i = (((size_t) x * Q4 + w / 4) * G + g) * 4 + (w % 4);
+        else if (R >= 2 && w < 4 * Q4 + 2) i = a_words + ((size_t) x * G + g) * 2 + (w - 4 * Q4);
+        else                                i = a_words + b_words + (size_t) x * G + g;
+        st[i] = v;
+      }
+      auto t = [&](int ww, int h) { return (uint32_t) (s_of(x, k_of(ww, h)) + 128); };
+      auto tword = [&](int w) { return t(w, 0) | (t(w + 1, 0) << 8) | (t(w, 1) << 16) | (t(w + 1, 1) << 24); };
+      for (int o = 0; o < NO; ++o)
+        for (int k = 0; k < 4; ++k)
+          st[a_words + b_words + c_words + (((size_t) x * NO + o) * G + g) * 4 + k] = tword(CF + 8 * o + 2 * k);
+      for (int k = 0; k < 2 * HALF; ++k)
+        st[a_words + b_words + c_words + d_words + ((size_t) x * G + g) * 2 + k] = tword(CF + 8 * NO + 2 * k);
+    }
+  return st;
+}
+
+extern "C" int msvgb_profile_set_ssv_int8_words(msvgb_profile *p, const msvgb_om *om, int words) {
+  if (!p || !om) return fail(MSVGB_eslEINVAL, "NULL argument");
+  if (om->M != p->M) return fail(MSVGB_eslEINVAL, "om does not match the profile");
+  if (p->G == 32 || !p->d_stab_g) return fail(MSVGB_eslEINVAL, "8-bit SSV words need 16 or 8 lanes per sequence");
+  if (words == p->CI) return MSVGB_eslOK;
+  if (words != 0 && !hyb_compiled(p->Cg, p->G, words))
+    return fail(MSVGB_eslEINVAL, "no mixed-width SSV kernel for this model length, lane count and word count");
+  const std::vector<uint32_t> st = words ? build_hyb_table(om, p->Cg, p->G, words)
+                                         : build_group_table(om, p->Cg, p->G);
+  CUDA_TRY(cudaSetDevice(p->device));
+  uint32_t *d = nullptr;
+  CUDA_TRY(cudaMalloc(&d, st.size() * 4));
+  cudaError_t e = cudaMemcpy(d, st.data(), st.size() * 4, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) { cudaFree(d); return fail(MSVGB_eslESYS, cudaGetErrorString(e)); }
+  cudaFree(p->d_stab_g);
+  p->d_stab_g = d; p->CI = words;
+  return MSVGB_eslOK;
+}
+
+extern "C" int msvgb_profile_ssv_int8_words(const msvgb_profile *p) { return p ? p->CI : -1; }
 
 // ------------------------------------------------------------------------------
 // per-length tables: tjb_b(L) and the smallest xJ that passes F1 at length L
@@ -799,7 +886,7 @@ extern "C" int msvgb_search_device(msvgb_ctx *c, const msvgb_profile *pc, const 
     CUDA_TRY(cudaEventRecord(c->ev_join, c->side));
   }
   if (n_long < db->n) {
-    CUDA_TRY(dispatch_group(p->Cg, p->G, g, c->num_sms));
+    CUDA_TRY(dispatch_group(p->Cg, p->G, p->CI, g, c->num_sms));
     count_launch();
   }
   ProfDev Pb;

@@ -67,21 +67,23 @@ __device__ __forceinline__ void ssv_row_group(uint32_t (&dp)[C], uint32_t &acc0,
 // the bits with integer instructions (ALU pipe) instead of f16 maxima (FMA
 // pipe).
 //
-// Layout for residue x (CF = C - CI f16 words, CI a multiple of 8): the f16
+// Layout for residue x (CF = C - CI f16 words, CI a multiple of 4): the f16
 // regions of GroupLayout<CF, G> (quads, pair, single), then 16-byte octets
-// [x][o][g][4 words]: word k of octet o of lane g holds the bytes
+// [x][o][g][4 words], then, when CI % 8 == 4, one 8-byte half octet
+// [x][g][2 words]: word k of octet o of lane g holds the bytes
 // [t(w, h0), t(w+1, h0), t(w, h1), t(w+1, h1)] of DP words w = CF + 8o + 2k
-// and w + 1.
+// and w + 1 (the half octet: w = CF + 8 * NO + 2k).
 template <int C, int CI, int G>
 struct HybLayout {
-  static_assert(CI % 8 == 0 && CI >= 8 && CI <= C, "8-bit words come in octets");
+  static_assert(CI % 4 == 0 && CI >= 4 && CI <= C, "8-bit words come in fours");
   static constexpr int CF = C - CI;
-  static constexpr int Q4 = CF / 4, R = CF % 4, NO = CI / 8;
+  static constexpr int Q4 = CF / 4, R = CF % 4, NO = CI / 8, HALF = (CI % 8) / 4;
   static constexpr int A_WORDS = NRES * Q4 * G * 4;
   static constexpr int B_WORDS = (R >= 2) ? NRES * G * 2 : 0;
   static constexpr int C_WORDS = (R & 1) ? NRES * G : 0;
   static constexpr int D_WORDS = NRES * NO * G * 4;
-  static constexpr int WORDS = A_WORDS + B_WORDS + C_WORDS + D_WORDS;
+  static constexpr int E_WORDS = NRES * HALF * G * 2;
+  static constexpr int WORDS = A_WORDS + B_WORDS + C_WORDS + D_WORDS + E_WORDS;
 };
 
 __device__ __forceinline__ uint32_t add_f16x2(uint32_t a, uint32_t b) {
@@ -115,6 +117,15 @@ __device__ __forceinline__ void ssv_row_hyb(uint32_t (&dp)[C], uint32_t &acc,
     for (int k = 0; k < 4; ++k) {
       s[CF + 8 * o + 2 * k]     = add_f16x2(prmt(tw[k], 0u, 0x4240u), m128);   // bytes 0, 2
       s[CF + 8 * o + 2 * k + 1] = add_f16x2(prmt(tw[k], 0u, 0x4341u), m128);   // bytes 1, 3
+    }
+  }
+  if constexpr (Lay::HALF) {
+    const uint2 v = *reinterpret_cast<const uint2 *>(td + Lay::D_WORDS + (x * G + glane) * 2);
+    const uint32_t tw[2] = {v.x, v.y};
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      s[CF + 8 * Lay::NO + 2 * k]     = add_f16x2(prmt(tw[k], 0u, 0x4240u), m128);
+      s[CF + 8 * Lay::NO + 2 * k + 1] = add_f16x2(prmt(tw[k], 0u, 0x4341u), m128);
     }
   }
   const uint32_t pred0 = pred_word0(dp[C - 1], src_lane);
@@ -247,7 +258,7 @@ __device__ __forceinline__ void ssv_group_loop(const ProfDev &P, const uint32_t 
 // ticket); undecided sequences go to a global list for the full-MSV launch.
 // Table words of the lane-group SSV pass: f16 (CI = 0) or mixed width.
 template <int C, int G, int CI>
-constexpr int group_table_words() {
+__host__ __device__ constexpr int group_table_words() {
   if constexpr (CI > 0) return HybLayout<C, CI, G>::WORDS;
   else return GroupLayout<C, G>::WORDS;
 }

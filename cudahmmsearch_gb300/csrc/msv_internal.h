@@ -78,7 +78,8 @@ struct msvgb_profile {
   int G = 32;                         // lanes per sequence in the SSV pass (32: fused kernel)
   bool lanes_auto = false;            // G chosen by msvgb_profile_create (small searches then use 32)
   int Cg = 0;                         // DP words per lane of the G-lane table
-  uint32_t *d_stab_g = nullptr;       // f16 SSV table in the G-lane layout
+  int CI = 0;                         // of those, words whose costs are bytes (mixed-width table); 0: all f16
+  uint32_t *d_stab_g = nullptr;       // SSV table in the G-lane layout (GroupLayout, or HybLayout when CI > 0)
   std::vector<LenTables *> tables;    // one per F1 value used
   std::mutex tables_mu;
 };
@@ -121,8 +122,14 @@ int xjmin_for(const msvgb_profile *p, int L, double F1);
 int profile_build_width(msvgb_ctx *ctx, const msvgb_om *om, int want_f16, int force_C, msvgb_profile **ret);
 // Host images of the device cost tables of a profile at DP width C.
 int build_cost_tables(const msvgb_om *om, int f16, int C, std::vector<uint32_t> &st, std::vector<uint32_t> &mt);
-// Launches the G-lane SSV pass (msv_group.cuh).
-cudaError_t dispatch_group(int C, int G, const msvgb::GroupArgs &a, int sms);
+// Launches the G-lane SSV pass (msv_group.cuh); CI > 0: the mixed-width table.
+cudaError_t dispatch_group(int C, int G, int CI, const msvgb::GroupArgs &a, int sms);
+// Default 8-bit words per lane of the G-lane SSV pass at DP width C (0: f16 only).
+int hyb_default_words(int C, int G);
+// Whether a mixed-width lane-group kernel is compiled for (C, G, CI).
+bool hyb_compiled(int C, int G, int CI);
+// Mixed-width lane-group SSV table (HybLayout<C, CI, G>, msv_group.cuh).
+std::vector<uint32_t> build_hyb_table(const msvgb_om *om, int C, int G, int CI);
 // Per-length tjb_b and pass-threshold tables of (profile, database, F1), cached in the profile.
 int ensure_tables(msvgb_profile *p, const msvgb_db *db, double F1, LenTables **out);
 // Lane-group SSV table of a profile (layout GroupLayout<C, G>, msv_group.cuh).

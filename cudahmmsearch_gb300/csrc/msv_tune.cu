@@ -48,11 +48,13 @@ constexpr int kNC = sizeof(kCand) / sizeof(kCand[0]);
 constexpr int kNV = kNB + 1;                                // values per candidate: bins, then the mix
 
 // The rule used without a measured table (from the tuner's measurements on
-// GB300): 8 lanes up to M = 479; up to M = 1023, 16 lanes for the length mix
-// and for targets shorter than 600 in the batched kernel, 32 for longer ones;
-// 32 above.
+// GB300): 8 lanes up to M = 511 (the widest 8-lane row, 32 words); up to
+// M = 1023, 16 lanes for the length mix and for targets shorter than 600 in
+// the batched kernel, 32 for longer ones; 32 above. (With the mixed-width
+// table 8 lanes beat 16 at M = 504: 18.0 vs 16.4 TCUPS on 1,000,000
+// sequences; with f16 tables alone, 16.6 vs 16.4.)
 int default_lanes(int M, int lbin) {
-  if (M >= 16 && M < 480) return 8;
+  if (M >= 16 && M < 512) return 8;
   if (M >= 32 && M < 1024 && lbin <= 1) return 16;
   return 32;
 }

@@ -123,6 +123,17 @@ int msvgb_profile_variant(const msvgb_profile *prof);
  * apply. */
 int msvgb_profile_set_lanes(msvgb_profile *prof, const msvgb_om *om, int lanes);
 int msvgb_profile_lanes(const msvgb_profile *prof);
+/* Mixed-width SSV cost table of the 16- or 8-lane pass (no reference
+ * counterpart): the last `words` DP words of every lane (a multiple of 4,
+ * 0 = none) keep their costs as single bytes, widened in registers; the rest
+ * stay 16-bit. Fewer shared-memory bytes per cell, more instructions; results
+ * are identical. eslEINVAL when the profile runs at 32 lanes or no kernel is
+ * compiled for (DP width, lanes, words). msvgb_profile_set_lanes (and so
+ * msvgb_profile_create) sets the default for the model length and lane
+ * count: 4 or 8 words from 10 DP words per lane up, measured 4-10% faster
+ * than all-16-bit costs. */
+int msvgb_profile_set_ssv_int8_words(msvgb_profile *prof, const msvgb_om *om, int words);
+int msvgb_profile_ssv_int8_words(const msvgb_profile *prof);
 
 /* ---- lane-count autotuner (no reference counterpart: the SSE filter has one
  * layout) ------------------------------------------------------------------

@@ -22,7 +22,7 @@ def valid(M, lanes):
 def test_rule_before_tuning():
     ctx = api.Context(0)
     try:
-        for M, want in ((1, 32), (15, 32), (16, 8), (100, 8), (479, 8), (480, 16), (1023, 16), (1024, 32), (3000, 32)):
+        for M, want in ((1, 32), (15, 32), (16, 8), (100, 8), (479, 8), (511, 8), (512, 16), (1023, 16), (1024, 32), (3000, 32)):
             assert ctx.tune_lanes(M)[0] == want, M
         for M, L, want in ((100, 50, 8), (100, 5000, 8), (600, 50, 16), (600, 599, 16), (600, 600, 32),
                            (1023, 149, 16), (1024, 50, 32)):
