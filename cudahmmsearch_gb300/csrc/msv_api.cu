@@ -411,18 +411,21 @@ std::vector<uint32_t> msvgb_detail::build_group_table(const msvgb_om *om, int C,
     uint16_t b; memcpy(&b, &h, 2); return b;
   };
   const int Q4 = C / 4, R = C % 4;
-  const size_t a_words = (size_t) NRES * Q4 * G * 4, b_words = (R >= 2) ? (size_t) NRES * G * 2 : 0;
-  std::vector<uint32_t> st((size_t) NRES * C * G);
+  const int pair = G < 16 ? 16 / G : 1, single = 32 / G;      // region copies (GroupCopies)
+  const size_t a_words = (size_t) NRES * Q4 * G * 4, b_words = (R >= 2) ? (size_t) NRES * pair * G * 2 : 0;
+  std::vector<uint32_t> st((size_t) group_words(C, G, 0));
   for (int x = 0; x < NRES; ++x)
     for (int g = 0; g < G; ++g)
       for (int w = 0; w < C; ++w) {
         const int k0 = g * 2 * C + w + 1, k1 = g * 2 * C + C + w + 1;
         const uint32_t v = f16bits(s_of(x, k0)) | (f16bits(s_of(x, k1)) << 16);
-        size_t i;                                           // GroupLayout<C, G>
-        if (w < 4 * Q4)                     i = (((size_t) x * Q4 + w / 4) * G + g) * 4 + (w % 4);
-        else if (R >= 2 && w < 4 * Q4 + 2) i = a_words + ((size_t) x * G + g) * 2 + (w - 4 * Q4);
-        else                                i = a_words + b_words + (size_t) x * G + g;
-        st[i] = v;
+        if (w < 4 * Q4) {                                   // GroupLayout<C, G>
+          st[(((size_t) x * Q4 + w / 4) * G + g) * 4 + (w % 4)] = v;
+        } else if (R >= 2 && w < 4 * Q4 + 2) {
+          for (int cp = 0; cp < pair; ++cp) st[a_words + (((size_t) x * pair + cp) * G + g) * 2 + (w - 4 * Q4)] = v;
+        } else {
+          for (int cp = 0; cp < single; ++cp) st[a_words + b_words + ((size_t) x * single + cp) * G + g] = v;
+        }
       }
   return st;
 }
@@ -463,19 +466,22 @@ std::vector<uint32_t> msvgb_detail::build_hyb_table(const msvgb_om *om, int C, i
   };
   auto sm16 = [](int v) -> uint32_t { return v < 0 ? 0x8000u | (uint32_t) (-v) : (uint32_t) v; };
   const int CF = C - CI, Q4 = CF / 4, R = CF % 4, NO = CI / 8, HALF = (CI % 8) / 4;
-  const size_t a_words = (size_t) NRES * Q4 * G * 4, b_words = (R >= 2) ? (size_t) NRES * G * 2 : 0;
-  const size_t c_words = (R & 1) ? (size_t) NRES * G : 0, d_words = (size_t) NRES * NO * G * 4;
-  std::vector<uint32_t> st(a_words + b_words + c_words + d_words + (size_t) NRES * HALF * G * 2);
+  const int pair = G < 16 ? 16 / G : 1, single = 32 / G;      // region copies (GroupCopies)
+  const size_t a_words = (size_t) NRES * Q4 * G * 4, b_words = (R >= 2) ? (size_t) NRES * pair * G * 2 : 0;
+  const size_t c_words = (R & 1) ? (size_t) NRES * single * G : 0, d_words = (size_t) NRES * NO * G * 4;
+  std::vector<uint32_t> st((size_t) group_words(C, G, CI));
   for (int x = 0; x < NRES; ++x)
     for (int g = 0; g < G; ++g) {
       auto k_of = [&](int w, int h) { return g * 2 * C + h * C + w + 1; };
       for (int w = 0; w < CF; ++w) {
         const uint32_t v = sm16(s_of(x, k_of(w, 0))) | (sm16(s_of(x, k_of(w, 1))) << 16);
-        size_t i;
-        if (w < 4 * Q4)                     i = (((size_t) x * Q4 + w / 4) * G + g) * 4 + (w % 4);
-        else if (R >= 2 && w < 4 * Q4 + 2) i = a_words + ((size_t) x * G + g) * 2 + (w - 4 * Q4);
-        else                                i = a_words + b_words + (size_t) x * G + g;
-        st[i] = v;
+        if (w < 4 * Q4) {
+          st[(((size_t) x * Q4 + w / 4) * G + g) * 4 + (w % 4)] = v;
+        } else if (R >= 2 && w < 4 * Q4 + 2) {
+          for (int cp = 0; cp < pair; ++cp) st[a_words + (((size_t) x * pair + cp) * G + g) * 2 + (w - 4 * Q4)] = v;
+        } else {
+          for (int cp = 0; cp < single; ++cp) st[a_words + b_words + ((size_t) x * single + cp) * G + g] = v;
+        }
       }
       auto t = [&](int ww, int h) { return (uint32_t) (s_of(x, k_of(ww, h)) + 128); };
       auto tword = [&](int w) { return t(w, 0) | (t(w + 1, 0) << 8) | (t(w, 1) << 16) | (t(w + 1, 1) << 24); };
@@ -483,7 +489,9 @@ std::vector<uint32_t> msvgb_detail::build_hyb_table(const msvgb_om *om, int C, i
         for (int k = 0; k < 4; ++k)
           st[a_words + b_words + c_words + (((size_t) x * NO + o) * G + g) * 4 + k] = tword(CF + 8 * o + 2 * k);
       for (int k = 0; k < 2 * HALF; ++k)
-        st[a_words + b_words + c_words + d_words + ((size_t) x * G + g) * 2 + k] = tword(CF + 8 * NO + 2 * k);
+        for (int cp = 0; cp < pair; ++cp)
+          st[a_words + b_words + c_words + d_words + (((size_t) x * pair + cp) * G + g) * 2 + k] =
+              tword(CF + 8 * NO + 2 * k);
     }
   return st;
 }
@@ -750,9 +758,11 @@ int msvgb_detail::db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64
       h_orig[s] = i; h_len[s] = (int32_t) L; h_src[s] = off[i] - off[0]; h_start[s] = pos;
       pos += (L + 15) / 16 * 16;
       if (L >= kLongTarget) db->n_long++;
-      if (s == 0 || h_len[s - 1] != L) db->distinct_len.push_back((int32_t) L);
+      if (s == 0 || h_len[s - 1] != L) { db->distinct_len.push_back((int32_t) L); db->len_count.push_back(0); }
+      db->len_count.back()++;
     }
     std::reverse(db->distinct_len.begin(), db->distinct_len.end());
+    std::reverse(db->len_count.begin(), db->len_count.end());
     e = keep((void **) &db->d_codes, pos + 64);
     if (e == cudaSuccess) e = cudaMemsetAsync(db->d_codes + pos, PAD_CODE, 64, st);
     if (e == cudaSuccess && n) e = cudaMemcpyAsync(db->d_start, h_start.data(), n * 8, cudaMemcpyHostToDevice, st);
@@ -784,6 +794,7 @@ int msvgb_detail::db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64
     for (int L = 0; L <= Lmax; ++L)
       if (hist[L]) {
         db->distinct_len.push_back(L);
+        db->len_count.push_back((int64_t) hist[L]);
         if (L >= kLongTarget) db->n_long += (int64_t) hist[L];
       }
   }
@@ -856,7 +867,13 @@ extern "C" int msvgb_search_device(msvgb_ctx *c, const msvgb_profile *pc, const 
   // Long targets (they sort first) on the 32-lane kernel in a side stream;
   // the rest: the G-lane SSV pass, then the full MSV on the sequences it left
   // undecided. The side stream forks from and joins back into the context's.
-  const int64_t n_long = std::min(db->n_long, db->n);
+  // Targets too long for a lane group to finish within the pass go to 32
+  // lanes: with the longest first, a group's latency only matters beyond
+  // about a third of the rows each group scores on average (SMs x 32 warps x
+  // 32/G groups), and never below kLongTarget residues.
+  const double groups = (double) c->num_sms * 32.0 * (32.0 / p->G);
+  const int t_long = (int) std::min<double>(1e9, std::max<double>(kLongTarget, (double) db->residues / groups / 3.0));
+  const int64_t n_long = std::min(db->count_at_least(t_long), db->n);
   if (c->list_cap < (size_t) db->n) {
     CUDA_TRY(cudaStreamSynchronize(c->stream));            // the old list may still be read
     cudaFree(c->d_list); c->d_list = nullptr; c->list_cap = 0;

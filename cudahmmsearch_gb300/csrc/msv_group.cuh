@@ -16,19 +16,33 @@
 
 namespace msvgb {
 
+// Copies of the 8-byte and 4-byte table regions. A shared-memory access is
+// served in phases of 128 bytes (8 lanes for 16-byte loads, 16 for 8-byte,
+// 32 for 4-byte loads); with 8-byte loads at 8 lanes per group, or 4-byte
+// loads at 8 or 16, one phase holds several groups, each reading its own
+// residue's row, and two rows whose offsets meet on the same banks conflict.
+// Those regions are therefore stored once per group of a phase, each copy on
+// its own banks: group j of the phase reads copy j.
+template <int G> struct GroupCopies {
+  static constexpr int PAIR = G < 16 ? 16 / G : 1;       // 8-byte loads: groups per 16 lanes
+  static constexpr int SINGLE = 32 / G;                   // 4-byte loads: groups per warp
+};
+
 template <int C, int G>
 struct GroupLayout {
   static constexpr int Q4 = C / 4, R = C % 4;
-  static constexpr int A_WORDS = NRES * Q4 * G * 4;              // quads [x][q][g][4]
-  static constexpr int B_WORDS = (R >= 2) ? NRES * G * 2 : 0;    // pair  [x][g][2]
-  static constexpr int C_WORDS = (R & 1) ? NRES * G : 0;         // single [x][g]
-  static constexpr int WORDS = A_WORDS + B_WORDS + C_WORDS;      // == NRES * C * G
+  static constexpr int A_WORDS = NRES * Q4 * G * 4;                                    // quads [x][q][g][4]
+  static constexpr int B_WORDS = (R >= 2) ? NRES * GroupCopies<G>::PAIR * G * 2 : 0;   // pair  [x][copy][g][2]
+  static constexpr int C_WORDS = (R & 1) ? NRES * GroupCopies<G>::SINGLE * G : 0;      // single [x][copy][g]
+  static constexpr int WORDS = A_WORDS + B_WORDS + C_WORDS;
 };
 
 template <int C, int G>
 __device__ __forceinline__ void ssv_row_group(uint32_t (&dp)[C], uint32_t &acc0, uint32_t &acc1,
-                                              const uint32_t *__restrict__ tab, int x, int glane, int src_lane) {
+                                              const uint32_t *__restrict__ tab, int x, int glane, int gidx,
+                                              int src_lane) {
   using Lay = GroupLayout<C, G>;
+  using Cp = GroupCopies<G>;
   constexpr uint32_t one2 = 0x3C003C00u;
   uint32_t s[C];
 #pragma unroll
@@ -37,10 +51,11 @@ __device__ __forceinline__ void ssv_row_group(uint32_t (&dp)[C], uint32_t &acc0,
     s[4 * q] = v.x; s[4 * q + 1] = v.y; s[4 * q + 2] = v.z; s[4 * q + 3] = v.w;
   }
   if constexpr (Lay::R >= 2) {
-    const uint2 v = *reinterpret_cast<const uint2 *>(tab + Lay::A_WORDS + (x * G + glane) * 2);
+    const int cp = gidx % Cp::PAIR;
+    const uint2 v = *reinterpret_cast<const uint2 *>(tab + Lay::A_WORDS + ((x * Cp::PAIR + cp) * G + glane) * 2);
     s[4 * Lay::Q4] = v.x; s[4 * Lay::Q4 + 1] = v.y;
   }
-  if constexpr (Lay::R & 1) s[C - 1] = tab[Lay::A_WORDS + Lay::B_WORDS + x * G + glane];
+  if constexpr (Lay::R & 1) s[C - 1] = tab[Lay::A_WORDS + Lay::B_WORDS + (x * Cp::SINGLE + gidx) * G + glane];
   const uint32_t pred0 = pred_word0(dp[C - 1], src_lane);   // all 32 lanes, every row
 #pragma unroll
   for (int w = C - 1; w >= 0; --w) {
@@ -70,7 +85,7 @@ __device__ __forceinline__ void ssv_row_group(uint32_t (&dp)[C], uint32_t &acc0,
 // Layout for residue x (CF = C - CI f16 words, CI a multiple of 4): the f16
 // regions of GroupLayout<CF, G> (quads, pair, single), then 16-byte octets
 // [x][o][g][4 words], then, when CI % 8 == 4, one 8-byte half octet
-// [x][g][2 words]: word k of octet o of lane g holds the bytes
+// [x][copy][g][2 words] (copies as GroupCopies): word k of octet o of lane g holds the bytes
 // [t(w, h0), t(w+1, h0), t(w, h1), t(w+1, h1)] of DP words w = CF + 8o + 2k
 // and w + 1 (the half octet: w = CF + 8 * NO + 2k).
 template <int C, int CI, int G>
@@ -79,10 +94,10 @@ struct HybLayout {
   static constexpr int CF = C - CI;
   static constexpr int Q4 = CF / 4, R = CF % 4, NO = CI / 8, HALF = (CI % 8) / 4;
   static constexpr int A_WORDS = NRES * Q4 * G * 4;
-  static constexpr int B_WORDS = (R >= 2) ? NRES * G * 2 : 0;
-  static constexpr int C_WORDS = (R & 1) ? NRES * G : 0;
+  static constexpr int B_WORDS = (R >= 2) ? NRES * GroupCopies<G>::PAIR * G * 2 : 0;
+  static constexpr int C_WORDS = (R & 1) ? NRES * GroupCopies<G>::SINGLE * G : 0;
   static constexpr int D_WORDS = NRES * NO * G * 4;
-  static constexpr int E_WORDS = NRES * HALF * G * 2;
+  static constexpr int E_WORDS = NRES * HALF * GroupCopies<G>::PAIR * G * 2;   // [x][copy][g][2]
   static constexpr int WORDS = A_WORDS + B_WORDS + C_WORDS + D_WORDS + E_WORDS;
 };
 
@@ -92,8 +107,10 @@ __device__ __forceinline__ uint32_t add_f16x2(uint32_t a, uint32_t b) {
 
 template <int C, int CI, int G>
 __device__ __forceinline__ void ssv_row_hyb(uint32_t (&dp)[C], uint32_t &acc,
-                                            const uint32_t *__restrict__ tab, int x, int glane, int src_lane) {
+                                            const uint32_t *__restrict__ tab, int x, int glane, int gidx,
+                                            int src_lane) {
   using Lay = HybLayout<C, CI, G>;
+  using Cp = GroupCopies<G>;
   constexpr int CF = Lay::CF;
   constexpr uint32_t one2 = 0x3C003C00u;        // f16x2 (1.0, 1.0)
   constexpr uint32_t m128 = 0x80808080u;        // f16x2 (-128, -128) units of 2^-24
@@ -104,10 +121,11 @@ __device__ __forceinline__ void ssv_row_hyb(uint32_t (&dp)[C], uint32_t &acc,
     s[4 * q] = v.x; s[4 * q + 1] = v.y; s[4 * q + 2] = v.z; s[4 * q + 3] = v.w;
   }
   if constexpr (Lay::R >= 2) {
-    const uint2 v = *reinterpret_cast<const uint2 *>(tab + Lay::A_WORDS + (x * G + glane) * 2);
+    const int cp = gidx % Cp::PAIR;
+    const uint2 v = *reinterpret_cast<const uint2 *>(tab + Lay::A_WORDS + ((x * Cp::PAIR + cp) * G + glane) * 2);
     s[4 * Lay::Q4] = v.x; s[4 * Lay::Q4 + 1] = v.y;
   }
-  if constexpr (Lay::R & 1) s[CF - 1] = tab[Lay::A_WORDS + Lay::B_WORDS + x * G + glane];
+  if constexpr (Lay::R & 1) s[CF - 1] = tab[Lay::A_WORDS + Lay::B_WORDS + (x * Cp::SINGLE + gidx) * G + glane];
   const uint32_t *td = tab + Lay::A_WORDS + Lay::B_WORDS + Lay::C_WORDS;
 #pragma unroll
   for (int o = 0; o < Lay::NO; ++o) {
@@ -120,7 +138,8 @@ __device__ __forceinline__ void ssv_row_hyb(uint32_t (&dp)[C], uint32_t &acc,
     }
   }
   if constexpr (Lay::HALF) {
-    const uint2 v = *reinterpret_cast<const uint2 *>(td + Lay::D_WORDS + (x * G + glane) * 2);
+    const int cp = gidx % Cp::PAIR;
+    const uint2 v = *reinterpret_cast<const uint2 *>(td + Lay::D_WORDS + ((x * Cp::PAIR + cp) * G + glane) * 2);
     const uint32_t tw[2] = {v.x, v.y};
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
@@ -170,7 +189,7 @@ template <int C, int G, int CI = 0, class Fetch, class Undecided>
 __device__ __forceinline__ void ssv_group_loop(const ProfDev &P, const uint32_t *__restrict__ tab, const DbDev &db,
                                                uint8_t *__restrict__ out_xj, uint8_t *__restrict__ out_flags,
                                                Fetch fetch, Undecided undecided) {
-  const int lane = threadIdx.x & 31, glane = lane % G, gbase = lane - glane;
+  const int lane = threadIdx.x & 31, glane = lane % G, gbase = lane - glane, gidx = lane / G;
   const int src_lane = gbase + (glane + G - 1) % G;
   const unsigned gmask = (G == 32) ? FULL : (((1u << G) - 1u) << gbase);
   const int tbm = P.tbm, tec = P.tec, base = P.base, bias = P.bias;
@@ -217,8 +236,8 @@ __device__ __forceinline__ void ssv_group_loop(const ProfDev &P, const uint32_t 
     if (active && i + 4 < L) nextw = __ldg(sq + (i >> 2) + 1);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      if constexpr (CI > 0) ssv_row_hyb<C, CI, G>(dp, acc0, tab, (w4 >> (8 * j)) & 0xFF, glane, src_lane);
-      else                  ssv_row_group<C, G>(dp, acc0, acc1, tab, (w4 >> (8 * j)) & 0xFF, glane, src_lane);
+      if constexpr (CI > 0) ssv_row_hyb<C, CI, G>(dp, acc0, tab, (w4 >> (8 * j)) & 0xFF, glane, gidx, src_lane);
+      else                  ssv_row_group<C, G>(dp, acc0, acc1, tab, (w4 >> (8 * j)) & 0xFF, glane, gidx, src_lane);
     }
     i += 4;
     const bool fin = active && i >= L;
@@ -256,6 +275,13 @@ __device__ __forceinline__ void ssv_group_loop(const ProfDev &P, const uint32_t 
 
 // Stand-alone SSV pass over the sorted sequences [s_begin, n) (global
 // ticket); undecided sequences go to a global list for the full-MSV launch.
+// Table words of a lane-group SSV table at run-time (Cg, G, CI): the layouts
+// above (GroupLayout, or HybLayout when CI > 0) with their region copies.
+__host__ __device__ constexpr int group_words(int Cg, int G, int CI) {
+  return NRES * G * ((Cg - CI) / 4 * 4 + ((Cg - CI) % 4 >= 2 ? 2 * (G < 16 ? 16 / G : 1) : 0) +
+                     (((Cg - CI) % 4) & 1 ? 32 / G : 0) + CI / 8 * 4 + ((CI % 8) / 4) * 2 * (G < 16 ? 16 / G : 1));
+}
+
 // Table words of the lane-group SSV pass: f16 (CI = 0) or mixed width.
 template <int C, int G, int CI>
 __host__ __device__ constexpr int group_table_words() {
@@ -305,6 +331,7 @@ __device__ __forceinline__ void ssv_group_chunk(const ProfDev &P, const uint32_t
 template <int C, int G, int CI = 0>
 cudaError_t launch_ssv_group(const GroupArgs &a, int num_sms) {
   auto kern = msv_ssv_group_kernel<C, G, CI>;
+  static_assert(group_words(C, G, CI) == group_table_words<C, G, CI>(), "host and device table sizes agree");
   constexpr size_t smem = (size_t) group_table_words<C, G, CI>() * 4;
   static std::atomic<unsigned long long> configured{0};
   {

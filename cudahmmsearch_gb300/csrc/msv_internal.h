@@ -93,8 +93,15 @@ struct msvgb_db {
   int64_t *d_start = nullptr, *d_orig = nullptr;
   int32_t *d_len = nullptr;
   std::vector<int32_t> distinct_len;  // sorted ascending
+  std::vector<int64_t> len_count;     // sequences of each distinct length
   uint64_t serial = 0;
   int64_t n_long = 0;                 // sequences of length >= kLongTarget (they sort first)
+  // Sequences of length >= T (they sort first).
+  int64_t count_at_least(int T) const {
+    int64_t c = 0;
+    for (size_t i = distinct_len.size(); i-- > 0 && distinct_len[i] >= T;) c += len_count[i];
+    return c;
+  }
   int64_t packed_bytes = 0;           // size of d_codes
   cudaEvent_t ready = nullptr;        // set when packed asynchronously: completes when the data is in place
   int64_t *d_inv = nullptr;           // original index -> sorted slot, built on first use

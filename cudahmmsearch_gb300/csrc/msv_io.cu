@@ -452,8 +452,13 @@ extern "C" int msvgb_db_load(msvgb_ctx *ctx, const char *path, msvgb_db **ret) {
   db->packed_bytes = h.packed_bytes;
   db->Lmax = h.n ? len[0] : 0;
   db->serial = msvgb_detail::next_db_serial();
-  for (int64_t s = h.n - 1; s >= 0; --s)                        // ascending distinct lengths
-    if (db->distinct_len.empty() || db->distinct_len.back() != len[s]) db->distinct_len.push_back(len[s]);
+  for (int64_t s = h.n - 1; s >= 0; --s) {                      // ascending distinct lengths
+    if (db->distinct_len.empty() || db->distinct_len.back() != len[s]) {
+      db->distinct_len.push_back(len[s]);
+      db->len_count.push_back(0);
+    }
+    db->len_count.back()++;
+  }
   db->n_long = std::partition_point(len.begin(), len.end(), [](int32_t L) { return L >= kLongTarget; }) - len.begin();
   cudaError_t e = cudaSetDevice(ctx->device);
   if (e == cudaSuccess) e = cudaMalloc(&db->d_codes, codes.size());

@@ -144,7 +144,7 @@ def test_mixed_width_rejects_uncompiled_and_32_lanes(ctx):
     dp.set_lanes(8)
     with pytest.raises(api.MSVError):
         dp.set_int8_words(24)          # not compiled for 26 words at 8 lanes
-    dp.set_int8_words(16)
+    dp.set_int8_words(12)
     dp.set_lanes(8)
     assert dp.int8_words == 8          # set_lanes restores the default share (26 words per lane: 8)
     dp.set_int8_words(0)
