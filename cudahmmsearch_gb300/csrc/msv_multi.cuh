@@ -95,9 +95,10 @@ struct ChunkShared {
   uint16_t und[kChunkMaxSeqs];
 };
 
-// Words of a profile's SSV table in shared memory (the MSV table follows it).
+// Words of a profile's SSV table in shared memory (the MSV table follows it):
+// the lane-group layout with its region copies (group_words), or the 32-lane one.
 __host__ __device__ inline int ssv_words(const ProfDev &P) {
-  return P.G < 32 ? NRES * P.Cg * P.G : NRES * P.C * 32;
+  return P.G < 32 ? group_words(P.Cg, P.G, 0) : NRES * P.C * 32;
 }
 
 // One CTA scores the sorted sequences [s0, s0 + nseq) against P, whose tables
