@@ -698,9 +698,9 @@ def main():
 
     # e2e through the public API from pinned host buffers
     codes_pin = torch.from_numpy(s.codes).pin_memory()
-    off_np = s.off
+    off_pin = torch.from_numpy(s.off).pin_memory()
     e2e_times, e2e_parts = [], []
-    seqset = F.SeqSet(codes_pin.numpy(), off_np)
+    seqset = F.SeqSet(codes_pin.numpy(), off_pin.numpy())
     for i in range(args.e2e_steps + 1 if args.e2e_steps > 0 else 0):
         torch.cuda.synchronize()
         t = time.perf_counter()
@@ -766,8 +766,9 @@ def main():
                            pass_fraction=float(((fl_all & api.FLAG_PASS) != 0).mean())),
             "e2e": {"value": e2e_val, "unit": "GCUPS", "h2d_bytes_per_step": int(s.total + 28 * s.n),
                     "d2h_bytes_per_step": int(2 * s.n),
-                    "path": "msvgb_search_host from pinned host memory: residues and per-sequence start/orig/"
-                            "src/len metadata uploaded and packed in chunks on a second stream under the search",
+                    "path": "msvgb_search_host from pinned host memory (residues and offsets): every chunk's "
+                            "lengths sorted on the GPU first, then per chunk its residues copied (under the "
+                            "previous chunk's search), packed and searched",
                     "separate_calls": e2e_parts[-1] if e2e_parts else None,
                     "steps_ms": [round(t * 1e3, 2) for t in e2e_times], "statistic": "median of the timed steps"},
             "gpu_launches": int(launches), "clocks": clocks, "roofline": roofline, "parity": parity}

@@ -682,11 +682,14 @@ int msvgb_detail::db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64
   if (e == cudaSuccess) e = alloc((void **) &d_len_in, (size_t) n1 * 4, st);
   if (e == cudaSuccess) e = alloc((void **) &d_scal, 16, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(d_off, off, (size_t) (n + 1) * 8, cudaMemcpyHostToDevice, st);
+  const bool defer = a && a->defer_residues;
   if (e == cudaSuccess) e = cudaEventRecord(ev_raw, st);
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->dma, ev_raw, 0);
-  if (e == cudaSuccess) e = alloc((void **) &d_raw, (size_t) total, ctx->dma);
-  if (e == cudaSuccess && total) e = cudaMemcpyAsync(d_raw, codes + off[0], total, cudaMemcpyHostToDevice, ctx->dma);
-  if (e == cudaSuccess) e = cudaEventRecord(ev_raw, ctx->dma);
+  if (!defer) {
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->dma, ev_raw, 0);
+    if (e == cudaSuccess) e = alloc((void **) &d_raw, (size_t) total, ctx->dma);
+    if (e == cudaSuccess && total) e = cudaMemcpyAsync(d_raw, codes + off[0], total, cudaMemcpyHostToDevice, ctx->dma);
+    if (e == cudaSuccess) e = cudaEventRecord(ev_raw, ctx->dma);
+  }
   pt.mark("copies issued");
   if (e == cudaSuccess && ctx->h_pin_cap < 64) e = grow_pinned(ctx, 64);
   unsigned *misc = (unsigned *) ctx->h_pin;
@@ -726,7 +729,8 @@ int msvgb_detail::db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64
     return cudaMallocFromPoolAsync(ptr, std::max<size_t>(bytes, 16), pool, st);
   };
   int64_t *d_src = nullptr;
-  e = alloc((void **) &d_src, (size_t) n1 * 8, st);
+  e = defer ? keep((void **) &d_src, (size_t) n1 * 8) : alloc((void **) &d_src, (size_t) n1 * 8, st);
+  if (e == cudaSuccess && defer) db->d_src_pending = d_src;
   if (e == cudaSuccess) e = keep((void **) &db->d_start, (size_t) n1 * 8);
   if (e == cudaSuccess) e = keep((void **) &db->d_orig, (size_t) n1 * 8);
   if (e == cudaSuccess) e = keep((void **) &db->d_len, (size_t) n1 * 4);
@@ -779,8 +783,9 @@ int msvgb_detail::db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64
   if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev_raw, 0);
   if (trace_on() && e == cudaSuccess) { e = cudaStreamSynchronize(st); pt.mark("residues up"); }
   if (e == cudaSuccess && !a) e = cudaMemsetAsync(d_bad, 0, sizeof(int), st);
-  if (e == cudaSuccess) e = launch_pack(d_raw, d_src, db->d_start, db->d_len, n, db->d_codes, d_bad,
-                                        ctx->num_sms, st);
+  if (e == cudaSuccess && !defer) e = launch_pack(d_raw, d_src, db->d_start, db->d_len, n, db->d_codes, d_bad,
+                                                  ctx->num_sms, st);
+  if (defer) { db->raw_begin = n ? off[0] : 0; db->raw_total = total; db->d_bad_pending = d_bad; }
   if (e == cudaSuccess) { h_scal[0] = 0; h_scal[1] = pos; }
   if (e == cudaSuccess && !a) e = cudaMemcpyAsync(h_scal, d_bad, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess && gpu_sort) e = cudaMemcpyAsync(h_scal + 1, d_scal + 1, 8, cudaMemcpyDeviceToHost, st);
@@ -800,7 +805,7 @@ int msvgb_detail::db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64
   }
   db->packed_bytes = pos + 64;
   if (e == cudaSuccess && a) e = cudaEventCreateWithFlags(&db->ready, cudaEventDisableTiming);
-  if (e == cudaSuccess && a) e = cudaEventRecord(db->ready, st);
+  if (e == cudaSuccess && a && !defer) e = cudaEventRecord(db->ready, st);
   if (e == cudaSuccess && n) count_launch();
   if (e != cudaSuccess) {
     cudaStreamSynchronize(st);
@@ -817,10 +822,38 @@ int msvgb_detail::db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64
   return MSVGB_eslOK;
 }
 
+int msvgb_detail::db_fill_on(msvgb_ctx *ctx, msvgb_db *db, const uint8_t *codes, cudaStream_t st) {
+  if (!db->d_src_pending) return fail(MSVGB_eslEINVAL, "database residues already in place");
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  cudaMemPool_t pool = scratch_pool(ctx->device);
+  if (!pool) return fail(MSVGB_eslESYS, "database upload: no memory pool");
+  uint8_t *d_raw = nullptr;
+  cudaEvent_t ev = nullptr;
+  CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  // the copy waits for nothing on st: the sorted placement it feeds was
+  // completed (and waited for) when the database was created
+  cudaError_t e = cudaMallocFromPoolAsync((void **) &d_raw, std::max<size_t>((size_t) db->raw_total, 16), pool, ctx->dma);
+  if (e == cudaSuccess && db->raw_total)
+    e = cudaMemcpyAsync(d_raw, codes + db->raw_begin, db->raw_total, cudaMemcpyHostToDevice, ctx->dma);
+  if (e == cudaSuccess) e = cudaEventRecord(ev, ctx->dma);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev, 0);
+  if (e == cudaSuccess) e = launch_pack(d_raw, db->d_src_pending, db->d_start, db->d_len, db->n, db->d_codes,
+                                        db->d_bad_pending, ctx->num_sms, st);
+  if (e == cudaSuccess) e = cudaFreeAsync(d_raw, st);
+  if (e == cudaSuccess) e = cudaFreeAsync(db->d_src_pending, st);
+  if (e == cudaSuccess) e = cudaEventRecord(db->ready, st);
+  cudaEventDestroy(ev);
+  if (e != cudaSuccess) return fail(MSVGB_eslESYS, std::string("database upload: ") + cudaGetErrorString(e));
+  db->d_src_pending = nullptr;
+  count_launch();
+  return MSVGB_eslOK;
+}
+
 extern "C" int msvgb_db_destroy(msvgb_db *db) {
   if (!db) return MSVGB_eslOK;
   cudaSetDevice(db->device);
   cudaFree(db->d_codes); cudaFree(db->d_start); cudaFree(db->d_orig); cudaFree(db->d_len);
+  cudaFree(db->d_src_pending);
   if (db->ready) cudaEventDestroy(db->ready);
   cudaFree(db->d_inv);
   delete db;
@@ -976,16 +1009,25 @@ extern "C" int msvgb_search_host(msvgb_ctx *c, const msvgb_profile *p, const uin
   std::vector<msvgb_db *> dbs;
   int st = MSVGB_eslOK;
   PhaseTimer pt;
+  // Every chunk's lengths are sorted first, while the GPU is otherwise idle
+  // (sorting a chunk while the previous chunk's persistent search holds every
+  // SM would wait for that search). Then chunk by chunk: its residues go up
+  // on the copy engine (the next chunk's copy runs under this chunk's
+  // search) and are packed, and it is searched.
   for (size_t k = 0; k + 1 < cut.size() && st == MSVGB_eslOK; ++k) {
     const int64_t b0 = cut[k], b1 = cut[k + 1];
     msvgb_db *db = nullptr;
-    const AsyncPack a{d_bad};
+    AsyncPack a{d_bad};
+    a.defer_residues = true;
     st = db_create_on(c, codes, off + b0, b1 - b0, c->upload, &db, &a);
+    if (st == MSVGB_eslOK) dbs.push_back(db);
+  }
+  pt.mark("search_host: chunks sorted");
+  for (size_t k = 0; k < dbs.size() && st == MSVGB_eslOK; ++k) {
+    const int64_t b0 = cut[k];
+    st = db_fill_on(c, dbs[k], codes, c->upload);
+    if (st == MSVGB_eslOK) st = msvgb_search_device(c, p, dbs[k], F1, d + b0, d + n + b0);
     pt.mark("search_host: chunk enqueued");
-    if (st == MSVGB_eslOK) {
-      dbs.push_back(db);
-      st = msvgb_search_device(c, p, db, F1, d + b0, d + n + b0);
-    }
   }
   int bad = 0;
   if (st == MSVGB_eslOK) {

@@ -104,6 +104,11 @@ struct msvgb_db {
   }
   int64_t packed_bytes = 0;           // size of d_codes
   cudaEvent_t ready = nullptr;        // set when packed asynchronously: completes when the data is in place
+  // Between a deferred creation and db_fill_on: where the residues go
+  // (scatter offsets, pool memory) and where they come from.
+  int64_t *d_src_pending = nullptr;
+  int64_t raw_begin = 0, raw_total = 0;
+  int *d_bad_pending = nullptr;
   int64_t *d_inv = nullptr;           // original index -> sorted slot, built on first use
 };
 
@@ -158,7 +163,15 @@ int batch_create(msvgb_ctx *ctx, const msvgb_om *const *oms, int nprof, const ms
 // Asynchronous packing of one chunk (db_create_on).
 struct AsyncPack {
   int *d_bad;      // device flag: set if a residue code is >= 29
+  // Sort only: the residues are not copied or packed now but by db_fill_on,
+  // which a search of the database must follow (db->ready is recorded then).
+  bool defer_residues = false;
 };
+// The residue copy and packing of a database created with defer_residues:
+// the raw residues of codes (the same buffer and offsets as at creation) go
+// up on the context's dma stream and are packed on stream st; db->ready then
+// completes when the database is in place.
+int db_fill_on(msvgb_ctx *ctx, msvgb_db *db, const uint8_t *codes, cudaStream_t st);
 // msvgb_db_create on stream st; with a, asynchronous (see msv_api.cu).
 int db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64_t *off, int64_t n, cudaStream_t st,
                  msvgb_db **ret, const AsyncPack *a = nullptr);
