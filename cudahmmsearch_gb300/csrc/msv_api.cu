@@ -865,20 +865,6 @@ extern "C" int64_t msvgb_db_residues(const msvgb_db *db) { return db ? db->resid
 // ------------------------------------------------------------------------------
 // search
 
-static int launch_one(msvgb_ctx *c, const msvgb_profile *p, const DbDev &dbv, const uint8_t *d_tjb,
-                      const uint8_t *d_xjmin, uint8_t *d_xj, uint8_t *d_flags, int skip_empty = 1) {
-  ProfDev P;
-  P.M = p->M; P.C = p->C; P.tbm = p->tbm; P.tec = p->tec; P.base = p->base; P.bias = p->bias;
-  P.stab = p->d_stab; P.mtab = p->d_mtab; P.tjb = d_tjb; P.xjmin = d_xjmin; P.ssv_f16 = p->f16;
-  LaunchArgs a;
-  a.P = P; a.db = dbv; a.out_xj = d_xj; a.out_flags = d_flags; a.ticket = c->d_ticket;
-  a.stream = c->stream; a.grid = 0; a.skip_empty = skip_empty;
-  CUDA_TRY(cudaMemsetAsync(c->d_ticket, 0, sizeof(unsigned long long), c->stream));
-  CUDA_TRY(dispatch(p->C, p->f16 != 0, a, c->num_sms));
-  g_launches.fetch_add(1);
-  return MSVGB_eslOK;
-}
-
 extern "C" int msvgb_search_device(msvgb_ctx *c, const msvgb_profile *pc, const msvgb_db *db, double F1,
                                    void *d_xj, void *d_flags) {
   if (!c || !pc || !db || (!d_xj && db->n) || (!d_flags && db->n)) return fail(MSVGB_eslEINVAL, "NULL argument");
@@ -890,64 +876,78 @@ extern "C" int msvgb_search_device(msvgb_ctx *c, const msvgb_profile *pc, const 
   int st = ensure_tables(p, db, F1, &t);
   if (st != MSVGB_eslOK) return st;
   if (db->ready) CUDA_TRY(cudaStreamWaitEvent(c->stream, db->ready, 0));   // still being packed
-  DbDev dbv{db->d_codes, db->d_start, db->d_len, db->d_orig, db->n};
-  // Lane groups lengthen each sequence's latency (2-4x): below ~40 G cells the
-  // launch tail they add outweighs their throughput, unless lanes were set
-  // explicitly.
-  const bool small = p->lanes_auto && (double) p->M * (double) db->residues < 4e10;
-  if (p->G == 32 || !p->d_stab_g || small)
-    return launch_one(c, p, dbv, t->d_tjb, t->d_xjmin, (uint8_t *) d_xj, (uint8_t *) d_flags);
-  // Long targets (they sort first) on the 32-lane kernel in a side stream;
-  // the rest: the G-lane SSV pass, then the full MSV on the sequences it left
-  // undecided. The side stream forks from and joins back into the context's.
-  // Targets too long for a lane group to finish within the pass go to 32
-  // lanes: with the longest first, a group's latency only matters beyond
-  // about a third of the rows each group scores on average (SMs x 32 warps x
-  // 32/G groups), and never below kLongTarget residues.
-  const double groups = (double) c->num_sms * 32.0 * (32.0 / p->G);
-  const int t_long = (int) std::min<double>(1e9, std::max<double>(kLongTarget, (double) db->residues / groups / 3.0));
-  const int64_t n_long = std::min(db->count_at_least(t_long), db->n);
   if (c->list_cap < (size_t) db->n) {
     CUDA_TRY(cudaStreamSynchronize(c->stream));            // the old list may still be read
     cudaFree(c->d_list); c->d_list = nullptr; c->list_cap = 0;
     CUDA_TRY(cudaMalloc(&c->d_list, sizeof(int64_t) * db->n));
     c->list_cap = db->n;
   }
+  SearchScratch sc;
+  sc.stream = c->stream; sc.side = c->side; sc.ev_fork = c->ev_fork; sc.ev_join = c->ev_join;
+  sc.ticket = c->d_ticket; sc.aux = c->d_aux; sc.list = c->d_list;
+  return enqueue_search(sc, p, db, t, (uint8_t *) d_xj, (uint8_t *) d_flags, c->num_sms);
+}
+
+int msvgb_detail::enqueue_search(const SearchScratch &sc, const msvgb_profile *p, const msvgb_db *db,
+                                 const LenTables *t, uint8_t *d_xj, uint8_t *d_flags, int num_sms) {
+  DbDev dbv{db->d_codes, db->d_start, db->d_len, db->d_orig, db->n};
+  ProfDev P32;
+  P32.M = p->M; P32.C = p->C; P32.tbm = p->tbm; P32.tec = p->tec; P32.base = p->base; P32.bias = p->bias;
+  P32.stab = p->d_stab; P32.mtab = p->d_mtab; P32.tjb = t->d_tjb; P32.xjmin = t->d_xjmin; P32.ssv_f16 = p->f16;
+  // Lane groups lengthen each sequence's latency (2-4x): below ~40 G cells the
+  // launch tail they add outweighs their throughput, unless lanes were set
+  // explicitly.
+  const bool small = p->lanes_auto && (double) p->M * (double) db->residues < 4e10;
+  if (p->G == 32 || !p->d_stab_g || small) {
+    LaunchArgs a;
+    a.P = P32; a.db = dbv; a.out_xj = d_xj; a.out_flags = d_flags; a.ticket = sc.ticket;
+    a.stream = sc.stream; a.grid = 0; a.skip_empty = 1;
+    CUDA_TRY(cudaMemsetAsync(sc.ticket, 0, sizeof(unsigned long long), sc.stream));
+    CUDA_TRY(dispatch(p->C, p->f16 != 0, a, num_sms));
+    count_launch();
+    return MSVGB_eslOK;
+  }
+  // Long targets (they sort first) on the 32-lane kernel, in the side stream
+  // when there is one; the rest: the G-lane SSV pass, then the full MSV on the
+  // sequences it left undecided. The side stream forks from and joins back
+  // into the search's. Targets too long for a lane group to finish within the
+  // pass go to 32 lanes: with the longest first, a group's latency only
+  // matters beyond about a third of the rows each group scores on average
+  // (SMs x 32 warps x 32/G groups), and never below kLongTarget residues.
+  const double groups = (double) num_sms * 32.0 * (32.0 / p->G);
+  const int t_long = (int) std::min<double>(1e9, std::max<double>(kLongTarget, (double) db->residues / groups / 3.0));
+  const int64_t n_long = std::min(db->count_at_least(t_long), db->n);
   ProfDev P;
   P.M = p->M; P.C = p->Cg; P.tbm = p->tbm; P.tec = p->tec; P.base = p->base; P.bias = p->bias;
   P.stab = p->d_stab_g; P.mtab = p->d_mtab; P.tjb = t->d_tjb; P.xjmin = t->d_xjmin; P.ssv_f16 = 1;
   GroupArgs g;
-  g.P = P; g.db = dbv; g.out_xj = (uint8_t *) d_xj; g.out_flags = (uint8_t *) d_flags;
-  g.ticket = c->d_ticket; g.undecided = c->d_list; g.n_undecided = c->d_aux + 1; g.stream = c->stream;
+  g.P = P; g.db = dbv; g.out_xj = d_xj; g.out_flags = d_flags;
+  g.ticket = sc.ticket; g.undecided = sc.list; g.n_undecided = sc.aux + 1; g.stream = sc.stream;
   g.s_begin = n_long;
-  CUDA_TRY(cudaMemsetAsync(c->d_ticket, 0, sizeof(unsigned long long), c->stream));
-  CUDA_TRY(cudaMemsetAsync(c->d_aux, 0, 3 * sizeof(unsigned long long), c->stream));
+  CUDA_TRY(cudaMemsetAsync(sc.ticket, 0, sizeof(unsigned long long), sc.stream));
+  CUDA_TRY(cudaMemsetAsync(sc.aux, 0, 3 * sizeof(unsigned long long), sc.stream));
   if (n_long > 0) {
     LaunchArgs l;
-    l.P = ProfDev{};
-    l.P.M = p->M; l.P.C = p->C; l.P.tbm = p->tbm; l.P.tec = p->tec; l.P.base = p->base; l.P.bias = p->bias;
-    l.P.stab = p->d_stab; l.P.mtab = p->d_mtab; l.P.tjb = t->d_tjb; l.P.xjmin = t->d_xjmin; l.P.ssv_f16 = p->f16;
-    l.db = dbv; l.out_xj = (uint8_t *) d_xj; l.out_flags = (uint8_t *) d_flags; l.ticket = c->d_aux + 2;
-    l.stream = c->side; l.grid = 0; l.skip_empty = 1; l.range_end = n_long;
-    CUDA_TRY(cudaEventRecord(c->ev_fork, c->stream));
-    CUDA_TRY(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
-    CUDA_TRY(dispatch(p->C, p->f16 != 0, l, c->num_sms));
+    l.P = P32; l.db = dbv; l.out_xj = d_xj; l.out_flags = d_flags; l.ticket = sc.aux + 2;
+    l.stream = sc.side ? sc.side : sc.stream; l.grid = 0; l.skip_empty = 1; l.range_end = n_long;
+    if (sc.side) {
+      CUDA_TRY(cudaEventRecord(sc.ev_fork, sc.stream));
+      CUDA_TRY(cudaStreamWaitEvent(sc.side, sc.ev_fork, 0));
+    }
+    CUDA_TRY(dispatch(p->C, p->f16 != 0, l, num_sms));
     count_launch();
-    CUDA_TRY(cudaEventRecord(c->ev_join, c->side));
+    if (sc.side) CUDA_TRY(cudaEventRecord(sc.ev_join, sc.side));
   }
   if (n_long < db->n) {
-    CUDA_TRY(dispatch_group(p->Cg, p->G, p->CI, g, c->num_sms));
+    CUDA_TRY(dispatch_group(p->Cg, p->G, p->CI, g, num_sms));
     count_launch();
   }
-  ProfDev Pb;
-  Pb.M = p->M; Pb.C = p->C; Pb.tbm = p->tbm; Pb.tec = p->tec; Pb.base = p->base; Pb.bias = p->bias;
-  Pb.stab = p->d_stab; Pb.mtab = p->d_mtab; Pb.tjb = t->d_tjb; Pb.xjmin = t->d_xjmin; Pb.ssv_f16 = p->f16;
   LaunchArgs a;
-  a.P = Pb; a.db = dbv; a.out_xj = (uint8_t *) d_xj; a.out_flags = (uint8_t *) d_flags; a.ticket = c->d_aux;
-  a.stream = c->stream; a.grid = 0; a.skip_empty = 1; a.list = c->d_list; a.list_count = c->d_aux + 1;
-  CUDA_TRY(dispatch(p->C, p->f16 != 0, a, c->num_sms));
+  a.P = P32; a.db = dbv; a.out_xj = d_xj; a.out_flags = d_flags; a.ticket = sc.aux;
+  a.stream = sc.stream; a.grid = 0; a.skip_empty = 1; a.list = sc.list; a.list_count = sc.aux + 1;
+  CUDA_TRY(dispatch(p->C, p->f16 != 0, a, num_sms));
   count_launch();
-  if (n_long > 0) CUDA_TRY(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
+  if (n_long > 0 && sc.side) CUDA_TRY(cudaStreamWaitEvent(sc.stream, sc.ev_join, 0));
   return MSVGB_eslOK;
 }
 

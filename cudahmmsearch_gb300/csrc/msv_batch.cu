@@ -94,6 +94,12 @@ struct msvgb_batch {
   cudaGraphExec_t exec = nullptr;
   size_t smem = 0;
   int threads = 256, grid = 0;
+  int nsolo = 0;                        // profiles scored by their own search (single-query kernels)
+  // per branch of those searches: its scratch (ticket, 3 counters, list) and capture stream
+  unsigned long long *d_solo_counters[2] = {nullptr, nullptr};
+  int64_t *d_solo_list[2] = {nullptr, nullptr};
+  cudaStream_t branch[2] = {nullptr, nullptr};
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
 };
 
 extern "C" int msvgb_batch_destroy(msvgb_batch *b) {
@@ -104,12 +110,22 @@ extern "C" int msvgb_batch_destroy(msvgb_batch *b) {
   cudaFree(b->d_vars); cudaFree(b->d_items); cudaFree(b->d_ticket);
   for (auto *t : b->gtabs) cudaFree(t);
   for (auto *p : b->own) msvgb_profile_destroy(p);
+  for (int k = 0; k < 2; ++k) {
+    cudaFree(b->d_solo_counters[k]); cudaFree(b->d_solo_list[k]);
+    if (b->branch[k]) cudaStreamDestroy(b->branch[k]);
+  }
+  for (auto ev : b->ev) if (ev) cudaEventDestroy(ev);
   delete b;
   return MSVGB_eslOK;
 }
 
-// Profiles above 2047 nodes (up to the single-query maximum) are scored by
-// their own launches, captured in the same graph after the persistent kernel.
+// Profiles whose search alone fills the GPU (M x residues >= 40e9 cells, the
+// size at which a single query switches to lane groups) are scored by their
+// own single-query searches -- lane-group pass, then the full MSV of its
+// undecided sequences -- on two graph branches that alternate, so that one
+// search's tail overlaps the next one's start; so are profiles above 2047
+// nodes (up to the single-query maximum). The other profiles share the
+// persistent kernel, on a third branch.
 // Work items: for each profile (largest models first), for each target-length
 // bin of the sorted database (longest first), chunks of about per_item
 // residues -- at most kChunkMaxSeqs sequences when the bin's lane count is
@@ -146,17 +162,21 @@ int msvgb_detail::batch_create(msvgb_ctx *ctx, const msvgb_om *const *oms, int n
   // lane-group tables its bins ask for
   std::vector<ProfDev> vars;
   std::vector<std::array<int, msvgb_detail::kNLBins>> var_of(nprof);
-  std::vector<std::pair<int, msvgb_profile *>> large;          // M > 2047: own launches in the graph
+  std::vector<std::pair<int, msvgb_profile *>> large;          // own searches in the graph
   size_t smem = 0;
   for (int i = 0; i < nprof; ++i) {
     if (!oms[i]) return bail(MSVGB_eslEINVAL, "NULL profile");
     const int M = oms[i]->M;
     const int C = multi_C(M);
-    if (C < 0) {
+    const bool solo = C < 0 || (!force_lanes && (double) M * (double) db->residues >= 4e10);
+    if (solo) {
       msvgb_profile *p = nullptr;
       int st = msvgb_detail::profile_build_width(ctx, oms[i], 1, 0, &p);
+      const int G = st == MSVGB_eslOK ? msvgb_detail::lanes_for(ctx, M, -1, nullptr) : 32;
+      if (st == MSVGB_eslOK && G < 32 && p->f16) st = msvgb_profile_set_lanes(p, oms[i], G);
+      if (p) b->own.push_back(p);
       if (st != MSVGB_eslOK) { msvgb_batch_destroy(b); return st; }
-      b->own.push_back(p);
+      p->lanes_auto = true;
       large.emplace_back(i, p);
       continue;
     }
@@ -203,9 +223,16 @@ int msvgb_detail::batch_create(msvgb_ctx *ctx, const msvgb_om *const *oms, int n
     if (st != MSVGB_eslOK) { msvgb_batch_destroy(b); return st; }
     large_tables.push_back(t);
   }
+  std::vector<char> is_solo(nprof, 0);
+  for (auto &lp : large) is_solo[lp.first] = 1;
   std::vector<int> order;
-  for (int i = 0; i < nprof; ++i) if (multi_C(oms[i]->M) > 0) order.push_back(i);
+  for (int i = 0; i < nprof; ++i) if (!is_solo[i]) order.push_back(i);
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return oms[x]->M > oms[y]->M; });
+  std::vector<size_t> solo_order(large.size());
+  for (size_t j = 0; j < large.size(); ++j) solo_order[j] = j;
+  std::stable_sort(solo_order.begin(), solo_order.end(),
+                   [&](size_t x, size_t y) { return large[x].second->M > large[y].second->M; });
+  b->nsolo = (int) large.size();
 
   b->smem = smem;
   b->threads = b->smem > 100 * 1024 ? 512 : 256;
@@ -236,7 +263,13 @@ int msvgb_detail::batch_create(msvgb_ctx *ctx, const msvgb_om *const *oms, int n
   b->nitems = (int64_t) items.size();
   e = cudaMalloc(&b->d_vars, sizeof(ProfDev) * std::max(1, b->nvars));
   if (e == cudaSuccess) e = cudaMalloc(&b->d_items, sizeof(BatchItem) * std::max<int64_t>(1, b->nitems));
-  if (e == cudaSuccess) e = cudaMalloc(&b->d_ticket, sizeof(unsigned long long) * (1 + large.size()));
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_ticket, sizeof(unsigned long long));
+  for (int k = 0; k < 2 && e == cudaSuccess && !large.empty(); ++k) {
+    e = cudaMalloc(&b->d_solo_counters[k], 4 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_solo_list[k], sizeof(int64_t) * std::max<int64_t>(1, db->n));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->branch[k], cudaStreamNonBlocking);
+  }
+  for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaEventCreateWithFlags(&b->ev[k], cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMemcpy(b->d_vars, vars.data(), sizeof(ProfDev) * b->nvars, cudaMemcpyHostToDevice);
   if (e == cudaSuccess && b->nitems)
     e = cudaMemcpy(b->d_items, items.data(), sizeof(BatchItem) * b->nitems, cudaMemcpyHostToDevice);
@@ -251,28 +284,33 @@ int msvgb_detail::batch_create(msvgb_ctx *ctx, const msvgb_om *const *oms, int n
   e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
-    cudaError_t e1 = cudaSuccess;
-    cudaMemsetAsync(b->d_ticket, 0, sizeof(unsigned long long) * (1 + large.size()), cs);
-    if (b->nitems) {
+    // the persistent kernel on the origin stream; the profiles' own searches
+    // alternate between two branches forked from it and joined back
+    cudaError_t e1 = cudaMemsetAsync(b->d_ticket, 0, sizeof(unsigned long long), cs);
+    const bool fork = !large.empty();
+    if (e1 == cudaSuccess && fork) {
+      e1 = cudaEventRecord(b->ev[2], cs);
+      for (int k = 0; k < 2 && e1 == cudaSuccess; ++k) e1 = cudaStreamWaitEvent(b->branch[k], b->ev[2], 0);
+    }
+    for (size_t jj = 0; jj < solo_order.size() && e1 == cudaSuccess; ++jj) {
+      const size_t j = solo_order[jj];
+      const int k = (int) (jj & 1);
+      msvgb_detail::SearchScratch sc;
+      sc.stream = b->branch[k]; sc.side = nullptr;
+      sc.ticket = b->d_solo_counters[k]; sc.aux = b->d_solo_counters[k] + 1; sc.list = b->d_solo_list[k];
+      const int st = msvgb_detail::enqueue_search(sc, large[j].second, db, large_tables[j],
+                                                  (uint8_t *) d_xj + (int64_t) large[j].first * db->n,
+                                                  (uint8_t *) d_flags + (int64_t) large[j].first * db->n,
+                                                  ctx->num_sms);
+      if (st != MSVGB_eslOK) e1 = cudaErrorInvalidValue;
+    }
+    if (e1 == cudaSuccess && b->nitems) {
       msv_batch_kernel<<<b->grid, b->threads, b->smem, cs>>>(a);
       e1 = cudaGetLastError();
     }
-    // models above 2047 nodes: one single-query launch each (32 lanes, tables
-    // in shared or global memory), in the same graph
-    for (size_t j = 0; j < large.size() && e1 == cudaSuccess; ++j) {
-      const msvgb_profile *p = large[j].second;
-      const LenTables *t = large_tables[j];
-      LaunchArgs la;
-      la.P = ProfDev{};
-      la.P.M = p->M; la.P.C = p->C; la.P.tbm = p->tbm; la.P.tec = p->tec; la.P.base = p->base; la.P.bias = p->bias;
-      la.P.stab = p->d_stab; la.P.mtab = p->d_mtab; la.P.tjb = t->d_tjb; la.P.xjmin = t->d_xjmin;
-      la.P.ssv_f16 = p->f16;
-      la.db = a.db;
-      la.out_xj = (uint8_t *) d_xj + (int64_t) large[j].first * db->n;
-      la.out_flags = (uint8_t *) d_flags + (int64_t) large[j].first * db->n;
-      la.ticket = b->d_ticket + 1 + j;
-      la.stream = cs; la.grid = 0; la.skip_empty = 1;
-      e1 = msvgb_detail::dispatch(p->C, p->f16 != 0, la, ctx->num_sms);
+    for (int k = 0; k < 2 && e1 == cudaSuccess && fork; ++k) {
+      e1 = cudaEventRecord(b->ev[k], b->branch[k]);
+      if (e1 == cudaSuccess) e1 = cudaStreamWaitEvent(cs, b->ev[k], 0);
     }
     e = cudaStreamEndCapture(cs, &b->graph);
     if (e == cudaSuccess) e = e1;

@@ -160,6 +160,20 @@ void tune_free(msvgb_ctx *c);
 // where the model length allows it (0: the context's choice).
 int batch_create(msvgb_ctx *ctx, const msvgb_om *const *oms, int nprof, const msvgb_db *db, double F1,
                  void *d_xj, void *d_flags, int force_lanes, msvgb_batch **ret);
+// Device scratch and streams of one single-profile search.
+struct SearchScratch {
+  cudaStream_t stream = nullptr;     // the search's stream
+  cudaStream_t side = nullptr;       // long targets run here, concurrently (null: on stream, first)
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;   // needed with side
+  unsigned long long *ticket = nullptr;               // 1 counter
+  unsigned long long *aux = nullptr;                  // 3 counters
+  int64_t *list = nullptr;                            // room for every sequence of the database
+};
+// Enqueues the single-profile search of db (per-length tables t) with the
+// lane-group pass when the profile has one (and the search is not small),
+// else the 32-lane kernel. The database must be in place on sc.stream.
+int enqueue_search(const SearchScratch &sc, const msvgb_profile *p, const msvgb_db *db, const LenTables *t,
+                   uint8_t *d_xj, uint8_t *d_flags, int num_sms);
 // Asynchronous packing of one chunk (db_create_on).
 struct AsyncPack {
   int *d_bad;      // device flag: set if a residue code is >= 29

@@ -85,3 +85,28 @@ def test_batch_rejects_oversize_profiles(ctx):
     with pytest.raises(api.MSVError) as e:
         api.search_batch(ctx, [big], db)
     assert e.value.code == api.eslEINVAL
+
+
+def test_batch_with_own_searches_equals_single_query_and_oracle(ctx):
+    """A database large enough that some profiles (M x residues >= 40e9
+    cells) are scored by their own single-query searches on the batch graph's
+    branches, beside the persistent kernel for the others: identical to the
+    single-query path, and the oracle on a sample."""
+    Ms = [120, 300, 700, 1100, 1500, 2500]
+    profs = make_profiles(ctx, Ms, seed0=300)
+    s = F.SeqSet.concat([F.synth_sequences(118_000, seed=51, lmax=12000)] +
+                        [F.emit_homologs(p, 300, seed=52 + i) for i, p in enumerate(profs)])
+    assert Ms[-2] * s.total >= 4e10 > Ms[1] * s.total     # both kinds of profile in the batch
+    db = api.DeviceDB(ctx, s)
+    bxj, bfl = api.search_batch(ctx, profs, db)
+    rng = np.random.default_rng(53)
+    sub = np.sort(rng.choice(s.n, size=1500, replace=False))
+    for i, p in enumerate(profs):
+        xj, fl = api.search(ctx, api.DeviceProfile(ctx, p), db)
+        assert np.array_equal(bxj[i], xj), f"profile {i} (M={p.M}) xj"
+        assert np.array_equal(bfl[i], fl), f"profile {i} (M={p.M}) flags"
+        o = O.msv_batch(p, s.subset(sub))
+        ok = o["status"] == F.eslOK
+        assert np.array_equal(bxj[i][sub][ok], o["xj"][ok])
+        assert np.array_equal((bfl[i][sub] & api.FLAG_ERANGE) != 0, o["status"] == F.eslERANGE)
+        assert np.array_equal((bfl[i][sub] & api.FLAG_PASS) != 0, o["pass"] == 1)
