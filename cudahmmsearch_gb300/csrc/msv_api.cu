@@ -184,6 +184,32 @@ cudaError_t msvgb_detail::dispatch_group(int C, int G, int CI, const GroupArgs &
 #undef G8
 }
 
+namespace msvgb {
+template <int C, int G>
+cudaError_t launch_list_group(const ProfDev &P, const DbDev &db, uint8_t *out_xj, uint8_t *out_flags,
+                              unsigned long long *ticket, const int64_t *list, const unsigned long long *list_count,
+                              int num_sms, cudaStream_t stream);
+}
+
+cudaError_t msvgb_detail::dispatch_list_group(int C, int G, const ProfDev &P, const DbDev &db, uint8_t *out_xj,
+                                              uint8_t *out_flags, unsigned long long *ticket, const int64_t *list,
+                                              const unsigned long long *list_count, int sms, cudaStream_t stream) {
+#define L16(c) case c: return launch_list_group<c, 16>(P, db, out_xj, out_flags, ticket, list, list_count, sms, stream);
+#define L8(c)  case c: return launch_list_group<c, 8>(P, db, out_xj, out_flags, ticket, list, list_count, sms, stream);
+  if (G == 16) {
+    switch (C) { L16(2) L16(3) L16(4) L16(5) L16(6) L16(7) L16(8) L16(9) L16(10) L16(11) L16(12) L16(13)
+                 L16(14) L16(15) L16(16) L16(17) L16(18) L16(19) L16(20) L16(21) L16(22) L16(23) L16(24)
+                 L16(25) L16(26) L16(27) L16(28) L16(29) L16(30) L16(31) L16(32) }
+  } else if (G == 8) {
+    switch (C) { L8(2) L8(3) L8(4) L8(5) L8(6) L8(7) L8(8) L8(9) L8(10) L8(11) L8(12) L8(13)
+                 L8(14) L8(15) L8(16) L8(17) L8(18) L8(19) L8(20) L8(21) L8(22) L8(23) L8(24)
+                 L8(25) L8(26) L8(27) L8(28) L8(29) L8(30) L8(31) L8(32) }
+  }
+  return cudaErrorInvalidValue;
+#undef L16
+#undef L8
+}
+
 // ------------------------------------------------------------------------------
 // context
 
@@ -392,20 +418,17 @@ extern "C" int msvgb_profile_destroy(msvgb_profile *p) {
     for (void *r : t->retired) cudaFree(r);
     delete t;
   }
-  cudaFree(p->d_stab); cudaFree(p->d_mtab); cudaFree(p->d_stab_g);
+  cudaFree(p->d_stab); cudaFree(p->d_mtab); cudaFree(p->d_stab_g); cudaFree(p->d_mtab_g);
   delete p;
   return MSVGB_eslOK;
 }
 
 extern "C" int msvgb_profile_M(const msvgb_profile *p) { return p ? p->M : -1; }
 
-// G-lane SSV table: node g*2C + h*C + w + 1 of lane g in word w, half h.
-std::vector<uint32_t> msvgb_detail::build_group_table(const msvgb_om *om, int C, int G) {
-  const int M = om->M, Q = std::max(2, (M - 1) / 16 + 1), bias = om->bias_b;
-  auto s_of = [&](int x, int k) -> int {
-    if (x >= 29 || k > M) return -128;
-    return std::min(127, std::max(-128, bias - rbv_at(om, Q, x, k)));
-  };
+// G-lane f16 table (GroupLayout<C, G>, with its region copies): node
+// g*2C + h*C + w + 1 of lane g in word w, half h, holding cost(x, node).
+template <class Cost>
+static std::vector<uint32_t> group_table_from(int C, int G, Cost cost) {
   auto f16bits = [](int v) -> uint32_t {
     const __half h = __float2half((float) v);
     uint16_t b; memcpy(&b, &h, 2); return b;
@@ -418,8 +441,8 @@ std::vector<uint32_t> msvgb_detail::build_group_table(const msvgb_om *om, int C,
     for (int g = 0; g < G; ++g)
       for (int w = 0; w < C; ++w) {
         const int k0 = g * 2 * C + w + 1, k1 = g * 2 * C + C + w + 1;
-        const uint32_t v = f16bits(s_of(x, k0)) | (f16bits(s_of(x, k1)) << 16);
-        if (w < 4 * Q4) {                                   // GroupLayout<C, G>
+        const uint32_t v = f16bits(cost(x, k0)) | (f16bits(cost(x, k1)) << 16);
+        if (w < 4 * Q4) {
           st[(((size_t) x * Q4 + w / 4) * G + g) * 4 + (w % 4)] = v;
         } else if (R >= 2 && w < 4 * Q4 + 2) {
           for (int cp = 0; cp < pair; ++cp) st[a_words + (((size_t) x * pair + cp) * G + g) * 2 + (w - 4 * Q4)] = v;
@@ -428,6 +451,25 @@ std::vector<uint32_t> msvgb_detail::build_group_table(const msvgb_om *om, int C,
         }
       }
   return st;
+}
+
+// G-lane SSV table: s = bias - rbv clamped to [-128, 127]; padding -128.
+std::vector<uint32_t> msvgb_detail::build_group_table(const msvgb_om *om, int C, int G) {
+  const int M = om->M, Q = std::max(2, (M - 1) / 16 + 1), bias = om->bias_b;
+  return group_table_from(C, G, [&](int x, int k) -> int {
+    if (x >= 29 || k > M) return -128;
+    return std::min(127, std::max(-128, bias - rbv_at(om, Q, x, k)));
+  });
+}
+
+// G-lane MSV table (the full recurrence, msv_row_group): c = bias - rbv
+// unclamped; padding nodes and the pad residue bias - 255 (rbv 255).
+std::vector<uint32_t> msvgb_detail::build_group_msv_table(const msvgb_om *om, int C, int G) {
+  const int M = om->M, Q = std::max(2, (M - 1) / 16 + 1), bias = om->bias_b;
+  return group_table_from(C, G, [&](int x, int k) -> int {
+    if (x >= 29 || k > M) return bias - 255;
+    return bias - rbv_at(om, Q, x, k);
+  });
 }
 
 extern "C" int msvgb_profile_set_lanes(msvgb_profile *p, const msvgb_om *om, int G) {
@@ -447,8 +489,14 @@ extern "C" int msvgb_profile_set_lanes(msvgb_profile *p, const msvgb_om *om, int
   CUDA_TRY(cudaMalloc(&d, st.size() * 4));
   cudaError_t e = cudaMemcpy(d, st.data(), st.size() * 4, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) { cudaFree(d); return fail(MSVGB_eslESYS, cudaGetErrorString(e)); }
+  const std::vector<uint32_t> mg = build_group_msv_table(om, C, G);
+  uint32_t *dm = nullptr;
+  e = cudaMalloc(&dm, mg.size() * 4);
+  if (e == cudaSuccess) e = cudaMemcpy(dm, mg.data(), mg.size() * 4, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) { cudaFree(d); cudaFree(dm); return fail(MSVGB_eslESYS, cudaGetErrorString(e)); }
   cudaFree(p->d_stab_g);
-  p->d_stab_g = d; p->Cg = C; p->G = G; p->CI = CI;
+  cudaFree(p->d_mtab_g);
+  p->d_stab_g = d; p->d_mtab_g = dm; p->Cg = C; p->G = G; p->CI = CI;
   return MSVGB_eslOK;
 }
 
@@ -942,10 +990,17 @@ int msvgb_detail::enqueue_search(const SearchScratch &sc, const msvgb_profile *p
     CUDA_TRY(dispatch_group(p->Cg, p->G, p->CI, g, num_sms));
     count_launch();
   }
-  LaunchArgs a;
-  a.P = P32; a.db = dbv; a.out_xj = d_xj; a.out_flags = d_flags; a.ticket = sc.aux;
-  a.stream = sc.stream; a.grid = 0; a.skip_empty = 1; a.list = sc.list; a.list_count = sc.aux + 1;
-  CUDA_TRY(dispatch(p->C, p->f16 != 0, a, num_sms));
+  if (p->d_mtab_g) {                                       // the full MSV on the same lane groups
+    ProfDev Pl = P;
+    Pl.mtab = p->d_mtab_g;
+    CUDA_TRY(dispatch_list_group(p->Cg, p->G, Pl, dbv, d_xj, d_flags, sc.aux, sc.list, sc.aux + 1, num_sms,
+                                 sc.stream));
+  } else {
+    LaunchArgs a;
+    a.P = P32; a.db = dbv; a.out_xj = d_xj; a.out_flags = d_flags; a.ticket = sc.aux;
+    a.stream = sc.stream; a.grid = 0; a.skip_empty = 1; a.list = sc.list; a.list_count = sc.aux + 1;
+    CUDA_TRY(dispatch(p->C, p->f16 != 0, a, num_sms));
+  }
   count_launch();
   if (n_long > 0 && sc.side) CUDA_TRY(cudaStreamWaitEvent(sc.stream, sc.ev_join, 0));
   return MSVGB_eslOK;

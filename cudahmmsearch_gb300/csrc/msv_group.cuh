@@ -356,3 +356,161 @@ cudaError_t launch_ssv_group(const GroupArgs &a, int num_sms) {
   template cudaError_t msvgb::launch_ssv_group<C, G, 0>(const msvgb::GroupArgs &, int);
 #define MSVGB_INSTANTIATE_HYB(C, G, CI) \
   template cudaError_t msvgb::launch_ssv_group<C, G, CI>(const msvgb::GroupArgs &, int);
+
+namespace msvgb {
+
+// ---- Full MSV (phase B) on lane groups -----------------------------------------
+// The sequences SSV leaves undecided are scored with the full MSV recurrence
+// (msvfilter.c:112-212) by the same lane groups, 32/G sequences per warp in
+// lockstep, instead of one warp per sequence: a lane holds C words (2C cells)
+// of its sequence's row, so the per-row work (shuffle, residue decode, the
+// row maximum and the J/B updates) is spread over more cells.
+//
+// Cells are f16 in unit 1, exact: every value is an integer in [0, 255] and
+// every sum below 255 + bias. The table (GroupLayout<C, G>, "MSV group
+// table") holds c = bias - rbv unclamped, and bias - 255 for padding nodes and
+// the pad residue, which keeps those cells at 0 (the previous row's overflow
+// test bounds every cell below 255 - bias). Per cell, as msv_row does in
+// 16-bit lanes: sv = max(max(mpv, xBc) + c, 0) with xBc = min(xB, 255 - bias).
+template <int C, int G>
+__device__ __forceinline__ uint32_t msv_row_group(uint32_t (&dp)[C], uint32_t xB2, const uint32_t *__restrict__ tab,
+                                                  int x, int glane, int gidx, int src_lane) {
+  using Lay = GroupLayout<C, G>;
+  using Cp = GroupCopies<G>;
+  constexpr uint32_t one2 = 0x3C003C00u;
+  uint32_t s[C];
+#pragma unroll
+  for (int q = 0; q < Lay::Q4; ++q) {
+    const uint4 v = *reinterpret_cast<const uint4 *>(tab + ((x * Lay::Q4 + q) * G + glane) * 4);
+    s[4 * q] = v.x; s[4 * q + 1] = v.y; s[4 * q + 2] = v.z; s[4 * q + 3] = v.w;
+  }
+  if constexpr (Lay::R >= 2) {
+    const int cp = gidx % Cp::PAIR;
+    const uint2 v = *reinterpret_cast<const uint2 *>(tab + Lay::A_WORDS + ((x * Cp::PAIR + cp) * G + glane) * 2);
+    s[4 * Lay::Q4] = v.x; s[4 * Lay::Q4 + 1] = v.y;
+  }
+  if constexpr (Lay::R & 1) s[C - 1] = tab[Lay::A_WORDS + Lay::B_WORDS + (x * Cp::SINGLE + gidx) * G + glane];
+  const uint32_t pred0 = pred_word0(dp[C - 1], src_lane);
+  uint32_t acc = 0u;
+#pragma unroll
+  for (int w = C - 1; w >= 0; --w) {
+    dp[w] = fma_relu_f16x2(max_f16x2(w ? dp[w - 1] : pred0, xB2), one2, s[w]);
+    acc = max_s16x2(acc, dp[w]);                     // non-negative f16 bits order like integers
+  }
+  return acc;
+}
+
+// Full MSV of the listed sequences list[*ticket .. *list_count) (taken one
+// per group from the ticket), written as msv_search_kernel's list mode does.
+template <int C, int G>
+__global__ void __launch_bounds__(256)
+msv_list_group_kernel(ProfDev P, DbDev db, uint8_t *__restrict__ out_xj, uint8_t *__restrict__ out_flags,
+                      unsigned long long *__restrict__ ticket, const int64_t *__restrict__ list,
+                      const unsigned long long *__restrict__ list_count) {
+  extern __shared__ __align__(16) uint32_t smem[];
+  {
+    const uint4 *gs = reinterpret_cast<const uint4 *>(P.mtab);
+    uint4 *ss = reinterpret_cast<uint4 *>(smem);
+    for (int i = threadIdx.x; i < GroupLayout<C, G>::WORDS / 4; i += blockDim.x) ss[i] = __ldg(gs + i);
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, glane = lane % G, gbase = lane - glane, gidx = lane / G;
+  const int src_lane = gbase + (glane + G - 1) % G;
+  const unsigned gmask = (((1u << G) - 1u) << gbase);
+  const int tbm = P.tbm, tec = P.tec, base = P.base, bias = P.bias;
+  const unsigned long long cnt = *list_count;
+
+  int64_t s = 0;
+  int L = 0, i = 0, tjbm = 0, xJ = 0, xB = 0;
+  const uint32_t *sq = nullptr;
+  uint32_t nextw = kPadWord;
+  bool need = true, done = false, er = false;
+  uint32_t dp[C];
+#pragma unroll
+  for (int w = 0; w < C; ++w) dp[w] = 0u;
+
+  for (;;) {
+    if (need && !done) {                              // group-uniform: take the next listed sequence
+      long long t = -1;
+      if (glane == 0) {
+        const unsigned long long k = atomicAdd(ticket, 1ull);
+        if (k < cnt) t = list[k];
+      }
+      t = __shfl_sync(gmask, t, gbase);
+      if (t < 0) {
+        done = true;
+      } else {
+        s = (int64_t) t;
+        L = db.len[s];
+        tjbm = (P.tjb[L] + tbm) & 0xFF;               // (int8_t) tjb + (int8_t) tbm, splatted as bytes
+        xJ = 0;
+        xB = max(base - tjbm, 0);
+        er = false;
+        sq = reinterpret_cast<const uint32_t *>(db.codes + db.start[s]);
+        nextw = __ldg(sq);
+        i = 0;
+        need = false;
+#pragma unroll
+        for (int w = 0; w < C; ++w) dp[w] = 0u;
+      }
+    }
+    if (__all_sync(FULL, done)) break;
+    const bool active = !need && !done;
+    const uint32_t w4 = active ? nextw : kPadWord;
+    if (active && i + 4 < L) nextw = __ldg(sq + (i >> 2) + 1);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const uint32_t xb = (uint32_t) __half_as_ushort(__int2half_rn(min(xB, 255 - bias)));
+      uint32_t a = msv_row_group<C, G>(dp, xb | (xb << 16), smem, (w4 >> (8 * j)) & 0xFF, glane, gidx, src_lane);
+      int m = max((int) (a & 0xFFFFu), (int) (a >> 16));   // f16 bits of values in [0, 255]
+#pragma unroll
+      for (int off = G / 2; off >= 1; off >>= 1) m = max(m, __shfl_xor_sync(FULL, m, off));
+      const int xE = (int) __half2float(__ushort_as_half((unsigned short) m));
+      if (active && !er && i + j < L) {               // rows past the end change nothing
+        if (xE + bias >= 255) er = true;              // adds(xE, bias) == 255: +inf
+        else {
+          xJ = max(xJ, max(xE - tec, 0));
+          xB = max(max(base, xJ) - tjbm, 0);
+        }
+      }
+    }
+    i += 4;
+    if (active && (er || i >= L)) {
+      if (glane == 0) {
+        const int64_t oi = db.orig[s];
+        int flags = 0x04;
+        if (er) flags |= 0x01 | 0x02;
+        else if (xJ >= P.xjmin[L]) flags |= 0x02;
+        out_xj[oi] = (uint8_t) (er ? 255 : xJ);
+        out_flags[oi] = (uint8_t) flags;
+      }
+      need = true;
+    }
+  }
+}
+
+template <int C, int G>
+cudaError_t launch_list_group(const ProfDev &P, const DbDev &db, uint8_t *out_xj, uint8_t *out_flags,
+                              unsigned long long *ticket, const int64_t *list, const unsigned long long *list_count,
+                              int num_sms, cudaStream_t stream) {
+  auto kern = msv_list_group_kernel<C, G>;
+  constexpr size_t smem = (size_t) GroupLayout<C, G>::WORDS * 4;
+  static std::atomic<unsigned long long> configured{0};
+  {
+    cudaError_t e = ensure_smem_attr((const void *) kern, smem, configured);
+    if (e != cudaSuccess) return e;
+  }
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem);
+  if (e != cudaSuccess) return e;
+  (void) cudaGetLastError();
+  kern<<<std::max(1, per_sm) * num_sms, 256, smem, stream>>>(P, db, out_xj, out_flags, ticket, list, list_count);
+  return cudaGetLastError();
+}
+
+}  // namespace msvgb
+
+#define MSVGB_INSTANTIATE_LIST(C, G)                                                                       \
+  template cudaError_t msvgb::launch_list_group<C, G>(const msvgb::ProfDev &, const msvgb::DbDev &, uint8_t *, \
+                                                      uint8_t *, unsigned long long *, const int64_t *,      \
+                                                      const unsigned long long *, int, cudaStream_t);

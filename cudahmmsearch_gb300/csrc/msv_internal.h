@@ -80,6 +80,7 @@ struct msvgb_profile {
   int Cg = 0;                         // DP words per lane of the G-lane table
   int CI = 0;                         // of those, words whose costs are bytes (mixed-width table); 0: all f16
   uint32_t *d_stab_g = nullptr;       // SSV table in the G-lane layout (GroupLayout, or HybLayout when CI > 0)
+  uint32_t *d_mtab_g = nullptr;       // MSV table in the G-lane layout (GroupLayout, unclamped costs)
   std::vector<LenTables *> tables;    // one per F1 value used
   std::mutex tables_mu;
 };
@@ -146,6 +147,12 @@ std::vector<uint32_t> build_hyb_table(const msvgb_om *om, int C, int G, int CI);
 int ensure_tables(msvgb_profile *p, const msvgb_db *db, double F1, LenTables **out);
 // Lane-group SSV table of a profile (layout GroupLayout<C, G>, msv_group.cuh).
 std::vector<uint32_t> build_group_table(const msvgb_om *om, int C, int G);
+// Lane-group MSV table of the full recurrence (GroupLayout<C, G>, msv_row_group).
+std::vector<uint32_t> build_group_msv_table(const msvgb_om *om, int C, int G);
+// Launches the full-MSV pass of a list on lane groups (msv_list_group_kernel).
+cudaError_t dispatch_list_group(int C, int G, const msvgb::ProfDev &P, const msvgb::DbDev &db, uint8_t *out_xj,
+                                uint8_t *out_flags, unsigned long long *ticket, const int64_t *list,
+                                const unsigned long long *list_count, int sms, cudaStream_t stream);
 // Target-length bins of the lane choice: [0,150) [150,600) [600,2400) [2400,inf).
 constexpr int kNLBins = 4;
 int lbin_of(int L);
