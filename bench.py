@@ -54,7 +54,16 @@ INT_LANE_OPS_PER_CLK_PER_SM = 128   # 4 SM sub-partitions x 32 lanes: nominal is
 # traffic scales with the residue count.
 DRAM_BYTES_PER_RESIDUE = 168.8e6 / 154.56e6
 SMEM_BYTES_PER_CLK_PER_SM = 128     # one 128-byte shared-memory wavefront per clock
-SSV_TABLE_BYTES_PER_CELL = 2        # f16 cost per DP cell read from shared memory
+
+
+def ssv_table_bytes_per_cell(M, lanes, int8_words):
+    """Shared-memory bytes of SSV cost read per DP cell: 2 (f16) for every
+    word of a lane's row, 1 for the words of a mixed-width table that hold
+    8-bit costs (lane groups: Cg = M / (2 lanes) + 1 words per lane)."""
+    if lanes >= 32 or int8_words <= 0:
+        return 2.0
+    cg = M // (2 * lanes) + 1
+    return (4.0 * (cg - int8_words) + 2.0 * int8_words) / (2.0 * cg)
 
 
 def workload(name, rank=0, args=None):
@@ -730,6 +739,7 @@ def main():
     nsm = torch.cuda.get_device_properties(local).multi_processor_count
     peak_tops = measure_peak("msvgb_measure_int_peak", local) / 1e12    # measured now, same GPU and clock regime
     smem_peak = measure_peak("msvgb_measure_smem_peak", local) / 1e9
+    tb = ssv_table_bytes_per_cell(p.M, prof.lanes, prof.int8_words)
     hbm_peak, hbm_note = 6800.0, "of fallback (6.8 TB/s: no measured peaks file)"
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -746,14 +756,15 @@ def main():
                 "peak_note": f"measured: msvgb_measure_int_peak (independent max.s32/xor over {nsm} SMs); "
                              f"nominal {nsm} SMs x {INT_LANE_OPS_PER_CLK_PER_SM} lane-ops/clk x {sm_mhz:.0f} MHz = "
                              f"{nsm * INT_LANE_OPS_PER_CLK_PER_SM * sm_mhz * 1e6 / 1e12:.1f} Tops/s",
-                "smem": {"achieved": SSV_TABLE_BYTES_PER_CELL * cells / (kern_ms * 1e-3) / 1e9,
+                "smem": {"achieved": tb * cells / (kern_ms * 1e-3) / 1e9,
                          "peak": smem_peak, "unit": "GB/s",
-                         "frac": SSV_TABLE_BYTES_PER_CELL * cells / (kern_ms * 1e-3) / 1e9 / smem_peak,
+                         "frac": tb * cells / (kern_ms * 1e-3) / 1e9 / smem_peak,
                          "nominal": nsm * SMEM_BYTES_PER_CLK_PER_SM * sm_mhz * 1e6 / 1e9,
                          "peak_note": "measured: msvgb_measure_smem_peak (conflict-free 16-byte loads over "
                                       f"{nsm} SMs); nominal {nsm} SMs x 128 B/clk x {sm_mhz:.0f} MHz. "
-                                      f"{SSV_TABLE_BYTES_PER_CELL} B of f16 SSV cost per cell: the binding "
-                                      "bound of the SSV pass"},
+                                      f"{tb:.3f} B of SSV cost per cell ({prof.int8_words} of each lane's words "
+                                      "8-bit, the rest f16): with issue, the bound the SSV pass runs "
+                                      "against"},
                 "hbm": {"achieved": (s.total + 2 * s.n) / (kern_ms * 1e-3) / 1e9, "peak": hbm_peak,
                         "unit": "GB/s", "frac": (s.total + 2 * s.n) / (kern_ms * 1e-3) / 1e9 / hbm_peak,
                         "peak_note": hbm_note}}
