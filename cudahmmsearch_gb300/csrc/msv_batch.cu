@@ -199,8 +199,9 @@ int msvgb_detail::batch_create(msvgb_ctx *ctx, const msvgb_om *const *oms, int n
       if (vidx[k] < 0) {
         ProfDev V = P;
         if (G < 32) {
-          V.G = G; V.Cg = group_C(M, G);
-          const std::vector<uint32_t> gt = msvgb_detail::build_group_table(oms[i], V.Cg, G);
+          V.G = G; V.Cg = group_C(M, G); V.CI = multi_hyb_words(V.Cg, G);
+          const std::vector<uint32_t> gt = V.CI ? msvgb_detail::build_hyb_table(oms[i], V.Cg, G, V.CI)
+                                                : msvgb_detail::build_group_table(oms[i], V.Cg, G);
           uint32_t *d = nullptr;
           e = cudaMalloc(&d, gt.size() * 4);
           if (e == cudaSuccess) b->gtabs.push_back(d);

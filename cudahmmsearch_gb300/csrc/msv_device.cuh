@@ -47,6 +47,7 @@ struct ProfDev {
   int      ssv_f16;      // 1: stab is f16x2 [NRES][C][32]; 0: int8x4 [NRES][C/2][32]
   int      G = 32;       // lanes per sequence of the SSV pass; < 32: stab is the lane-group table
   int      Cg = 0;       // DP words per lane of the lane-group SSV pass (G < 32)
+  int      CI = 0;       // of those, words with 8-bit costs (mixed-width table, HybLayout); 0: f16 table
 };
 
 struct DbDev {

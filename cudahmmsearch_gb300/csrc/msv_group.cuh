@@ -319,12 +319,12 @@ msv_ssv_group_kernel(ProfDev P, DbDev db, uint8_t *__restrict__ out_xj, uint8_t 
 // SSV pass of one CTA over the sorted sequences [s0, s0 + nseq) (a work item
 // of the multi-profile kernels): next_seq and n_und are shared counters the
 // caller zeroed; und (room for nseq entries) receives the chunk-relative
-// indices of the undecided sequences.
-template <int C, int G>
+// indices of the undecided sequences. CI > 0: the mixed-width table.
+template <int C, int G, int CI = 0>
 __device__ __forceinline__ void ssv_group_chunk(const ProfDev &P, const uint32_t *tab, const DbDev &db, int64_t s0,
                                                 int nseq, uint8_t *oxj, uint8_t *ofl, unsigned *next_seq,
                                                 uint16_t *und, unsigned *n_und) {
-  ssv_group_loop<C, G>(
+  ssv_group_loop<C, G, CI>(
       P, tab, db, oxj, ofl,
       [&]() -> long long {
         const unsigned k = atomicAdd(next_seq, 1u);

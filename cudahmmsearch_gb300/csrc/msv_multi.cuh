@@ -70,15 +70,29 @@ __device__ __forceinline__ void run_seq_any(int C, const ProfDev &P, const uint3
   }
 }
 
+// 8-bit words per lane of the mixed-width table the multi-profile kernels
+// use at lane-group width Cg (0: f16 table): the single-query default
+// (hyb_default_words) at the group widths these kernels compile (kMultiC).
+__host__ __device__ constexpr int multi_hyb_words(int Cg, int G) {
+  return G == 8 ? (Cg < 10 ? 0 : Cg < 18 ? 4 : 8) : G == 16 ? (Cg < 13 ? 0 : Cg < 24 ? 4 : 8) : 0;
+}
+
+// The lane-group SSV pass of one chunk at (G, Cg), with the f16 or the
+// mixed-width table as P.CI says (0, or multi_hyb_words(Cg, G)).
 __device__ __forceinline__ void ssv_group_chunk_any(int G, int Cg, const ProfDev &P, const uint32_t *tab,
                                                     const DbDev &db, int64_t s0, int nseq, uint8_t *oxj,
                                                     uint8_t *ofl, unsigned *next_seq, uint16_t *und,
                                                     unsigned *n_und) {
-#define MSVGB_GROUP_CASE(c)                                                                  \
-  case c:                                                                                    \
-    if (G == 8) ssv_group_chunk<c, 8>(P, tab, db, s0, nseq, oxj, ofl, next_seq, und, n_und); \
-    else        ssv_group_chunk<c, 16>(P, tab, db, s0, nseq, oxj, ofl, next_seq, und, n_und); \
-    break;
+#define MSVGB_GROUP_VARIANT(c, g)                                                                          \
+  if (G == g) {                                                                                            \
+    constexpr int ci = multi_hyb_words(c, g);                                                              \
+    bool done = false;                                                                                     \
+    if constexpr (ci > 0) {                                                                                \
+      if (P.CI == ci) { ssv_group_chunk<c, g, ci>(P, tab, db, s0, nseq, oxj, ofl, next_seq, und, n_und); done = true; } \
+    }                                                                                                      \
+    if (!done) ssv_group_chunk<c, g, 0>(P, tab, db, s0, nseq, oxj, ofl, next_seq, und, n_und);             \
+  }
+#define MSVGB_GROUP_CASE(c) case c: MSVGB_GROUP_VARIANT(c, 8) else MSVGB_GROUP_VARIANT(c, 16) break;
   switch (Cg) {
     MSVGB_GROUP_CASE(2) MSVGB_GROUP_CASE(3) MSVGB_GROUP_CASE(4) MSVGB_GROUP_CASE(5)
     MSVGB_GROUP_CASE(6) MSVGB_GROUP_CASE(7) MSVGB_GROUP_CASE(8) MSVGB_GROUP_CASE(10)
@@ -87,6 +101,7 @@ __device__ __forceinline__ void ssv_group_chunk_any(int G, int Cg, const ProfDev
     default: break;
   }
 #undef MSVGB_GROUP_CASE
+#undef MSVGB_GROUP_VARIANT
 }
 
 // Shared state of one CTA's work item.
@@ -98,7 +113,7 @@ struct ChunkShared {
 // Words of a profile's SSV table in shared memory (the MSV table follows it):
 // the lane-group layout with its region copies (group_words), or the 32-lane one.
 __host__ __device__ inline int ssv_words(const ProfDev &P) {
-  return P.G < 32 ? group_words(P.Cg, P.G, 0) : NRES * P.C * 32;
+  return P.G < 32 ? group_words(P.Cg, P.G, P.CI) : NRES * P.C * 32;
 }
 
 // One CTA scores the sorted sequences [s0, s0 + nseq) against P, whose tables

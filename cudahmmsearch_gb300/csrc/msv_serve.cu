@@ -296,7 +296,8 @@ extern "C" int msvgb_server_submit(msvgb_server *s, const msvgb_om *om, uint64_t
   int G = msvgb_detail::lanes_for(s->ctx, om->M, -1, nullptr);   // lanes per sequence of the SSV pass
   if (G < 32 && group_C(om->M, G) < 0) G = 32;
   const int Cg = G < 32 ? group_C(om->M, G) : 0;
-  if (G < 32) st = msvgb_detail::build_group_table(om, Cg, G);
+  const int CI = G < 32 ? multi_hyb_words(Cg, G) : 0;          // mixed-width table where the width has one
+  if (G < 32) st = CI ? msvgb_detail::build_hyb_table(om, Cg, G, CI) : msvgb_detail::build_group_table(om, Cg, G);
   msvgb_profile tmp;                                   // scalar view for the threshold search
   tmp.M = om->M; tmp.C = C; tmp.tbm = om->tbm_b; tmp.tec = om->tec_b; tmp.base = om->base_b;
   tmp.bias = om->bias_b; tmp.scale = om->scale_b; tmp.mmu = om->mmu; tmp.mlambda = om->mlambda;
@@ -324,7 +325,7 @@ extern "C" int msvgb_server_submit(msvgb_server *s, const msvgb_om *om, uint64_t
   uint8_t *base = s->d_slot_mem + s->slot_bytes * slot;
   ProfDev P;
   P.M = om->M; P.C = C; P.tbm = om->tbm_b; P.tec = om->tec_b; P.base = om->base_b; P.bias = om->bias_b;
-  P.G = G; P.Cg = Cg;
+  P.G = G; P.Cg = Cg; P.CI = CI;
   P.stab = (const uint32_t *) base; P.mtab = (const uint32_t *) (base + st.size() * 4);
   P.tjb = base + s->tab_off_tjb; P.xjmin = base + s->tab_off_xjm; P.ssv_f16 = 1;
   __atomic_store_n(&s->h_ctl->done[slot], 0ull, __ATOMIC_SEQ_CST);
