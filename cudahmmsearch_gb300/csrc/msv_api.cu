@@ -1064,23 +1064,27 @@ extern "C" int msvgb_search_host(msvgb_ctx *c, const msvgb_profile *p, const uin
   std::vector<msvgb_db *> dbs;
   int st = MSVGB_eslOK;
   PhaseTimer pt;
-  // Every chunk's lengths are sorted first, while the GPU is otherwise idle
-  // (sorting a chunk while the previous chunk's persistent search holds every
-  // SM would wait for that search). Then chunk by chunk: its residues go up
-  // on the copy engine (the next chunk's copy runs under this chunk's
-  // search) and are packed, and it is searched.
+  // Every chunk is sorted before the first search, while the GPU is otherwise
+  // idle (sorting a chunk while the previous chunk's persistent search holds
+  // every SM would wait for that search): the first chunk completely, its
+  // residues going up while it is sorted, the others by their offsets only.
+  // Then chunk by chunk: the residues of a later chunk go up on the copy
+  // engine (under the previous chunk's search) and are packed, and the chunk
+  // is searched. (A later chunk's residue copy is queued only after the
+  // sorting: queued earlier, it would hold the copy engine in front of the
+  // sorting's offset copies.)
   for (size_t k = 0; k + 1 < cut.size() && st == MSVGB_eslOK; ++k) {
     const int64_t b0 = cut[k], b1 = cut[k + 1];
     msvgb_db *db = nullptr;
     AsyncPack a{d_bad};
-    a.defer_residues = true;
+    a.defer_residues = k > 0;
     st = db_create_on(c, codes, off + b0, b1 - b0, c->upload, &db, &a);
     if (st == MSVGB_eslOK) dbs.push_back(db);
   }
   pt.mark("search_host: chunks sorted");
   for (size_t k = 0; k < dbs.size() && st == MSVGB_eslOK; ++k) {
     const int64_t b0 = cut[k];
-    st = db_fill_on(c, dbs[k], codes, c->upload);
+    if (k > 0) st = db_fill_on(c, dbs[k], codes, c->upload);
     if (st == MSVGB_eslOK) st = msvgb_search_device(c, p, dbs[k], F1, d + b0, d + n + b0);
     pt.mark("search_host: chunk enqueued");
   }
