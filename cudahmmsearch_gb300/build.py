@@ -20,7 +20,7 @@ LIB = os.path.join(HERE, "libmsvgb.so")
 PROBE_SRC = "msv_probe.cu"
 PROBE_LIB = os.path.join(HERE, "libmsvgb_probe.so")
 
-SOURCES = ["msv_batch.cu", "msv_serve.cu", "inst_g16.cu", "inst_g8.cu", "inst_hyb0.cu", "inst_l8.cu", "inst_l16.cu", "inst_hyb1.cu", "inst_hyb2.cu", "msv_api.cu", "msv_tune.cu", "msv_io.cu", "msv_vit.cu", "msv_noalloc.cu", "msv_pack.cu", "msv_sample.cu", "msv_pipeline.cu", "msv_bias.cu", "inst_a.cu", "inst_b.cu", "inst_c.cu", "inst_d.cu",
+SOURCES = ["msv_batch.cu", "msv_serve.cu", "inst_g16.cu", "inst_g8.cu", "inst_hyb0.cu", "inst_l8.cu", "inst_l16.cu", "inst_w32.cu", "inst_hyb1.cu", "inst_hyb2.cu", "msv_api.cu", "msv_tune.cu", "msv_io.cu", "msv_vit.cu", "msv_noalloc.cu", "msv_pack.cu", "msv_sample.cu", "msv_pipeline.cu", "msv_bias.cu", "inst_a.cu", "inst_b.cu", "inst_c.cu", "inst_d.cu",
            "inst_e.cu", "inst_f.cu", "inst_h.cu", "inst_i.cu"]
 HEADERS = ["msv_device.cuh", "msv_kernel_impl.cuh", "msv_internal.h", "msv_multi.cuh", "msv_group.cuh",
            "msv_hyb_list.h",

@@ -151,6 +151,7 @@ template <int C, int G, int CI> cudaError_t launch_ssv_group(const GroupArgs &a,
 int msvgb_detail::hyb_default_words(int C, int G) {
   if (G == 8) return C < 10 ? 0 : C < 18 ? 4 : 8;
   if (G == 16) return C < 13 ? 0 : C < 24 ? 4 : 8;
+  if (G == 32) return C < 17 ? 0 : 8;     // the split 32-lane passes (M 1024-2047): always mixed width
   return 0;
 }
 
@@ -194,6 +195,13 @@ cudaError_t launch_list_group(const ProfDev &P, const DbDev &db, uint8_t *out_xj
 cudaError_t msvgb_detail::dispatch_list_group(int C, int G, const ProfDev &P, const DbDev &db, uint8_t *out_xj,
                                               uint8_t *out_flags, unsigned long long *ticket, const int64_t *list,
                                               const unsigned long long *list_count, int sms, cudaStream_t stream) {
+#define L32(c) case c: return launch_list_group<c, 32>(P, db, out_xj, out_flags, ticket, list, list_count, sms, stream);
+  if (G == 32) {
+    switch (C) { L32(17) L32(18) L32(19) L32(20) L32(21) L32(22) L32(23) L32(24) L32(25) L32(26) L32(27)
+                 L32(28) L32(29) L32(30) L32(31) L32(32) }
+    return cudaErrorInvalidValue;
+  }
+#undef L32
 #define L16(c) case c: return launch_list_group<c, 16>(P, db, out_xj, out_flags, ticket, list, list_count, sms, stream);
 #define L8(c)  case c: return launch_list_group<c, 8>(P, db, out_xj, out_flags, ticket, list, list_count, sms, stream);
   if (G == 16) {
@@ -392,8 +400,9 @@ extern "C" int msvgb_profile_create(msvgb_ctx *ctx, const msvgb_om *om, msvgb_pr
   if (!om) return fail(MSVGB_eslEINVAL, "om is NULL");
   int variant = default_f16();
   const int G = om->M >= 1 ? msvgb_detail::lanes_for(ctx, om->M, -1, &variant) : 32;
-  int st = profile_build(ctx, om, G < 32 ? 1 : variant, ret);
-  if (st == MSVGB_eslOK && G < 32 && (*ret)->f16) {
+  const bool wide = G == 32 && om->M >= kWideSplitMinM && om->M / 64 + 1 <= 32;
+  int st = profile_build(ctx, om, (G < 32 || wide) ? 1 : variant, ret);
+  if (st == MSVGB_eslOK && (G < 32 || wide) && (*ret)->f16) {
     st = msvgb_profile_set_lanes(*ret, om, G);
     if (st != MSVGB_eslOK) { msvgb_profile_destroy(*ret); *ret = nullptr; }
   }
@@ -476,8 +485,17 @@ extern "C" int msvgb_profile_set_lanes(msvgb_profile *p, const msvgb_om *om, int
   if (!p || !om) return fail(MSVGB_eslEINVAL, "NULL argument");
   if (om->M != p->M) return fail(MSVGB_eslEINVAL, "om does not match the profile");
   p->lanes_auto = false;                                  // set by the caller: applies at any size
-  if (G == 32) { p->G = 32; p->CI = 0; return MSVGB_eslOK; }
-  if (G != 16 && G != 8) return fail(MSVGB_eslEINVAL, "lanes per sequence must be 32, 16 or 8");
+  // 32 lanes: the fused kernel, and for models of 1024 to 2047 nodes also
+  // the split passes (32-lane groups, mixed-width SSV table), which large
+  // searches use
+  const bool wide = G == 32 && p->M >= kWideSplitMinM && p->M / 64 + 1 <= 32;
+  if (G == 32 && !wide) {
+    cudaFree(p->d_stab_g); cudaFree(p->d_mtab_g);
+    p->d_stab_g = p->d_mtab_g = nullptr;
+    p->G = 32; p->CI = 0;
+    return MSVGB_eslOK;
+  }
+  if (G != 16 && G != 8 && G != 32) return fail(MSVGB_eslEINVAL, "lanes per sequence must be 32, 16 or 8");
   const int C = p->M / (2 * G) + 1;                       // 2*C*G > M: the last node is padding
   if (C > 32) return fail(MSVGB_eslEINVAL, "model too long for this many lanes per sequence");
   if (C < 2) return fail(MSVGB_eslEINVAL, "model too short for this many lanes per sequence");
@@ -547,7 +565,8 @@ std::vector<uint32_t> msvgb_detail::build_hyb_table(const msvgb_om *om, int C, i
 extern "C" int msvgb_profile_set_ssv_int8_words(msvgb_profile *p, const msvgb_om *om, int words) {
   if (!p || !om) return fail(MSVGB_eslEINVAL, "NULL argument");
   if (om->M != p->M) return fail(MSVGB_eslEINVAL, "om does not match the profile");
-  if (p->G == 32 || !p->d_stab_g) return fail(MSVGB_eslEINVAL, "8-bit SSV words need 16 or 8 lanes per sequence");
+  if (p->G == 32 || !p->d_stab_g)
+    return fail(MSVGB_eslEINVAL, "8-bit SSV words are set for 16 or 8 lanes per sequence (32 lanes: fixed)");
   if (words == p->CI) return MSVGB_eslOK;
   if (words != 0 && !hyb_compiled(p->Cg, p->G, words))
     return fail(MSVGB_eslEINVAL, "no mixed-width SSV kernel for this model length, lane count and word count");
@@ -946,7 +965,7 @@ int msvgb_detail::enqueue_search(const SearchScratch &sc, const msvgb_profile *p
   // launch tail they add outweighs their throughput, unless lanes were set
   // explicitly.
   const bool small = p->lanes_auto && (double) p->M * (double) db->residues < 4e10;
-  if (p->G == 32 || !p->d_stab_g || small) {
+  if (!p->d_stab_g || small) {
     LaunchArgs a;
     a.P = P32; a.db = dbv; a.out_xj = d_xj; a.out_flags = d_flags; a.ticket = sc.ticket;
     a.stream = sc.stream; a.grid = 0; a.skip_empty = 1;

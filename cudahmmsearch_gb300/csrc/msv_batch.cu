@@ -173,7 +173,7 @@ int msvgb_detail::batch_create(msvgb_ctx *ctx, const msvgb_om *const *oms, int n
       msvgb_profile *p = nullptr;
       int st = msvgb_detail::profile_build_width(ctx, oms[i], 1, 0, &p);
       const int G = st == MSVGB_eslOK ? msvgb_detail::lanes_for(ctx, M, -1, nullptr) : 32;
-      if (st == MSVGB_eslOK && G < 32 && p->f16) st = msvgb_profile_set_lanes(p, oms[i], G);
+      if (st == MSVGB_eslOK && p->f16) st = msvgb_profile_set_lanes(p, oms[i], G);   // 32: split passes for M 1024-2047
       if (p) b->own.push_back(p);
       if (st != MSVGB_eslOK) { msvgb_batch_destroy(b); return st; }
       p->lanes_auto = true;

@@ -421,7 +421,7 @@ msv_list_group_kernel(ProfDev P, DbDev db, uint8_t *__restrict__ out_xj, uint8_t
   __syncthreads();
   const int lane = threadIdx.x & 31, glane = lane % G, gbase = lane - glane, gidx = lane / G;
   const int src_lane = gbase + (glane + G - 1) % G;
-  const unsigned gmask = (((1u << G) - 1u) << gbase);
+  const unsigned gmask = (G == 32) ? FULL : (((1u << G) - 1u) << gbase);
   const int tbm = P.tbm, tec = P.tec, base = P.base, bias = P.bias;
   const unsigned long long cnt = *list_count;
 

@@ -118,6 +118,13 @@ struct msvgb_db {
 // 2-4x longer, and a single long target would set the length of the launch.
 constexpr int kLongTarget = 2400;
 
+// From this model length up to 2047 nodes, 32-lane profiles also get the
+// split passes (32-lane groups with the mixed-width SSV table, then the full
+// MSV of the undecided), which large searches use instead of the fused
+// kernel (measured on 1,000,000 sequences: +2% at M = 1100, +8% at 1500,
+// +2% at 1984).
+constexpr int kWideSplitMinM = 1024;
+
 namespace msvgb_detail {
 // The database's original-index -> sorted-slot table (db->d_inv), built on
 // the context's stream at first use.

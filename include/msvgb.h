@@ -111,10 +111,13 @@ int msvgb_profile_create(msvgb_ctx *ctx, const msvgb_om *om, msvgb_profile **ret
 int msvgb_profile_create_ex(msvgb_ctx *ctx, const msvgb_om *om, int ssv_variant, msvgb_profile **ret_prof);
 int msvgb_profile_variant(const msvgb_profile *prof);
 /* Lanes per sequence of the SSV pass: 32 (one warp per sequence, SSV
- * and full MSV in one kernel), or 16 / 8 (2 / 4 sequences per warp in
+ * and full MSV in one kernel; for models of 1024 to 2047 nodes, searches of
+ * at least ~40e9 cells -- or any search, when lanes are set here -- run the
+ * SSV pass and the full MSV as two launches on 32-lane groups instead, with
+ * the mixed-width table), or 16 / 8 (2 / 4 sequences per warp in
  * lockstep, for small models: each lane then holds more DP words per row);
  * with 16 or 8 the sequences SSV leaves undecided are finished by the full
- * MSV in a second launch, and targets of 2400 residues or more run at 32
+ * MSV in a second launch on the same lane groups, and targets of 2400 residues or more run at 32
  * lanes in a concurrent launch (one long target must not set the length of
  * the search). om must be the profile's own MSV fields. Needs M < 64 * G and,
  * for G < 32, M >= 2 * G. Lanes chosen by msvgb_profile_create apply to
@@ -127,8 +130,9 @@ int msvgb_profile_lanes(const msvgb_profile *prof);
  * counterpart): the last `words` DP words of every lane (a multiple of 4,
  * 0 = none) keep their costs as single bytes, widened in registers; the rest
  * stay 16-bit. Fewer shared-memory bytes per cell, more instructions; results
- * are identical. eslEINVAL when the profile runs at 32 lanes or no kernel is
- * compiled for (DP width, lanes, words). msvgb_profile_set_lanes (and so
+ * are identical. eslEINVAL when the profile runs at 32 lanes (fixed: 8 words
+ * where the 32-lane split passes apply) or no kernel is compiled for
+ * (DP width, lanes, words). msvgb_profile_set_lanes (and so
  * msvgb_profile_create) sets the default for the model length and lane
  * count: 4 or 8 words from 10 DP words per lane up, measured 4-10% faster
  * than all-16-bit costs. */

@@ -149,3 +149,43 @@ def test_mixed_width_rejects_uncompiled_and_32_lanes(ctx):
     assert dp.int8_words == 8          # set_lanes restores the default share (26 words per lane: 8)
     dp.set_int8_words(0)
     assert dp.int8_words == 0
+
+
+@pytest.mark.parametrize("M", [1024, 1100, 1500, 1984, 2047])
+def test_split_32_lane_passes_match_oracle(ctx, M):
+    """Models of 1024 to 2047 nodes at 32 lanes: the SSV pass on 32-lane
+    groups with the mixed-width table, then the full MSV of the undecided on
+    the same groups, with ordinary and extreme scalar costs."""
+    rng = np.random.default_rng(M + 7)
+    for bias, tbm in ((int(rng.integers(5, 40)), int(rng.integers(5, 60))), (90, 130), (14, 120)):
+        p = _random_profile(rng, M, bias, tbm)
+        seqs = [rng.integers(0, 20, size=L).astype(np.uint8) for L in (1, 2, 3, 5, 17, 250, 2999)]
+        s = F.SeqSet.concat([F.SeqSet.from_list(seqs + [np.zeros(0, np.uint8)]),
+                             F.synth_sequences(200, seed=M, lmax=4000)])
+        o = O.msv_batch(p, s)
+        dp = api.DeviceProfile(ctx, p)
+        dp.set_lanes(32)
+        assert dp.lanes == 32 and dp.int8_words == 8
+        xj, fl = api.search(ctx, dp, api.DeviceDB(ctx, s))
+        ok = o["status"] == F.eslOK
+        nonempty = s.lengths > 0
+        assert np.array_equal((fl & api.FLAG_ERANGE) != 0, o["status"] == F.eslERANGE)
+        assert np.array_equal(xj[ok], o["xj"][ok])
+        assert np.array_equal(((fl & api.FLAG_PASS) != 0)[nonempty], o["pass"][nonempty] == 1)
+        assert np.array_equal(((fl & api.FLAG_FULL) != 0)[nonempty], o["path"][nonempty] == 1)
+
+
+@pytest.mark.parametrize("name", ["m1500_s2", "m2400_s1"])
+def test_32_lanes_match_reference_golden(ctx, name):
+    """32 lanes: the split passes at M = 1500, the fused kernel at M = 2400."""
+    p = F.read_profile(os.path.join(GOLDEN, name + ".prof"))
+    s = F.read_seqs(os.path.join(GOLDEN, name + ".seqs"))
+    r = F.read_results(os.path.join(GOLDEN, name + ".res"))
+    dp = api.DeviceProfile(ctx, p)
+    dp.set_lanes(32)
+    assert dp.int8_words == (8 if p.M < 2048 else 0)
+    xj, fl = api.search(ctx, dp, api.DeviceDB(ctx, s))
+    assert np.array_equal((fl & api.FLAG_ERANGE) != 0, r.status == F.eslERANGE)
+    assert np.array_equal((fl & api.FLAG_PASS) != 0, r.passed == 1)
+    sc = api.scores(p, s.lengths, xj, fl)
+    assert np.array_equal(sc.view(np.uint32), r.sc.view(np.uint32))
