@@ -32,7 +32,7 @@ EXPORTS = [
     "msvgb_search_static", "msvgb_sample_om", "msvgb_calibrate",
     "msvgb_batch_create", "msvgb_batch_run", "msvgb_batch_items", "msvgb_batch_destroy", "msvgb_search_batch",
     "msvgb_server_create", "msvgb_server_slots", "msvgb_server_submit", "msvgb_server_wait",
-    "msvgb_server_launches", "msvgb_server_destroy", "msvgb_pipeline_run",
+    "msvgb_server_launches", "msvgb_server_solo_searches", "msvgb_server_destroy", "msvgb_pipeline_run",
     "msvgb_autotune", "msvgb_tune_save", "msvgb_tune_load", "msvgb_tune_lanes",
     "msvgb_h3f_open", "msvgb_h3f_read", "msvgb_h3f_close", "msvgb_h3f_write", "msvgb_fasta_read",
     "msvgb_seqs_n", "msvgb_seqs_codes", "msvgb_seqs_offsets", "msvgb_seqs_name", "msvgb_seqs_free",
@@ -166,6 +166,7 @@ def lib():
         "msvgb_server_submit": (i32, [vp, ctypes.POINTER(_Om), ctypes.POINTER(ctypes.c_uint64)]),
         "msvgb_server_wait": (i32, [vp, ctypes.c_uint64, vp, vp, f64]),
         "msvgb_server_launches": (ctypes.c_uint64, [vp]),
+        "msvgb_server_solo_searches": (ctypes.c_uint64, [vp]),
         "msvgb_server_destroy": (i32, [vp]),
         "msvgb_pipeline_run": (i32, [vp, ctypes.POINTER(_Om), vp, vp, i64, i64, f64, i32, vp, vp,
                                      ctypes.POINTER(i64)]),
@@ -617,7 +618,13 @@ class Server:
 
     @property
     def launches(self) -> int:
+        """Launches of the persistent serving kernel."""
         return int(lib().msvgb_server_launches(self.h))
+
+    @property
+    def solo_searches(self) -> int:
+        """Requests run as their own single-query searches (M x residues >= 40e9)."""
+        return int(lib().msvgb_server_solo_searches(self.h))
 
     def close(self):
         if self.h:

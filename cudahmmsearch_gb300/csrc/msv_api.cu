@@ -352,18 +352,45 @@ int msvgb_detail::build_cost_tables(const msvgb_om *om, int f16, int C, std::vec
   return MSVGB_eslOK;
 }
 
-int msvgb_detail::profile_build_width(msvgb_ctx *ctx, const msvgb_om *om, int want_f16, int force_C,
-                                      msvgb_profile **ret) {
-  if (!om || !ret) return fail(MSVGB_eslEINVAL, "NULL argument");
+// DP width and table type of a profile's 32-lane tables: f16 when asked for
+// and possible, and whenever the int8 layout cannot hold M; force_C > 0
+// imposes the width.
+static int width_for(const msvgb_om *om, int want_f16, int force_C, int *ret_C, bool *ret_f16) {
+  if (!om) return fail(MSVGB_eslEINVAL, "NULL argument");
   if (om->M < 1) return fail(MSVGB_eslEINVAL, "profile M must be >= 1");
   if (om->Kp != 29) return fail(MSVGB_eslEINVAL, "only the amino alphabet (Kp = 29) is supported");
   if (!om->rbv) return fail(MSVGB_eslEINVAL, "rbv is NULL");
-  // f16 when asked for and possible, and whenever the int8 layout cannot hold M
   const int c16 = force_C > 0 ? force_C : choose_C(om->M, true);
   const bool f16 = c16 > 0 && c16 <= kMaxF16C && (want_f16 || (force_C <= 0 && choose_C(om->M, false) < 0));
   const int C = force_C > 0 ? force_C : choose_C(om->M, f16);
   if (C < 0) return fail(MSVGB_eslEINVAL, "profile M exceeds the supported maximum (8191 nodes)");
   if (C < need_C(om->M) || (!f16 && (C & 1))) return fail(MSVGB_eslEINVAL, "DP width too small for M");
+  *ret_C = C;
+  *ret_f16 = f16;
+  return MSVGB_eslOK;
+}
+
+// DP words per lane and 8-bit words per lane of the G-lane tables (G = 16 or
+// 8, or 32 for the split passes of models of 1024-2047 nodes).
+static int group_width(int M, int G, int *ret_C, int *ret_CI) {
+  if (G != 16 && G != 8 && G != 32) return fail(MSVGB_eslEINVAL, "lanes per sequence must be 32, 16 or 8");
+  const int C = M / (2 * G) + 1;                          // 2*C*G > M: the last node is padding
+  if (C > 32) return fail(MSVGB_eslEINVAL, "model too long for this many lanes per sequence");
+  if (C < 2) return fail(MSVGB_eslEINVAL, "model too short for this many lanes per sequence");
+  int CI = msvgb_detail::hyb_default_words(C, G);
+  if (CI > 0 && !msvgb_detail::hyb_compiled(C, G, CI)) CI = 0;
+  *ret_C = C;
+  *ret_CI = CI;
+  return MSVGB_eslOK;
+}
+
+int msvgb_detail::profile_build_width(msvgb_ctx *ctx, const msvgb_om *om, int want_f16, int force_C,
+                                      msvgb_profile **ret) {
+  if (!om || !ret) return fail(MSVGB_eslEINVAL, "NULL argument");
+  int C = 0;
+  bool f16 = true;
+  const int ws = width_for(om, want_f16, force_C, &C, &f16);
+  if (ws != MSVGB_eslOK) return ws;
   std::vector<uint32_t> st, mt;
   build_cost_tables(om, f16 ? 1 : 0, C, st, mt);
   const size_t swords = st.size(), mwords = mt.size();
@@ -394,15 +421,27 @@ static int default_f16() { return 1; }
 
 // Lanes per sequence and SSV table type from the context's tuning table (or
 // the fixed rule) for the whole length mix.
+// The choice msvgb_profile_create makes for a model of M nodes: G lanes per
+// sequence in the SSV pass; *split: lane-group tables are built (G < 32, or
+// the split 32-lane passes of models of 1024-2047 nodes); *want_f16: the
+// table type of the 32-lane tables.
+static void create_choice(msvgb_ctx *ctx, int M, int *G, bool *split, int *want_f16) {
+  int variant = default_f16();
+  *G = M >= 1 ? msvgb_detail::lanes_for(ctx, M, -1, &variant) : 32;
+  const bool wide = *G == 32 && M >= kWideSplitMinM && M / 64 + 1 <= 32;
+  *split = *G < 32 || wide;
+  *want_f16 = *split ? 1 : variant;
+}
+
 extern "C" int msvgb_profile_create(msvgb_ctx *ctx, const msvgb_om *om, msvgb_profile **ret) {
   if (!ctx) return fail(MSVGB_eslEINVAL, "ctx is NULL");
   if (ret) *ret = nullptr;
   if (!om) return fail(MSVGB_eslEINVAL, "om is NULL");
-  int variant = default_f16();
-  const int G = om->M >= 1 ? msvgb_detail::lanes_for(ctx, om->M, -1, &variant) : 32;
-  const bool wide = G == 32 && om->M >= kWideSplitMinM && om->M / 64 + 1 <= 32;
-  int st = profile_build(ctx, om, (G < 32 || wide) ? 1 : variant, ret);
-  if (st == MSVGB_eslOK && (G < 32 || wide) && (*ret)->f16) {
+  int G = 32, want_f16 = 1;
+  bool split = false;
+  create_choice(ctx, om->M, &G, &split, &want_f16);
+  int st = profile_build(ctx, om, want_f16, ret);
+  if (st == MSVGB_eslOK && split && (*ret)->f16) {
     st = msvgb_profile_set_lanes(*ret, om, G);
     if (st != MSVGB_eslOK) { msvgb_profile_destroy(*ret); *ret = nullptr; }
   }
@@ -495,12 +534,9 @@ extern "C" int msvgb_profile_set_lanes(msvgb_profile *p, const msvgb_om *om, int
     p->G = 32; p->CI = 0;
     return MSVGB_eslOK;
   }
-  if (G != 16 && G != 8 && G != 32) return fail(MSVGB_eslEINVAL, "lanes per sequence must be 32, 16 or 8");
-  const int C = p->M / (2 * G) + 1;                       // 2*C*G > M: the last node is padding
-  if (C > 32) return fail(MSVGB_eslEINVAL, "model too long for this many lanes per sequence");
-  if (C < 2) return fail(MSVGB_eslEINVAL, "model too short for this many lanes per sequence");
-  int CI = hyb_default_words(C, G);
-  if (CI > 0 && !hyb_compiled(C, G, CI)) CI = 0;
+  int C = 0, CI = 0;
+  const int gs = group_width(p->M, G, &C, &CI);
+  if (gs != MSVGB_eslOK) return gs;
   std::vector<uint32_t> st = CI ? build_hyb_table(om, C, G, CI) : build_group_table(om, C, G);
   CUDA_TRY(cudaSetDevice(p->device));
   uint32_t *d = nullptr;
@@ -519,6 +555,26 @@ extern "C" int msvgb_profile_set_lanes(msvgb_profile *p, const msvgb_om *om, int
 }
 
 extern "C" int msvgb_profile_lanes(const msvgb_profile *p) { return p ? p->G : -1; }
+
+int msvgb_detail::build_profile_tables(msvgb_ctx *ctx, const msvgb_om *om, ProfileTables &t) {
+  if (!ctx || !om) return fail(MSVGB_eslEINVAL, "NULL argument");
+  int G = 32, want_f16 = 1;
+  bool split = false, f16 = true;
+  create_choice(ctx, om->M, &G, &split, &want_f16);
+  t = ProfileTables();
+  int st = width_for(om, want_f16, 0, &t.C, &f16);
+  if (st != MSVGB_eslOK) return st;
+  t.f16 = f16 ? 1 : 0;
+  build_cost_tables(om, t.f16, t.C, t.st, t.mt);
+  if (split && f16) {
+    st = group_width(om->M, G, &t.Cg, &t.CI);
+    if (st != MSVGB_eslOK) return st;
+    t.G = G;
+    t.stg = t.CI ? build_hyb_table(om, t.Cg, G, t.CI) : build_group_table(om, t.Cg, G);
+    t.mtg = build_group_msv_table(om, t.Cg, G);
+  }
+  return MSVGB_eslOK;
+}
 
 // Mixed-width lane-group table: the first C - CI words of every lane as f16
 // bits of s units of 2^-24 (sign-magnitude: s < 0 -> 0x8000 | -s), the last

@@ -142,6 +142,15 @@ int xjmin_for(const msvgb_profile *p, int L, double F1);
 int profile_build_width(msvgb_ctx *ctx, const msvgb_om *om, int want_f16, int force_C, msvgb_profile **ret);
 // Host images of the device cost tables of a profile at DP width C.
 int build_cost_tables(const msvgb_om *om, int f16, int C, std::vector<uint32_t> &st, std::vector<uint32_t> &mt);
+// Host images of every device table msvgb_profile_create makes for om, at the
+// same widths, lane choice and table types.
+struct ProfileTables {
+  int C = 0, f16 = 1;                   // 32-lane tables: DP width, f16 or int8 SSV costs
+  int G = 32, Cg = 0, CI = 0;           // lane-group tables: lanes, DP width, 8-bit words (none when empty)
+  std::vector<uint32_t> st, mt;         // 32-lane SSV and MSV tables
+  std::vector<uint32_t> stg, mtg;       // G-lane SSV (mixed width when CI > 0) and MSV tables
+};
+int build_profile_tables(msvgb_ctx *ctx, const msvgb_om *om, ProfileTables &t);
 // Launches the G-lane SSV pass (msv_group.cuh); CI > 0: the mixed-width table.
 cudaError_t dispatch_group(int C, int G, int CI, const msvgb::GroupArgs &a, int sms);
 // Default 8-bit words per lane of the G-lane SSV pass at DP width C (0: f16 only).

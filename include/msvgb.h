@@ -369,6 +369,10 @@ int     msvgb_search_batch(msvgb_ctx *ctx, const msvgb_om *const *oms, int nprof
  * device-memory slot (its cost tables, per-length tables and n-byte results);
  * the number of slots is min(max_slots, mem_budget / slot size), and
  * msvgb_server_submit blocks until a slot is free (admission by memory).
+ * A request whose search fills the GPU alone (M x residues >= 40e9) runs
+ * instead as its own single-query search (the tables and lane choice of
+ * msvgb_profile_create), on one of two streams taken in turn; results are
+ * the same either way.
  * Profiles up to M = 2047. The database must outlive the server.
  * The counterpart in the reference is the fork's per-block pipeline thread
  * (code/src/cudaHmmsearch.cu:725-810) and hmmpgmd's resident sequence cache
@@ -383,7 +387,9 @@ int      msvgb_server_submit(msvgb_server *server, const msvgb_om *om, uint64_t 
  * host buffers (either may be NULL) and frees its slot. */
 int      msvgb_server_wait(msvgb_server *server, uint64_t ticket, uint8_t *out_xj, uint8_t *out_flags,
                            double timeout_s);
+/* Launches of the persistent kernel, and requests run as their own searches. */
 uint64_t msvgb_server_launches(const msvgb_server *server);
+uint64_t msvgb_server_solo_searches(const msvgb_server *server);
 int      msvgb_server_destroy(msvgb_server *server);
 
 /* ---- pipeline driver: streamed blocks, GPU MSV stage, CPU continuation -----------

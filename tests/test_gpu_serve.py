@@ -70,3 +70,30 @@ def test_memory_budget_bounds_slots(env):
     gx, gf = srv.wait(srv.submit(profs[1]))
     assert np.array_equal(gf, alone[1][1])
     srv.close()
+
+
+def test_requests_that_fill_the_gpu_run_as_own_searches():
+    """A database large enough that the larger models' requests (M x residues
+    >= 40e9 cells) run as their own single-query searches while the smaller
+    ones go through the serving kernel, all in flight together: every result
+    equals the plain path's, whichever way it ran."""
+    ctx = api.Context(0)
+    Ms = [60, 300, 1100, 1500, 2047, 900]
+    profs = [api.sample_profile(M, 700 + i, ctx) for i, M in enumerate(Ms)]
+    s = F.SeqSet.concat([F.synth_sequences(80_000, seed=71, lmax=12000)] +
+                        [F.emit_homologs(p, 50, seed=72 + i) for i, p in enumerate(profs)])
+    n_solo = sum(M * s.total >= 4e10 for M in Ms)
+    assert 0 < n_solo < len(Ms)                       # both kinds of request
+    db = api.DeviceDB(ctx, s)
+    alone = [api.search(ctx, api.DeviceProfile(ctx, p), db) for p in profs]
+    srv = api.Server(ctx, db, max_slots=16)          # every request admitted at once
+    order = list(range(len(Ms))) + list(range(len(Ms)))[::-1]
+    tickets = [srv.submit(profs[i]) for i in order]
+    for t, i in zip(tickets, order):
+        gx, gf = srv.wait(t)
+        assert np.array_equal(gx, alone[i][0]), f"M={Ms[i]} xj"
+        assert np.array_equal(gf, alone[i][1]), f"M={Ms[i]} flags"
+    assert srv.solo_searches == 2 * n_solo
+    assert srv.launches >= 1
+    srv.close()
+    ctx.close()
