@@ -439,15 +439,24 @@ def read_fasta(path: str):
     return F.SeqSet(codes, off), names
 
 
-def search_host(ctx: Context, prof: DeviceProfile, seqs: F.SeqSet, F1: float = 0.02, chunk_residues: int = 0):
+def search_host(ctx: Context, prof: DeviceProfile, seqs: F.SeqSet, F1: float = 0.02, chunk_residues: int = 0,
+                out=None):
     """End to end from host buffers (msvgb_search_host): chunked upload and
-    packing overlapped with the search. Returns (xj, flags) as search()."""
+    packing overlapped with the search. Returns (xj, flags) as search();
+    out: optional (xj, flags) uint8 arrays of n entries to write them to
+    (pinned ones make the results' copy a direct DMA)."""
     codes = np.ascontiguousarray(seqs.codes, dtype=np.uint8)
     if codes.size == 0:
         codes = np.zeros(1, np.uint8)
     off = np.ascontiguousarray(seqs.off, dtype=np.int64)
-    xj = np.zeros(seqs.n, np.uint8)
-    fl = np.zeros(seqs.n, np.uint8)
+    if out is not None:
+        xj, fl = out
+        if (xj.dtype != np.uint8 or fl.dtype != np.uint8 or xj.size != seqs.n or fl.size != seqs.n
+                or not xj.flags.c_contiguous or not fl.flags.c_contiguous):
+            raise ValueError("out must be two contiguous uint8 arrays of n entries")
+    else:
+        xj = np.zeros(seqs.n, np.uint8)
+        fl = np.zeros(seqs.n, np.uint8)
     _check(lib().msvgb_search_host(ctx.h, prof.h, codes.ctypes.data, off.ctypes.data, seqs.n, F1,
                                    chunk_residues, xj.ctypes.data, fl.ctypes.data))
     return xj, fl

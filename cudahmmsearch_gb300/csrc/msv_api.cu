@@ -9,6 +9,7 @@
 // Host floating point must round exactly like the reference's x86 build, so
 // this file is compiled with -ffp-contract=off (no fused multiply-add).
 #include <algorithm>
+#include <map>
 #include <atomic>
 #include <chrono>
 #include <cmath>
@@ -730,6 +731,36 @@ struct PhaseTimer {
   }
 };
 
+// Device-side timeline of one call (MSVGB_GPU_TRACE; unlike MSVGB_TRACE it
+// adds no synchronization): timed events recorded on the streams the work
+// runs on, printed relative to the first one once the call's work is done.
+static bool gpu_trace_on() { static const bool on = getenv("MSVGB_GPU_TRACE") != nullptr; return on; }
+struct GpuTrace {
+  struct Mark { std::string what; cudaEvent_t ev; std::chrono::steady_clock::time_point host; };
+  std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+  std::vector<Mark> marks;
+  // s: the stream to time on; null: host time only
+  void mark(const std::string &what, cudaStream_t s) {
+    if (!gpu_trace_on()) return;
+    cudaEvent_t e = nullptr;
+    if (s && cudaEventCreate(&e) == cudaSuccess && cudaEventRecord(e, s) != cudaSuccess) { cudaEventDestroy(e); e = nullptr; }
+    marks.push_back(Mark{what, e, std::chrono::steady_clock::now()});
+  }
+  // gpu times relative to the first timed mark; host times (when enqueued) relative to the trace's creation
+  void print() {
+    cudaEvent_t first = nullptr;
+    for (auto &m : marks) if (m.ev) { first = m.ev; break; }
+    for (auto &m : marks) {
+      float ms = -1.f;
+      if (m.ev && cudaEventSynchronize(m.ev) == cudaSuccess) cudaEventElapsedTime(&ms, first, m.ev);
+      fprintf(stderr, "msvgb trace: %-30s gpu %8.3f ms   host %8.3f ms\n", m.what.c_str(), ms,
+              std::chrono::duration<double, std::milli>(m.host - t0).count());
+    }
+    for (auto &m : marks) if (m.ev) cudaEventDestroy(m.ev);      // after the loop: first is the reference
+    marks.clear();
+  }
+};
+
 extern "C" int msvgb_db_create(msvgb_ctx *ctx, const uint8_t *codes, const int64_t *off, int64_t n,
                                msvgb_db **ret) {
   if (!ctx) return fail(MSVGB_eslEINVAL, "NULL argument");
@@ -768,16 +799,18 @@ cudaMemPool_t msvgb_detail::scratch_pool(int device) {
 // AsyncPack it returns when the database is complete on the device. With one,
 // it returns once everything is enqueued: invalid codes are OR-ed into
 // a->d_bad (checked by the caller) and db->ready completes when the database
-// is on the device.
+// is on the device; chunked (a->cuts), the chunks' residues are only copied,
+// and pack_chunk_on packs each.
 //
-// The offsets go up first, then the raw residues in one DMA on the context's
-// dma stream. Meanwhile the lengths are sorted on the device: lengths and
-// their maximum (the only value the host waits for before the end), per-length
-// counts, a scan of the counts by descending length (first sorted slot and
-// first packed byte of every length), placement; then the residues are
-// scattered into the packed layout. The counts come back to the host at the
-// end, for the distinct lengths the per-length tables need. Databases with
-// sequences longer than 4M residues are sorted on the host instead.
+// The offsets go up first, then the raw residues in one DMA (one per chunk)
+// on the context's dma stream. Meanwhile the lengths are sorted on the
+// device: lengths and their maximum (the only value the host waits for
+// before the end), counts per (chunk, length), a scan of the counts chunk by
+// chunk and by descending length (first sorted slot and first packed byte of
+// every key), placement; then the residues are scattered into the packed
+// layout. The counts come back to the host at the end, for the distinct
+// lengths the per-length tables need. Databases with sequences longer than 4M
+// residues are sorted on the host instead.
 int msvgb_detail::db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64_t *off, int64_t n,
                                cudaStream_t st, msvgb_db **ret, const AsyncPack *a) {
   if (!ctx || !ret || (n > 0 && (!off || !codes))) return fail(MSVGB_eslEINVAL, "NULL argument");
@@ -786,6 +819,19 @@ int msvgb_detail::db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64
   if (n < 0) return fail(MSVGB_eslEINVAL, "n < 0");
   const int64_t total = n ? off[n] - off[0] : 0;
   if (total < 0) return fail(MSVGB_eslEINVAL, "bad sequence offsets");
+  const bool chunked = a && a->cuts;
+  ChunkCuts cuts;                                             // one chunk unless chunked
+  cuts.cut[1] = n;
+  if (chunked) {
+    const std::vector<int64_t> &c = *a->cuts;
+    if (c.size() < 2 || c.size() > (size_t) kMaxChunks + 1 || c.front() != 0 || c.back() != n)
+      return fail(MSVGB_eslEINVAL, "bad chunk cuts");
+    for (size_t k = 0; k + 1 < c.size(); ++k)
+      if (c[k + 1] < c[k]) return fail(MSVGB_eslEINVAL, "bad chunk cuts");
+    cuts.K = (int) c.size() - 1;
+    for (size_t k = 0; k < c.size(); ++k) cuts.cut[k] = c[k];
+  }
+  const int K = cuts.K;
   CUDA_TRY(cudaSetDevice(ctx->device));
   const int64_t n1 = std::max<int64_t>(n, 1);
   cudaMemPool_t pool = scratch_pool(ctx->device);
@@ -799,20 +845,35 @@ int msvgb_detail::db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64
   int64_t *d_off = nullptr, *d_scal = nullptr;                // d_scal: [0] Lmax | bad << 32, [1] packed size
   int32_t *d_len_in = nullptr;
   uint8_t *d_raw = nullptr;
+  std::vector<cudaEvent_t> chunk_up;
   cudaEvent_t ev_raw = nullptr;
   CUDA_TRY(cudaEventCreateWithFlags(&ev_raw, cudaEventDisableTiming));
   cudaError_t e = alloc((void **) &d_off, (size_t) (n + 1) * 8, st);
   if (e == cudaSuccess) e = alloc((void **) &d_len_in, (size_t) n1 * 4, st);
   if (e == cudaSuccess) e = alloc((void **) &d_scal, 16, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(d_off, off, (size_t) (n + 1) * 8, cudaMemcpyHostToDevice, st);
-  const bool defer = a && a->defer_residues;
   if (e == cudaSuccess) e = cudaEventRecord(ev_raw, st);
-  if (!defer) {
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->dma, ev_raw, 0);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->dma, ev_raw, 0);
+  if (!chunked) {
     if (e == cudaSuccess) e = alloc((void **) &d_raw, (size_t) total, ctx->dma);
     if (e == cudaSuccess && total) e = cudaMemcpyAsync(d_raw, codes + off[0], total, cudaMemcpyHostToDevice, ctx->dma);
     if (e == cudaSuccess) e = cudaEventRecord(ev_raw, ctx->dma);
+  } else {
+    // kept past this call (pack_chunk_on reads it): not scratch
+    if (e == cudaSuccess) e = cudaMallocFromPoolAsync((void **) &d_raw, std::max<size_t>((size_t) total, 16), pool, ctx->dma);
+    for (int k = 0; k < K && e == cudaSuccess; ++k) {
+      const int64_t r0 = off[cuts.cut[k]] - off[0], r1 = off[cuts.cut[k + 1]] - off[0];
+      if (r1 > r0) e = cudaMemcpyAsync(d_raw + r0, codes + off[0] + r0, r1 - r0, cudaMemcpyHostToDevice, ctx->dma);
+      cudaEvent_t ev = nullptr;
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+      if (e == cudaSuccess) { chunk_up.push_back(ev); e = cudaEventRecord(ev, ctx->dma); }
+    }
   }
+  auto drop_chunk_inputs = [&]() {
+    for (cudaEvent_t ev : chunk_up) cudaEventDestroy(ev);
+    chunk_up.clear();
+    if (chunked && d_raw) { cudaStreamSynchronize(ctx->dma); cudaFreeAsync(d_raw, ctx->dma); d_raw = nullptr; }
+  };
   pt.mark("copies issued");
   if (e == cudaSuccess && ctx->h_pin_cap < 64) e = grow_pinned(ctx, 64);
   unsigned *misc = (unsigned *) ctx->h_pin;
@@ -832,6 +893,7 @@ int msvgb_detail::db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64
   };
   if (e != cudaSuccess || bad_len) {
     finish();
+    drop_chunk_inputs();
     cudaStreamSynchronize(st);
     if (e != cudaSuccess) return fail(MSVGB_eslESYS, std::string("database upload: ") + cudaGetErrorString(e));
     return fail(MSVGB_eslEINVAL, "bad sequence offsets");
@@ -840,8 +902,9 @@ int msvgb_detail::db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64
   msvgb_db *db = new msvgb_db();
   db->ctx = ctx; db->device = ctx->device; db->n = n; db->residues = total; db->Lmax = Lmax;
   db->serial = g_db_serial.fetch_add(1);
-  const bool gpu_sort = Lmax <= (1 << 22);
   const size_t nb = (size_t) Lmax + 1;
+  // the (chunk, length) keys of the device sort must fit an int and a modest table
+  const bool gpu_sort = Lmax <= (1 << 22) && (size_t) K * nb <= (size_t) (1 << 24);
   // packed size: exact after a host sort, an upper bound before the device scan
   int64_t pos = 0;
   const int64_t bound = gpu_sort ? total + 15 * n : 0;
@@ -852,44 +915,45 @@ int msvgb_detail::db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64
     return cudaMallocFromPoolAsync(ptr, std::max<size_t>(bytes, 16), pool, st);
   };
   int64_t *d_src = nullptr;
-  e = defer ? keep((void **) &d_src, (size_t) n1 * 8) : alloc((void **) &d_src, (size_t) n1 * 8, st);
-  if (e == cudaSuccess && defer) db->d_src_pending = d_src;
+  e = chunked ? keep((void **) &d_src, (size_t) n1 * 8) : alloc((void **) &d_src, (size_t) n1 * 8, st);
   if (e == cudaSuccess) e = keep((void **) &db->d_start, (size_t) n1 * 8);
   if (e == cudaSuccess) e = keep((void **) &db->d_orig, (size_t) n1 * 8);
   if (e == cudaSuccess) e = keep((void **) &db->d_len, (size_t) n1 * 4);
   unsigned long long *d_hist = nullptr;
+  std::map<std::pair<int, int32_t>, int64_t> host_hist;       // host sort: counts per (chunk, length)
+  auto chunk_of = [&](int64_t i) { int k = 0; while (k + 1 < K && i >= cuts.cut[k + 1]) ++k; return k; };
   if (e == cudaSuccess && gpu_sort) {
-    int64_t *d_bins = nullptr;                                // [0, Lmax] first slot, then first byte
+    int64_t *d_bins = nullptr;                                // per key: first slot, then first byte
     e = keep((void **) &db->d_codes, bound + 64);
-    if (e == cudaSuccess) e = alloc((void **) &d_hist, nb * 8, st);
-    if (e == cudaSuccess) e = alloc((void **) &d_bins, 2 * nb * 8, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(d_hist, 0, nb * 8, st);
-    if (e == cudaSuccess) e = launch_histogram(d_len_in, n, d_hist, ctx->num_sms, st);
-    if (e == cudaSuccess) e = launch_bins(d_hist, Lmax, d_bins, d_bins + nb, d_scal + 1, db->d_codes, st);
+    if (e == cudaSuccess) e = alloc((void **) &d_hist, K * nb * 8, st);
+    if (e == cudaSuccess) e = alloc((void **) &d_bins, 2 * K * nb * 8, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_hist, 0, K * nb * 8, st);
+    if (e == cudaSuccess) e = launch_histogram(d_len_in, n, d_hist, cuts, (int) nb, ctx->num_sms, st);
+    if (e == cudaSuccess) e = launch_bins(d_hist, Lmax, K, d_bins, d_bins + K * nb, d_scal + 1, db->d_codes, st);
     unsigned long long *cursor = nullptr;
-    if (e == cudaSuccess) e = alloc((void **) &cursor, nb * 8, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(cursor, d_bins, nb * 8, cudaMemcpyDeviceToDevice, st);
-    if (e == cudaSuccess) e = launch_place(d_off, d_len_in, n, cursor, d_bins, d_bins + nb, db->d_start,
-                                           db->d_orig, db->d_len, d_src, ctx->num_sms, st);
+    if (e == cudaSuccess) e = alloc((void **) &cursor, K * nb * 8, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(cursor, d_bins, K * nb * 8, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = launch_place(d_off, d_len_in, n, cursor, d_bins, d_bins + K * nb, db->d_start,
+                                           db->d_orig, db->d_len, d_src, cuts, (int) nb, ctx->num_sms, st);
     pt.mark("sort enqueued");
   } else if (e == cudaSuccess) {
-    // host fallback for very long sequences: stable sort by descending length
+    // host fallback for very long sequences: stable sort by chunk, then by
+    // descending length
     std::vector<int64_t> idx(n);
     for (int64_t i = 0; i < n; ++i) idx[i] = i;
-    std::stable_sort(idx.begin(), idx.end(),
-                     [&](int64_t x, int64_t y) { return off[x + 1] - off[x] > off[y + 1] - off[y]; });
+    std::stable_sort(idx.begin(), idx.end(), [&](int64_t x, int64_t y) {
+      const int cx = chunk_of(x), cy = chunk_of(y);
+      if (cx != cy) return cx < cy;
+      return off[x + 1] - off[x] > off[y + 1] - off[y];
+    });
     std::vector<int64_t> h_start(n), h_orig(n), h_src(n);
     std::vector<int32_t> h_len(n);
     for (int64_t s = 0; s < n; ++s) {
       const int64_t i = idx[s], L = off[i + 1] - off[i];
       h_orig[s] = i; h_len[s] = (int32_t) L; h_src[s] = off[i] - off[0]; h_start[s] = pos;
       pos += (L + 15) / 16 * 16;
-      if (L >= kLongTarget) db->n_long++;
-      if (s == 0 || h_len[s - 1] != L) { db->distinct_len.push_back((int32_t) L); db->len_count.push_back(0); }
-      db->len_count.back()++;
+      host_hist[{chunk_of(i), (int32_t) L}]++;
     }
-    std::reverse(db->distinct_len.begin(), db->distinct_len.end());
-    std::reverse(db->len_count.begin(), db->len_count.end());
     e = keep((void **) &db->d_codes, pos + 64);
     if (e == cudaSuccess) e = cudaMemsetAsync(db->d_codes + pos, PAD_CODE, 64, st);
     if (e == cudaSuccess && n) e = cudaMemcpyAsync(db->d_start, h_start.data(), n * 8, cudaMemcpyHostToDevice, st);
@@ -900,39 +964,73 @@ int msvgb_detail::db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64
     pt.mark("host sort");
   }
   // scatter the residues once they are up; then the counts and flags come back
-  if (e == cudaSuccess && ctx->h_pin_cap < 16 + nb * 8) e = grow_pinned(ctx, 16 + nb * 8);
+  const size_t hist_bytes = gpu_sort ? K * nb * 8 : 0;
+  if (e == cudaSuccess && ctx->h_pin_cap < 16 + hist_bytes) e = grow_pinned(ctx, 16 + hist_bytes);
   int *d_bad = a ? a->d_bad : ctx->d_bad;
   int64_t *h_scal = (int64_t *) ctx->h_pin;                   // [0] bad flag, [1] packed size, then counts
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev_raw, 0);
-  if (trace_on() && e == cudaSuccess) { e = cudaStreamSynchronize(st); pt.mark("residues up"); }
-  if (e == cudaSuccess && !a) e = cudaMemsetAsync(d_bad, 0, sizeof(int), st);
-  if (e == cudaSuccess && !defer) e = launch_pack(d_raw, d_src, db->d_start, db->d_len, n, db->d_codes, d_bad,
-                                                  ctx->num_sms, st);
-  if (defer) { db->raw_begin = n ? off[0] : 0; db->raw_total = total; db->d_bad_pending = d_bad; }
+  if (!chunked) {
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev_raw, 0);
+    if (trace_on() && e == cudaSuccess) { e = cudaStreamSynchronize(st); pt.mark("residues up"); }
+    if (e == cudaSuccess && !a) e = cudaMemsetAsync(d_bad, 0, sizeof(int), st);
+    if (e == cudaSuccess) e = launch_pack(d_raw, d_src, db->d_start, db->d_len, n, db->d_codes, d_bad,
+                                          ctx->num_sms, st);
+  }
   if (e == cudaSuccess) { h_scal[0] = 0; h_scal[1] = pos; }
   if (e == cudaSuccess && !a) e = cudaMemcpyAsync(h_scal, d_bad, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess && gpu_sort) e = cudaMemcpyAsync(h_scal + 1, d_scal + 1, 8, cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess && gpu_sort) e = cudaMemcpyAsync(h_scal + 2, d_hist, nb * 8, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && gpu_sort) e = cudaMemcpyAsync(h_scal + 2, d_hist, hist_bytes, cudaMemcpyDeviceToHost, st);
   finish();
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   pt.mark("pack");
-  if (e == cudaSuccess && gpu_sort) {
-    pos = h_scal[1];
-    const unsigned long long *hist = (const unsigned long long *) (h_scal + 2);
-    for (int L = 0; L <= Lmax; ++L)
-      if (hist[L]) {
-        db->distinct_len.push_back(L);
-        db->len_count.push_back((int64_t) hist[L]);
-        if (L >= kLongTarget) db->n_long += (int64_t) hist[L];
+  // distinct lengths (ascending) with their counts, over all chunks and per chunk (descending)
+  db->chunk_len.assign(K, {});
+  db->chunk_cnt.assign(K, {});
+  if (e == cudaSuccess) {
+    auto add = [&](int k, int32_t L, int64_t c) {
+      db->chunk_len[k].push_back(L);
+      db->chunk_cnt[k].push_back(c);
+    };
+    auto add_total = [&](int32_t L, int64_t c) {
+      db->distinct_len.push_back(L);
+      db->len_count.push_back(c);
+      if (L >= kLongTarget) db->n_long += c;
+    };
+    if (gpu_sort) {
+      pos = h_scal[1];
+      const unsigned long long *hist = (const unsigned long long *) (h_scal + 2);
+      for (int k = 0; k < K; ++k)
+        for (int L = Lmax; L >= 0; --L)
+          if (hist[(size_t) k * nb + L]) add(k, L, (int64_t) hist[(size_t) k * nb + L]);
+      for (int L = 0; L <= Lmax; ++L) {
+        int64_t c = 0;
+        for (int k = 0; k < K; ++k) c += (int64_t) hist[(size_t) k * nb + L];
+        if (c) add_total(L, c);
       }
+    } else {
+      std::map<int32_t, int64_t> all;
+      for (auto it = host_hist.rbegin(); it != host_hist.rend(); ++it) {   // within a chunk: descending length
+        add(it->first.first, it->first.second, it->second);
+        all[it->first.second] += it->second;
+      }
+      for (const auto &v : all) add_total(v.first, v.second);
+    }
   }
   db->packed_bytes = pos + 64;
-  if (e == cudaSuccess && a) e = cudaEventCreateWithFlags(&db->ready, cudaEventDisableTiming);
-  if (e == cudaSuccess && a && !defer) e = cudaEventRecord(db->ready, st);
-  if (e == cudaSuccess && n) count_launch();
+  if (chunked) {
+    db->chunk_slot.assign(cuts.cut, cuts.cut + K + 1);        // every chunk keeps its size
+    db->chunk_up = chunk_up;
+    chunk_up.clear();
+    db->d_raw = d_raw; d_raw = nullptr;
+    db->d_src = d_src;
+    db->d_bad_chunks = d_bad;
+  }
+  if (e == cudaSuccess && a && !chunked) e = cudaEventCreateWithFlags(&db->ready, cudaEventDisableTiming);
+  if (e == cudaSuccess && a && !chunked) e = cudaEventRecord(db->ready, st);
+  if (e == cudaSuccess && n && !chunked) count_launch();
   if (e != cudaSuccess) {
     cudaStreamSynchronize(st);
     cudaStreamSynchronize(ctx->dma);
+    drop_chunk_inputs();
     msvgb_db_destroy(db);
     return fail(e == cudaErrorMemoryAllocation ? MSVGB_eslEMEM : MSVGB_eslESYS,
                 std::string("database upload: ") + cudaGetErrorString(e));
@@ -945,38 +1043,31 @@ int msvgb_detail::db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64
   return MSVGB_eslOK;
 }
 
-int msvgb_detail::db_fill_on(msvgb_ctx *ctx, msvgb_db *db, const uint8_t *codes, cudaStream_t st) {
-  if (!db->d_src_pending) return fail(MSVGB_eslEINVAL, "database residues already in place");
-  CUDA_TRY(cudaSetDevice(ctx->device));
-  cudaMemPool_t pool = scratch_pool(ctx->device);
-  if (!pool) return fail(MSVGB_eslESYS, "database upload: no memory pool");
-  uint8_t *d_raw = nullptr;
-  cudaEvent_t ev = nullptr;
-  CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-  // the copy waits for nothing on st: the sorted placement it feeds was
-  // completed (and waited for) when the database was created
-  cudaError_t e = cudaMallocFromPoolAsync((void **) &d_raw, std::max<size_t>((size_t) db->raw_total, 16), pool, ctx->dma);
-  if (e == cudaSuccess && db->raw_total)
-    e = cudaMemcpyAsync(d_raw, codes + db->raw_begin, db->raw_total, cudaMemcpyHostToDevice, ctx->dma);
-  if (e == cudaSuccess) e = cudaEventRecord(ev, ctx->dma);
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev, 0);
-  if (e == cudaSuccess) e = launch_pack(d_raw, db->d_src_pending, db->d_start, db->d_len, db->n, db->d_codes,
-                                        db->d_bad_pending, ctx->num_sms, st);
-  if (e == cudaSuccess) e = cudaFreeAsync(d_raw, st);
-  if (e == cudaSuccess) e = cudaFreeAsync(db->d_src_pending, st);
-  if (e == cudaSuccess) e = cudaEventRecord(db->ready, st);
-  cudaEventDestroy(ev);
-  if (e != cudaSuccess) return fail(MSVGB_eslESYS, std::string("database upload: ") + cudaGetErrorString(e));
-  db->d_src_pending = nullptr;
-  count_launch();
+int msvgb_detail::pack_chunk_on(msvgb_ctx *ctx, msvgb_db *db, int k, cudaStream_t st) {
+  if (!db->d_raw || k < 0 || k + 1 >= (int) db->chunk_slot.size()) return fail(MSVGB_eslEINVAL, "no such chunk");
+  const int64_t s0 = db->chunk_slot[k], s1 = db->chunk_slot[k + 1];
+  CUDA_TRY(cudaStreamWaitEvent(st, db->chunk_up[k], 0));
+  if (s1 > s0) {
+    CUDA_TRY(launch_pack(db->d_raw, db->d_src + s0, db->d_start + s0, db->d_len + s0, s1 - s0, db->d_codes,
+                         db->d_bad_chunks, ctx->num_sms, st));
+    count_launch();
+  }
   return MSVGB_eslOK;
+}
+
+void msvgb_detail::release_chunks_on(msvgb_db *db, cudaStream_t st) {
+  if (db->d_raw) cudaFreeAsync(db->d_raw, st);
+  if (db->d_src) cudaFreeAsync(db->d_src, st);
+  db->d_raw = nullptr;
+  db->d_src = nullptr;
 }
 
 extern "C" int msvgb_db_destroy(msvgb_db *db) {
   if (!db) return MSVGB_eslOK;
   cudaSetDevice(db->device);
   cudaFree(db->d_codes); cudaFree(db->d_start); cudaFree(db->d_orig); cudaFree(db->d_len);
-  cudaFree(db->d_src_pending);
+  cudaFree(db->d_raw); cudaFree(db->d_src);
+  for (cudaEvent_t ev : db->chunk_up) cudaEventDestroy(ev);
   if (db->ready) cudaEventDestroy(db->ready);
   cudaFree(db->d_inv);
   delete db;
@@ -1100,81 +1191,165 @@ extern "C" int msvgb_search(msvgb_ctx *c, const msvgb_profile *p, const msvgb_db
   return st;
 }
 
-// End to end from host buffers. The sequences are cut into chunks by residue
-// count (below); while the GPU searches chunk k on the context's
-// stream, the host sorts chunk k+1 and its residues go up and are packed on
-// the upload stream. Results of all chunks land in one device buffer and come
-// back in one copy at the end.
-extern "C" int msvgb_search_host(msvgb_ctx *c, const msvgb_profile *p, const uint8_t *codes, const int64_t *off,
+// The search of a chunked database (db_create_on with cuts), chunk by chunk
+// as each chunk's residues arrive, on two streams taken in turn (S[0] the
+// context's stream, S[1] its upload stream): the chunk is packed, then its
+// long targets run on the 32-lane kernel and the rest in the lane-group SSV
+// pass (or everything in the 32-lane kernel for small searches and profiles
+// without lane groups). A chunk's packing and start fill the SMs the previous
+// chunk's pass leaves in its tail. All chunks append to one undecided list,
+// scored by one full-MSV pass at the end, on S[0].
+// ctr: 6 zeroed counters (per-stream tickets for the long and main passes,
+// the list count, the list ticket); list: room for db->n entries.
+static int search_chunked(msvgb_ctx *c, const msvgb_profile *p, msvgb_db *db, const LenTables *t, uint8_t *d_xj,
+                          uint8_t *d_flags, unsigned long long *ctr, int64_t *list, GpuTrace &gt) {
+  using namespace msvgb_detail;
+  const int sms = c->num_sms;
+  cudaStream_t S[2] = {c->stream, c->upload};
+  const DbDev full{db->d_codes, db->d_start, db->d_len, db->d_orig, db->n};
+  ProfDev P32;
+  P32.M = p->M; P32.C = p->C; P32.tbm = p->tbm; P32.tec = p->tec; P32.base = p->base; P32.bias = p->bias;
+  P32.stab = p->d_stab; P32.mtab = p->d_mtab; P32.tjb = t->d_tjb; P32.xjmin = t->d_xjmin; P32.ssv_f16 = p->f16;
+  // as in enqueue_search: lane groups only where the whole search is large
+  const bool small = p->lanes_auto && (double) p->M * (double) db->residues < 4e10;
+  const bool groups = p->d_stab_g && !small;
+  ProfDev P = P32;
+  int t_long = INT32_MAX;
+  if (groups) {
+    P.C = p->Cg; P.stab = p->d_stab_g; P.ssv_f16 = 1;
+    const double ngroups = (double) sms * 32.0 * (32.0 / p->G);
+    t_long = (int) std::min<double>(1e9, std::max<double>(kLongTarget, (double) db->residues / ngroups / 3.0));
+  }
+  const int K = (int) db->chunk_slot.size() - 1;
+  for (int k = 0; k < K; ++k) {
+    cudaStream_t s = S[k & 1];
+    unsigned long long *tk_long = ctr + (k & 1), *tk = ctr + 2 + (k & 1);
+    int st = pack_chunk_on(c, db, k, s);
+    if (st != MSVGB_eslOK) return st;
+    gt.mark("chunk " + std::to_string(k) + " packed", s);
+    const int64_t s0 = db->chunk_slot[k], s1 = db->chunk_slot[k + 1];
+    if (s1 == s0) continue;
+    const DbDev part{db->d_codes, db->d_start + s0, db->d_len + s0, db->d_orig + s0, s1 - s0};
+    const int64_t n_long = groups ? std::min(db->chunk_count_at_least(k, t_long), s1 - s0) : s1 - s0;
+    if (n_long > 0) {                                       // 32 lanes: long targets, or the whole chunk
+      LaunchArgs l;
+      l.P = P32; l.db = part; l.out_xj = d_xj; l.out_flags = d_flags; l.ticket = tk_long;
+      l.stream = s; l.grid = 0; l.skip_empty = 1; l.range_end = n_long;
+      CUDA_TRY(cudaMemsetAsync(tk_long, 0, sizeof(unsigned long long), s));
+      CUDA_TRY(dispatch(p->C, p->f16 != 0, l, sms));
+      count_launch();
+    }
+    if (groups && s0 + n_long < s1) {
+      GroupArgs g;
+      g.P = P; g.db = full; g.db.n = s1; g.out_xj = d_xj; g.out_flags = d_flags;
+      g.ticket = tk; g.undecided = list; g.n_undecided = ctr + 4; g.stream = s; g.s_begin = s0 + n_long;
+      CUDA_TRY(cudaMemsetAsync(tk, 0, sizeof(unsigned long long), s));
+      CUDA_TRY(dispatch_group(p->Cg, p->G, p->CI, g, sms));
+      count_launch();
+    }
+    gt.mark("chunk " + std::to_string(k) + " passed", s);
+  }
+  CUDA_TRY(cudaEventRecord(c->ev_join, S[1]));
+  CUDA_TRY(cudaStreamWaitEvent(S[0], c->ev_join, 0));
+  release_chunks_on(db, S[0]);
+  if (groups) {                                             // the full MSV of the undecided sequences
+    if (p->d_mtab_g) {
+      ProfDev Pl = P;
+      Pl.mtab = p->d_mtab_g;
+      CUDA_TRY(dispatch_list_group(p->Cg, p->G, Pl, full, d_xj, d_flags, ctr + 5, list, ctr + 4, sms, S[0]));
+    } else {
+      LaunchArgs a;
+      a.P = P32; a.db = full; a.out_xj = d_xj; a.out_flags = d_flags; a.ticket = ctr + 5;
+      a.stream = S[0]; a.grid = 0; a.skip_empty = 1; a.list = list; a.list_count = ctr + 4;
+      CUDA_TRY(dispatch(p->C, p->f16 != 0, a, sms));
+    }
+    count_launch();
+    gt.mark("list passed", S[0]);
+  }
+  return MSVGB_eslOK;
+}
+
+// End to end from host buffers. The input is cut into chunks of consecutive
+// sequences and sorted once, chunk by chunk (search_chunked). Its offsets go
+// up first and then every chunk's residues, back to back on the copy engine;
+// the first chunk is small, so that its search starts as soon as the sort
+// ends, and the copy (at ~4x the rate the search consumes residues) stays
+// ahead of the search from then on. Results land in one device buffer and
+// come back in one copy at the end.
+extern "C" int msvgb_search_host(msvgb_ctx *c, const msvgb_profile *pc, const uint8_t *codes, const int64_t *off,
                                  int64_t n, double F1, int64_t chunk_residues, uint8_t *out_xj,
                                  uint8_t *out_flags) {
-  if (!c || !p || n < 0 || (n && (!codes || !off || !out_xj || !out_flags)))
+  if (!c || !pc || n < 0 || (n && (!codes || !off || !out_xj || !out_flags)))
     return fail(MSVGB_eslEINVAL, "NULL argument");
+  if (pc->ctx != c) return fail(MSVGB_eslEINVAL, "objects belong to another context");
   if (n == 0) return MSVGB_eslOK;
+  msvgb_profile *p = const_cast<msvgb_profile *>(pc);
+  GpuTrace gt;
   CUDA_TRY(cudaSetDevice(c->device));
-  // chunk boundaries [cut[k], cut[k+1]): by default a sixth of the residues,
-  // then the rest (the rest's copy, at ~5x the search's residue rate, is up
-  // before the first sixth is searched; every further chunk adds a launch
-  // tail and a full-MSV pass, ~0.5 ms each), and one chunk when the whole
-  // copy takes less than that (kOneChunkResidues); with chunk_residues,
-  // chunks growing from a quarter of it to it
+  // chunk boundaries: by default a sixth of the residues, then chunks of a
+  // third (the remainder last); one chunk below kOneChunkResidues, where
+  // the whole copy is shorter than the sort; with chunk_residues, chunks
+  // growing from a quarter of it to it. At most kMaxChunks.
   std::vector<int64_t> cut(1, 0);
   const int64_t total = off[n] - off[0];
   constexpr int64_t kOneChunkResidues = 64 << 20;
   int64_t want = chunk_residues > 0 ? std::max<int64_t>(1, chunk_residues / 4)
-                                    : (total < kOneChunkResidues ? total : total / 6 + 1);
+                                    : (total < kOneChunkResidues ? std::max<int64_t>(1, total) : total / 6 + 1);
   for (int64_t b0 = 0; b0 < n;) {
-    int64_t b1 = b0 + 1;
-    while (b1 < n && off[b1] - off[b0] < want) ++b1;
+    // the first sequence boundary at least want residues past b0's start, or n
+    int64_t b1 = std::lower_bound(off + b0 + 1, off + n, off[b0] + want) - off;
+    if ((int) cut.size() == kMaxChunks) b1 = n;               // the last chunk takes the rest
     cut.push_back(b1);
     b0 = b1;
-    want = chunk_residues > 0 ? std::min(chunk_residues, 2 * want) : total;
+    want = chunk_residues > 0 ? std::min(chunk_residues, 2 * want) : total / 3 + 1;
   }
+  gt.mark("chunks cut", nullptr);
+  // device scratch: results [xj n | flags n], the invalid-code flag, 6 counters; the undecided list
+  const size_t o_bad = (2 * (size_t) n + 15) / 16 * 16, o_ctr = o_bad + 16;
   uint8_t *d = nullptr;
-  CUDA_TRY(cudaMallocAsync((void **) &d, 2 * (size_t) n + 64, c->stream));
-  int *d_bad = (int *) (d + ((2 * (size_t) n + 15) / 16) * 16);
-  CUDA_TRY(cudaMemsetAsync(d_bad, 0, sizeof(int), c->stream));
-  CUDA_TRY(cudaEventRecord(c->ev_fork, c->stream));
-  CUDA_TRY(cudaStreamWaitEvent(c->upload, c->ev_fork, 0));     // the flag is zero before any pack
-  std::vector<msvgb_db *> dbs;
-  int st = MSVGB_eslOK;
+  int64_t *d_list = nullptr;
+  CUDA_TRY(cudaMallocAsync((void **) &d, o_ctr + 6 * sizeof(unsigned long long), c->stream));
+  int *d_bad = (int *) (d + o_bad);
+  unsigned long long *ctr = (unsigned long long *) (d + o_ctr);
+  cudaError_t e = cudaMallocAsync((void **) &d_list, sizeof(int64_t) * (size_t) n, c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d + o_bad, 0, 16 + 6 * sizeof(unsigned long long), c->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(c->ev_fork, c->stream);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(c->upload, c->ev_fork, 0);   // scratch ready before any pack
+  if (e != cudaSuccess) {
+    cudaFreeAsync(d_list, c->stream);
+    cudaFreeAsync(d, c->stream);
+    cudaStreamSynchronize(c->stream);
+    return fail(MSVGB_eslESYS, std::string("search: ") + cudaGetErrorString(e));
+  }
+  gt.mark("start", c->stream);
   PhaseTimer pt;
-  // Every chunk is sorted before the first search, while the GPU is otherwise
-  // idle (sorting a chunk while the previous chunk's persistent search holds
-  // every SM would wait for that search): the first chunk completely, its
-  // residues going up while it is sorted, the others by their offsets only.
-  // Then chunk by chunk: the residues of a later chunk go up on the copy
-  // engine (under the previous chunk's search) and are packed, and the chunk
-  // is searched. (A later chunk's residue copy is queued only after the
-  // sorting: queued earlier, it would hold the copy engine in front of the
-  // sorting's offset copies.)
-  for (size_t k = 0; k + 1 < cut.size() && st == MSVGB_eslOK; ++k) {
-    const int64_t b0 = cut[k], b1 = cut[k + 1];
-    msvgb_db *db = nullptr;
-    AsyncPack a{d_bad};
-    a.defer_residues = k > 0;
-    st = db_create_on(c, codes, off + b0, b1 - b0, c->upload, &db, &a);
-    if (st == MSVGB_eslOK) dbs.push_back(db);
-  }
-  pt.mark("search_host: chunks sorted");
-  for (size_t k = 0; k < dbs.size() && st == MSVGB_eslOK; ++k) {
-    const int64_t b0 = cut[k];
-    if (k > 0) st = db_fill_on(c, dbs[k], codes, c->upload);
-    if (st == MSVGB_eslOK) st = msvgb_search_device(c, p, dbs[k], F1, d + b0, d + n + b0);
-    pt.mark("search_host: chunk enqueued");
-  }
+  msvgb_db *db = nullptr;
+  AsyncPack a{d_bad};
+  a.cuts = &cut;
+  int st = db_create_on(c, codes, off, n, c->upload, &db, &a);
+  gt.mark("sorted", c->upload);
+  pt.mark("search_host: sorted");
+  LenTables *t = nullptr;
+  if (st == MSVGB_eslOK) st = ensure_tables(p, db, F1, &t);
+  if (st == MSVGB_eslOK) st = search_chunked(c, p, db, t, d, d + n, ctr, d_list, gt);
+  pt.mark("search_host: enqueued");
   int bad = 0;
   if (st == MSVGB_eslOK) {
-    cudaError_t e = cudaMemcpyAsync(out_xj, d, n, cudaMemcpyDeviceToHost, c->stream);
+    e = cudaMemcpyAsync(out_xj, d, n, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(out_flags, d + n, n, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
     if (e != cudaSuccess) st = fail(MSVGB_eslESYS, std::string("search: ") + cudaGetErrorString(e));
   }
   cudaStreamSynchronize(c->upload);
+  cudaStreamSynchronize(c->dma);
+  cudaFreeAsync(d_list, c->stream);
   cudaFreeAsync(d, c->stream);
-  const cudaError_t e = cudaStreamSynchronize(c->stream);
-  pt.mark("search_host: last search done");
-  for (auto *db : dbs) msvgb_db_destroy(db);
+  e = cudaStreamSynchronize(c->stream);
+  pt.mark("search_host: done");
+  gt.mark("results back", c->stream);
+  msvgb_db_destroy(db);
+  gt.mark("database freed", nullptr);
+  gt.print();
   if (st == MSVGB_eslOK && e != cudaSuccess) st = fail(MSVGB_eslESYS, std::string("search: ") + cudaGetErrorString(e));
   if (st == MSVGB_eslOK && bad) st = fail(MSVGB_eslEINVAL, "residue code >= 29 (Kp)");
   return st;

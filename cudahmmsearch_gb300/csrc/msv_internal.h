@@ -105,12 +105,24 @@ struct msvgb_db {
   }
   int64_t packed_bytes = 0;           // size of d_codes
   cudaEvent_t ready = nullptr;        // set when packed asynchronously: completes when the data is in place
-  // Between a deferred creation and db_fill_on: where the residues go
-  // (scatter offsets, pool memory) and where they come from.
-  int64_t *d_src_pending = nullptr;
-  int64_t raw_begin = 0, raw_total = 0;
-  int *d_bad_pending = nullptr;
   int64_t *d_inv = nullptr;           // original index -> sorted slot, built on first use
+  // Created in chunks (msvgb_search_host): sorted slots [chunk_slot[k],
+  // chunk_slot[k+1]) hold the input's chunk k, longest first within it; the
+  // chunk's residues are in d_raw once chunk_up[k] completes and are packed
+  // by pack_chunk_on (then d_raw and d_src are released by release_chunks_on).
+  std::vector<int64_t> chunk_slot;
+  std::vector<std::vector<int32_t>> chunk_len;    // per chunk: its distinct lengths, descending
+  std::vector<std::vector<int64_t>> chunk_cnt;    // and their counts
+  std::vector<cudaEvent_t> chunk_up;
+  uint8_t *d_raw = nullptr;
+  int64_t *d_src = nullptr;
+  int *d_bad_chunks = nullptr;
+  // Sequences of length >= T in chunk k (they open its range).
+  int64_t chunk_count_at_least(size_t k, int T) const {
+    int64_t c = 0;
+    for (size_t i = 0; i < chunk_len[k].size() && chunk_len[k][i] >= T; ++i) c += chunk_cnt[k][i];
+    return c;
+  }
 };
 
 // Targets this long are scored with 32 lanes per sequence even when the
@@ -197,18 +209,27 @@ struct SearchScratch {
 // else the 32-lane kernel. The database must be in place on sc.stream.
 int enqueue_search(const SearchScratch &sc, const msvgb_profile *p, const msvgb_db *db, const LenTables *t,
                    uint8_t *d_xj, uint8_t *d_flags, int num_sms);
-// Asynchronous packing of one chunk (db_create_on).
+// Chunks of consecutive input sequences [cut[k], cut[k+1]), k < K, sorted
+// each on its own (msv_pack.cu).
+constexpr int kMaxChunks = 16;
+struct ChunkCuts {
+  int K = 1;
+  int64_t cut[kMaxChunks + 1] = {0};
+};
+// Asynchronous creation (db_create_on).
 struct AsyncPack {
   int *d_bad;      // device flag: set if a residue code is >= 29
-  // Sort only: the residues are not copied or packed now but by db_fill_on,
-  // which a search of the database must follow (db->ready is recorded then).
-  bool defer_residues = false;
+  // Chunked: the input cut at these sequence indices (0 first, n last, at
+  // most kMaxChunks chunks) is sorted chunk by chunk into one database; every
+  // chunk's residues go up on the context's dma stream right after the
+  // offsets, and nothing is packed: pack_chunk_on packs a chunk.
+  const std::vector<int64_t> *cuts = nullptr;
 };
-// The residue copy and packing of a database created with defer_residues:
-// the raw residues of codes (the same buffer and offsets as at creation) go
-// up on the context's dma stream and are packed on stream st; db->ready then
-// completes when the database is in place.
-int db_fill_on(msvgb_ctx *ctx, msvgb_db *db, const uint8_t *codes, cudaStream_t st);
+// Packs chunk k of a chunked database on stream st, once its residues are up.
+int pack_chunk_on(msvgb_ctx *ctx, msvgb_db *db, int k, cudaStream_t st);
+// Frees a chunked database's raw residues and scatter offsets on stream st,
+// which must be ordered after every pack_chunk_on.
+void release_chunks_on(msvgb_db *db, cudaStream_t st);
 // msvgb_db_create on stream st; with a, asynchronous (see msv_api.cu).
 int db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64_t *off, int64_t n, cudaStream_t st,
                  msvgb_db **ret, const AsyncPack *a = nullptr);
@@ -224,8 +245,9 @@ cudaError_t launch_pack(const uint8_t *raw, const int64_t *src, const int64_t *s
 // validity flag; per-length counts; sorted placement.
 cudaError_t launch_lengths(const int64_t *off, int64_t n, int32_t *len, unsigned *lmax, int *bad, int num_sms,
                            cudaStream_t stream);
-cudaError_t launch_histogram(const int32_t *len, int64_t n, unsigned long long *hist, int num_sms,
-                             cudaStream_t stream);
+// Counts per (chunk, length): hist[k * nb + L].
+cudaError_t launch_histogram(const int32_t *len, int64_t n, unsigned long long *hist, const ChunkCuts &cuts, int nb,
+                             int num_sms, cudaStream_t stream);
 // inv[orig[s]] = s (original index -> sorted slot); ids[j] = inv[ids[j]].
 cudaError_t launch_invert(const int64_t *orig, int64_t n, int64_t *inv, int num_sms, cudaStream_t stream);
 cudaError_t launch_gather_ids(int64_t *ids, int64_t n, const int64_t *inv, int num_sms, cudaStream_t stream);
@@ -234,15 +256,16 @@ cudaError_t launch_gather_ids(int64_t *ids, int64_t n, const int64_t *inv, int n
 // a bucket); nslots: the database's size; cnt: 1024 int32 of scratch.
 cudaError_t launch_order_by_slot(const int64_t *slots, int64_t n, int64_t nslots, int32_t *cnt, int64_t *order,
                                  int num_sms, cudaStream_t stream);
-cudaError_t launch_bins(const unsigned long long *hist, int Lmax, int64_t *bin_slot, int64_t *bin_byte, int64_t *pos,
-                        uint8_t *codes, cudaStream_t stream);
+cudaError_t launch_bins(const unsigned long long *hist, int Lmax, int K, int64_t *bin_slot, int64_t *bin_byte,
+                        int64_t *pos, uint8_t *codes, cudaStream_t stream);
 // Stream-ordered scratch allocations of database creation come from this
 // pool, which keeps up to 4 GiB mapped between calls (the default pool would
 // unmap and map again every time).
 cudaMemPool_t scratch_pool(int device);
 cudaError_t launch_place(const int64_t *off, const int32_t *len_in, int64_t n, unsigned long long *cursor,
                          const int64_t *bin_slot, const int64_t *bin_byte, int64_t *start, int64_t *orig,
-                         int32_t *len, int64_t *src, int num_sms, cudaStream_t stream);
+                         int32_t *len, int64_t *src, const ChunkCuts &cuts, int nb, int num_sms,
+                         cudaStream_t stream);
 }  // namespace msvgb_detail
 
 // Returns eslESYS (with the failing call in the message) from the enclosing

@@ -8,6 +8,9 @@
 // scans) and scatter the residues into the padded layout the search kernels
 // read, checking every code on the way. Sequences of equal length may land in
 // any order among themselves: each result is written to its original index.
+// The input may be cut into chunks of consecutive sequences (ChunkCuts): the
+// sort key is then (chunk, length), so every chunk keeps its own range of
+// sorted slots and of packed bytes, longest first within it.
 #include <algorithm>
 
 #include <cuda_runtime.h>
@@ -32,7 +35,10 @@ pack_kernel(const uint8_t *__restrict__ raw, const int64_t *__restrict__ src, co
       uint8_t c = (uint8_t) msvgb::PAD_CODE;
       if (j < L) {
         c = in[j];
-        badl |= (c >= 29);
+        if (c >= 29) {                 // flagged, and stored as padding: a search enqueued before the
+          badl = 1;                    // flag is read must never index past the cost tables' rows
+          c = (uint8_t) msvgb::PAD_CODE;
+        }
       }
       out[j] = c;
     }
@@ -59,29 +65,38 @@ len_kernel(const int64_t *__restrict__ off, int64_t n, int32_t *__restrict__ len
   if (__any_sync(0xffffffffu, b) && (threadIdx.x & 31) == 0) atomicOr(bad, 1);
 }
 
-// hist[L] = number of sequences of length L (warp-aggregated atomics).
+// Chunk of input sequence i.
+__device__ __forceinline__ int chunk_of(const msvgb_detail::ChunkCuts &c, int64_t i) {
+  int k = 0;
+  while (k + 1 < c.K && i >= c.cut[k + 1]) ++k;
+  return k;
+}
+
+// hist[k * nb + L] = number of sequences of length L in chunk k
+// (warp-aggregated atomics).
 __global__ void __launch_bounds__(256)
-hist_kernel(const int32_t *__restrict__ len, int64_t n, unsigned long long *__restrict__ hist) {
+hist_kernel(const int32_t *__restrict__ len, int64_t n, unsigned long long *__restrict__ hist,
+            msvgb_detail::ChunkCuts cuts, int nb) {
   const int64_t stride = (int64_t) gridDim.x * blockDim.x;
   for (int64_t i0 = (int64_t) blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
     const int64_t i = i0 + threadIdx.x;
     const bool in = i < n;
     const unsigned act = __ballot_sync(0xffffffffu, in);
     if (!in) continue;
-    const int L = len[i];
-    const unsigned peers = __match_any_sync(act, L);
-    if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&hist[L], (unsigned long long) __popc(peers));
+    const int key = chunk_of(cuts, i) * nb + len[i];
+    const unsigned peers = __match_any_sync(act, key);
+    if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&hist[key], (unsigned long long) __popc(peers));
   }
 }
 
-// Sorted slot of every sequence: the next free slot of its length
-// (cursor[L] starts at the first slot of length L); its padded start follows
-// from the slot's rank within the length.
+// Sorted slot of every sequence: the next free slot of its key (chunk,
+// length) (cursor[key] starts at the key's first slot); its padded start
+// follows from the slot's rank within the key.
 __global__ void __launch_bounds__(256)
 place_kernel(const int64_t *__restrict__ off, const int32_t *__restrict__ len_in, int64_t n,
              unsigned long long *__restrict__ cursor, const int64_t *__restrict__ bin_slot,
              const int64_t *__restrict__ bin_byte, int64_t *__restrict__ start, int64_t *__restrict__ orig,
-             int32_t *__restrict__ len, int64_t *__restrict__ src) {
+             int32_t *__restrict__ len, int64_t *__restrict__ src, msvgb_detail::ChunkCuts cuts, int nb) {
   const int64_t stride = (int64_t) gridDim.x * blockDim.x;
   for (int64_t i0 = (int64_t) blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
     const int64_t i = i0 + threadIdx.x;
@@ -89,35 +104,37 @@ place_kernel(const int64_t *__restrict__ off, const int32_t *__restrict__ len_in
     const unsigned act = __ballot_sync(0xffffffffu, in);
     if (!in) continue;
     const int L = len_in[i];
-    const unsigned peers = __match_any_sync(act, L);
+    const int key = chunk_of(cuts, i) * nb + L;
+    const unsigned peers = __match_any_sync(act, key);
     const int leader = __ffs(peers) - 1, lane = threadIdx.x & 31;
     unsigned long long base = 0;
-    if (lane == leader) base = atomicAdd(&cursor[L], (unsigned long long) __popc(peers));
+    if (lane == leader) base = atomicAdd(&cursor[key], (unsigned long long) __popc(peers));
     base = __shfl_sync(peers, base, leader);
     const int64_t s = (int64_t) base + __popc(peers & ((1u << lane) - 1u));
     const int64_t padded = ((int64_t) L + 15) / 16 * 16;
-    start[s] = bin_byte[L] + (s - bin_slot[L]) * padded;
+    start[s] = bin_byte[key] + (s - bin_slot[key]) * padded;
     orig[s] = i;
     len[s] = L;
     src[s] = off[i] - off[0];
   }
 }
 
-// Descending-length exclusive scans of the per-length counts: the first
-// sorted slot and first packed byte of every length, the packed size *pos,
-// and the padding tail after it in the packed buffer. One block of 1024.
+// Exclusive scans of the per-key counts, chunk by chunk and within a chunk
+// by descending length: the first sorted slot and first packed byte of every
+// key (chunk, length), the packed size *pos, and the padding tail after it
+// in the packed buffer. One block of 1024.
 __global__ void __launch_bounds__(1024)
-bins_kernel(const unsigned long long *__restrict__ hist, int Lmax, int64_t *__restrict__ bin_slot,
+bins_kernel(const unsigned long long *__restrict__ hist, int Lmax, int K, int64_t *__restrict__ bin_slot,
             int64_t *__restrict__ bin_byte, int64_t *__restrict__ pos_out, uint8_t *__restrict__ codes) {
   __shared__ int64_t s_cnt[1024], s_byt[1024];
   const int T = blockDim.x, t = threadIdx.x;
-  const int nb = Lmax + 1, per = (nb + T - 1) / T;
-  const int r0 = min(nb, t * per), r1 = min(nb, (t + 1) * per);   // descending ranks: L = Lmax - r
+  const int nb = Lmax + 1, nr = K * nb, per = (nr + T - 1) / T;
+  const int r0 = min(nr, t * per), r1 = min(nr, (t + 1) * per);   // rank r: chunk r / nb, L = Lmax - r % nb
   int64_t c = 0, b = 0;
   for (int r = r0; r < r1; ++r) {
-    const int L = Lmax - r;
-    c += (int64_t) hist[L];
-    b += (int64_t) hist[L] * (((int64_t) L + 15) / 16 * 16);
+    const int L = Lmax - r % nb, key = (r / nb) * nb + L;
+    c += (int64_t) hist[key];
+    b += (int64_t) hist[key] * (((int64_t) L + 15) / 16 * 16);
   }
   s_cnt[t] = c; s_byt[t] = b;
   __syncthreads();
@@ -129,10 +146,10 @@ bins_kernel(const unsigned long long *__restrict__ hist, int Lmax, int64_t *__re
   }
   int64_t slot = t ? s_cnt[t - 1] : 0, byte = t ? s_byt[t - 1] : 0;
   for (int r = r0; r < r1; ++r) {
-    const int L = Lmax - r;
-    bin_slot[L] = slot; bin_byte[L] = byte;
-    slot += (int64_t) hist[L];
-    byte += (int64_t) hist[L] * (((int64_t) L + 15) / 16 * 16);
+    const int L = Lmax - r % nb, key = (r / nb) * nb + L;
+    bin_slot[key] = slot; bin_byte[key] = byte;
+    slot += (int64_t) hist[key];
+    byte += (int64_t) hist[key] * (((int64_t) L + 15) / 16 * 16);
   }
   const int64_t pos = s_byt[T - 1];
   if (t == 0) *pos_out = pos;
@@ -209,11 +226,11 @@ cudaError_t msvgb_detail::launch_lengths(const int64_t *off, int64_t n, int32_t 
   return cudaGetLastError();
 }
 
-cudaError_t msvgb_detail::launch_histogram(const int32_t *len, int64_t n, unsigned long long *hist, int num_sms,
-                                           cudaStream_t stream) {
+cudaError_t msvgb_detail::launch_histogram(const int32_t *len, int64_t n, unsigned long long *hist,
+                                           const ChunkCuts &cuts, int nb, int num_sms, cudaStream_t stream) {
   if (n == 0) return cudaSuccess;
   (void) cudaGetLastError();
-  hist_kernel<<<grid_for(n, num_sms), 256, 0, stream>>>(len, n, hist);
+  hist_kernel<<<grid_for(n, num_sms), 256, 0, stream>>>(len, n, hist, cuts, nb);
   return cudaGetLastError();
 }
 
@@ -245,21 +262,21 @@ cudaError_t msvgb_detail::launch_order_by_slot(const int64_t *slots, int64_t n, 
   return cudaGetLastError();
 }
 
-cudaError_t msvgb_detail::launch_bins(const unsigned long long *hist, int Lmax, int64_t *bin_slot, int64_t *bin_byte,
-                                      int64_t *pos, uint8_t *codes, cudaStream_t stream) {
+cudaError_t msvgb_detail::launch_bins(const unsigned long long *hist, int Lmax, int K, int64_t *bin_slot,
+                                      int64_t *bin_byte, int64_t *pos, uint8_t *codes, cudaStream_t stream) {
   (void) cudaGetLastError();
-  bins_kernel<<<1, 1024, 0, stream>>>(hist, Lmax, bin_slot, bin_byte, pos, codes);
+  bins_kernel<<<1, 1024, 0, stream>>>(hist, Lmax, K, bin_slot, bin_byte, pos, codes);
   return cudaGetLastError();
 }
 
 cudaError_t msvgb_detail::launch_place(const int64_t *off, const int32_t *len_in, int64_t n,
                                        unsigned long long *cursor, const int64_t *bin_slot, const int64_t *bin_byte,
-                                       int64_t *start, int64_t *orig, int32_t *len, int64_t *src, int num_sms,
-                                       cudaStream_t stream) {
+                                       int64_t *start, int64_t *orig, int32_t *len, int64_t *src,
+                                       const ChunkCuts &cuts, int nb, int num_sms, cudaStream_t stream) {
   if (n == 0) return cudaSuccess;
   (void) cudaGetLastError();
   place_kernel<<<grid_for(n, num_sms), 256, 0, stream>>>(off, len_in, n, cursor, bin_slot, bin_byte, start, orig,
-                                                         len, src);
+                                                         len, src, cuts, nb);
   return cudaGetLastError();
 }
 

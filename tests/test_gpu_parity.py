@@ -240,3 +240,43 @@ def test_models_with_tables_in_global_memory(ctx, M):
     xj, fl = api.search(ctx, dp, api.DeviceDB(ctx, s))
     check_against_oracle(p, s, xj, fl, o)
     assert o["pass"].sum() >= 20
+
+
+def test_search_host_default_chunks_equal_resident_search(ctx):
+    """A database large enough for the default chunking (several chunks,
+    sorted chunk by chunk, searched as each chunk's residues arrive, one
+    full-MSV list at the end) and for lane groups: identical to the resident
+    search, and to the oracle on a sample."""
+    p, _, _ = load_case("m400_s1")
+    s = F.SeqSet.concat([F.synth_sequences(200_000, seed=81, lmax=20000), F.emit_homologs(p, 2000, seed=82),
+                         F.emit_homologs(p, 50, seed=83, repeat=20),
+                         F.SeqSet.from_list([np.zeros(0, np.uint8), np.array([7], np.uint8)])])
+    assert s.total >= 64 << 20
+    dp = api.DeviceProfile(ctx, p)
+    assert dp.lanes < 32
+    a = api.search(ctx, dp, api.DeviceDB(ctx, s))
+    for chunk in (0, s.total // 5):
+        b = api.search_host(ctx, dp, s, chunk_residues=chunk)
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    sub = np.random.default_rng(84).choice(s.n, size=3000, replace=False)
+    sub = np.sort(np.concatenate([sub, np.arange(s.n - 1052, s.n)]))
+    check_against_oracle(p, s.subset(sub), b[0][sub], b[1][sub], O.msv_batch(p, s.subset(sub)))
+
+
+@pytest.mark.parametrize("code", [29, 30, 200, 255])
+def test_search_host_rejects_invalid_codes_in_a_later_chunk(ctx, code):
+    """An invalid residue code in a chunk searched after the first: the call
+    fails with eslEINVAL (the chunk's search runs before the flag is read, on
+    the padding code stored in its place), and the context stays usable."""
+    p, _, _ = load_case("m200_s1")
+    s = F.synth_sequences(4000, seed=91, lmax=3000)
+    codes = s.codes.copy()
+    codes[s.off[3500] + 1] = code
+    bad = F.SeqSet(codes, s.off)
+    dp = api.DeviceProfile(ctx, p)
+    with pytest.raises(api.MSVError) as e:
+        api.search_host(ctx, dp, bad, chunk_residues=s.total // 8)
+    assert e.value.code == api.eslEINVAL
+    good = api.search_host(ctx, dp, s, chunk_residues=s.total // 8)
+    ref = api.search(ctx, dp, api.DeviceDB(ctx, s))
+    assert np.array_equal(good[0], ref[0]) and np.array_equal(good[1], ref[1])
