@@ -855,12 +855,12 @@ int msvgb_detail::db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64
   if (e == cudaSuccess) e = cudaEventRecord(ev_raw, st);
   if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->dma, ev_raw, 0);
   if (!chunked) {
-    if (e == cudaSuccess) e = alloc((void **) &d_raw, (size_t) total, ctx->dma);
+    if (e == cudaSuccess) e = alloc((void **) &d_raw, (size_t) total + 64, ctx->dma);   // slack: pack_kernel
     if (e == cudaSuccess && total) e = cudaMemcpyAsync(d_raw, codes + off[0], total, cudaMemcpyHostToDevice, ctx->dma);
     if (e == cudaSuccess) e = cudaEventRecord(ev_raw, ctx->dma);
   } else {
     // kept past this call (pack_chunk_on reads it): not scratch
-    if (e == cudaSuccess) e = cudaMallocFromPoolAsync((void **) &d_raw, std::max<size_t>((size_t) total, 16), pool, ctx->dma);
+    if (e == cudaSuccess) e = cudaMallocFromPoolAsync((void **) &d_raw, (size_t) total + 64, pool, ctx->dma);
     for (int k = 0; k < K && e == cudaSuccess; ++k) {
       const int64_t r0 = off[cuts.cut[k]] - off[0], r1 = off[cuts.cut[k + 1]] - off[0];
       if (r1 > r0) e = cudaMemcpyAsync(d_raw + r0, codes + off[0] + r0, r1 - r0, cudaMemcpyHostToDevice, ctx->dma);

@@ -19,6 +19,24 @@
 
 namespace {
 
+// One packed word: bytes at or past the sequence's end (valid = the bytes of
+// w still inside it, any value) become padding; codes >= 29 inside it are
+// flagged and become padding too (a search enqueued before the flag is read
+// must never index past the cost tables' rows). Per byte b, bit 7 of
+// ((b & 0x7f) + 99) | b is set exactly when b >= 29, with no carry between
+// bytes ((b & 0x7f) + 99 <= 226).
+__device__ __forceinline__ uint32_t pack_word(uint32_t w, int valid, int &badl) {
+  const uint32_t keep = valid >= 4 ? 0xFFFFFFFFu : valid <= 0 ? 0u : (1u << (8 * valid)) - 1u;
+  const uint32_t ge = ((((w & 0x7F7F7F7Fu) + 0x63636363u) | w) & 0x80808080u) & keep;
+  badl |= ge != 0u;
+  const uint32_t pad = ~keep | ((ge >> 7) * 0xFFu);
+  return (w & ~pad) | (0x1D1D1D1Du & pad);
+}
+
+// One warp per sequence; each lane writes 16 packed bytes at a time (the
+// packed starts are 16-byte aligned and the padded length a multiple of 16),
+// from the five aligned words that cover them in the raw buffer, shifted
+// into place. The raw buffer has 64 bytes of slack after its last residue.
 __global__ void __launch_bounds__(256)
 pack_kernel(const uint8_t *__restrict__ raw, const int64_t *__restrict__ src, const int64_t *__restrict__ start,
             const int32_t *__restrict__ len, int64_t n, uint8_t *__restrict__ packed, int *__restrict__ bad) {
@@ -29,18 +47,20 @@ pack_kernel(const uint8_t *__restrict__ raw, const int64_t *__restrict__ src, co
   for (int64_t s = warp; s < n; s += nwarps) {
     const int L = len[s];
     const int padded = (L + 15) & ~15;
-    const uint8_t *in = raw + src[s];
-    uint8_t *out = packed + start[s];
-    for (int j = lane; j < padded; j += 32) {
-      uint8_t c = (uint8_t) msvgb::PAD_CODE;
-      if (j < L) {
-        c = in[j];
-        if (c >= 29) {                 // flagged, and stored as padding: a search enqueued before the
-          badl = 1;                    // flag is read must never index past the cost tables' rows
-          c = (uint8_t) msvgb::PAD_CODE;
-        }
-      }
-      out[j] = c;
+    const uintptr_t in = (uintptr_t) (raw + src[s]);
+    const uint32_t *w = reinterpret_cast<const uint32_t *>(in & ~(uintptr_t) 3);
+    const unsigned sh = (unsigned) (in & 3) * 8u;
+    uint4 *out = reinterpret_cast<uint4 *>(packed + start[s]);
+    for (int j = lane * 16; j < padded; j += 32 * 16) {
+      const uint32_t *q = w + j / 4;
+      const uint32_t x0 = __ldg(q), x1 = __ldg(q + 1), x2 = __ldg(q + 2), x3 = __ldg(q + 3);
+      const uint32_t x4 = sh ? __ldg(q + 4) : 0u;
+      uint4 o;
+      o.x = pack_word(__funnelshift_r(x0, x1, sh), L - j, badl);
+      o.y = pack_word(__funnelshift_r(x1, x2, sh), L - j - 4, badl);
+      o.z = pack_word(__funnelshift_r(x2, x3, sh), L - j - 8, badl);
+      o.w = pack_word(__funnelshift_r(x3, x4, sh), L - j - 12, badl);
+      out[j / 16] = o;
     }
   }
   if (__any_sync(0xffffffffu, badl) && lane == 0) atomicOr(bad, 1);
