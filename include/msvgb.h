@@ -293,11 +293,15 @@ int msvgb_search_device(msvgb_ctx *ctx, const msvgb_profile *prof, const msvgb_d
                         void *d_xj, void *d_flags);
 
 /* End to end from host buffers, for a database that is not kept resident:
- * sequences codes[off[i] .. off[i+1]) (as msvgb_db_create takes them) are
- * uploaded and packed in chunks while earlier chunks are searched (by default
- * a sixth of the residues, then the rest, or one chunk below 64 M residues;
- * with chunk_residues > 0, chunks growing from a quarter of that size to it);
- * results as msvgb_search. The batched pre-pass the fork's p7_PipelineShort consumed
+ * sequences codes[off[i] .. off[i+1]) (as msvgb_db_create takes them) are cut
+ * into chunks of consecutive sequences (by default a sixth of the residues,
+ * then thirds, or one chunk below 64 M residues; with chunk_residues > 0,
+ * chunks growing from a quarter of that size to it; at most 16); the offsets
+ * go up and are sorted chunk by chunk while the chunks' residues follow, and
+ * every chunk is packed and searched as soon as it is up, the full MSV of all
+ * chunks' undecided sequences last. Results as msvgb_search; eslEINVAL for a
+ * code >= 29 (found while packing). Pinned host buffers make every copy a
+ * direct DMA. The batched pre-pass the fork's p7_PipelineShort consumed
  * (src/p7_pipeline.c:887-929), with the upload hidden behind the search. */
 int msvgb_search_host(msvgb_ctx *ctx, const msvgb_profile *prof, const uint8_t *codes, const int64_t *off,
                       int64_t n, double F1, int64_t chunk_residues, uint8_t *out_xj, uint8_t *out_flags);
