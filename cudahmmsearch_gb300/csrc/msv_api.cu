@@ -833,6 +833,8 @@ int msvgb_detail::db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64
   }
   const int K = cuts.K;
   CUDA_TRY(cudaSetDevice(ctx->device));
+  GpuTrace gt;
+  gt.mark("db: start", st);
   const int64_t n1 = std::max<int64_t>(n, 1);
   cudaMemPool_t pool = scratch_pool(ctx->device);
   if (!pool) return fail(MSVGB_eslESYS, "database upload: no memory pool");
@@ -852,6 +854,7 @@ int msvgb_detail::db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64
   if (e == cudaSuccess) e = alloc((void **) &d_len_in, (size_t) n1 * 4, st);
   if (e == cudaSuccess) e = alloc((void **) &d_scal, 16, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(d_off, off, (size_t) (n + 1) * 8, cudaMemcpyHostToDevice, st);
+  gt.mark("db: offsets up", st);
   if (e == cudaSuccess) e = cudaEventRecord(ev_raw, st);
   if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->dma, ev_raw, 0);
   if (!chunked) {
@@ -883,6 +886,7 @@ int msvgb_detail::db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64
   if (e == cudaSuccess) e = cudaMemcpyAsync(misc, d_scal, 8, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   pt.mark("lengths");
+  gt.mark("db: lengths (host waited)", st);
   const bool bad_len = e == cudaSuccess && misc[1] != 0;
   const int Lmax = e == cudaSuccess ? (int) misc[0] : 0;
   auto finish = [&]() {                                       // scratch frees, ordered after all use
@@ -923,19 +927,21 @@ int msvgb_detail::db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64
   std::map<std::pair<int, int32_t>, int64_t> host_hist;       // host sort: counts per (chunk, length)
   auto chunk_of = [&](int64_t i) { int k = 0; while (k + 1 < K && i >= cuts.cut[k + 1]) ++k; return k; };
   if (e == cudaSuccess && gpu_sort) {
-    int64_t *d_bins = nullptr;                                // per key: first slot, then first byte
+    int64_t *d_bins = nullptr;                                // per key: first slot, then first byte; scan scratch
     e = keep((void **) &db->d_codes, bound + 64);
     if (e == cudaSuccess) e = alloc((void **) &d_hist, K * nb * 8, st);
-    if (e == cudaSuccess) e = alloc((void **) &d_bins, 2 * K * nb * 8, st);
+    if (e == cudaSuccess) e = alloc((void **) &d_bins, (2 * K * nb + bins_scratch_words(Lmax, K)) * 8, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(d_hist, 0, K * nb * 8, st);
-    if (e == cudaSuccess) e = launch_histogram(d_len_in, n, d_hist, cuts, (int) nb, ctx->num_sms, st);
-    if (e == cudaSuccess) e = launch_bins(d_hist, Lmax, K, d_bins, d_bins + K * nb, d_scal + 1, db->d_codes, st);
+    if (e == cudaSuccess) e = launch_histogram(d_len_in, n, d_hist, cuts, Lmax, ctx->num_sms, st);
+    if (e == cudaSuccess) e = launch_bins(d_hist, Lmax, K, d_bins, d_bins + K * nb, d_bins + 2 * K * nb, d_scal + 1,
+                                          db->d_codes, st);
     unsigned long long *cursor = nullptr;
     if (e == cudaSuccess) e = alloc((void **) &cursor, K * nb * 8, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(cursor, d_bins, K * nb * 8, cudaMemcpyDeviceToDevice, st);
     if (e == cudaSuccess) e = launch_place(d_off, d_len_in, n, cursor, d_bins, d_bins + K * nb, db->d_start,
-                                           db->d_orig, db->d_len, d_src, cuts, (int) nb, ctx->num_sms, st);
+                                           db->d_orig, db->d_len, d_src, cuts, Lmax, ctx->num_sms, st);
     pt.mark("sort enqueued");
+    gt.mark("db: placed", st);
   } else if (e == cudaSuccess) {
     // host fallback for very long sequences: stable sort by chunk, then by
     // descending length
@@ -980,6 +986,7 @@ int msvgb_detail::db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64
   if (e == cudaSuccess && gpu_sort) e = cudaMemcpyAsync(h_scal + 1, d_scal + 1, 8, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess && gpu_sort) e = cudaMemcpyAsync(h_scal + 2, d_hist, hist_bytes, cudaMemcpyDeviceToHost, st);
   finish();
+  gt.mark("db: counts back", st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   pt.mark("pack");
   // distinct lengths (ascending) with their counts, over all chunks and per chunk (descending)
@@ -998,12 +1005,13 @@ int msvgb_detail::db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64
     if (gpu_sort) {
       pos = h_scal[1];
       const unsigned long long *hist = (const unsigned long long *) (h_scal + 2);
+      // hist in sorted key order: chunk k's lengths descending from k * nb
       for (int k = 0; k < K; ++k)
-        for (int L = Lmax; L >= 0; --L)
-          if (hist[(size_t) k * nb + L]) add(k, L, (int64_t) hist[(size_t) k * nb + L]);
+        for (int r = 0; r < (int) nb; ++r)
+          if (hist[(size_t) k * nb + r]) add(k, Lmax - r, (int64_t) hist[(size_t) k * nb + r]);
       for (int L = 0; L <= Lmax; ++L) {
         int64_t c = 0;
-        for (int k = 0; k < K; ++k) c += (int64_t) hist[(size_t) k * nb + L];
+        for (int k = 0; k < K; ++k) c += (int64_t) hist[(size_t) k * nb + (Lmax - L)];
         if (c) add_total(L, c);
       }
     } else {
@@ -1015,6 +1023,8 @@ int msvgb_detail::db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64
       for (const auto &v : all) add_total(v.first, v.second);
     }
   }
+  gt.mark("db: counts read", nullptr);
+  gt.print();
   db->packed_bytes = pos + 64;
   if (chunked) {
     db->chunk_slot.assign(cuts.cut, cuts.cut + K + 1);        // every chunk keeps its size

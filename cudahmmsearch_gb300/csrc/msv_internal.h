@@ -245,9 +245,9 @@ cudaError_t launch_pack(const uint8_t *raw, const int64_t *src, const int64_t *s
 // validity flag; per-length counts; sorted placement.
 cudaError_t launch_lengths(const int64_t *off, int64_t n, int32_t *len, unsigned *lmax, int *bad, int num_sms,
                            cudaStream_t stream);
-// Counts per (chunk, length): hist[k * nb + L].
-cudaError_t launch_histogram(const int32_t *len, int64_t n, unsigned long long *hist, const ChunkCuts &cuts, int nb,
-                             int num_sms, cudaStream_t stream);
+// Counts per (chunk, length), in sorted key order: hist[k * (Lmax + 1) + Lmax - L].
+cudaError_t launch_histogram(const int32_t *len, int64_t n, unsigned long long *hist, const ChunkCuts &cuts,
+                             int Lmax, int num_sms, cudaStream_t stream);
 // inv[orig[s]] = s (original index -> sorted slot); ids[j] = inv[ids[j]].
 cudaError_t launch_invert(const int64_t *orig, int64_t n, int64_t *inv, int num_sms, cudaStream_t stream);
 cudaError_t launch_gather_ids(int64_t *ids, int64_t n, const int64_t *inv, int num_sms, cudaStream_t stream);
@@ -256,15 +256,18 @@ cudaError_t launch_gather_ids(int64_t *ids, int64_t n, const int64_t *inv, int n
 // a bucket); nslots: the database's size; cnt: 1024 int32 of scratch.
 cudaError_t launch_order_by_slot(const int64_t *slots, int64_t n, int64_t nslots, int32_t *cnt, int64_t *order,
                                  int num_sms, cudaStream_t stream);
+// First slot and first packed byte of every key (scratch: bins_scratch_words
+// int64); *pos the packed size, and 64 padding codes after it in codes.
+int bins_scratch_words(int Lmax, int K);
 cudaError_t launch_bins(const unsigned long long *hist, int Lmax, int K, int64_t *bin_slot, int64_t *bin_byte,
-                        int64_t *pos, uint8_t *codes, cudaStream_t stream);
+                        int64_t *scratch, int64_t *pos, uint8_t *codes, cudaStream_t stream);
 // Stream-ordered scratch allocations of database creation come from this
 // pool, which keeps up to 4 GiB mapped between calls (the default pool would
 // unmap and map again every time).
 cudaMemPool_t scratch_pool(int device);
 cudaError_t launch_place(const int64_t *off, const int32_t *len_in, int64_t n, unsigned long long *cursor,
                          const int64_t *bin_slot, const int64_t *bin_byte, int64_t *start, int64_t *orig,
-                         int32_t *len, int64_t *src, const ChunkCuts &cuts, int nb, int num_sms,
+                         int32_t *len, int64_t *src, const ChunkCuts &cuts, int Lmax, int num_sms,
                          cudaStream_t stream);
 }  // namespace msvgb_detail
 

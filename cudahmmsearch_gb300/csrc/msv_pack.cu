@@ -92,18 +92,22 @@ __device__ __forceinline__ int chunk_of(const msvgb_detail::ChunkCuts &c, int64_
   return k;
 }
 
-// hist[k * nb + L] = number of sequences of length L in chunk k
+// Keys in sorted order: chunk k, then descending length L, at k * nb + (Lmax - L)
+// (nb = Lmax + 1).
+__device__ __forceinline__ int sort_key(int k, int L, int Lmax) { return k * (Lmax + 1) + (Lmax - L); }
+
+// hist[sort_key(k, L)] = number of sequences of length L in chunk k
 // (warp-aggregated atomics).
 __global__ void __launch_bounds__(256)
 hist_kernel(const int32_t *__restrict__ len, int64_t n, unsigned long long *__restrict__ hist,
-            msvgb_detail::ChunkCuts cuts, int nb) {
+            msvgb_detail::ChunkCuts cuts, int Lmax) {
   const int64_t stride = (int64_t) gridDim.x * blockDim.x;
   for (int64_t i0 = (int64_t) blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
     const int64_t i = i0 + threadIdx.x;
     const bool in = i < n;
     const unsigned act = __ballot_sync(0xffffffffu, in);
     if (!in) continue;
-    const int key = chunk_of(cuts, i) * nb + len[i];
+    const int key = sort_key(chunk_of(cuts, i), len[i], Lmax);
     const unsigned peers = __match_any_sync(act, key);
     if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&hist[key], (unsigned long long) __popc(peers));
   }
@@ -116,7 +120,7 @@ __global__ void __launch_bounds__(256)
 place_kernel(const int64_t *__restrict__ off, const int32_t *__restrict__ len_in, int64_t n,
              unsigned long long *__restrict__ cursor, const int64_t *__restrict__ bin_slot,
              const int64_t *__restrict__ bin_byte, int64_t *__restrict__ start, int64_t *__restrict__ orig,
-             int32_t *__restrict__ len, int64_t *__restrict__ src, msvgb_detail::ChunkCuts cuts, int nb) {
+             int32_t *__restrict__ len, int64_t *__restrict__ src, msvgb_detail::ChunkCuts cuts, int Lmax) {
   const int64_t stride = (int64_t) gridDim.x * blockDim.x;
   for (int64_t i0 = (int64_t) blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
     const int64_t i = i0 + threadIdx.x;
@@ -124,7 +128,7 @@ place_kernel(const int64_t *__restrict__ off, const int32_t *__restrict__ len_in
     const unsigned act = __ballot_sync(0xffffffffu, in);
     if (!in) continue;
     const int L = len_in[i];
-    const int key = chunk_of(cuts, i) * nb + L;
+    const int key = sort_key(chunk_of(cuts, i), L, Lmax);
     const unsigned peers = __match_any_sync(act, key);
     const int leader = __ffs(peers) - 1, lane = threadIdx.x & 31;
     unsigned long long base = 0;
@@ -139,41 +143,98 @@ place_kernel(const int64_t *__restrict__ off, const int32_t *__restrict__ len_in
   }
 }
 
-// Exclusive scans of the per-key counts, chunk by chunk and within a chunk
-// by descending length: the first sorted slot and first packed byte of every
-// key (chunk, length), the packed size *pos, and the padding tail after it
-// in the packed buffer. One block of 1024.
-__global__ void __launch_bounds__(1024)
-bins_kernel(const unsigned long long *__restrict__ hist, int Lmax, int K, int64_t *__restrict__ bin_slot,
-            int64_t *__restrict__ bin_byte, int64_t *__restrict__ pos_out, uint8_t *__restrict__ codes) {
-  __shared__ int64_t s_cnt[1024], s_byt[1024];
-  const int T = blockDim.x, t = threadIdx.x;
-  const int nb = Lmax + 1, nr = K * nb, per = (nr + T - 1) / T;
-  const int r0 = min(nr, t * per), r1 = min(nr, (t + 1) * per);   // rank r: chunk r / nb, L = Lmax - r % nb
-  int64_t c = 0, b = 0;
-  for (int r = r0; r < r1; ++r) {
-    const int L = Lmax - r % nb, key = (r / nb) * nb + L;
-    c += (int64_t) hist[key];
-    b += (int64_t) hist[key] * (((int64_t) L + 15) / 16 * 16);
-  }
-  s_cnt[t] = c; s_byt[t] = b;
+// Exclusive scans of the per-key counts in key order (chunk by chunk, and
+// within a chunk by descending length): the first sorted slot and first
+// packed byte of every key, the packed size *pos, and the padding tail after
+// it in the packed buffer. Three phases over tiles of kScanTile keys: per-tile
+// totals, a scan of the totals in one block, then every tile's own scan from
+// its offset. A thread takes kScanPer consecutive keys.
+constexpr int kScanPer = 16, kScanThreads = 256, kScanTile = kScanPer * kScanThreads;
+
+__device__ __forceinline__ int64_t key_bytes(int r, int Lmax) {   // packed bytes of one sequence of key r
+  const int L = Lmax - r % (Lmax + 1);
+  return ((int64_t) L + 15) / 16 * 16;
+}
+
+// Inclusive scan of (a, b) over the block (Hillis-Steele in shared memory); T threads.
+template <int T>
+__device__ __forceinline__ void block_scan2(int64_t &a, int64_t &b, int64_t *sa, int64_t *sb) {
+  const int t = threadIdx.x;
+  sa[t] = a; sb[t] = b;
   __syncthreads();
-  for (int d = 1; d < T; d <<= 1) {                 // inclusive scan
-    const int64_t vc = t >= d ? s_cnt[t - d] : 0, vb = t >= d ? s_byt[t - d] : 0;
+  for (int d = 1; d < T; d <<= 1) {
+    const int64_t va = t >= d ? sa[t - d] : 0, vb = t >= d ? sb[t - d] : 0;
     __syncthreads();
-    s_cnt[t] += vc; s_byt[t] += vb;
+    sa[t] += va; sb[t] += vb;
     __syncthreads();
   }
-  int64_t slot = t ? s_cnt[t - 1] : 0, byte = t ? s_byt[t - 1] : 0;
-  for (int r = r0; r < r1; ++r) {
-    const int L = Lmax - r % nb, key = (r / nb) * nb + L;
-    bin_slot[key] = slot; bin_byte[key] = byte;
-    slot += (int64_t) hist[key];
-    byte += (int64_t) hist[key] * (((int64_t) L + 15) / 16 * 16);
+  a = sa[t]; b = sb[t];
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+bins_tile_kernel(const unsigned long long *__restrict__ hist, int nr, int Lmax, int64_t *__restrict__ tile_cnt,
+                 int64_t *__restrict__ tile_byt) {
+  __shared__ int64_t sa[kScanThreads], sb[kScanThreads];
+  const int r0 = blockIdx.x * kScanTile + threadIdx.x * kScanPer;
+  int64_t c = 0, b = 0;
+#pragma unroll
+  for (int j = 0; j < kScanPer; ++j)
+    if (r0 + j < nr) {
+      const int64_t h = (int64_t) hist[r0 + j];
+      c += h;
+      b += h * key_bytes(r0 + j, Lmax);
+    }
+  block_scan2<kScanThreads>(c, b, sa, sb);
+  if (threadIdx.x == kScanThreads - 1) { tile_cnt[blockIdx.x] = c; tile_byt[blockIdx.x] = b; }
+}
+
+// Exclusive scan of the ntiles totals in place (one block of 1024; ntiles <=
+// 4 * 1024); the grand total of bytes is the packed size.
+__global__ void __launch_bounds__(1024)
+bins_top_kernel(int64_t *__restrict__ tile_cnt, int64_t *__restrict__ tile_byt, int ntiles,
+                int64_t *__restrict__ pos_out, uint8_t *__restrict__ codes) {
+  __shared__ int64_t sa[1024], sb[1024];
+  const int t = threadIdx.x, per = (ntiles + 1023) / 1024;
+  const int i0 = min(ntiles, t * per), i1 = min(ntiles, (t + 1) * per);
+  int64_t c = 0, b = 0;
+  for (int i = i0; i < i1; ++i) { c += tile_cnt[i]; b += tile_byt[i]; }
+  int64_t ic = c, ib = b;
+  block_scan2<1024>(ic, ib, sa, sb);
+  int64_t oc = ic - c, ob = ib - b;                  // exclusive offsets of this thread's first tile
+  for (int i = i0; i < i1; ++i) {
+    const int64_t tc = tile_cnt[i], tb = tile_byt[i];
+    tile_cnt[i] = oc; tile_byt[i] = ob;
+    oc += tc; ob += tb;
   }
-  const int64_t pos = s_byt[T - 1];
+  const int64_t pos = sb[1023];
   if (t == 0) *pos_out = pos;
   if (t < 64) codes[pos + t] = (uint8_t) msvgb::PAD_CODE;
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+bins_fill_kernel(const unsigned long long *__restrict__ hist, int nr, int Lmax, const int64_t *__restrict__ tile_cnt,
+                 const int64_t *__restrict__ tile_byt, int64_t *__restrict__ bin_slot,
+                 int64_t *__restrict__ bin_byte) {
+  __shared__ int64_t sa[kScanThreads], sb[kScanThreads];
+  const int r0 = blockIdx.x * kScanTile + threadIdx.x * kScanPer;
+  int64_t h[kScanPer];
+  int64_t c = 0, b = 0;
+#pragma unroll
+  for (int j = 0; j < kScanPer; ++j) {
+    h[j] = r0 + j < nr ? (int64_t) hist[r0 + j] : 0;
+    c += h[j];
+    b += h[j] * key_bytes(r0 + j, Lmax);
+  }
+  int64_t ic = c, ib = b;
+  block_scan2<kScanThreads>(ic, ib, sa, sb);
+  int64_t slot = tile_cnt[blockIdx.x] + ic - c, byte = tile_byt[blockIdx.x] + ib - b;
+#pragma unroll
+  for (int j = 0; j < kScanPer; ++j)
+    if (r0 + j < nr) {
+      bin_slot[r0 + j] = slot; bin_byte[r0 + j] = byte;
+      slot += h[j];
+      byte += h[j] * key_bytes(r0 + j, Lmax);
+    }
 }
 
 // inv[orig[s]] = s: original index -> sorted slot
@@ -247,10 +308,10 @@ cudaError_t msvgb_detail::launch_lengths(const int64_t *off, int64_t n, int32_t 
 }
 
 cudaError_t msvgb_detail::launch_histogram(const int32_t *len, int64_t n, unsigned long long *hist,
-                                           const ChunkCuts &cuts, int nb, int num_sms, cudaStream_t stream) {
+                                           const ChunkCuts &cuts, int Lmax, int num_sms, cudaStream_t stream) {
   if (n == 0) return cudaSuccess;
   (void) cudaGetLastError();
-  hist_kernel<<<grid_for(n, num_sms), 256, 0, stream>>>(len, n, hist, cuts, nb);
+  hist_kernel<<<grid_for(n, num_sms), 256, 0, stream>>>(len, n, hist, cuts, Lmax);
   return cudaGetLastError();
 }
 
@@ -282,21 +343,32 @@ cudaError_t msvgb_detail::launch_order_by_slot(const int64_t *slots, int64_t n, 
   return cudaGetLastError();
 }
 
+int msvgb_detail::bins_scratch_words(int Lmax, int K) {
+  const int nr = K * (Lmax + 1);
+  return 2 * ((nr + kScanTile - 1) / kScanTile);
+}
+
 cudaError_t msvgb_detail::launch_bins(const unsigned long long *hist, int Lmax, int K, int64_t *bin_slot,
-                                      int64_t *bin_byte, int64_t *pos, uint8_t *codes, cudaStream_t stream) {
+                                      int64_t *bin_byte, int64_t *scratch, int64_t *pos, uint8_t *codes,
+                                      cudaStream_t stream) {
+  const int nr = K * (Lmax + 1), ntiles = (nr + kScanTile - 1) / kScanTile;
+  if (ntiles > 4 * 1024) return cudaErrorInvalidValue;                 // bins_top_kernel's limit
+  int64_t *tile_cnt = scratch, *tile_byt = scratch + ntiles;
   (void) cudaGetLastError();
-  bins_kernel<<<1, 1024, 0, stream>>>(hist, Lmax, K, bin_slot, bin_byte, pos, codes);
+  bins_tile_kernel<<<ntiles, kScanThreads, 0, stream>>>(hist, nr, Lmax, tile_cnt, tile_byt);
+  bins_top_kernel<<<1, 1024, 0, stream>>>(tile_cnt, tile_byt, ntiles, pos, codes);
+  bins_fill_kernel<<<ntiles, kScanThreads, 0, stream>>>(hist, nr, Lmax, tile_cnt, tile_byt, bin_slot, bin_byte);
   return cudaGetLastError();
 }
 
 cudaError_t msvgb_detail::launch_place(const int64_t *off, const int32_t *len_in, int64_t n,
                                        unsigned long long *cursor, const int64_t *bin_slot, const int64_t *bin_byte,
                                        int64_t *start, int64_t *orig, int32_t *len, int64_t *src,
-                                       const ChunkCuts &cuts, int nb, int num_sms, cudaStream_t stream) {
+                                       const ChunkCuts &cuts, int Lmax, int num_sms, cudaStream_t stream) {
   if (n == 0) return cudaSuccess;
   (void) cudaGetLastError();
   place_kernel<<<grid_for(n, num_sms), 256, 0, stream>>>(off, len_in, n, cursor, bin_slot, bin_byte, start, orig,
-                                                         len, src, cuts, nb);
+                                                         len, src, cuts, Lmax);
   return cudaGetLastError();
 }
 
