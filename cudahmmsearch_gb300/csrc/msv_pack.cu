@@ -96,21 +96,16 @@ __device__ __forceinline__ int chunk_of(const msvgb_detail::ChunkCuts &c, int64_
 // (nb = Lmax + 1).
 __device__ __forceinline__ int sort_key(int k, int L, int Lmax) { return k * (Lmax + 1) + (Lmax - L); }
 
-// hist[sort_key(k, L)] = number of sequences of length L in chunk k
-// (warp-aggregated atomics).
+// hist[sort_key(k, L)] = number of sequences of length L in chunk k, one
+// atomic per sequence (a warp's 32 lengths are mostly distinct; aggregating
+// equal ones with a warp match first measured the same: 0.11 ms for
+// 2,000,000 sequences, bound by the atomics on the most frequent lengths).
 __global__ void __launch_bounds__(256)
 hist_kernel(const int32_t *__restrict__ len, int64_t n, unsigned long long *__restrict__ hist,
             msvgb_detail::ChunkCuts cuts, int Lmax) {
   const int64_t stride = (int64_t) gridDim.x * blockDim.x;
-  for (int64_t i0 = (int64_t) blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
-    const int64_t i = i0 + threadIdx.x;
-    const bool in = i < n;
-    const unsigned act = __ballot_sync(0xffffffffu, in);
-    if (!in) continue;
-    const int key = sort_key(chunk_of(cuts, i), len[i], Lmax);
-    const unsigned peers = __match_any_sync(act, key);
-    if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&hist[key], (unsigned long long) __popc(peers));
-  }
+  for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    atomicAdd(&hist[sort_key(chunk_of(cuts, i), len[i], Lmax)], 1ull);
 }
 
 // Sorted slot of every sequence: the next free slot of its key (chunk,
@@ -122,19 +117,10 @@ place_kernel(const int64_t *__restrict__ off, const int32_t *__restrict__ len_in
              const int64_t *__restrict__ bin_byte, int64_t *__restrict__ start, int64_t *__restrict__ orig,
              int32_t *__restrict__ len, int64_t *__restrict__ src, msvgb_detail::ChunkCuts cuts, int Lmax) {
   const int64_t stride = (int64_t) gridDim.x * blockDim.x;
-  for (int64_t i0 = (int64_t) blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
-    const int64_t i = i0 + threadIdx.x;
-    const bool in = i < n;
-    const unsigned act = __ballot_sync(0xffffffffu, in);
-    if (!in) continue;
+  for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     const int L = len_in[i];
     const int key = sort_key(chunk_of(cuts, i), L, Lmax);
-    const unsigned peers = __match_any_sync(act, key);
-    const int leader = __ffs(peers) - 1, lane = threadIdx.x & 31;
-    unsigned long long base = 0;
-    if (lane == leader) base = atomicAdd(&cursor[key], (unsigned long long) __popc(peers));
-    base = __shfl_sync(peers, base, leader);
-    const int64_t s = (int64_t) base + __popc(peers & ((1u << lane) - 1u));
+    const int64_t s = (int64_t) atomicAdd(&cursor[key], 1ull);      // one atomic per sequence, as hist_kernel
     const int64_t padded = ((int64_t) L + 15) / 16 * 16;
     start[s] = bin_byte[key] + (s - bin_slot[key]) * padded;
     orig[s] = i;
