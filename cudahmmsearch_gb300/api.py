@@ -714,7 +714,8 @@ def pipeline_filters(ctx: Context, p: F.Profile, seqs: F.SeqSet, *, vprof: F.VPr
         if sink.n <= cap:
             break
         cap = sink.n
-    hits = np.sort(buf[:sink.n], order="seq_index")
+    hits = buf[:sink.n]
+    hits = hits[np.argsort(hits["seq_index"], kind="stable")]   # a structured-array sort compares whole records
     return hits, stats
 
 

@@ -644,11 +644,25 @@ extern "C" int msvgb_profile_ssv_int8_words(const msvgb_profile *p) { return p ?
 // ------------------------------------------------------------------------------
 // per-length tables: tjb_b(L) and the smallest xJ that passes F1 at length L
 
-int msvgb_detail::xjmin_for(const msvgb_profile *p, int L, double F1) {
+int msvgb_detail::xjmin_for(const msvgb_profile *p, int L, double F1, int hint) {
   const int tjb = msvgb_tjb_b(p->scale, L);
   auto pass = [&](int xj) {
     return msvgb_f1_pass(score_from_xj(xj, tjb, p->base, p->scale), L, p->mmu, p->mlambda, F1, nullptr) != 0;
   };
+  if (hint >= 0 && hint <= 255) {
+    // Walk from a nearby length's answer (the boundary moves by a unit or two
+    // between neighbouring lengths): down while xJ - 1 still passes, or up
+    // until xJ passes. Every step evaluates the predicate on both sides of
+    // the boundary it returns, as the checks below do.
+    int b = hint;
+    if (b == 255 || pass(b)) {
+      while (b > 0 && pass(b - 1)) --b;
+    } else {
+      ++b;
+      while (b < 255 && !pass(b)) ++b;
+    }
+    return b;
+  }
   // P is non-increasing in xJ; binary search, then confirm the boundary.
   int lo = 0, hi = 255;                  // answer in [lo, hi]; 255 = no xJ < 255 passes
   while (lo < hi) {
@@ -689,11 +703,14 @@ int msvgb_detail::ensure_tables(msvgb_profile *p, const msvgb_db *db, double F1,
     t->cap = cap;
     dirty = true;
   }
+  int hint = -1;                                        // the last length's answer (lengths ascend)
   for (int L : db->distinct_len) {
-    if (L == 0 || t->xjm[L] >= 0) continue;
-    const int v = xjmin_for(p, L, F1);
+    if (L == 0) continue;
+    if (t->xjm[L] >= 0) { hint = t->xjm[L]; continue; }
+    const int v = xjmin_for(p, L, F1, hint);
     if (v < 0) return fail(MSVGB_eslESYS, "F1 pass set is not monotone in xJ");
     t->xjm[L] = (int16_t) v;
+    hint = v;
     dirty = true;
   }
   if (dirty) {
@@ -728,36 +745,6 @@ struct PhaseTimer {
     const auto now = std::chrono::steady_clock::now();
     fprintf(stderr, "msvgb: %-28s %8.3f ms\n", what, std::chrono::duration<double, std::milli>(now - t).count());
     t = now;
-  }
-};
-
-// Device-side timeline of one call (MSVGB_GPU_TRACE; unlike MSVGB_TRACE it
-// adds no synchronization): timed events recorded on the streams the work
-// runs on, printed relative to the first one once the call's work is done.
-static bool gpu_trace_on() { static const bool on = getenv("MSVGB_GPU_TRACE") != nullptr; return on; }
-struct GpuTrace {
-  struct Mark { std::string what; cudaEvent_t ev; std::chrono::steady_clock::time_point host; };
-  std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
-  std::vector<Mark> marks;
-  // s: the stream to time on; null: host time only
-  void mark(const std::string &what, cudaStream_t s) {
-    if (!gpu_trace_on()) return;
-    cudaEvent_t e = nullptr;
-    if (s && cudaEventCreate(&e) == cudaSuccess && cudaEventRecord(e, s) != cudaSuccess) { cudaEventDestroy(e); e = nullptr; }
-    marks.push_back(Mark{what, e, std::chrono::steady_clock::now()});
-  }
-  // gpu times relative to the first timed mark; host times (when enqueued) relative to the trace's creation
-  void print() {
-    cudaEvent_t first = nullptr;
-    for (auto &m : marks) if (m.ev) { first = m.ev; break; }
-    for (auto &m : marks) {
-      float ms = -1.f;
-      if (m.ev && cudaEventSynchronize(m.ev) == cudaSuccess) cudaEventElapsedTime(&ms, first, m.ev);
-      fprintf(stderr, "msvgb trace: %-30s gpu %8.3f ms   host %8.3f ms\n", m.what.c_str(), ms,
-              std::chrono::duration<double, std::milli>(m.host - t0).count());
-    }
-    for (auto &m : marks) if (m.ev) cudaEventDestroy(m.ev);      // after the loop: first is the reference
-    marks.clear();
   }
 };
 
@@ -833,7 +820,7 @@ int msvgb_detail::db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64
   }
   const int K = cuts.K;
   CUDA_TRY(cudaSetDevice(ctx->device));
-  GpuTrace gt;
+  msvgb_detail::GpuTrace gt;
   gt.mark("db: start", st);
   const int64_t n1 = std::max<int64_t>(n, 1);
   cudaMemPool_t pool = scratch_pool(ctx->device);
@@ -1072,6 +1059,17 @@ void msvgb_detail::release_chunks_on(msvgb_db *db, cudaStream_t st) {
   db->d_src = nullptr;
 }
 
+void msvgb_detail::db_release_on(msvgb_db *db, cudaStream_t st) {
+  if (!db) return;
+  cudaSetDevice(db->device);
+  for (void *q : {(void *) db->d_codes, (void *) db->d_start, (void *) db->d_orig, (void *) db->d_len,
+                  (void *) db->d_raw, (void *) db->d_src, (void *) db->d_inv})
+    if (q) cudaFreeAsync(q, st);
+  for (cudaEvent_t ev : db->chunk_up) cudaEventDestroy(ev);
+  if (db->ready) cudaEventDestroy(db->ready);
+  delete db;
+}
+
 extern "C" int msvgb_db_destroy(msvgb_db *db) {
   if (!db) return MSVGB_eslOK;
   cudaSetDevice(db->device);
@@ -1212,7 +1210,7 @@ extern "C" int msvgb_search(msvgb_ctx *c, const msvgb_profile *p, const msvgb_db
 // ctr: 6 zeroed counters (per-stream tickets for the long and main passes,
 // the list count, the list ticket); list: room for db->n entries.
 static int search_chunked(msvgb_ctx *c, const msvgb_profile *p, msvgb_db *db, const LenTables *t, uint8_t *d_xj,
-                          uint8_t *d_flags, unsigned long long *ctr, int64_t *list, GpuTrace &gt) {
+                          uint8_t *d_flags, unsigned long long *ctr, int64_t *list, msvgb_detail::GpuTrace &gt) {
   using namespace msvgb_detail;
   const int sms = c->num_sms;
   cudaStream_t S[2] = {c->stream, c->upload};
@@ -1286,15 +1284,17 @@ static int search_chunked(msvgb_ctx *c, const msvgb_profile *p, msvgb_db *db, co
 // ends, and the copy (at ~4x the rate the search consumes residues) stays
 // ahead of the search from then on. Results land in one device buffer and
 // come back in one copy at the end.
-extern "C" int msvgb_search_host(msvgb_ctx *c, const msvgb_profile *pc, const uint8_t *codes, const int64_t *off,
-                                 int64_t n, double F1, int64_t chunk_residues, uint8_t *out_xj,
-                                 uint8_t *out_flags) {
+int msvgb_detail::host_search(msvgb_ctx *c, const msvgb_profile *pc, const uint8_t *codes, const int64_t *off,
+                              int64_t n, double F1, int64_t chunk_residues, uint8_t *out_xj, uint8_t *out_flags,
+                              msvgb_db **keep_db) {
+  if (keep_db) *keep_db = nullptr;
   if (!c || !pc || n < 0 || (n && (!codes || !off || !out_xj || !out_flags)))
     return fail(MSVGB_eslEINVAL, "NULL argument");
   if (pc->ctx != c) return fail(MSVGB_eslEINVAL, "objects belong to another context");
-  if (n == 0) return MSVGB_eslOK;
+  if (n == 0 && !keep_db) return MSVGB_eslOK;
+  if (n == 0) return db_create_on(c, codes, off, 0, c->stream, keep_db);
   msvgb_profile *p = const_cast<msvgb_profile *>(pc);
-  GpuTrace gt;
+  msvgb_detail::GpuTrace gt;
   CUDA_TRY(cudaSetDevice(c->device));
   // chunk boundaries: by default a sixth of the residues, then chunks of a
   // third (the remainder last); one chunk below kOneChunkResidues, where
@@ -1357,12 +1357,22 @@ extern "C" int msvgb_search_host(msvgb_ctx *c, const msvgb_profile *pc, const ui
   e = cudaStreamSynchronize(c->stream);
   pt.mark("search_host: done");
   gt.mark("results back", c->stream);
-  msvgb_db_destroy(db);
-  gt.mark("database freed", nullptr);
-  gt.print();
   if (st == MSVGB_eslOK && e != cudaSuccess) st = fail(MSVGB_eslESYS, std::string("search: ") + cudaGetErrorString(e));
   if (st == MSVGB_eslOK && bad) st = fail(MSVGB_eslEINVAL, "residue code >= 29 (Kp)");
+  if (keep_db && st == MSVGB_eslOK) {                       // packed and complete: the stream was synchronized
+    db->d_bad_chunks = nullptr;                               // pointed into this call's scratch
+    *keep_db = db;
+  }
+  else msvgb_db_destroy(db);
+  gt.mark("database kept or freed", nullptr);
+  gt.print();
   return st;
+}
+
+extern "C" int msvgb_search_host(msvgb_ctx *c, const msvgb_profile *p, const uint8_t *codes, const int64_t *off,
+                                 int64_t n, double F1, int64_t chunk_residues, uint8_t *out_xj,
+                                 uint8_t *out_flags) {
+  return msvgb_detail::host_search(c, p, codes, off, n, F1, chunk_residues, out_xj, out_flags, nullptr);
 }
 
 // ------------------------------------------------------------------------------

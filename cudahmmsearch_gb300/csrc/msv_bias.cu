@@ -347,7 +347,7 @@ extern "C" int msvgb_biasfilter(msvgb_ctx *c, const float *compo, int M, const m
   cudaError_t e = cudaMemcpyAsync(d_ids, ids, nids * 8, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess) e = msvgb_detail::launch_gather_ids(d_ids, nids, db->d_inv, c->num_sms, c->stream);
   if (e == cudaSuccess)
-    e = msvgb_detail::launch_order_by_slot(d_ids, nids, db->n, d_cnt, d_order, c->num_sms, c->stream);
+    e = msvgb_detail::launch_order_by_length(d_ids, nids, db->d_len, db->Lmax, d_cnt, d_order, c->num_sms, c->stream);
   DbDev dbv{db->d_codes, db->d_start, db->d_len, db->d_orig, db->n};
   if (e == cudaSuccess) {
     (void) cudaGetLastError();

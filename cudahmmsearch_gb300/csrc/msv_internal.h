@@ -1,7 +1,10 @@
 // msv_internal.h -- definitions shared by the translation units of the C ABI
 // (not part of the public interface).
 #pragma once
+#include <chrono>
 #include <cstdint>
+#include <cstdio>
+#include <cstdlib>
 #include <mutex>
 #include <string>
 #include <unordered_map>
@@ -138,6 +141,39 @@ constexpr int kLongTarget = 2400;
 constexpr int kWideSplitMinM = 1024;
 
 namespace msvgb_detail {
+// Device-side timeline of one call (MSVGB_GPU_TRACE; unlike MSVGB_TRACE it
+// adds no synchronization): timed events recorded on the streams the work
+// runs on (and host times of the marks), printed relative to the first
+// timed mark once the call's work is done. Marks may come from several
+// threads.
+inline bool gpu_trace_on() { static const bool on = getenv("MSVGB_GPU_TRACE") != nullptr; return on; }
+struct GpuTrace {
+  struct Mark { std::string what; cudaEvent_t ev; std::chrono::steady_clock::time_point host; };
+  std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+  std::vector<Mark> marks;
+  std::mutex mu;
+  // s: the stream to time on; null: host time only
+  void mark(const std::string &what, cudaStream_t s) {
+    if (!gpu_trace_on()) return;
+    cudaEvent_t e = nullptr;
+    if (s && cudaEventCreate(&e) == cudaSuccess && cudaEventRecord(e, s) != cudaSuccess) { cudaEventDestroy(e); e = nullptr; }
+    std::lock_guard<std::mutex> lk(mu);
+    marks.push_back(Mark{what, e, std::chrono::steady_clock::now()});
+  }
+  void print() {
+    std::lock_guard<std::mutex> lk(mu);
+    cudaEvent_t first = nullptr;
+    for (auto &m : marks) if (m.ev) { first = m.ev; break; }
+    for (auto &m : marks) {
+      float ms = -1.f;
+      if (m.ev && cudaEventSynchronize(m.ev) == cudaSuccess) cudaEventElapsedTime(&ms, first, m.ev);
+      fprintf(stderr, "msvgb trace: %-30s gpu %8.3f ms   host %8.3f ms\n", m.what.c_str(), ms,
+              std::chrono::duration<double, std::milli>(m.host - t0).count());
+    }
+    for (auto &m : marks) if (m.ev) cudaEventDestroy(m.ev);      // after the loop: first is the reference
+    marks.clear();
+  }
+};
 // The database's original-index -> sorted-slot table (db->d_inv), built on
 // the context's stream at first use.
 cudaError_t ensure_inverse(msvgb_ctx *c, const msvgb_db *db);
@@ -149,7 +185,8 @@ int fail(int code, const std::string &msg);
 cudaError_t dispatch(int C, bool f16, const msvgb::LaunchArgs &a, int sms);
 // Smallest xJ passing the F1 gate at length L (255: none); -1 if the pass set
 // is not monotone in xJ.
-int xjmin_for(const msvgb_profile *p, int L, double F1);
+// hint: the answer at a nearby length (walked from instead of a binary search), or -1.
+int xjmin_for(const msvgb_profile *p, int L, double F1, int hint = -1);
 // Device tables of a profile; force_C > 0 imposes the DP width.
 int profile_build_width(msvgb_ctx *ctx, const msvgb_om *om, int want_f16, int force_C, msvgb_profile **ret);
 // Host images of the device cost tables of a profile at DP width C.
@@ -225,6 +262,10 @@ struct AsyncPack {
   // offsets, and nothing is packed: pack_chunk_on packs a chunk.
   const std::vector<int64_t> *cuts = nullptr;
 };
+// msvgb_search_host; with keep_db, the packed database is returned (resident,
+// complete) instead of freed, for later stages on the same sequences.
+int host_search(msvgb_ctx *c, const msvgb_profile *p, const uint8_t *codes, const int64_t *off, int64_t n,
+                double F1, int64_t chunk_residues, uint8_t *out_xj, uint8_t *out_flags, msvgb_db **keep_db);
 // Packs chunk k of a chunked database on stream st, once its residues are up.
 int pack_chunk_on(msvgb_ctx *ctx, msvgb_db *db, int k, cudaStream_t st);
 // Frees a chunked database's raw residues and scatter offsets on stream st,
@@ -233,6 +274,10 @@ void release_chunks_on(msvgb_db *db, cudaStream_t st);
 // msvgb_db_create on stream st; with a, asynchronous (see msv_api.cu).
 int db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64_t *off, int64_t n, cudaStream_t st,
                  msvgb_db **ret, const AsyncPack *a = nullptr);
+// msvgb_db_destroy of a database made by db_create_on (every array pool
+// memory) without cudaFree's device-wide wait: the arrays are freed in
+// stream order on st, which must follow the database's last use.
+void db_release_on(msvgb_db *db, cudaStream_t st);
 // A fresh database serial (keys the per-length table caches).
 uint64_t next_db_serial();
 // Adds one to the count msvgb_kernel_launches() reports.
@@ -251,11 +296,11 @@ cudaError_t launch_histogram(const int32_t *len, int64_t n, unsigned long long *
 // inv[orig[s]] = s (original index -> sorted slot); ids[j] = inv[ids[j]].
 cudaError_t launch_invert(const int64_t *orig, int64_t n, int64_t *inv, int num_sms, cudaStream_t stream);
 cudaError_t launch_gather_ids(int64_t *ids, int64_t n, const int64_t *inv, int num_sms, cudaStream_t stream);
-// order[k] = the list positions j sorted by slots[j] in 1024 buckets of
-// consecutive slots (database order, the longest first, up to the order within
-// a bucket); nslots: the database's size; cnt: 1024 int32 of scratch.
-cudaError_t launch_order_by_slot(const int64_t *slots, int64_t n, int64_t nslots, int32_t *cnt, int64_t *order,
-                                 int num_sms, cudaStream_t stream);
+// order[k] = the list positions j sorted longest first by len[slots[j]] in
+// 1024 length buckets (up to the order within a bucket); Lmax: the
+// database's longest; cnt: 1024 int32 of scratch.
+cudaError_t launch_order_by_length(const int64_t *slots, int64_t n, const int32_t *len, int Lmax, int32_t *cnt,
+                                   int64_t *order, int num_sms, cudaStream_t stream);
 // First slot and first packed byte of every key (scratch: bins_scratch_words
 // int64); *pos the packed size, and 64 padding codes after it in codes.
 int bins_scratch_words(int Lmax, int K);

@@ -237,21 +237,24 @@ gather_ids_kernel(int64_t *__restrict__ ids, int64_t n, const int64_t *__restric
     ids[j] = inv[ids[j]];
 }
 
-// Listed sequences in database order (longest first): a counting sort of the
-// list positions j into kOrderBuckets buckets of consecutive slots (the
-// database is sorted by length, so a bucket holds similar lengths; within one
-// the order is arbitrary). cnt[bucket] counts, is scanned to the first
-// position of each bucket, then hands out positions.
+// Listed sequences longest first: a counting sort of the list positions j
+// into kOrderBuckets buckets of descending length (bucket 1023 - 1023 *
+// sqrt(L / Lmax): finer where lengths are common; within a bucket the order
+// is arbitrary). It does not assume the database's own order (a database
+// built chunk by chunk is sorted within each chunk only). cnt[bucket] counts,
+// is scanned to the first position of each bucket, then hands out positions.
 constexpr int kOrderBuckets = 1024;
 
-__device__ __forceinline__ int slot_bucket(int64_t slot, int64_t nslots) {
-  return (int) ((slot * kOrderBuckets) / nslots);
+__device__ __forceinline__ int len_bucket(int L, int Lmax) {
+  const float r = Lmax > 0 ? sqrtf((float) min(L, Lmax) / (float) Lmax) : 0.f;
+  return (kOrderBuckets - 1) - min(kOrderBuckets - 1, (int) (r * (float) (kOrderBuckets - 1)));
 }
 
 __global__ void __launch_bounds__(256)
-slot_count_kernel(const int64_t *__restrict__ slots, int64_t n, int64_t nslots, int32_t *__restrict__ cnt) {
+slot_count_kernel(const int64_t *__restrict__ slots, int64_t n, const int32_t *__restrict__ len, int Lmax,
+                  int32_t *__restrict__ cnt) {
   for (int64_t j = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t) gridDim.x * blockDim.x)
-    atomicAdd(&cnt[slot_bucket(slots[j], nslots)], 1);
+    atomicAdd(&cnt[len_bucket(len[slots[j]], Lmax)], 1);
 }
 
 // exclusive scan of the kOrderBuckets counts in place; one block, one count per thread
@@ -272,10 +275,10 @@ slot_scan_kernel(int32_t *__restrict__ cnt) {
 }
 
 __global__ void __launch_bounds__(256)
-slot_place_kernel(const int64_t *__restrict__ slots, int64_t n, int64_t nslots, int32_t *__restrict__ cnt,
-                  int64_t *__restrict__ order) {
+slot_place_kernel(const int64_t *__restrict__ slots, int64_t n, const int32_t *__restrict__ len, int Lmax,
+                  int32_t *__restrict__ cnt, int64_t *__restrict__ order) {
   for (int64_t j = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t) gridDim.x * blockDim.x)
-    order[atomicAdd(&cnt[slot_bucket(slots[j], nslots)], 1)] = j;
+    order[atomicAdd(&cnt[len_bucket(len[slots[j]], Lmax)], 1)] = j;
 }
 
 int grid_for(int64_t n, int num_sms) {
@@ -317,15 +320,15 @@ cudaError_t msvgb_detail::launch_gather_ids(int64_t *ids, int64_t n, const int64
   return cudaGetLastError();
 }
 
-cudaError_t msvgb_detail::launch_order_by_slot(const int64_t *slots, int64_t n, int64_t nslots, int32_t *cnt,
+cudaError_t msvgb_detail::launch_order_by_length(const int64_t *slots, int64_t n, const int32_t *len, int Lmax, int32_t *cnt,
                                                int64_t *order, int num_sms, cudaStream_t stream) {
   if (n == 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(cnt, 0, kOrderBuckets * sizeof(int32_t), stream);
   if (e != cudaSuccess) return e;
   (void) cudaGetLastError();
-  slot_count_kernel<<<grid_for(n, num_sms), 256, 0, stream>>>(slots, n, nslots, cnt);
+  slot_count_kernel<<<grid_for(n, num_sms), 256, 0, stream>>>(slots, n, len, Lmax, cnt);
   slot_scan_kernel<<<1, kOrderBuckets, 0, stream>>>(cnt);
-  slot_place_kernel<<<grid_for(n, num_sms), 256, 0, stream>>>(slots, n, nslots, cnt, order);
+  slot_place_kernel<<<grid_for(n, num_sms), 256, 0, stream>>>(slots, n, len, Lmax, cnt, order);
   return cudaGetLastError();
 }
 

@@ -123,14 +123,17 @@ struct HitBlock {
 // F1 survivors. Appends the sequences past the last stage to out.
 int filter_block(msvgb_ctx *ctx, const msvgb_filters *f, msvgb_vprofile *vp, const msvgb_db *db, int64_t b0,
                  const int64_t *off, const std::vector<int64_t> &keep, const std::vector<float> &usc,
-                 msvgb_filter_stats &stats, std::vector<msvgb_filter_hit> &out) {
+                 msvgb_filter_stats &stats, std::vector<msvgb_filter_hit> &out, msvgb_detail::GpuTrace &gt) {
+  const std::string tag = "b" + std::to_string(b0) + " ";
   const size_t ns = keep.size();
   std::vector<float> fsc(ns), nsc(ns);
   std::vector<double> P(ns);
   for (size_t j = 0; j < ns; ++j) nsc[j] = msvgb_null_score((int) (off[b0 + keep[j] + 1] - off[b0 + keep[j]]));
   if (f->compo) {
+    gt.mark(tag + "bias start", ctx->stream);
     int st = msvgb_biasfilter(ctx, f->compo, f->om->M, db, keep.data(), (int64_t) ns, fsc.data());
     if (st != MSVGB_eslOK) return st;
+    gt.mark(tag + "bias done", ctx->stream);
   } else {
     fsc = nsc;                                                   // --nobias: filtersc = nullsc
   }
@@ -138,6 +141,7 @@ int filter_block(msvgb_ctx *ctx, const msvgb_filters *f, msvgb_vprofile *vp, con
   for (size_t j = 0; j < ns; ++j)
     if (msvgb_stage_pass(usc[j], fsc[j], f->om->mmu, f->om->mlambda, f->F1, &P[j])) past.push_back(j);
   stats.n_past_bias += (int64_t) past.size();
+  gt.mark(tag + "bias gate", nullptr);
   std::vector<int64_t> vids;
   std::vector<size_t> vpos;
   auto hit = [&](size_t j, float vfsc) {
@@ -155,8 +159,10 @@ int filter_block(msvgb_ctx *ctx, const msvgb_filters *f, msvgb_vprofile *vp, con
   if (!vids.empty()) {
     std::vector<int> xc(vids.size());
     std::vector<uint8_t> vst(vids.size());
+    gt.mark(tag + "vit start", ctx->stream);
     int st = msvgb_vitfilter(ctx, vp, db, vids.data(), (int64_t) vids.size(), xc.data(), vst.data());
     if (st != MSVGB_eslOK) return st;
+    gt.mark(tag + "vit done", ctx->stream);
     for (size_t t = 0; t < vids.size(); ++t) {
       const size_t j = vpos[t];
       const int L = (int) (off[b0 + keep[j] + 1] - off[b0 + keep[j]]);
@@ -168,6 +174,7 @@ int filter_block(msvgb_ctx *ctx, const msvgb_filters *f, msvgb_vprofile *vp, con
     }
   }
   stats.n_past_vit += passed;
+  gt.mark(tag + "vit gate", nullptr);
   return MSVGB_eslOK;
 }
 
@@ -203,6 +210,7 @@ extern "C" int msvgb_pipeline_filters(msvgb_ctx *ctx, const msvgb_filters *f, co
     return fail(MSVGB_eslEINVAL, "msvgb_pipeline_filters: bad arguments");
   if (f->vom && f->vom->M != f->om->M) return fail(MSVGB_eslEINVAL, "MSV and Viterbi parts of different models");
   if (n_workers < 1) n_workers = 1;
+  msvgb_detail::GpuTrace gt;
   msvgb_ctx *fctx = nullptr;
   msvgb_profile *prof = nullptr;
   msvgb_vprofile *vp = nullptr;
@@ -216,6 +224,7 @@ extern "C" int msvgb_pipeline_filters(msvgb_ctx *ctx, const msvgb_filters *f, co
   }
 
   msvgb_filter_stats stats{};
+  gt.mark("set up", nullptr);
   std::mutex mu;
   std::condition_variable cv;                 // any change of the two queues or the flags below
   std::deque<MsvBlock *> scored;              // MSV stage -> filter thread
@@ -242,18 +251,21 @@ extern "C" int msvgb_pipeline_filters(msvgb_ctx *ctx, const msvgb_filters *f, co
       if (!abort_flag.load()) {
         std::vector<int64_t> keep;
         std::vector<float> usc;
+        stats.nseqs += b->nb;
+        stats.nres += off[b->b0 + b->nb] - off[b->b0];
+        const uint8_t *fl = b->fl.data();
         for (int64_t i = 0; i < b->nb; ++i) {
+          if (!(fl[i] & MSVGB_FLAG_PASS)) continue;                 // P > F1 at the MSV stage (or empty)
           const int L = (int) (off[b->b0 + i + 1] - off[b->b0 + i]);
-          stats.nseqs++;
-          stats.nres += L;
-          if (L == 0 || !(b->fl[i] & MSVGB_FLAG_PASS)) continue;   // empty, or P > F1 at the MSV stage
+          if (L == 0) continue;
           keep.push_back(i);
-          usc.push_back(msvgb_score(b->xj[i], b->fl[i], L, f->om->base_b, f->om->scale_b));
+          usc.push_back(msvgb_score(b->xj[i], fl[i], L, f->om->base_b, f->om->scale_b));
         }
         stats.n_past_msv += (int64_t) keep.size();
-        s2 = filter_block(fctx, f, vp, b->db, b->b0, off, keep, usc, stats, hb->hits);
+        gt.mark("b" + std::to_string(b->b0) + " survivors listed", nullptr);
+        s2 = filter_block(fctx, f, vp, b->db, b->b0, off, keep, usc, stats, hb->hits, gt);
       }
-      msvgb_db_destroy(b->db);
+      msvgb_detail::db_release_on(b->db, fctx->stream);   // after its filter stages, without a device-wide wait
       delete b;
       if (s2 != MSVGB_eslOK) {
         delete hb;
@@ -302,8 +314,11 @@ extern "C" int msvgb_pipeline_filters(msvgb_ctx *ctx, const msvgb_filters *f, co
     b->nb = std::min(n, b0 + block_size) - b0;
     b->xj.resize(b->nb);
     b->fl.resize(b->nb);
-    st = msvgb_db_create(ctx, codes, off + b0, b->nb, &b->db);
-    if (st == MSVGB_eslOK) st = msvgb_search(ctx, prof, b->db, f->F1, b->xj.data(), b->fl.data());
+    // the block's residues go up chunk by chunk under its own search; the
+    // packed block stays resident for the bias and Viterbi stages
+    gt.mark("b" + std::to_string(b0) + " msv start", ctx->stream);
+    st = msvgb_detail::host_search(ctx, prof, codes, off + b0, b->nb, f->F1, 0, b->xj.data(), b->fl.data(), &b->db);
+    gt.mark("b" + std::to_string(b0) + " msv done", ctx->stream);
     if (st != MSVGB_eslOK) {
       msvgb_db_destroy(b->db);
       delete b;
@@ -321,11 +336,14 @@ extern "C" int msvgb_pipeline_filters(msvgb_ctx *ctx, const msvgb_filters *f, co
   cv.notify_all();
   ft.join();
   for (auto &t : workers) t.join();
+  gt.mark("continuation done", nullptr);
   for (MsvBlock *b : scored) { msvgb_db_destroy(b->db); delete b; }
   for (HitBlock *b : hits) delete b;
   msvgb_vprofile_destroy(vp);
   msvgb_profile_destroy(prof);
   msvgb_ctx_destroy(fctx);
+  gt.mark("torn down", nullptr);
+  gt.print();
   if (ret_stats) *ret_stats = stats;
   if (st == MSVGB_eslOK && fst != MSVGB_eslOK) return fail(fst, fmsg);
   if (st == MSVGB_eslOK && abort_flag.load()) return fail(MSVGB_eslFAIL, "the continuation asked to stop");

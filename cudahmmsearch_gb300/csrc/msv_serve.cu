@@ -422,11 +422,13 @@ extern "C" int msvgb_server_submit(msvgb_server *s, const msvgb_om *om, uint64_t
   const int Lmax = s->db->Lmax;
   std::vector<uint8_t> xjm(Lmax + 1, 255), tjb(Lmax + 1);
   for (int L = 0; L <= Lmax; ++L) tjb[L] = msvgb_tjb_b(om->scale_b, L);
+  int hint = -1;                                       // the last length's answer (lengths ascend)
   for (int L : s->db->distinct_len) {
     if (L == 0) continue;
-    const int v = msvgb_detail::xjmin_for(&tmp, L, s->F1);
+    const int v = msvgb_detail::xjmin_for(&tmp, L, s->F1, hint);
     if (v < 0) return fail(MSVGB_eslESYS, "F1 pass set is not monotone in xJ");
     xjm[L] = (uint8_t) v;
+    hint = v;
   }
   // admission: wait for a free slot
   int slot;

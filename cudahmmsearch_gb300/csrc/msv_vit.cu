@@ -562,10 +562,19 @@ cudaError_t msvgb_detail::ensure_inverse(msvgb_ctx *c, const msvgb_db *db) {
   static std::mutex mu;                      // a database may be listed from several contexts at once
   std::lock_guard<std::mutex> lk(mu);
   if (db->d_inv) return cudaSuccess;
+  // pool memory (freed in stream order with the database's other arrays);
+  // complete before it is published, so that a search on another context's
+  // stream never reads it half built
+  cudaMemPool_t pool = scratch_pool(c->device);
+  if (!pool) return cudaErrorMemoryAllocation;
   int64_t *inv = nullptr;
-  cudaError_t e = cudaMalloc(&inv, std::max<int64_t>(db->n, 1) * 8);
+  cudaError_t e = cudaMallocFromPoolAsync((void **) &inv, std::max<int64_t>(db->n, 1) * 8, pool, c->stream);
   if (e == cudaSuccess) e = launch_invert(db->d_orig, db->n, inv, c->num_sms, c->stream);
-  if (e != cudaSuccess) { cudaFree(inv); return e; }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {
+    if (inv) { cudaFreeAsync(inv, c->stream); cudaStreamSynchronize(c->stream); }
+    return e;
+  }
   const_cast<msvgb_db *>(db)->d_inv = inv;   // a cache of the database's own order: logically const
   return cudaSuccess;
 }
@@ -734,7 +743,7 @@ extern "C" int msvgb_vitfilter(msvgb_ctx *c, msvgb_vprofile *p, const msvgb_db *
   cudaError_t e = cudaMemcpyAsync(d_ids, ids, nids * 8, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess) e = msvgb_detail::launch_gather_ids(d_ids, nids, db->d_inv, c->num_sms, c->stream);
   if (e == cudaSuccess)
-    e = msvgb_detail::launch_order_by_slot(d_ids, nids, db->n, d_cnt, d_order, c->num_sms, c->stream);
+    e = msvgb_detail::launch_order_by_length(d_ids, nids, db->d_len, db->Lmax, d_cnt, d_order, c->num_sms, c->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(c->d_ticket, 0, sizeof(unsigned long long), c->stream);
   VitDev V;
   V.CV = p->CV; V.base_w = p->base_w; V.ddbound_w = p->ddbound_w;
