@@ -336,9 +336,8 @@ int msvgb_calibrate(msvgb_ctx *ctx, msvgb_om *om, double lambda);
  * array: calls whose work overlaps on the GPU (different streams, or
  * different host threads) race and must be serialised by the caller. The
  * first call on a device looks up the array's device address
- * (cudaGetSymbolAddress) and keeps it for the process: make that first call
- * before any stream capture, and do not call this again after a
- * cudaDeviceReset. Work is enqueued on cuda_stream (NULL: the context's
+ * (cudaGetSymbolAddress) and keeps it for the process; do not call this
+ * again after a cudaDeviceReset. Work is enqueued on cuda_stream (NULL: the context's
  * stream); the two per-length tables go up from pageable host memory, so the
  * call first waits for the stream's earlier work. It always runs the fused
  * 32-lane search kernel (the lane-group pass that msvgb_search_device may
