@@ -918,14 +918,17 @@ int msvgb_detail::db_create_on(msvgb_ctx *ctx, const uint8_t *codes, const int64
     e = keep((void **) &db->d_codes, bound + 64);
     if (e == cudaSuccess) e = alloc((void **) &d_hist, K * nb * 8, st);
     if (e == cudaSuccess) e = alloc((void **) &d_bins, (2 * K * nb + bins_scratch_words(Lmax, K)) * 8, st);
+    uint32_t *d_blk = nullptr;                                // per part and short key: counts, then first ranks
+    const size_t blk_words = (size_t) sort_parts(ctx->num_sms) * K * sort_small_bound(Lmax, K);
+    if (e == cudaSuccess) e = alloc((void **) &d_blk, blk_words * 4, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(d_hist, 0, K * nb * 8, st);
-    if (e == cudaSuccess) e = launch_histogram(d_len_in, n, d_hist, cuts, Lmax, ctx->num_sms, st);
+    if (e == cudaSuccess) e = launch_histogram(d_len_in, n, d_hist, d_blk, cuts, Lmax, ctx->num_sms, st);
     if (e == cudaSuccess) e = launch_bins(d_hist, Lmax, K, d_bins, d_bins + K * nb, d_bins + 2 * K * nb, d_scal + 1,
                                           db->d_codes, st);
     unsigned long long *cursor = nullptr;
     if (e == cudaSuccess) e = alloc((void **) &cursor, K * nb * 8, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(cursor, d_bins, K * nb * 8, cudaMemcpyDeviceToDevice, st);
-    if (e == cudaSuccess) e = launch_place(d_off, d_len_in, n, cursor, d_bins, d_bins + K * nb, db->d_start,
+    if (e == cudaSuccess) e = launch_place(d_off, d_len_in, n, cursor, d_blk, d_bins, d_bins + K * nb, db->d_start,
                                            db->d_orig, db->d_len, d_src, cuts, Lmax, ctx->num_sms, st);
     pt.mark("sort enqueued");
     gt.mark("db: placed", st);
@@ -1296,22 +1299,24 @@ int msvgb_detail::host_search(msvgb_ctx *c, const msvgb_profile *pc, const uint8
   msvgb_profile *p = const_cast<msvgb_profile *>(pc);
   msvgb_detail::GpuTrace gt;
   CUDA_TRY(cudaSetDevice(c->device));
-  // chunk boundaries: by default a sixth of the residues, then chunks of a
-  // third (the remainder last); one chunk below kOneChunkResidues, where
-  // the whole copy is shorter than the sort; with chunk_residues, chunks
-  // growing from a quarter of it to it. At most kMaxChunks.
+  // chunk boundaries: chunks growing from a quarter of chunk_residues to it
+  // (by default a third of the residues: a first chunk of a twelfth, whose
+  // copy ends about when the sort does, then a sixth, then thirds, the
+  // remainder last); one chunk below kOneChunkResidues, where the whole copy
+  // is shorter than the sort. At most kMaxChunks.
   std::vector<int64_t> cut(1, 0);
   const int64_t total = off[n] - off[0];
   constexpr int64_t kOneChunkResidues = 64 << 20;
-  int64_t want = chunk_residues > 0 ? std::max<int64_t>(1, chunk_residues / 4)
-                                    : (total < kOneChunkResidues ? std::max<int64_t>(1, total) : total / 6 + 1);
+  const bool one = chunk_residues <= 0 && total < kOneChunkResidues;
+  if (chunk_residues <= 0) chunk_residues = one ? std::max<int64_t>(1, total) : total / 3 + 1;
+  int64_t want = one ? std::max<int64_t>(1, total) : std::max<int64_t>(1, chunk_residues / 4);
   for (int64_t b0 = 0; b0 < n;) {
     // the first sequence boundary at least want residues past b0's start, or n
     int64_t b1 = std::lower_bound(off + b0 + 1, off + n, off[b0] + want) - off;
     if ((int) cut.size() == kMaxChunks) b1 = n;               // the last chunk takes the rest
     cut.push_back(b1);
     b0 = b1;
-    want = chunk_residues > 0 ? std::min(chunk_residues, 2 * want) : total / 3 + 1;
+    want = std::min(chunk_residues, 2 * want);
   }
   gt.mark("chunks cut", nullptr);
   // device scratch: results [xj n | flags n], the invalid-code flag, 6 counters; the undecided list

@@ -290,9 +290,13 @@ cudaError_t launch_pack(const uint8_t *raw, const int64_t *src, const int64_t *s
 // validity flag; per-length counts; sorted placement.
 cudaError_t launch_lengths(const int64_t *off, int64_t n, int32_t *len, unsigned *lmax, int *bad, int num_sms,
                            cudaStream_t stream);
-// Counts per (chunk, length), in sorted key order: hist[k * (Lmax + 1) + Lmax - L].
-cudaError_t launch_histogram(const int32_t *len, int64_t n, unsigned long long *hist, const ChunkCuts &cuts,
-                             int Lmax, int num_sms, cudaStream_t stream);
+// Counts per (chunk, length), in sorted key order: hist[k * (Lmax + 1) + Lmax - L]
+// (zeroed by the caller); blk: sort_parts x K x sort_small_bound uint32 of
+// scratch, left holding each part's first rank per short key for launch_place.
+int sort_parts(int num_sms);
+int sort_small_bound(int Lmax, int K);
+cudaError_t launch_histogram(const int32_t *len, int64_t n, unsigned long long *hist, uint32_t *blk,
+                             const ChunkCuts &cuts, int Lmax, int num_sms, cudaStream_t stream);
 // inv[orig[s]] = s (original index -> sorted slot); ids[j] = inv[ids[j]].
 cudaError_t launch_invert(const int64_t *orig, int64_t n, int64_t *inv, int num_sms, cudaStream_t stream);
 cudaError_t launch_gather_ids(int64_t *ids, int64_t n, const int64_t *inv, int num_sms, cudaStream_t stream);
@@ -310,9 +314,11 @@ cudaError_t launch_bins(const unsigned long long *hist, int Lmax, int K, int64_t
 // pool, which keeps up to 4 GiB mapped between calls (the default pool would
 // unmap and map again every time).
 cudaMemPool_t scratch_pool(int device);
+// cursor: each key's first slot (used by the long sequences); blk as
+// launch_histogram left it.
 cudaError_t launch_place(const int64_t *off, const int32_t *len_in, int64_t n, unsigned long long *cursor,
-                         const int64_t *bin_slot, const int64_t *bin_byte, int64_t *start, int64_t *orig,
-                         int32_t *len, int64_t *src, const ChunkCuts &cuts, int Lmax, int num_sms,
+                         const uint32_t *blk, const int64_t *bin_slot, const int64_t *bin_byte, int64_t *start,
+                         int64_t *orig, int32_t *len, int64_t *src, const ChunkCuts &cuts, int Lmax, int num_sms,
                          cudaStream_t stream);
 }  // namespace msvgb_detail
 

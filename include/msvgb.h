@@ -294,9 +294,9 @@ int msvgb_search_device(msvgb_ctx *ctx, const msvgb_profile *prof, const msvgb_d
 
 /* End to end from host buffers, for a database that is not kept resident:
  * sequences codes[off[i] .. off[i+1]) (as msvgb_db_create takes them) are cut
- * into chunks of consecutive sequences (by default a sixth of the residues,
- * then thirds, or one chunk below 64 M residues; with chunk_residues > 0,
- * chunks growing from a quarter of that size to it; at most 16); the offsets
+ * into chunks of consecutive sequences growing from a quarter of
+ * chunk_residues to it (by default a third of the residues, or one chunk
+ * below 64 M residues; at most 16 chunks); the offsets
  * go up and are sorted chunk by chunk while the chunks' residues follow, and
  * every chunk is packed and searched as soon as it is up, the full MSV of all
  * chunks' undecided sequences last. Results as msvgb_search; eslEINVAL for a
