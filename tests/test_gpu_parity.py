@@ -280,3 +280,19 @@ def test_search_host_rejects_invalid_codes_in_a_later_chunk(ctx, code):
     good = api.search_host(ctx, dp, s, chunk_residues=s.total // 8)
     ref = api.search(ctx, dp, api.DeviceDB(ctx, s))
     assert np.array_equal(good[0], ref[0]) and np.array_equal(good[1], ref[1])
+
+
+def test_host_sort_for_sequences_over_4M_residues(ctx):
+    """A target longer than 4M residues sends the length sort to the host
+    (resident creation, and the chunked host search with its per-chunk key):
+    results equal the oracle's for every sequence, the long one included."""
+    p, _, _ = load_case("m200_s1")
+    rng = np.random.default_rng(97)
+    long_seq = rng.integers(0, 20, size=4_300_000).astype(np.uint8)
+    s = F.SeqSet.concat([F.synth_sequences(3000, seed=98, lmax=4000), F.emit_homologs(p, 20, seed=99),
+                         F.SeqSet.from_list([long_seq]), F.synth_sequences(500, seed=100, lmax=900)])
+    dp = api.DeviceProfile(ctx, p)
+    a = api.search(ctx, dp, api.DeviceDB(ctx, s))
+    b = api.search_host(ctx, dp, s, chunk_residues=s.total // 3)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    check_against_oracle(p, s, a[0], a[1], O.msv_batch(p, s))
