@@ -396,12 +396,15 @@ __device__ __forceinline__ uint32_t msv_row_group(uint32_t (&dp)[C], uint32_t xB
   }
   if constexpr (Lay::R & 1) s[C - 1] = tab[Lay::A_WORDS + Lay::B_WORDS + (x * Cp::SINGLE + gidx) * G + glane];
   const uint32_t pred0 = pred_word0(dp[C - 1], src_lane);
-  uint32_t acc[4] = {0u, 0u, 0u, 0u};                // four short chains: the row maximum is on the critical path
 #pragma unroll
-  for (int w = C - 1; w >= 0; --w) {
-    dp[w] = fma_relu_f16x2(max_f16x2(w ? dp[w - 1] : pred0, xB2), one2, s[w]);
-    acc[w & 3] = max_s16x2(acc[w & 3], dp[w]);       // non-negative f16 bits order like integers
-  }
+  for (int w = C - 1; w >= 0; --w) dp[w] = fma_relu_f16x2(max_f16x2(w ? dp[w - 1] : pred0, xB2), one2, s[w]);
+  // the row maximum on the bits (non-negative f16 bits order like integers):
+  // one three-input maximum per two words, in four short chains (the
+  // maximum is on the critical path of the next row)
+  uint32_t acc[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+  for (int w = 0; w + 1 < C; w += 2) acc[(w / 2) & 3] = __vimax3_s16x2(acc[(w / 2) & 3], dp[w], dp[w + 1]);
+  if constexpr (C & 1) acc[3] = max_s16x2(acc[3], dp[C - 1]);
   return max_s16x2(max_s16x2(acc[0], acc[1]), max_s16x2(acc[2], acc[3]));
 }
 
