@@ -140,3 +140,25 @@ def test_biasfilter_matches_oracle_at_scale(ctx):
     want = O.bias_batch(r.compo, r.M, s)
     assert s.total > 2_500_000
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_pipeline_filters_large_block_equals_small_blocks(ctx):
+    """A block above 64M residues goes through the MSV stage in several
+    chunks (sorted chunk by chunk, searched as they arrive) and stays resident
+    for the bias and Viterbi stages, which then list their sequences by
+    length: the same hits, scores and counters as small blocks (one chunk
+    each)."""
+    p = F.read_profile(os.path.join(GOLDEN, "pipe_m400_s1.prof"))
+    vp = F.read_vprofile(os.path.join(GOLDEN, "vit_m400_s1.vprof"))
+    r = F.read_pipe(os.path.join(GOLDEN, "pipe_m400_s1.pres"))
+    s = F.SeqSet.concat([F.synth_sequences(200_000, seed=1200, lmax=35000),
+                         F.emit_homologs(p, 4000, seed=1201, lmax=35000)])
+    assert s.total >= 64 << 20
+    kw = dict(vprof=vp, compo=r.compo, vmu=r.vmu, vlambda=r.vlambda, n_workers=3)
+    big, sb = api.pipeline_filters(ctx, p, s, block_size=s.n, **kw)
+    small, ss = api.pipeline_filters(ctx, p, s, block_size=s.n // 4 + 1, **kw)
+    assert sb.n_past_msv == ss.n_past_msv > 0 and sb.n_past_bias == ss.n_past_bias
+    assert sb.n_past_vit == ss.n_past_vit > 0
+    assert np.array_equal(big["seq_index"], small["seq_index"])
+    for f in ("usc", "nullsc", "filtersc", "vfsc"):
+        assert np.array_equal(bits(big[f]), bits(small[f])), f
