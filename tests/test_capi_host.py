@@ -120,3 +120,15 @@ def test_bias_length_term_matches_reference():
         got = lib.msvgb_bias_length_term(float(fwd), L)
         want = np.float32(np.float32(fwd) + np.float32(L) * np.float32(np.log(p1))) + np.float32(np.log(np.float32(1.0 - np.float64(p1))))
         assert abs(float(got) - float(want)) <= 1e-5 * max(1.0, abs(float(want)))
+
+
+@pytest.mark.parametrize("bad", ["dtype", "size", "stride"])
+def test_search_host_rejects_bad_result_buffers(bad):
+    """search_host's out=(xj, flags) must be two contiguous uint8 arrays of n
+    entries; anything else is refused on the host, before any GPU call."""
+    s = F.synth_sequences(10, seed=3, lmax=50)
+    ok = np.zeros(s.n, np.uint8)
+    wrong = {"dtype": np.zeros(s.n, np.int16), "size": np.zeros(s.n + 1, np.uint8),
+             "stride": np.zeros(2 * s.n, np.uint8)[::2]}[bad]
+    with pytest.raises(ValueError):
+        api.search_host(None, None, s, out=(ok, wrong))
